@@ -1,0 +1,142 @@
+/*
+ * onionpir_gpu.h -- C ABI of the GB300-native OnionPIRv2 server query path.
+ *
+ * This is the boundary a PirServer implementation calls instead of running
+ * the reference's single-threaded CPU loops.  Every entry point names the
+ * reference interface it replaces (paths are within chenyue42/OnionPIRv2).
+ *
+ * Conventions
+ *   - N = 2048 (DatabaseConstants::PolyDegree), one ciphertext prime q plus
+ *     SEAL's special key-switching prime p (CoeffMods = {60, 60}: rns = 1).
+ *   - A ciphertext is uint64_t[2][N] (c0 then c1), fully reduced mod q,
+ *     coefficient form -- SEAL's in-memory layout for rns = 1.
+ *   - "NTT form" means the negacyclic transform A[k] = a(psi^(2 brv(k)+1)),
+ *     psi the smallest primitive 2N-th root of unity mod the prime.
+ *   - Host buffers are caller-owned; the context owns all device memory.
+ *   - Every call returns an opir_status; opir_last_error() explains the
+ *     most recent failure.  No C++ exception crosses this ABI.
+ *   - Calls on one context are serialised by an internal mutex.
+ */
+#ifndef ONIONPIR_GPU_H
+#define ONIONPIR_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  OPIR_OK = 0,
+  OPIR_ERR_ARG = -1,            /* invalid argument / parameter set        */
+  OPIR_ERR_UNKNOWN_CLIENT = -2, /* no keys for this client id (server.cpp:389 .at()) */
+  OPIR_ERR_UNKNOWN_DB = -3,
+  OPIR_ERR_OOM = -4,            /* device allocation failed                 */
+  OPIR_ERR_CUDA = -5,           /* CUDA runtime error                       */
+  OPIR_ERR_STATE = -6,          /* call not valid in the current state      */
+  OPIR_ERR_NO_DEVICE = -7
+} opir_status;
+
+/* Ciphertext-side parameters (PirParams, pir.cpp:9-54; database_constants.h). */
+typedef struct opir_params {
+  uint32_t poly_degree;     /* N; must be 2048                                  */
+  uint64_t coeff_modulus;   /* q  (CoeffModulus::Create(N,{60,60})[0])          */
+  uint64_t special_modulus; /* p  (the last, key-switching prime)               */
+  uint64_t plain_modulus;   /* t  (utils::generate_prime(PlainMod))             */
+  uint64_t small_modulus;   /* small_q (pir.cpp:40-41)                          */
+  uint32_t gsw_l;           /* l      (GSW_L)                                   */
+  uint32_t gsw_base_log2;   /* log2 B (pir.cpp:53)                              */
+  uint32_t gsw_l_key;       /* l_key  (GSW_L_KEY)                               */
+  uint32_t gsw_base_log2_key; /* (pir.cpp:54)                                   */
+} opir_params;
+
+/* Database shape (PirParams::get_dims / get_entry_size, pir.cpp:29-95). */
+typedef struct opir_db_shape {
+  uint32_t fst_dim_sz;      /* n1                                                */
+  uint32_t other_dim_sz;    /* n_rest = 2^(ndim-1)                               */
+  uint32_t entry_size;      /* bytes per entry                                   */
+  uint32_t entries_per_pt;  /* entries packed per plaintext                      */
+  uint32_t bits_per_coeff;  /* bits of entry data per plaintext coefficient      */
+} opir_db_shape;
+
+typedef struct opir_ctx opir_ctx;
+
+/* PirServer::PirServer (server.cpp:25-39): parameters, NTT tables, device. */
+int opir_ctx_create(const opir_params *params, int device, opir_ctx **out);
+void opir_ctx_destroy(opir_ctx *ctx);
+/* Run all work of this context on a caller-provided cudaStream_t (NULL =
+ * the context's own stream). */
+int opir_ctx_set_stream(opir_ctx *ctx, void *cuda_stream);
+const char *opir_last_error(const opir_ctx *ctx);
+uint64_t opir_response_bytes(const opir_ctx *ctx);
+
+/* ---- database (server.h:22-25; server.cpp:47-78, 635-748) ---- */
+int opir_db_create(opir_ctx *ctx, const opir_db_shape *shape, uint32_t *db_id);
+int opir_db_destroy(opir_ctx *ctx, uint32_t db_id);
+/* PirServer::push_database_chunk (server.cpp:635-701) + preprocess_ntt
+ * (703-719) + realign_db (722-748) for one chunk: chunk_idx selects
+ * plaintexts [chunk_idx*n1, (chunk_idx+1)*n1); `entries` holds
+ * n1*entries_per_pt entries of entry_size bytes each. */
+int opir_db_push_chunk(opir_ctx *ctx, uint32_t db_id, const uint8_t *entries,
+                       uint64_t num_entries, uint64_t chunk_idx);
+/* PirServer::gen_data (server.cpp:47-78) with entries derived from `seed`
+ * (8-byte big-endian index + seeded bytes, utils.cpp:160-172), generated and
+ * ingested on the device. */
+int opir_db_fill_synthetic(opir_ctx *ctx, uint32_t db_id, uint64_t seed);
+/* Upload an already-NTT'd database in the reference layout
+ * db_aligned_[c*num_pt + row*n1 + col] (server.cpp:740). */
+int opir_db_upload_aligned(opir_ctx *ctx, uint32_t db_id, const uint64_t *db_aligned);
+
+/* ---- per-client keys (server.cpp:480-500) ---- */
+/* set_client_galois_key: keys[level][k][mod][N], NTT form, level a is the
+ * Galois element 1 + (N >> a) (client.cpp:235-237), mod 0 = q, 1 = p. */
+int opir_set_galois_key(opir_ctx *ctx, uint64_t client_id, const uint64_t *keys,
+                        uint32_t levels);
+/* set_client_gsw_key: 2*l_key RGSW(sk) rows [row][2][N], coefficient form;
+ * transformed to NTT form on the device (gsw_eval.cpp:15-31). */
+int opir_set_gsw_key(opir_ctx *ctx, uint64_t client_id, const uint64_t *rows);
+int opir_erase_client(opir_ctx *ctx, uint64_t client_id);
+
+/* ---- queries (server.cpp:520-633) ---- */
+/* PirServer::make_query + mod_switch_inplace + save_resp_to_stream:
+ * query[2][N] (coefficient form, mod q) -> resp[2][N] (mod small_q, may be
+ * NULL) and packed (opir_response_bytes() bytes, may be NULL).  Blocking. */
+int opir_make_query(opir_ctx *ctx, uint32_t db_id, uint64_t client_id, const uint64_t *query,
+                    uint64_t *resp, uint8_t *packed);
+/* The same for `batch` independent queries against one database in one
+ * pass: queries[batch][2][N], resps[batch][2][N], packed[batch][bytes]. */
+int opir_make_query_batch(opir_ctx *ctx, uint32_t db_id, uint32_t batch,
+                          const uint64_t *client_ids, const uint64_t *queries, uint64_t *resps,
+                          uint8_t *packed);
+/* Device-pointer variant, asynchronous on the context stream. */
+int opir_make_query_device(opir_ctx *ctx, uint32_t db_id, uint32_t batch,
+                           const uint64_t *client_ids, const uint64_t *d_queries,
+                           uint64_t *d_resps, uint8_t *d_packed);
+/* make_query with every intermediate copied out, for parity tests:
+ * leaves[u][2][N] (after fast_expand_qry), gsw[(ndim-1)][2l][2][N] (NTT form),
+ * first_dim[n_rest][2][N] (after evaluate_first_dim, coefficient form).
+ * Any output pointer may be NULL. */
+int opir_make_query_trace(opir_ctx *ctx, uint32_t db_id, uint64_t client_id,
+                          const uint64_t *query, uint64_t *leaves, uint64_t *gsw,
+                          uint64_t *first_dim, uint64_t *resp, uint8_t *packed);
+
+/* ---- timing and accounting ---- */
+/* Enable per-stage CUDA-event timing of subsequent queries. */
+int opir_set_timing(opir_ctx *ctx, int enable);
+/* Device milliseconds of the last timed query for the reference's sections
+ * (logging.h): [0] Expand, [1] Convert, [2] First dim, [3] Other dim,
+ * [4] Mod switch; [5] = the first-dimension scan kernel alone. */
+int opir_stage_times(opir_ctx *ctx, float *ms6);
+/* Number of kernels this context has launched since creation. */
+uint64_t opir_launch_count(const opir_ctx *ctx);
+
+/* ---- primitives (tests) ---- */
+/* Negacyclic NTT of `count` polynomials mod q (mod = 0) or p (mod = 1),
+ * host buffers, in place. */
+int opir_ntt(opir_ctx *ctx, int mod, int inverse, uint64_t *polys, uint64_t count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

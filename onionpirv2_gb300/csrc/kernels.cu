@@ -1,0 +1,635 @@
+// kernels.cu -- OnionPIRv2 server query path on GB300 (sm_103a).
+//
+// Each kernel restates one stage of PirServer::make_query (server.cpp:520-579)
+// with exact integer arithmetic.  One CTA of 256 threads owns one
+// polynomial pair (a ciphertext) and keeps it in registers, 8 coefficients
+// per thread; NTTs exchange through shared memory (common.cuh).
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace opir {
+
+namespace {
+
+constexpr int T = kNttThreads;
+
+// ---------------------------------------------------------------------------
+// generic batched NTT
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(T) ntt_kernel(ModTab M, uint64_t *polys, int inverse) {
+  __shared__ uint64_t sa[kSmemPoly], sb[kSmemPoly];
+  uint64_t *p = polys + (size_t)blockIdx.x * kN;
+  const int tid = threadIdx.x;
+  uint64_t r[8];
+  if (!inverse) {
+#pragma unroll
+    for (int e = 0; e < 8; ++e) r[e] = p[strided_idx(tid, e)];
+    ntt_fwd(r, sa, sb, M);
+#pragma unroll
+    for (int e = 0; e < 8; ++e) p[slot_idx(tid, e)] = r[e];
+  } else {
+#pragma unroll
+    for (int e = 0; e < 8; ++e) r[e] = p[slot_idx(tid, e)];
+    ntt_inv(r, sa, sb, M);
+#pragma unroll
+    for (int e = 0; e < 8; ++e) p[strided_idx(tid, e)] = r[e];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// expansion: one level of fast_expand_qry (server.cpp:383-428)
+//   c' = apply_galois(c_i, N/k + 1)   (automorphism + key switch with p)
+//   c_2i = c_i + c';  c_2i+1 = (c_i - c') * x^-k
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(T) expand_level_kernel(const uint64_t *cur, uint64_t *nxt,
+                                                         size_t in_stride, size_t out_stride,
+                                                         const QueryDesc *qd, int level,
+                                                         ModTab Mq, ModTab Mp, Consts C) {
+  extern __shared__ uint64_t smem[];
+  uint64_t *sa = smem, *sb = smem + kSmemPoly;
+  uint64_t *s_sig0 = smem + 2 * kSmemPoly;  // sigma(c0), natural index
+  uint64_t *s_sig1 = s_sig0 + kN;           // sigma(c1)
+  const int tid = threadIdx.x;
+  const int node = blockIdx.x, b = blockIdx.y;
+  const int k = 1 << level;
+  const uint64_t g = (uint64_t)(kN / k + 1);
+  const uint64_t q = C.q, p = C.p;
+  const uint64_t *ci = cur + b * in_stride + (size_t)node * 2 * kN;
+
+  // automorphism x -> x^g on both polynomials (scatter to shared memory)
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const int i = strided_idx(tid, e);
+    const uint32_t j = (uint32_t)(((uint64_t)i * g) & (2 * kN - 1));
+    const uint64_t v0 = ci[i], v1 = ci[kN + i];
+    if (j < (uint32_t)kN) {
+      s_sig0[j] = v0;
+      s_sig1[j] = v1;
+    } else {
+      s_sig0[j - kN] = neg_mod(v0, q);
+      s_sig1[j - kN] = neg_mod(v1, q);
+    }
+  }
+  __syncthreads();
+
+  // T = sigma(c1) in NTT form mod q and mod p
+  uint64_t tq[8], tp[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const uint64_t v = s_sig1[strided_idx(tid, e)];
+    tq[e] = v;
+    tp[e] = v >= p ? v - p : v;  // q < 2p
+  }
+  ntt_fwd(tq, sa, sb, Mq);
+  ntt_fwd(tp, sa, sb, Mp);
+
+  const uint64_t *key = qd[b].galois + (size_t)level * 4 * kN;
+  uint64_t out[2][8];
+#pragma unroll
+  for (int kk = 0; kk < 2; ++kk) {
+    const uint64_t *kq = key + (2 * kk + 0) * kN, *kp = key + (2 * kk + 1) * kN;
+    uint64_t aq[8], ap[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const int si = slot_idx(tid, e);
+      aq[e] = mul_mod(tq[e], __ldg(kq + si), Mq);
+      ap[e] = mul_mod(tp[e], __ldg(kp + si), Mp);
+    }
+    ntt_inv(aq, sa, sb, Mq);
+    ntt_inv(ap, sa, sb, Mp);
+    // round(X / p) mod q = (x_q + p/2 - ((x_p + p/2) mod p)) * p^-1 mod q
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const uint64_t rr = add_mod(ap[e], C.p_half, p);
+      const uint64_t v = sub_mod(add_mod(aq[e], C.p_half_mod_q, q), rr, q);
+      out[kk][e] = mul_shoup(v, C.p_inv_q, C.p_inv_q_s, q);
+    }
+  }
+
+  uint64_t *ce = nxt + b * out_stride + (size_t)(2 * node) * 2 * kN;
+  uint64_t *co = ce + 2 * kN;
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const int i = strided_idx(tid, e);
+    const uint64_t cp0 = add_mod(s_sig0[i], out[0][e], q);
+    const uint64_t cp1 = out[1][e];
+    const uint64_t x0 = ci[i], x1 = ci[kN + i];
+    ce[i] = add_mod(x0, cp0, q);
+    ce[kN + i] = add_mod(x1, cp1, q);
+    const uint64_t d0 = sub_mod(x0, cp0, q), d1 = sub_mod(x1, cp1, q);
+    // multiply by x^-k (utils.cpp:6-26): coefficient i moves to i - k, wrapping
+    // ones are negated (zero stays zero)
+    if (i >= k) {
+      co[i - k] = d0;
+      co[kN + i - k] = d1;
+    } else {
+      co[kN - k + i] = neg_mod(d0, q);
+      co[2 * kN - k + i] = neg_mod(d1, q);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// RGSW external product core (gsw_eval.cpp:33-106, 184-252):
+// decompose both polynomials of ct (coefficient form, given in the strided
+// distribution) into l digits of base_log2 bits each, NTT every digit, and
+// accumulate digit_j * gsw[j][k] in 128 bits; reduce mod q.  Output: NTT
+// form, slot distribution.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void ext_product_core(const uint64_t x[2][8], const uint64_t *gsw,
+                                                 int l, int base_log2, uint64_t *sa,
+                                                 uint64_t *sb, const ModTab &M,
+                                                 uint64_t out[2][8]) {
+  const int tid = threadIdx.x;
+  const uint64_t mask = (1ULL << base_log2) - 1;
+  U128 acc0[8], acc1[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) acc0[e] = acc1[e] = U128{0, 0};
+#pragma unroll
+  for (int poly = 0; poly < 2; ++poly) {
+    for (int pp = l - 1; pp >= 0; --pp) {
+      const int j = poly * l + (l - 1 - pp);
+      const int sh = pp * base_log2;
+      uint64_t d[8];
+#pragma unroll
+      for (int e = 0; e < 8; ++e) d[e] = (x[poly][e] >> sh) & mask;
+      ntt_fwd(d, sa, sb, M);
+      const uint64_t *g0 = gsw + (size_t)j * 2 * kN, *g1 = g0 + kN;
+#pragma unroll
+      for (int e = 0; e < 8; ++e) {
+        const int si = slot_idx(tid, e);
+        mac_to(acc0[e], d[e], __ldg(g0 + si));
+        mac_to(acc1[e], d[e], __ldg(g1 + si));
+      }
+    }
+  }
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    out[0][e] = barrett128(acc0[e], M.q, M.mu_lo, M.mu_hi);
+    out[1][e] = barrett128(acc1[e], M.q, M.mu_lo, M.mu_hi);
+  }
+}
+
+// query_to_gsw (gsw_eval.cpp:254-286) for every leaf n1 + j, j < num_cts:
+// row (j % l) of RGSW (j / l) = NTT(ct); row l + (j % l) = RGSW(sk) x ct.
+__global__ void __launch_bounds__(T) query_to_gsw_kernel(const uint64_t *leaves,
+                                                         size_t leaves_stride, uint64_t *gsw_out,
+                                                         size_t gsw_stride, const QueryDesc *qd,
+                                                         int n1, ModTab M, Consts C) {
+  __shared__ uint64_t sa[kSmemPoly], sb[kSmemPoly];
+  const int tid = threadIdx.x;
+  const int j = blockIdx.x, b = blockIdx.y;
+  const int l = C.l;
+  const int dim = j / l, kk = j % l;
+  const uint64_t *ct = leaves + b * leaves_stride + (size_t)(n1 + j) * 2 * kN;
+  uint64_t *rgsw = gsw_out + b * gsw_stride + (size_t)dim * 2 * l * 2 * kN;
+  uint64_t x[2][8];
+#pragma unroll
+  for (int poly = 0; poly < 2; ++poly)
+#pragma unroll
+    for (int e = 0; e < 8; ++e) x[poly][e] = ct[poly * kN + strided_idx(tid, e)];
+  // first half: the ciphertext itself in NTT form
+  uint64_t *row0 = rgsw + (size_t)kk * 2 * kN;
+#pragma unroll
+  for (int poly = 0; poly < 2; ++poly) {
+    uint64_t r[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) r[e] = x[poly][e];
+    ntt_fwd(r, sa, sb, M);
+#pragma unroll
+    for (int e = 0; e < 8; ++e) row0[poly * kN + slot_idx(tid, e)] = r[e];
+  }
+  // second half: external product with RGSW(sk) under the key gadget
+  uint64_t out[2][8];
+  ext_product_core(x, qd[b].gsw_key, C.l_key, C.base_log2_key, sa, sb, M, out);
+  uint64_t *row1 = rgsw + (size_t)(l + kk) * 2 * kN;
+#pragma unroll
+  for (int poly = 0; poly < 2; ++poly)
+#pragma unroll
+    for (int e = 0; e < 8; ++e) row1[poly * kN + slot_idx(tid, e)] = out[poly][e];
+}
+
+// other_dim_mux (server.cpp:295-334) for pair j: y -= x; y = RGSW x y; y =
+// INTT(y); x += y.
+__global__ void __launch_bounds__(T) fold_kernel(uint64_t *res, size_t res_stride,
+                                                 const uint64_t *gsw, size_t gsw_stride, int half,
+                                                 ModTab M, Consts C) {
+  __shared__ uint64_t sa[kSmemPoly], sb[kSmemPoly];
+  const int tid = threadIdx.x;
+  const int j = blockIdx.x, b = blockIdx.y;
+  const uint64_t q = C.q;
+  uint64_t *xp = res + b * res_stride + (size_t)j * 2 * kN;
+  const uint64_t *yp = res + b * res_stride + (size_t)(j + half) * 2 * kN;
+  uint64_t d[2][8];
+#pragma unroll
+  for (int poly = 0; poly < 2; ++poly)
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const int i = poly * kN + strided_idx(tid, e);
+      d[poly][e] = sub_mod(yp[i], xp[i], q);
+    }
+  uint64_t out[2][8];
+  ext_product_core(d, gsw + b * gsw_stride, C.l, C.base_log2, sa, sb, M, out);
+#pragma unroll
+  for (int poly = 0; poly < 2; ++poly) {
+    ntt_inv(out[poly], sa, sb, M);
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const int i = poly * kN + strided_idx(tid, e);
+      xp[i] = add_mod(xp[i], out[poly][e], q);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// first dimension
+// ---------------------------------------------------------------------------
+
+// evaluate_first_dim's NTT of the selection vector (server.cpp:137-139) and
+// prep_query's transpose (server.cpp:80-118), into the scan operand:
+// qs[c * n1 + k] = {lo30(Q0), hi30(Q0), lo30(Q1), hi30(Q1)} of leaf k.
+__global__ void __launch_bounds__(T) query_prep_kernel(const uint64_t *leaves,
+                                                       size_t leaves_stride, uint4 *qs,
+                                                       size_t qs_stride, int n1, ModTab M) {
+  __shared__ uint64_t sa[kSmemPoly], sb[kSmemPoly];
+  const int tid = threadIdx.x;
+  const int k = blockIdx.x, b = blockIdx.y;
+  const uint64_t *ct = leaves + b * leaves_stride + (size_t)k * 2 * kN;
+  uint64_t r0[8], r1[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    r0[e] = ct[strided_idx(tid, e)];
+    r1[e] = ct[kN + strided_idx(tid, e)];
+  }
+  ntt_fwd(r0, sa, sb, M);
+  ntt_fwd(r1, sa, sb, M);
+  uint4 *dst = qs + b * qs_stride;
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const int c = slot_idx(tid, e);
+    uint4 v;
+    v.x = (uint32_t)(r0[e] & 0x3FFFFFFFu);
+    v.y = (uint32_t)(r0[e] >> 30);
+    v.z = (uint32_t)(r1[e] & 0x3FFFFFFFu);
+    v.w = (uint32_t)(r1[e] >> 30);
+    dst[(size_t)c * n1 + k] = v;
+  }
+}
+
+// Exact sum of 60x60-bit products with 30-bit halves: for a = a1 2^30 + a0,
+// b = b1 2^30 + b0 the product is a0 b0 + (a0 b1 + a1 b0) 2^30 + a1 b1 2^60.
+// Each half-product is < 2^60, so the three 64-bit partial sums absorb 16,
+// 8 and 16 k-steps; every 8 steps they are folded into 128-bit totals.
+struct Acc3 {
+  uint64_t ll, mid, hh;
+  U128 LL, MID, HH;
+};
+
+__device__ __forceinline__ void acc3_zero(Acc3 &a) {
+  a.ll = a.mid = a.hh = 0;
+  a.LL = a.MID = a.HH = U128{0, 0};
+}
+__device__ __forceinline__ void acc3_mac(Acc3 &a, uint32_t a0, uint32_t a1, uint32_t b0,
+                                         uint32_t b1) {
+  a.ll += (uint64_t)a0 * b0;
+  a.mid += (uint64_t)a0 * b1;
+  a.mid += (uint64_t)a1 * b0;
+  a.hh += (uint64_t)a1 * b1;
+}
+__device__ __forceinline__ void acc3_flush(Acc3 &a) {
+  add_to(a.LL, U128{a.ll, 0});
+  add_to(a.MID, U128{a.mid, 0});
+  add_to(a.HH, U128{a.hh, 0});
+  a.ll = a.mid = a.hh = 0;
+}
+__device__ __forceinline__ uint64_t acc3_reduce(Acc3 &a, const Consts &C, uint64_t mu_lo,
+                                                uint64_t mu_hi) {
+  acc3_flush(a);
+  const uint64_t q = C.q;
+  const uint64_t rl = barrett128(a.LL, q, mu_lo, mu_hi);
+  const uint64_t rm = barrett128(a.MID, q, mu_lo, mu_hi);
+  const uint64_t rh = barrett128(a.HH, q, mu_lo, mu_hi);
+  uint64_t r = add_mod(rl, mul_shoup(rm, C.two30, C.two30_s, q), q);
+  return add_mod(r, mul_shoup(rh, C.two60, C.two60_s, q), q);
+}
+
+// Database x query product (naive_level_mat_mat_128 / mat_mat_128,
+// matrix.cpp:79-97,220-235, plus delay_modulus's reduction, server.cpp:178-243).
+// Thread owns R consecutive rows of one coefficient plane c and streams
+// down the n1 columns: DB[c][k][row0..row0+R) is one R*8-byte load, Q[c][k]
+// one 16-byte broadcast load.
+template <int R>
+__global__ void __launch_bounds__(256) scan_kernel(const uint64_t *__restrict__ dbs,
+                                                   const uint4 *__restrict__ qs,
+                                                   size_t qs_stride, uint64_t *out,
+                                                   size_t out_stride, int n1, int n_rest,
+                                                   Consts C, uint64_t mu_lo, uint64_t mu_hi) {
+  const int b = blockIdx.y;
+  const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int groups = n_rest / R;
+  const size_t c = g / groups;
+  if (c >= (size_t)kN) return;
+  const int row0 = (int)(g % groups) * R;
+  const uint64_t *plane = dbs + c * (size_t)n1 * n_rest + row0;
+  const uint4 *qv = qs + b * qs_stride + c * (size_t)n1;
+
+  Acc3 acc[R][2];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    acc3_zero(acc[r][0]);
+    acc3_zero(acc[r][1]);
+  }
+  constexpr int U = 8;
+  int k = 0;
+  for (; k + U <= n1; k += U) {
+    uint64_t a[U][R];
+    uint4 bq[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const uint64_t *src = plane + (size_t)(k + u) * n_rest;
+      if constexpr (R == 2) {
+        const ulonglong2 v = __ldcs(reinterpret_cast<const ulonglong2 *>(src));
+        a[u][0] = v.x;
+        a[u][R - 1] = v.y;
+      } else {
+        a[u][0] = __ldcs(src);
+      }
+      bq[u] = __ldg(qv + k + u);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const uint32_t a0 = (uint32_t)a[u][r], a1 = (uint32_t)(a[u][r] >> 32);
+        acc3_mac(acc[r][0], a0, a1, bq[u].x, bq[u].y);
+        acc3_mac(acc[r][1], a0, a1, bq[u].z, bq[u].w);
+      }
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      acc3_flush(acc[r][0]);
+      acc3_flush(acc[r][1]);
+    }
+  }
+  for (; k < n1; ++k) {
+    const uint64_t *src = plane + (size_t)k * n_rest;
+    const uint4 bq = __ldg(qv + k);
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const uint64_t av = src[r];
+      const uint32_t a0 = (uint32_t)av, a1 = (uint32_t)(av >> 32);
+      acc3_mac(acc[r][0], a0, a1, bq.x, bq.y);
+      acc3_mac(acc[r][1], a0, a1, bq.z, bq.w);
+    }
+  }
+  uint64_t *o = out + b * out_stride;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const size_t row = (size_t)row0 + r;
+    o[row * 2 * kN + c] = acc3_reduce(acc[r][0], C, mu_lo, mu_hi);
+    o[row * 2 * kN + kN + c] = acc3_reduce(acc[r][1], C, mu_lo, mu_hi);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// mod switch (server.cpp:779-801) + response packing (server.cpp:581-633)
+// ---------------------------------------------------------------------------
+
+// (uint64_t)round((long double)x * scale) with the x87 semantics: the exact
+// product x * ms_mant rounded to a 64-bit significand (nearest-even), then
+// scaled by 2^-ms_shift and rounded half away from zero.
+__device__ __forceinline__ uint64_t mod_switch_coeff(uint64_t x, const Consts &C) {
+  if (x == 0) return 0;
+  unsigned __int128 P = (unsigned __int128)x * C.ms_mant;
+  const uint64_t hi = (uint64_t)(P >> 64);
+  const int bits = hi ? 128 - __clzll((long long)hi) : 64 - __clzll((long long)(uint64_t)P);
+  if (bits > 64) {
+    const int sh = bits - 64;
+    unsigned __int128 keep = P >> sh;
+    const unsigned __int128 rem = P & ((((unsigned __int128)1) << sh) - 1);
+    const unsigned __int128 half = ((unsigned __int128)1) << (sh - 1);
+    if (rem > half || (rem == half && (keep & 1))) keep += 1;
+    P = keep << sh;
+  }
+  const int s = C.ms_shift;
+  return (uint64_t)((P + (((unsigned __int128)1) << (s - 1))) >> s);
+}
+
+__global__ void __launch_bounds__(T) modswitch_pack_kernel(const uint64_t *res, size_t res_stride,
+                                                           uint64_t *resp, uint8_t *packed,
+                                                           int packed_bytes, Consts C) {
+  extern __shared__ uint32_t words[];
+  const int tid = threadIdx.x, b = blockIdx.x;
+  const int w = C.small_q_width;
+  const int nwords = (packed_bytes + 3) / 4;
+  for (int i = tid; i < nwords; i += T) words[i] = 0;
+  __syncthreads();
+  const uint64_t *ct = res + b * res_stride;
+  const uint64_t mask = (1ULL << w) - 1;
+  for (int i = tid; i < 2 * kN; i += T) {
+    const uint64_t v = mod_switch_coeff(ct[i], C);
+    if (resp) resp[(size_t)b * 2 * kN + i] = v;
+    const uint64_t m = v & mask;
+    const uint64_t bit = (uint64_t)i * w;
+    const int wi = (int)(bit >> 5), sh = (int)(bit & 31);
+    atomicOr(&words[wi], (uint32_t)(m << sh));
+    if (sh + w > 32) atomicOr(&words[wi + 1], (uint32_t)(m >> (32 - sh)));
+    if (sh + w > 64) atomicOr(&words[wi + 2], (uint32_t)(m >> (64 - sh)));
+  }
+  __syncthreads();
+  if (packed) {
+    uint8_t *dst = packed + (size_t)b * packed_bytes;
+    for (int i = tid; i < packed_bytes; i += T) dst[i] = (uint8_t)(words[i >> 2] >> (8 * (i & 3)));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// database ingest (push_database_chunk, preprocess_ntt, realign_db:
+// server.cpp:635-748)
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+
+// byte j of synthetic entry e: 8-byte big-endian index, then seeded bytes
+__device__ __forceinline__ uint32_t gen_entry_byte(uint64_t seed, uint64_t e, uint64_t j) {
+  if (j < 8) return (uint32_t)((e >> (8 * (7 - j))) & 0xFF);
+  const uint64_t w = mix64(seed * 0x9E3779B97F4A7C15ULL + e * 0xD1B54A32D192ED03ULL + ((j - 8) >> 3));
+  return (uint32_t)((w >> (8 * ((j - 8) & 7))) & 0xFF);
+}
+
+// Coefficient c of a plaintext = bits [bpc*c, bpc*c + bpc) of the
+// concatenated bytes of its entries, LSB-first; bits past the end are 0.
+template <bool kSynthetic>
+__global__ void __launch_bounds__(T) db_pack_kernel(const uint8_t *entries, uint64_t seed,
+                                                    size_t pt0, uint64_t *coeffs, int entry_size,
+                                                    int epp, int bpc) {
+  const size_t pt = blockIdx.x;
+  const uint64_t total_bits = (uint64_t)epp * entry_size * 8;
+  const uint8_t *base = entries ? entries + pt * (size_t)epp * entry_size : nullptr;
+  for (int c = threadIdx.x; c < kN; c += T) {
+    const uint64_t bit0 = (uint64_t)c * bpc;
+    uint64_t v = 0;
+    if (bit0 < total_bits) {
+      const uint64_t byte0 = bit0 >> 3;
+      const int off = (int)(bit0 & 7);
+      const uint64_t nbytes_total = total_bits >> 3;
+      uint64_t acc = 0;
+      for (int j = 0; j < 4; ++j) {  // bpc <= 24 bits spans at most 4 bytes
+        const uint64_t by = byte0 + j;
+        if (by >= nbytes_total) break;
+        uint32_t val;
+        if (kSynthetic) {
+          const uint64_t e = (pt0 + pt) * (uint64_t)epp + by / entry_size;
+          val = gen_entry_byte(seed, e, by % entry_size);
+        } else {
+          val = base[by];
+        }
+        acc |= (uint64_t)val << (8 * j);
+      }
+      v = (acc >> off) & ((1ULL << bpc) - 1);
+    }
+    coeffs[pt * kN + c] = v;
+  }
+}
+
+// transform_to_ntt_inplace(Plaintext) (server.cpp:709): centred lift of the
+// t-residues into Z_q, forward NTT; then realign_db into the scan layout
+// dbs[c][col][row] with each value stored as lo30 | hi30 << 32.
+__global__ void __launch_bounds__(T) db_ntt_scatter_kernel(const uint64_t *coeffs, size_t pt0,
+                                                           uint64_t *dbs, int n1, int n_rest,
+                                                           ModTab M, Consts C) {
+  __shared__ uint64_t sa[kSmemPoly], sb[kSmemPoly];
+  const int tid = threadIdx.x;
+  const size_t pt = pt0 + blockIdx.x;
+  const uint64_t *src = coeffs + (size_t)blockIdx.x * kN;
+  const uint64_t thr = (C.t + 1) >> 1, inc = C.q - C.t;
+  uint64_t r[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const uint64_t v = src[strided_idx(tid, e)];
+    r[e] = v >= thr ? v + inc : v;
+  }
+  ntt_fwd(r, sa, sb, M);
+  const size_t row = pt / n1, col = pt % n1;
+  const size_t plane = (size_t)n1 * n_rest;
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const size_t c = slot_idx(tid, e);
+    dbs[c * plane + col * n_rest + row] = (r[e] & 0x3FFFFFFFULL) | ((r[e] >> 30) << 32);
+  }
+}
+
+__global__ void db_from_aligned_kernel(const uint64_t *aligned, uint64_t *dbs, int n1,
+                                       int n_rest) {
+  const size_t plane = (size_t)n1 * n_rest;
+  const size_t total = plane * kN;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const size_t c = i / plane, rem = i % plane;
+    const size_t col = rem / n_rest, row = rem % n_rest;
+    const uint64_t v = aligned[c * plane + row * n1 + col];
+    dbs[i] = (v & 0x3FFFFFFFULL) | ((v >> 30) << 32);
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+
+constexpr size_t kExpandSmem = (2 * kSmemPoly + 2 * kN) * sizeof(uint64_t);
+
+cudaError_t init_kernel_attributes() {
+  return cudaFuncSetAttribute(expand_level_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)kExpandSmem);
+}
+
+void launch_ntt(const ModTab &M, uint64_t *polys, size_t count, bool inverse, cudaStream_t s) {
+  if (!count) return;
+  ntt_kernel<<<(unsigned)count, T, 0, s>>>(M, polys, inverse ? 1 : 0);
+}
+
+void launch_expand_level(const uint64_t *cur, uint64_t *nxt, size_t in_stride, size_t out_stride,
+                         const QueryDesc *qd, int level, int live_nodes, int batch,
+                         const ModTab &Mq, const ModTab &Mp, const Consts &C, cudaStream_t s) {
+  const size_t smem = kExpandSmem;
+  expand_level_kernel<<<dim3(live_nodes, batch), T, smem, s>>>(cur, nxt, in_stride, out_stride,
+                                                              qd, level, Mq, Mp, C);
+}
+
+void launch_query_to_gsw(const uint64_t *leaves, size_t leaves_stride, uint64_t *gsw_out,
+                         size_t gsw_stride, const QueryDesc *qd, int n1, int num_cts, int batch,
+                         const ModTab &Mq, const Consts &C, cudaStream_t s) {
+  if (num_cts <= 0) return;
+  query_to_gsw_kernel<<<dim3(num_cts, batch), T, 0, s>>>(leaves, leaves_stride, gsw_out,
+                                                        gsw_stride, qd, n1, Mq, C);
+}
+
+void launch_query_prep(const uint64_t *leaves, size_t leaves_stride, uint4 *qs, size_t qs_stride,
+                       int n1, int batch, const ModTab &Mq, cudaStream_t s) {
+  query_prep_kernel<<<dim3(n1, batch), T, 0, s>>>(leaves, leaves_stride, qs, qs_stride, n1, Mq);
+}
+
+void launch_scan(const uint64_t *dbs, const uint4 *qs, size_t qs_stride, uint64_t *out,
+                 size_t out_stride, int n1, int n_rest, int batch, const Consts &C,
+                 uint64_t mu_lo, uint64_t mu_hi, cudaStream_t s) {
+  if (n_rest % 2 == 0) {
+    const size_t threads = (size_t)kN * (n_rest / 2);
+    const unsigned blocks = (unsigned)((threads + 255) / 256);
+    scan_kernel<2><<<dim3(blocks, batch), 256, 0, s>>>(dbs, qs, qs_stride, out, out_stride, n1,
+                                                      n_rest, C, mu_lo, mu_hi);
+  } else {
+    const size_t threads = (size_t)kN * n_rest;
+    const unsigned blocks = (unsigned)((threads + 255) / 256);
+    scan_kernel<1><<<dim3(blocks, batch), 256, 0, s>>>(dbs, qs, qs_stride, out, out_stride, n1,
+                                                      n_rest, C, mu_lo, mu_hi);
+  }
+}
+
+void launch_fold(uint64_t *res, size_t res_stride, const uint64_t *gsw, size_t gsw_stride,
+                 int half, int batch, const ModTab &Mq, const Consts &C, cudaStream_t s) {
+  fold_kernel<<<dim3(half, batch), T, 0, s>>>(res, res_stride, gsw, gsw_stride, half, Mq, C);
+}
+
+void launch_modswitch_pack(const uint64_t *res, size_t res_stride, uint64_t *resp,
+                           uint8_t *packed, size_t packed_bytes, int batch, const Consts &C,
+                           cudaStream_t s) {
+  const size_t smem = ((packed_bytes + 3) / 4 + 2) * sizeof(uint32_t);
+  modswitch_pack_kernel<<<batch, T, smem, s>>>(res, res_stride, resp, packed, (int)packed_bytes,
+                                               C);
+}
+
+void launch_db_pack(const uint8_t *entries, uint64_t *coeffs, size_t num_pt, int entry_size,
+                    int entries_per_pt, int bits_per_coeff, cudaStream_t s) {
+  if (!num_pt) return;
+  db_pack_kernel<false><<<(unsigned)num_pt, T, 0, s>>>(entries, 0, 0, coeffs, entry_size,
+                                                      entries_per_pt, bits_per_coeff);
+}
+
+void launch_db_gen_pack(uint64_t seed, size_t pt0, uint64_t *coeffs, size_t num_pt,
+                        int entry_size, int entries_per_pt, int bits_per_coeff, cudaStream_t s) {
+  if (!num_pt) return;
+  db_pack_kernel<true><<<(unsigned)num_pt, T, 0, s>>>(nullptr, seed, pt0, coeffs, entry_size,
+                                                     entries_per_pt, bits_per_coeff);
+}
+
+void launch_db_ntt_scatter(uint64_t *coeffs, size_t pt0, size_t count, uint64_t *dbs, int n1,
+                           int n_rest, const ModTab &Mq, const Consts &C, cudaStream_t s) {
+  if (!count) return;
+  db_ntt_scatter_kernel<<<(unsigned)count, T, 0, s>>>(coeffs, pt0, dbs, n1, n_rest, Mq, C);
+}
+
+void launch_db_from_aligned(const uint64_t *aligned, uint64_t *dbs, int n1, int n_rest,
+                            cudaStream_t s) {
+  db_from_aligned_kernel<<<152 * 8, 256, 0, s>>>(aligned, dbs, n1, n_rest);
+}
+
+}  // namespace opir

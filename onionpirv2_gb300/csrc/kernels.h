@@ -1,0 +1,89 @@
+// kernels.h -- launchers for the OnionPIRv2 query-path kernels (sm_103a).
+// Host code calls these; every launcher enqueues on the given stream and
+// returns without synchronising.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace opir {
+
+// Per-query pointers for a batch (device array, one entry per query).
+struct QueryDesc {
+  const uint64_t *galois;   // [h][2][2][N]   key k, modulus (q, p), NTT form
+  const uint64_t *gsw_key;  // [2 l_key][2][N] RGSW(sk), NTT form
+};
+
+// Scalars of the parameter set shared by all kernels.
+struct Consts {
+  uint64_t q, p, t;
+  uint64_t p_half;            // p >> 1
+  uint64_t p_half_mod_q;
+  uint64_t p_inv_q, p_inv_q_s;  // p^-1 mod q and Shoup companion
+  uint64_t two30, two30_s;    // 2^30 mod q
+  uint64_t two60, two60_s;    // 2^60 mod q
+  uint64_t ms_mant;           // (double)small_q / (double)q == ms_mant * 2^-ms_shift
+  int ms_shift;
+  int small_q_width;
+  int l, base_log2, l_key, base_log2_key;
+};
+
+// Per-device kernel attributes (dynamic shared memory opt-in); call once per
+// device before the first launch.
+cudaError_t init_kernel_attributes();
+
+// ---- batched transforms on polynomials in global memory (natural order in,
+// NTT slot order out for forward; slot order in, natural out for inverse)
+void launch_ntt(const ModTab &M, uint64_t *polys, size_t count, bool inverse, cudaStream_t s);
+
+// ---- query expansion, one tree level for every query of the batch
+// cur: [B][nodes_in][2][N], nxt: [B][2*nodes_in][2][N]
+void launch_expand_level(const uint64_t *cur, uint64_t *nxt, size_t in_stride, size_t out_stride,
+                         const QueryDesc *qd, int level, int live_nodes, int batch,
+                         const ModTab &Mq, const ModTab &Mp, const Consts &C, cudaStream_t s);
+
+// ---- RGSW reconstruction (query_to_gsw) for all further dimensions
+// leaves: [B][u][2][N] (coefficient form), gsw_out: [B][ndim-1][2l][2][N]
+void launch_query_to_gsw(const uint64_t *leaves, size_t leaves_stride, uint64_t *gsw_out,
+                         size_t gsw_stride, const QueryDesc *qd, int n1, int num_cts, int batch,
+                         const ModTab &Mq, const Consts &C, cudaStream_t s);
+
+// ---- first dimension
+// NTT the first n1 leaves and transpose to the scan operand Qs[b][c][k]
+void launch_query_prep(const uint64_t *leaves, size_t leaves_stride, uint4 *qs, size_t qs_stride,
+                       int n1, int batch, const ModTab &Mq, cudaStream_t s);
+// out[b][row][poly][c] = sum_k DB[c][k][row] * Q[b][c][k][poly] mod q  (NTT form)
+void launch_scan(const uint64_t *dbs, const uint4 *qs, size_t qs_stride, uint64_t *out,
+                 size_t out_stride, int n1, int n_rest, int batch, const Consts &C,
+                 uint64_t mu_lo, uint64_t mu_hi, cudaStream_t s);
+
+// ---- one folding level (other_dim_mux): res[b][j] += INTT(RGSW x (res[j+half]-res[j]))
+void launch_fold(uint64_t *res, size_t res_stride, const uint64_t *gsw, size_t gsw_stride,
+                 int half, int batch, const ModTab &Mq, const Consts &C, cudaStream_t s);
+
+// ---- mod switch to small_q + response bit packing
+void launch_modswitch_pack(const uint64_t *res, size_t res_stride, uint64_t *resp,
+                           uint8_t *packed, size_t packed_bytes, int batch, const Consts &C,
+                           cudaStream_t s);
+
+// ---- database ingest
+// entry bytes (device) -> plaintext coefficients (bits_per_coeff LSB-first)
+void launch_db_pack(const uint8_t *entries, uint64_t *coeffs, size_t num_pt, int entry_size,
+                    int entries_per_pt, int bits_per_coeff, cudaStream_t s);
+// seeded synthetic entries straight to plaintext coefficients
+void launch_db_gen_pack(uint64_t seed, size_t pt0, uint64_t *coeffs, size_t num_pt,
+                        int entry_size, int entries_per_pt, int bits_per_coeff, cudaStream_t s);
+// centred lift + NTT + scatter into the scan layout dbs[c][col][row] (30-bit split words)
+void launch_db_ntt_scatter(uint64_t *coeffs, size_t pt0, size_t count, uint64_t *dbs, int n1,
+                           int n_rest, const ModTab &Mq, const Consts &C, cudaStream_t s);
+// reference layout db_aligned[c][row*n1+col] (NTT form) -> scan layout
+void launch_db_from_aligned(const uint64_t *aligned, uint64_t *dbs, int n1, int n_rest,
+                            cudaStream_t s);
+
+// ---- keys: coefficient-form RGSW rows -> NTT form (in place, slot order)
+// (same as launch_ntt forward; kept for readability at the call site)
+
+}  // namespace opir

@@ -1,0 +1,267 @@
+"""PirServer: the reference server interface (src/includes/server.h:13-51)
+on the GB300 query path.
+
+Method names, argument meaning and error behaviour follow the reference:
+  gen_data()                        server.cpp:47-78   (seeded entries, ingested on the GPU)
+  push_database_chunk(chunk, idx)   server.cpp:635-701 (+ preprocess_ntt, realign_db)
+  set_client_galois_key(id, keys)   server.cpp:480-484
+  set_client_gsw_key(id, rows)      server.cpp:486-500
+  make_query(id, query)             server.cpp:520-579
+  save_resp_to_stream(resp, stream) server.cpp:581-633
+  direct_get_entry(idx)             server.cpp:503-517
+Unknown client ids raise UnknownClientError (a KeyError, like the
+reference's std::map::at); malformed arguments raise ValueError.
+
+Ciphertexts are numpy uint64 arrays of shape (2, N) in SEAL's rns = 1
+layout (c0 then c1, coefficient form).  Every computation runs in the CUDA
+library through the C ABI; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import io
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _capi
+from .params import POLY_DEGREE, PirParams
+
+N = POLY_DEGREE
+
+
+def _mix64(z: np.ndarray) -> np.ndarray:
+    z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+    z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return z ^ (z >> np.uint64(31))
+
+
+def synthetic_entries(seed: int, first: int, count: int, entry_size: int) -> np.ndarray:
+    """Entries of the seeded database (utils.cpp:160-172 with a seeded
+    generator in place of /dev/urandom): 8-byte big-endian index, then bytes
+    of mix64(seed * phi + entry * c + word)."""
+    out = np.zeros((count, entry_size), np.uint8)
+    idx = np.arange(first, first + count, dtype=np.uint64)
+    for i in range(8):
+        out[:, 7 - i] = ((idx >> np.uint64(8 * i)) & np.uint64(0xFF)).astype(np.uint8)
+    nwords = (entry_size - 8 + 7) // 8
+    with np.errstate(over="ignore"):
+        base = np.uint64(seed) * np.uint64(0x9E3779B97F4A7C15) + idx * np.uint64(0xD1B54A32D192ED03)
+        words = _mix64(base[:, None] + np.arange(nwords, dtype=np.uint64)[None, :])
+    raw = words.astype("<u8").view(np.uint8).reshape(count, nwords * 8)
+    out[:, 8:] = raw[:, : entry_size - 8]
+    return out
+
+
+class ResponseCiphertext(np.ndarray):
+    """Response ciphertext mod small_q (2, N) carrying its packed wire bytes."""
+
+    packed: Optional[bytes] = None
+
+
+class PirServer:
+    """GPU-backed PirServer (one CUDA context, one database)."""
+
+    def __init__(self, pir_params: PirParams, device: int = 0):
+        self.pir_params = pir_params
+        self._L = _capi.load()
+        P = pir_params
+        prm = _capi.OpirParams(
+            poly_degree=P.poly_degree, coeff_modulus=P.coeff_modulus[0],
+            special_modulus=P.coeff_modulus[-1], plain_modulus=P.plain_mod,
+            small_modulus=P.small_q, gsw_l=P.gsw_l, gsw_base_log2=P.base_log2,
+            gsw_l_key=P.gsw_l_key, gsw_base_log2_key=P.base_log2_key)
+        ctx = ctypes.c_void_p()
+        rc = self._L.opir_ctx_create(ctypes.byref(prm), device, ctypes.byref(ctx))
+        if rc != 0:
+            raise _capi.OpirError(rc, "opir_ctx_create failed")
+        self._ctx = ctx
+        shape = _capi.OpirDbShape(
+            fst_dim_sz=P.get_fst_dim_sz(), other_dim_sz=P.get_other_dim_sz(),
+            entry_size=P.get_entry_size(), entries_per_pt=P.get_num_entries_per_plaintext(),
+            bits_per_coeff=P.get_num_bits_per_coeff())
+        db = ctypes.c_uint32()
+        self._check(self._L.opir_db_create(self._ctx, ctypes.byref(shape), ctypes.byref(db)))
+        self.db_id = db.value
+        self._seed: Optional[int] = None
+        self._raw_chunks = {}
+        self.resp_bytes = int(self._L.opir_response_bytes(self._ctx))
+
+    # ---- plumbing
+    def _check(self, rc: int):
+        _capi.check(self._ctx, rc)
+
+    def close(self):
+        if getattr(self, "_ctx", None):
+            self._L.opir_ctx_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def ctx(self):
+        return self._ctx
+
+    def set_stream(self, stream_handle: int):
+        """Run on a caller's cudaStream_t (e.g. torch.cuda.Stream().cuda_stream)."""
+        self._check(self._L.opir_ctx_set_stream(self._ctx, ctypes.c_void_p(stream_handle)))
+
+    # ---- database
+    def gen_data(self, seed: int = 0x0B1A7):
+        """Fill the whole database with seeded entries (server.cpp:47-78)."""
+        self._check(self._L.opir_db_fill_synthetic(self._ctx, self.db_id, seed))
+        self._seed = seed
+        self._raw_chunks.clear()
+
+    def push_database_chunk(self, chunk_entry, chunk_idx: int):
+        """Pack, NTT and realign one chunk of fst_dim_sz plaintexts
+        (server.cpp:635-748).  Entries shorter than entry_size are zero-padded;
+        longer ones raise ValueError."""
+        P = self.pir_params
+        es = P.get_entry_size()
+        n = P.get_fst_dim_sz() * P.get_num_entries_per_plaintext()
+        if isinstance(chunk_entry, np.ndarray) and chunk_entry.dtype == np.uint8 and chunk_entry.ndim == 2:
+            if chunk_entry.shape[1] > es:
+                raise ValueError("Entry size is too large")
+            arr = np.zeros((chunk_entry.shape[0], es), np.uint8)
+            arr[:, : chunk_entry.shape[1]] = chunk_entry
+        else:
+            rows = list(chunk_entry)
+            arr = np.zeros((len(rows), es), np.uint8)
+            for i, e in enumerate(rows):
+                b = np.frombuffer(bytes(e), np.uint8)
+                if b.size > es:
+                    raise ValueError("Entry size is too large")
+                arr[i, : b.size] = b
+        if arr.shape[0] != n:
+            raise ValueError(f"a chunk holds {n} entries, got {arr.shape[0]}")
+        arr = np.ascontiguousarray(arr)
+        self._check(self._L.opir_db_push_chunk(self._ctx, self.db_id, _capi.p8(arr.reshape(-1)),
+                                               n, chunk_idx))
+        self._raw_chunks[chunk_idx] = arr
+        self._seed = None
+
+    def upload_ntt_db(self, db_aligned: np.ndarray):
+        """Install an NTT-form database given in the reference layout
+        db_aligned_[c * num_pt + row * n1 + col] (server.cpp:740)."""
+        a = np.ascontiguousarray(db_aligned, np.uint64)
+        if a.size != self.pir_params.get_num_pt() * N:
+            raise ValueError("database has the wrong size")
+        self._check(self._L.opir_db_upload_aligned(self._ctx, self.db_id, _capi.p64(a.reshape(-1))))
+        self._seed = None
+
+    def direct_get_entry(self, entry_idx: int) -> np.ndarray:
+        """Non-private lookup of an entry, for testing (server.cpp:503-517)."""
+        P = self.pir_params
+        if self._seed is not None:
+            return synthetic_entries(self._seed, entry_idx, 1, P.get_entry_size())[0]
+        per_chunk = P.get_fst_dim_sz() * P.get_num_entries_per_plaintext()
+        chunk, off = divmod(entry_idx, per_chunk)
+        if chunk not in self._raw_chunks:
+            raise ValueError("Unable to open file for reading")
+        return self._raw_chunks[chunk][off].copy()
+
+    # ---- keys
+    def set_client_galois_key(self, client_id: int, galois_keys):
+        keys = _read_u64(galois_keys)
+        levels = keys.size // (4 * N)
+        if levels * 4 * N != keys.size or levels == 0:
+            raise ValueError("Galois keys must be [levels][2][2][N] uint64")
+        self._check(self._L.opir_set_galois_key(self._ctx, client_id, _capi.p64(keys), levels))
+
+    def set_client_gsw_key(self, client_id: int, gsw_rows):
+        rows = _read_u64(gsw_rows)
+        if rows.size != 2 * self.pir_params.get_l_key() * 2 * N:
+            raise ValueError("RGSW key must be [2*l_key][2][N] uint64")
+        self._check(self._L.opir_set_gsw_key(self._ctx, client_id, _capi.p64(rows)))
+
+    def erase_client(self, client_id: int):
+        self._check(self._L.opir_erase_client(self._ctx, client_id))
+
+    # ---- queries
+    def make_query(self, client_id: int, query) -> ResponseCiphertext:
+        """Answer one query (server.cpp:520-579); returns the response
+        ciphertext mod small_q with its packed bytes attached."""
+        q = _read_u64(query)
+        if q.size != 2 * N:
+            raise ValueError("query must be one ciphertext [2][N]")
+        resp = np.zeros(2 * N, np.uint64)
+        packed = np.zeros(self.resp_bytes, np.uint8)
+        self._check(self._L.opir_make_query(self._ctx, self.db_id, client_id, _capi.p64(q),
+                                            _capi.p64(resp), _capi.p8(packed)))
+        out = resp.reshape(2, N).view(ResponseCiphertext)
+        out.packed = packed.tobytes()
+        return out
+
+    def make_query_batch(self, client_ids: Sequence[int], queries: np.ndarray):
+        """Answer len(client_ids) queries in one batched pass."""
+        ids = np.ascontiguousarray(np.asarray(client_ids, dtype=np.uint64))
+        q = np.ascontiguousarray(queries, np.uint64).reshape(-1)
+        B = ids.size
+        if q.size != B * 2 * N:
+            raise ValueError("queries must be [batch][2][N]")
+        resp = np.zeros(B * 2 * N, np.uint64)
+        packed = np.zeros(B * self.resp_bytes, np.uint8)
+        self._check(self._L.opir_make_query_batch(self._ctx, self.db_id, B, _capi.p64(ids),
+                                                  _capi.p64(q), _capi.p64(resp), _capi.p8(packed)))
+        return resp.reshape(B, 2, N), packed.reshape(B, self.resp_bytes)
+
+    def make_query_trace(self, client_id: int, query):
+        """make_query returning every intermediate (parity tests)."""
+        P = self.pir_params
+        q = _read_u64(query)
+        ndim = len(P.get_dims())
+        u = P.get_fst_dim_sz() + P.get_l() * (ndim - 1)
+        leaves = np.zeros(u * 2 * N, np.uint64)
+        gsw = np.zeros(max(ndim - 1, 1) * 2 * P.get_l() * 2 * N, np.uint64)
+        fd = np.zeros(P.get_other_dim_sz() * 2 * N, np.uint64)
+        resp = np.zeros(2 * N, np.uint64)
+        packed = np.zeros(self.resp_bytes, np.uint8)
+        self._check(self._L.opir_make_query_trace(
+            self._ctx, self.db_id, client_id, _capi.p64(q), _capi.p64(leaves), _capi.p64(gsw),
+            _capi.p64(fd), _capi.p64(resp), _capi.p8(packed)))
+        return dict(leaves=leaves.reshape(u, 2, N),
+                    gsw=gsw.reshape(max(ndim - 1, 1), 2 * P.get_l(), 2, N),
+                    first_dim=fd.reshape(-1, 2, N), resp=resp.reshape(2, N), packed=packed)
+
+    def save_resp_to_stream(self, response: ResponseCiphertext, stream: io.IOBase) -> int:
+        """Write the response's packed bytes (server.cpp:581-633); returns the
+        number of bytes written."""
+        packed = getattr(response, "packed", None)
+        if packed is None:
+            raise ValueError("response was not produced by make_query")
+        stream.write(packed)
+        return len(packed)
+
+    # ---- timing / accounting
+    def set_timing(self, enable: bool = True):
+        self._check(self._L.opir_set_timing(self._ctx, 1 if enable else 0))
+
+    def stage_times(self):
+        """Device ms of the last timed query: Expand, Convert, First dim,
+        Other dim, Mod switch, and the scan kernel alone."""
+        ms = (ctypes.c_float * 6)()
+        self._check(self._L.opir_stage_times(self._ctx, ms))
+        keys = ("expand", "convert", "first_dim", "other_dim", "mod_switch", "scan_kernel")
+        return dict(zip(keys, [float(x) for x in ms]))
+
+    def launch_count(self) -> int:
+        return int(self._L.opir_launch_count(self._ctx))
+
+    def ntt(self, polys: np.ndarray, mod: int = 0, inverse: bool = False) -> np.ndarray:
+        a = np.ascontiguousarray(polys, np.uint64).copy()
+        self._check(self._L.opir_ntt(self._ctx, mod, 1 if inverse else 0, _capi.p64(a.reshape(-1)),
+                                     a.size // N))
+        return a
+
+
+def _read_u64(x) -> np.ndarray:
+    if isinstance(x, (io.IOBase, io.BytesIO)):
+        return np.frombuffer(x.read(), dtype="<u8").astype(np.uint64)
+    if isinstance(x, (bytes, bytearray, memoryview)):
+        return np.frombuffer(bytes(x), dtype="<u8").astype(np.uint64)
+    return np.ascontiguousarray(x, np.uint64).reshape(-1)

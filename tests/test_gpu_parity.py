@@ -1,0 +1,153 @@
+"""GPU path vs the CPU oracle: every stage of make_query, bit for bit.
+
+The oracle restates the reference server (src/server.cpp) and client
+(src/client.cpp); all comparisons are exact (integer arithmetic, tolerance 0).
+"""
+import io
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+N = 2048
+
+
+@pytest.fixture(scope="module")
+def setup_db4096(oracle_lib, gpu_lib):
+    from onionpirv2_gb300 import PirParams, PirServer
+    o = oracle_lib.Oracle(4096, 256)
+    params = PirParams(num_entries=4096, max_fst_dim=256)
+    server = PirServer(params)
+    seed = 12345
+    server.gen_data(seed)
+    db = o.build_db(seed)
+    return o, params, server, db, seed
+
+
+def make_client(o, seed):
+    sk = o.keygen(seed)
+    gk = o.galois_keys(sk, seed + 1)
+    gswk = o.gsw_key(sk, seed + 2)
+    return sk, gk, gswk
+
+
+def test_ntt_matches_oracle(setup_db4096):
+    o, params, server, _, _ = setup_db4096
+    rng = np.random.default_rng(1)
+    for mod, q in ((0, o.P.q), (1, o.P.p)):
+        a = (rng.integers(0, 2**63, size=(7, N), dtype=np.uint64) % np.uint64(q))
+        fwd = server.ntt(a, mod=mod)
+        assert np.array_equal(fwd, o.ntt_fwd(a, mod))
+        back = server.ntt(fwd, mod=mod, inverse=True)
+        assert np.array_equal(back, a)
+
+
+def test_query_stages_match_oracle(setup_db4096):
+    o, params, server, db, seed = setup_db4096
+    P = o.P
+    sk, gk, gswk = make_client(o, 77)
+    cid = 9001
+    server.set_client_galois_key(cid, gk)
+    server.set_client_gsw_key(cid, gswk)
+    idx = 2741
+    query = o.make_query(sk, 4242, idx)
+    tr = server.make_query_trace(cid, query)
+    # expansion (fast_expand_qry)
+    leaves = o.expand(query, gk)
+    assert np.array_equal(tr["leaves"], leaves)
+    # RGSW reconstruction (query_to_gsw)
+    gsw_ntt = o.gsw_key_to_ntt(gswk)
+    for i in range(1, P.ndim):
+        s = P.n1 + (i - 1) * P.l
+        rg = o.query_to_gsw(leaves[s:s + P.l], gsw_ntt)
+        assert np.array_equal(tr["gsw"][i - 1], rg), f"dim {i}"
+    # first dimension
+    fd, wraps = o.first_dim(db, leaves[:P.n1])
+    assert wraps == 0
+    assert np.array_equal(tr["first_dim"], fd)
+    # whole response, packed bytes
+    resp, packed, _, _ = o.make_query_server(db, gk, gsw_ntt, query)
+    assert np.array_equal(tr["resp"], resp)
+    assert np.array_equal(tr["packed"], packed)
+
+
+@pytest.mark.parametrize("idx", [0, 1, 255, 256, 4095, 1777])
+def test_end_to_end_decrypts_entry(setup_db4096, idx):
+    """tests.cpp:110-134: the decrypted entry equals the database entry."""
+    o, params, server, db, seed = setup_db4096
+    sk, gk, gswk = make_client(o, 1000 + idx)
+    cid = 50 + idx
+    server.set_client_galois_key(cid, gk)
+    server.set_client_gsw_key(cid, gswk)
+    query = o.make_query(sk, 99 + idx, idx)
+    resp = server.make_query(cid, query)
+    buf = io.BytesIO()
+    n = server.save_resp_to_stream(resp, buf)
+    assert n == o.response_bytes() == 13824
+    ct = o.unpack_response(np.frombuffer(buf.getvalue(), np.uint8))
+    plain, budget = o.decrypt(sk, ct, 2)
+    entry = o.entry_from_plain(idx, plain)
+    assert np.array_equal(entry, server.direct_get_entry(idx))
+    assert budget > 0
+    gsw_ntt = o.gsw_key_to_ntt(gswk)
+    ref, ref_packed, _, _ = o.make_query_server(db, gk, gsw_ntt, query)
+    assert np.array_equal(resp, ref)
+    assert resp.packed == ref_packed.tobytes()
+
+
+def test_batch_equals_single(setup_db4096):
+    o, params, server, db, seed = setup_db4096
+    ids, queries, singles = [], [], []
+    for j in range(5):
+        sk, gk, gswk = make_client(o, 3000 + j)
+        cid = 7000 + j
+        server.set_client_galois_key(cid, gk)
+        server.set_client_gsw_key(cid, gswk)
+        q = o.make_query(sk, 555 + j, (j * 977) % 4096)
+        ids.append(cid)
+        queries.append(q)
+        singles.append(server.make_query(cid, q))
+    resp, packed = server.make_query_batch(ids, np.stack(queries))
+    for j in range(5):
+        assert np.array_equal(resp[j], singles[j])
+        assert packed[j].tobytes() == singles[j].packed
+
+
+def test_unknown_client_raises(setup_db4096):
+    from onionpirv2_gb300 import UnknownClientError
+    o, params, server, db, seed = setup_db4096
+    with pytest.raises(UnknownClientError):
+        server.make_query(123456789, np.zeros((2, N), np.uint64))
+
+
+def test_push_chunk_matches_reference_layout(oracle_lib, gpu_lib):
+    """push_database_chunk path (host entries) == oracle packing + NTT."""
+    from onionpirv2_gb300 import PirParams, PirServer
+    o = oracle_lib.Oracle(4096, 256)
+    params = PirParams(num_entries=4096, max_fst_dim=256)
+    server = PirServer(params)
+    P = o.P
+    rng = np.random.default_rng(5)
+    entries = rng.integers(0, 256, size=(P.num_pt, P.entry_size), dtype=np.uint8)
+    for row in range(P.n_rest):
+        server.push_database_chunk(entries[row * P.n1:(row + 1) * P.n1], row)
+    coeffs = o.pack_plaintexts(entries, P.num_pt)
+    ntt = o.plain_to_ntt(coeffs)
+    db = np.ascontiguousarray(ntt.T)  # db_aligned[c][pt]
+    sk, gk, gswk = make_client(o, 31)
+    server.set_client_galois_key(1, gk)
+    server.set_client_gsw_key(1, gswk)
+    for idx in (3, 2222):
+        query = o.make_query(sk, idx, idx)
+        resp = server.make_query(1, query)
+        ref, _, _, _ = o.make_query_server(db, gk, o.gsw_key_to_ntt(gswk), query)
+        assert np.array_equal(resp, ref)
+        plain, _ = o.decrypt(sk, resp, 2)
+        assert np.array_equal(o.entry_from_plain(idx, plain), entries[idx])
+    # the aligned-upload path gives the same database
+    server.upload_ntt_db(db)
+    query = o.make_query(sk, 8, 1234)
+    resp = server.make_query(1, query)
+    ref, _, _, _ = o.make_query_server(db, gk, o.gsw_key_to_ntt(gswk), query)
+    assert np.array_equal(resp, ref)
