@@ -1,0 +1,380 @@
+#!/usr/bin/env python3
+"""Benchmark of the OnionPIRv2 server query path on GB300.
+
+Workload (default): the 262,144-plaintext database (n1 x n_rest = 512 x 512,
+N = 2048, one 60-bit q, ~1 GB of raw entries, 4.29 GB in NTT form), one
+query per step through the whole pipeline of PirServer::make_query
+(expansion, RGSW reconstruction, first-dimension scan, 9 folds, modulus
+switch, packing).
+
+  value  queries/s with queries resident in HBM, CUDA events on the
+         library's stream around K steps (each step one query).
+  e2e    the same through the public host API (opir_make_query): host query
+         -> pinned staging -> device -> response and packed bytes -> host.
+  roofline  the dominant kernel (first-dimension scan): NTT-form DB bytes per
+         launch / mean launch time (CUDA events around the launch), against
+         the measured HBM copy bandwidth.
+  cpu_baseline  the CPU restatement of the reference server (oracle/), all
+         host threads, full queries on the same database and inputs; its
+         responses are also compared bit for bit with the GPU's.
+
+Inputs: the database is seeded entries ingested on the GPU; Galois keys, the
+RGSW key and the query ciphertexts are seeded uniform residues (an RLWE
+ciphertext or key is uniform mod q, so they have the distribution of real
+ones).  The NTT-form database (4.29 GB) is larger than L2 (129 MB), so no
+L2 flush is needed between steps.
+
+--impl reference times the reference algorithm on the host cores (the
+oracle port: the reference itself needs the absent SEAL fork) on the same
+workload and prints its own JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "server queries/s and DB GB/s scanned, batched limb-TC vs plain GPU, bit-exact"
+N = 2048
+DB_SEED = 0xDB5EED
+NUM_CLIENTS = 4
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="db262144")
+    ap.add_argument("--cpu-queries", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_inputs(params, count, seed=1):
+    """Seeded uniform Galois keys, RGSW keys and query ciphertexts."""
+    rng = np.random.default_rng(seed)
+    q, p = params.coeff_modulus[0], params.coeff_modulus[-1]
+    h = params.get_expan_height()
+    clients = []
+    for _ in range(NUM_CLIENTS):
+        gk = np.empty((h, 2, 2, N), np.uint64)
+        gk[:, :, 0, :] = rng.integers(0, q, size=(h, 2, N), dtype=np.uint64)
+        gk[:, :, 1, :] = rng.integers(0, p, size=(h, 2, N), dtype=np.uint64)
+        gsw = rng.integers(0, q, size=(2 * params.get_l_key(), 2, N), dtype=np.uint64)
+        clients.append((gk, gsw))
+    queries = rng.integers(0, q, size=(count, 2, N), dtype=np.uint64)
+    return clients, queries
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 8:
+                self.samples.append((time.time(), parts))
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self, t0, t1):
+        sel = [s for t, s in self.samples if t0 - 0.25 <= t <= t1 + 0.25] or \
+              [s for _, s in self.samples]
+        if not sel:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(s[0]) for s in sel if num(s[0]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in sel for i in range(4) if s[4 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": num(sel[0][1]), "reasons": reasons, "samples": len(sel)}
+
+
+def read_traffic(workload):
+    """DRAM bytes per scan launch from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", f"scan_kernel_{workload}.md")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.strip().startswith("traffic_bytes_per_launch:"):
+                    return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def cpu_baseline(params, workload, clients, queries, gpu_resps, nq):
+    """Time the oracle (CPU restatement of the reference server) on full
+    queries with all host threads; check its responses against the GPU's."""
+    from oracle import oracle as orc
+    orc.build()
+    threads = os.cpu_count() or 1
+    orc.set_threads(threads)
+    o = orc.Oracle(params.num_entries, params.max_fst_dim)
+    t = time.perf_counter()
+    db = o.build_db(DB_SEED)
+    build_s = time.perf_counter() - t
+    times, match = [], True
+    gsw_ntt = [o.gsw_key_to_ntt(c[1]) for c in clients]
+    for i in range(nq):
+        gk = clients[i % NUM_CLIENTS][0]
+        t = time.perf_counter()
+        resp, packed, stages, wraps = o.make_query_server(db, gk, gsw_ntt[i % NUM_CLIENTS], queries[i])
+        times.append(time.perf_counter() - t)
+        if gpu_resps is not None and i < len(gpu_resps):
+            match &= bool(np.array_equal(resp, gpu_resps[i]))
+    del db
+    qps = nq / sum(times)
+    return {
+        "value": qps, "unit": "queries/s", "cores": threads, "kind": "port",
+        "sample": (f"{nq} full queries (all stages) on the {workload} database "
+                   f"({params.get_num_pt()} plaintexts), {threads} threads; "
+                   f"database build {build_s:.1f} s untimed"),
+    }, match
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from onionpirv2_gb300.params import PirParams
+    from oracle import oracle as orc
+    orc.build()
+    threads = os.cpu_count() or 1
+    orc.set_threads(threads)
+    params = PirParams.preset(args.workload)
+    o = orc.Oracle(params.num_entries, params.max_fst_dim)
+    db = o.build_db(DB_SEED)
+    clients, queries = make_inputs(params, args.warmup + args.steps)
+    gsw_ntt = [o.gsw_key_to_ntt(c[1]) for c in clients]
+    for i in range(args.warmup):
+        o.make_query_server(db, clients[i % NUM_CLIENTS][0], gsw_ntt[i % NUM_CLIENTS], queries[i])
+    t = time.perf_counter()
+    for i in range(args.warmup, args.warmup + args.steps):
+        o.make_query_server(db, clients[i % NUM_CLIENTS][0], gsw_ntt[i % NUM_CLIENTS], queries[i])
+    el = time.perf_counter() - t
+    qps = args.steps / el
+    db_bytes = params.get_num_pt() * N * 8
+    line = {
+        "impl": "reference", "metric": METRIC, "value": qps, "unit": "queries/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+        "config": {"workload": args.workload, "db_plaintexts": params.get_num_pt(),
+                   "n1": params.get_fst_dim_sz(), "n_rest": params.get_other_dim_sz(),
+                   "batch": 1, "ntt_db_bytes": db_bytes},
+        "db_gbs_scanned": db_bytes * qps / 1e9,
+        "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} full queries after {args.warmup} warm-up, "
+                                   f"{threads} threads (CPU restatement of the reference "
+                                   "server; the reference needs the absent SEAL fork)"},
+        "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    rank, world, local = dist_env()
+    import torch
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU")
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        pg = dist
+    from onionpirv2_gb300 import PirParams, PirServer
+
+    params = PirParams.preset(args.workload)
+    server = PirServer(params, device=local)
+    stream = torch.cuda.Stream(device=local)
+    server.set_stream(stream.cuda_stream)
+    t_ingest = time.perf_counter()
+    server.gen_data(DB_SEED)
+    ingest_s = time.perf_counter() - t_ingest
+    total = args.warmup + args.steps
+    clients, queries = make_inputs(params, total)
+    for cid, (gk, gsw) in enumerate(clients):
+        server.set_client_galois_key(cid, gk)
+        server.set_client_gsw_key(cid, gsw)
+    rb = server.resp_bytes
+    dq = torch.from_numpy(queries.view(np.int64)).to(f"cuda:{local}")
+    dresp = torch.empty((total, 2, N), dtype=torch.int64, device=f"cuda:{local}")
+    dpack = torch.empty((total, rb), dtype=torch.uint8, device=f"cuda:{local}")
+    torch.cuda.synchronize()
+    qbytes = 2 * N * 8
+
+    def step(i):
+        server.make_query_device([i % NUM_CLIENTS], dq.data_ptr() + i * qbytes,
+                                 dresp.data_ptr() + i * qbytes, dpack.data_ptr() + i * rb)
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.5)
+    # ---- value: device-resident inputs, CUDA events on the library stream
+    with torch.cuda.stream(stream):
+        for i in range(args.warmup):
+            step(i)
+        stream.synchronize()
+        if pg:
+            pg.barrier()
+        torch.cuda.synchronize()
+        l0 = server.launch_count()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.time()
+        ev0.record(stream)
+        for i in range(args.warmup, total):
+            step(i)
+        ev1.record(stream)
+        ev1.synchronize()
+        t1 = time.time()
+        torch.cuda.synchronize()
+    launches = server.launch_count() - l0
+    ms = ev0.elapsed_time(ev1)
+    if pg:
+        import torch.distributed as dist
+        tt = torch.tensor([ms], device=f"cuda:{local}")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    qps = args.steps * world / (ms / 1e3)
+    gpu_resps = dresp[: args.cpu_queries].cpu().numpy().view(np.uint64)
+
+    # ---- roofline pass: per-stage CUDA events inside the library
+    server.set_timing(True)
+    kt = min(args.steps, 50)
+    stages = []
+    with torch.cuda.stream(stream):
+        for i in range(kt):
+            step(args.warmup + i)
+            stream.synchronize()
+            stages.append(server.stage_times())
+    server.set_timing(False)
+    mean = {k: statistics.mean(s[k] for s in stages) for k in stages[0]}
+
+    # ---- e2e: public host API, host buffers, copies inside the region
+    e2e_steps = min(args.steps, 100)
+    with torch.cuda.stream(stream):
+        for i in range(min(args.warmup, 5)):
+            server.make_query(i % NUM_CLIENTS, queries[i])
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for i in range(e2e_steps):
+            r = server.make_query(i % NUM_CLIENTS, queries[i % total])
+        e1.record(stream)
+        e1.synchronize()
+    e2e_ms = e0.elapsed_time(e1)
+    clocks.stop()
+    e2e_qps = e2e_steps * world / (e2e_ms / 1e3)
+
+    db_bytes = params.get_num_pt() * N * 8
+    peak, peak_kind = measured_peak()
+    achieved = db_bytes / (mean["scan_kernel"] / 1e3) / 1e9
+    traffic = read_traffic(args.workload)
+    line = {
+        "metric": METRIC, "value": qps, "unit": "queries/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+        "data": "synthetic",
+        "config": {"workload": args.workload, "db_plaintexts": params.get_num_pt(),
+                   "n1": params.get_fst_dim_sz(), "n_rest": params.get_other_dim_sz(),
+                   "ndim": len(params.get_dims()), "batch": 1, "ntt_db_bytes": db_bytes,
+                   "raw_db_mb": params.get_DBSize_MB(), "parallelism": f"replicas{world}",
+                   "l2": "inputs larger than L2 (NTT-form database 4.29 GB > 129 MB)"},
+        "db_gbs_scanned": db_bytes * qps / 1e9,
+        "raw_db_mbs": params.get_DBSize_MB() * qps,
+        "stages_ms": mean,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "kernel": "scan_kernel (first-dimension DB x query product)",
+                     "peak_source": f"{peak_kind} hbm_gbs"},
+        "e2e": {"value": e2e_qps, "unit": "queries/s", "h2d_bytes_per_step": qbytes,
+                "d2h_bytes_per_step": qbytes + rb},
+        "gpu_launches": launches,
+        "clocks": clocks.summary(t0, t1),
+        "ingest_s": ingest_s,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cb, match = cpu_baseline(params, args.workload, clients, queries, gpu_resps,
+                                 args.cpu_queries)
+        line["cpu_baseline"] = cb
+        line["full_size_parity"] = "bit-exact vs oracle" if match else "MISMATCH vs oracle"
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    server.close()
+    if pg:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -151,7 +151,7 @@ struct Client {
 
 struct Workspace {
   // sized for (batch, shape); grown on demand
-  DevBuf exp0, exp1, gsw, qs, res, resp, packed, queries, qdesc, ingest, coeffs;
+  DevBuf exp0, exp1, gsw, qs, res, resp, packed, queries, ingest, coeffs;
   PinnedBuf h_in, h_out;
 };
 
@@ -255,7 +255,6 @@ int ensure_workspace(opir_ctx *ctx, const Db &db, int batch) {
   CK(W.resp.alloc(batch * CT), "alloc response");
   CK(W.packed.alloc(batch * ctx->resp_bytes + 16), "alloc packed");
   CK(W.queries.alloc(batch * CT), "alloc queries");
-  CK(W.qdesc.alloc(batch * sizeof(QueryDesc)), "alloc descriptors");
   return OPIR_OK;
 }
 
@@ -292,9 +291,7 @@ int run_pipeline(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
   if (rc) return rc;
   Workspace &W = ctx->ws;
   cudaStream_t s = ctx->stream;
-  CK(cudaMemcpyAsync(W.qdesc.p, desc.data(), batch * sizeof(QueryDesc), cudaMemcpyHostToDevice, s),
-     "upload descriptors");
-  const QueryDesc *qd = W.qdesc.as<QueryDesc>();
+  const QueryDesc *qd = desc.data();  // host array: launchers pass it by value
   const size_t CTW = 2 * (size_t)kN;  // words per ciphertext
   const int h = db.h, u = db.u;
   const size_t w = (size_t)1 << h;

@@ -47,8 +47,9 @@ __global__ void __launch_bounds__(T) ntt_kernel(ModTab M, uint64_t *polys, int i
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(T) expand_level_kernel(const uint64_t *cur, uint64_t *nxt,
                                                          size_t in_stride, size_t out_stride,
-                                                         const QueryDesc *qd, int level,
-                                                         ModTab Mq, ModTab Mp, Consts C) {
+                                                         const __grid_constant__ KeyBatch kb,
+                                                         int level, ModTab Mq, ModTab Mp,
+                                                         Consts C) {
   extern __shared__ uint64_t smem[];
   uint64_t *sa = smem, *sb = smem + kSmemPoly;
   uint64_t *s_sig0 = smem + 2 * kSmemPoly;  // sigma(c0), natural index
@@ -87,7 +88,7 @@ __global__ void __launch_bounds__(T) expand_level_kernel(const uint64_t *cur, ui
   ntt_fwd(tq, sa, sb, Mq);
   ntt_fwd(tp, sa, sb, Mp);
 
-  const uint64_t *key = qd[b].galois + (size_t)level * 4 * kN;
+  const uint64_t *key = kb.q[b].galois + (size_t)level * 4 * kN;
   uint64_t out[2][8];
 #pragma unroll
   for (int kk = 0; kk < 2; ++kk) {
@@ -178,7 +179,8 @@ __device__ __forceinline__ void ext_product_core(const uint64_t x[2][8], const u
 // row (j % l) of RGSW (j / l) = NTT(ct); row l + (j % l) = RGSW(sk) x ct.
 __global__ void __launch_bounds__(T) query_to_gsw_kernel(const uint64_t *leaves,
                                                          size_t leaves_stride, uint64_t *gsw_out,
-                                                         size_t gsw_stride, const QueryDesc *qd,
+                                                         size_t gsw_stride,
+                                                         const __grid_constant__ KeyBatch kb,
                                                          int n1, ModTab M, Consts C) {
   __shared__ uint64_t sa[kSmemPoly], sb[kSmemPoly];
   const int tid = threadIdx.x;
@@ -205,7 +207,7 @@ __global__ void __launch_bounds__(T) query_to_gsw_kernel(const uint64_t *leaves,
   }
   // second half: external product with RGSW(sk) under the key gadget
   uint64_t out[2][8];
-  ext_product_core(x, qd[b].gsw_key, C.l_key, C.base_log2_key, sa, sb, M, out);
+  ext_product_core(x, kb.q[b].gsw_key, C.l_key, C.base_log2_key, sa, sb, M, out);
   uint64_t *row1 = rgsw + (size_t)(l + kk) * 2 * kN;
 #pragma unroll
   for (int poly = 0; poly < 2; ++poly)
@@ -560,17 +562,27 @@ void launch_ntt(const ModTab &M, uint64_t *polys, size_t count, bool inverse, cu
 void launch_expand_level(const uint64_t *cur, uint64_t *nxt, size_t in_stride, size_t out_stride,
                          const QueryDesc *qd, int level, int live_nodes, int batch,
                          const ModTab &Mq, const ModTab &Mp, const Consts &C, cudaStream_t s) {
-  const size_t smem = kExpandSmem;
-  expand_level_kernel<<<dim3(live_nodes, batch), T, smem, s>>>(cur, nxt, in_stride, out_stride,
-                                                              qd, level, Mq, Mp, C);
+  for (int b0 = 0; b0 < batch; b0 += kMaxKeyBatch) {
+    const int nb = batch - b0 < kMaxKeyBatch ? batch - b0 : kMaxKeyBatch;
+    KeyBatch kb;
+    for (int i = 0; i < nb; ++i) kb.q[i] = qd[b0 + i];
+    expand_level_kernel<<<dim3(live_nodes, nb), T, kExpandSmem, s>>>(
+        cur + b0 * in_stride, nxt + b0 * out_stride, in_stride, out_stride, kb, level, Mq, Mp, C);
+  }
 }
 
 void launch_query_to_gsw(const uint64_t *leaves, size_t leaves_stride, uint64_t *gsw_out,
                          size_t gsw_stride, const QueryDesc *qd, int n1, int num_cts, int batch,
                          const ModTab &Mq, const Consts &C, cudaStream_t s) {
   if (num_cts <= 0) return;
-  query_to_gsw_kernel<<<dim3(num_cts, batch), T, 0, s>>>(leaves, leaves_stride, gsw_out,
-                                                        gsw_stride, qd, n1, Mq, C);
+  for (int b0 = 0; b0 < batch; b0 += kMaxKeyBatch) {
+    const int nb = batch - b0 < kMaxKeyBatch ? batch - b0 : kMaxKeyBatch;
+    KeyBatch kb;
+    for (int i = 0; i < nb; ++i) kb.q[i] = qd[b0 + i];
+    query_to_gsw_kernel<<<dim3(num_cts, nb), T, 0, s>>>(
+        leaves + b0 * leaves_stride, leaves_stride, gsw_out + b0 * gsw_stride, gsw_stride, kb, n1,
+        Mq, C);
+  }
 }
 
 void launch_query_prep(const uint64_t *leaves, size_t leaves_stride, uint4 *qs, size_t qs_stride,

@@ -11,10 +11,17 @@
 
 namespace opir {
 
-// Per-query pointers for a batch (device array, one entry per query).
+// Per-query key pointers.
 struct QueryDesc {
   const uint64_t *galois;   // [h][2][2][N]   key k, modulus (q, p), NTT form
   const uint64_t *gsw_key;  // [2 l_key][2][N] RGSW(sk), NTT form
+};
+
+// Key pointers of up to kMaxKeyBatch queries, passed to kernels by value
+// (no per-query host->device copy); launchers split larger batches.
+constexpr int kMaxKeyBatch = 64;
+struct KeyBatch {
+  QueryDesc q[kMaxKeyBatch];
 };
 
 // Scalars of the parameter set shared by all kernels.

@@ -210,6 +210,15 @@ class PirServer:
                                                   _capi.p64(q), _capi.p64(resp), _capi.p8(packed)))
         return resp.reshape(B, 2, N), packed.reshape(B, self.resp_bytes)
 
+    def make_query_device(self, client_ids: Sequence[int], d_queries: int, d_resps: int,
+                          d_packed: int):
+        """Enqueue a batch on the context stream with device pointers
+        (queries [B][2][N] u64, responses [B][2][N] u64, packed [B][bytes])."""
+        ids = np.ascontiguousarray(np.asarray(client_ids, dtype=np.uint64))
+        self._check(self._L.opir_make_query_device(
+            self._ctx, self.db_id, ids.size, _capi.p64(ids), ctypes.c_void_p(d_queries),
+            ctypes.c_void_p(d_resps), ctypes.c_void_p(d_packed)))
+
     def make_query_trace(self, client_id: int, query):
         """make_query returning every intermediate (parity tests)."""
         P = self.pir_params
