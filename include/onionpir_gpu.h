@@ -35,7 +35,8 @@ typedef enum {
   OPIR_ERR_OOM = -4,            /* device allocation failed                 */
   OPIR_ERR_CUDA = -5,           /* CUDA runtime error                       */
   OPIR_ERR_STATE = -6,          /* call not valid in the current state      */
-  OPIR_ERR_NO_DEVICE = -7
+  OPIR_ERR_NO_DEVICE = -7,
+  OPIR_ERR_TIMEOUT = -8         /* a bounded device-side wait gave up       */
 } opir_status;
 
 /* Ciphertext-side parameters (PirParams, pir.cpp:9-54; database_constants.h). */
@@ -130,6 +131,9 @@ int opir_set_timing(opir_ctx *ctx, int enable);
 int opir_stage_times(opir_ctx *ctx, float *ms6);
 /* Number of kernels this context has launched since creation. */
 uint64_t opir_launch_count(const opir_ctx *ctx);
+/* Wait for the context stream and report (then clear) any device-side
+ * error recorded by asynchronous queries (OPIR_ERR_TIMEOUT). */
+int opir_sync(opir_ctx *ctx);
 
 /* ---- primitives (tests) ---- */
 /* Negacyclic NTT of `count` polynomials mod q (mod = 0) or p (mod = 1),

@@ -25,6 +25,7 @@ STATUS = {
     -5: "OPIR_ERR_CUDA",
     -6: "OPIR_ERR_STATE",
     -7: "OPIR_ERR_NO_DEVICE",
+    -8: "OPIR_ERR_TIMEOUT",
 }
 
 # every symbol include/onionpir_gpu.h declares
@@ -34,7 +35,7 @@ EXPORTS = (
     "opir_db_fill_synthetic", "opir_db_upload_aligned", "opir_set_galois_key",
     "opir_set_gsw_key", "opir_erase_client", "opir_make_query", "opir_make_query_batch",
     "opir_make_query_device", "opir_make_query_trace", "opir_set_timing", "opir_stage_times",
-    "opir_launch_count", "opir_ntt",
+    "opir_launch_count", "opir_sync", "opir_ntt",
 )
 
 
@@ -112,6 +113,7 @@ def load(path: str = LIB):
     L.opir_stage_times.argtypes = [_vp, ctypes.POINTER(ctypes.c_float)]
     L.opir_launch_count.argtypes = [_vp]
     L.opir_launch_count.restype = ctypes.c_uint64
+    L.opir_sync.argtypes = [_vp]
     L.opir_ntt.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _u64p, ctypes.c_uint64]
     _lib = L
     return L

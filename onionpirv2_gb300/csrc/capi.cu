@@ -174,6 +174,7 @@ struct opir_ctx {
   uint32_t next_db = 1;
   std::map<uint64_t, std::unique_ptr<Client>> clients;
   Workspace ws;
+  DevBuf status;  // device status word: bounded-wait timeouts (async.cuh)
   bool timing = false;
   cudaEvent_t ev[8] = {};
   float stage_ms[6] = {};
@@ -331,7 +332,7 @@ int run_pipeline(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
   record(ctx, 6);
   launch_scan(db.dbs.as<uint64_t>(), W.qs.as<uint4>(), qs_stride, W.res.as<uint64_t>(),
               res_stride, (int)n1, (int)nr, batch, ctx->C, ctx->Mq.tab.mu_lo, ctx->Mq.tab.mu_hi,
-              s);
+              ctx->status.as<uint32_t>(), s);
   record(ctx, 7);
   launch_ntt(ctx->Mq.tab, W.res.as<uint64_t>(), (size_t)batch * nr * 2, true, s);
   ctx->launches += 3;
@@ -365,6 +366,17 @@ int run_pipeline(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
          "trace gsw");
   }
   ctx->stage_valid = ctx->timing;
+  return OPIR_OK;
+}
+
+// Read and clear the device status word (call with the stream idle).
+int check_status(opir_ctx *ctx) {
+  uint32_t st = 0;
+  CK(cudaMemcpy(&st, ctx->status.p, sizeof st, cudaMemcpyDeviceToHost), "read status");
+  if (st) {
+    CK(cudaMemset(ctx->status.p, 0, sizeof st), "clear status");
+    return ctx->fail(OPIR_ERR_TIMEOUT, "device pipeline wait timed out (status 0x%x)", st);
+  }
   return OPIR_OK;
 }
 
@@ -435,7 +447,11 @@ int opir_ctx_create(const opir_params *P, int device, opir_ctx **out) {
   if (rc) return rc;
   rc = build_modtab(c, c->Mp, p);
   if (rc) return rc;
-  if (init_kernel_attributes() != cudaSuccess) return OPIR_ERR_CUDA;
+  if (init_kernel_attributes() != cudaSuccess || init_scan_attributes() != cudaSuccess)
+    return OPIR_ERR_CUDA;
+  if (c->status.alloc(sizeof(uint32_t)) != cudaSuccess ||
+      cudaMemset(c->status.p, 0, sizeof(uint32_t)) != cudaSuccess)
+    return OPIR_ERR_CUDA;
   if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess)
     return OPIR_ERR_CUDA;
   c->stream = c->own_stream;
@@ -675,6 +691,10 @@ static int query_host(opir_ctx *ctx, uint32_t db_id, uint32_t batch, const uint6
                        ctx->stream),
        "download responses");
   CK(cudaStreamSynchronize(ctx->stream), "query");
+  {
+    int rc2 = check_status(ctx);
+    if (rc2) return rc2;
+  }
   if (resps) std::memcpy(resps, h_resp, batch * CTB);
   if (packed) std::memcpy(packed, h_packed, batch * ctx->resp_bytes);
   return collect_times(ctx);
@@ -735,6 +755,14 @@ int opir_stage_times(opir_ctx *ctx, float *ms6) {
 }
 
 uint64_t opir_launch_count(const opir_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+int opir_sync(opir_ctx *ctx) {
+  if (!ctx) return OPIR_ERR_ARG;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  cudaSetDevice(ctx->device);
+  CK(cudaStreamSynchronize(ctx->stream), "sync");
+  return check_status(ctx);
+}
 
 int opir_ntt(opir_ctx *ctx, int mod, int inverse, uint64_t *polys, uint64_t count) {
   if (!ctx || !polys || (mod != 0 && mod != 1)) return OPIR_ERR_ARG;

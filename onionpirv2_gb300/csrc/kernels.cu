@@ -282,120 +282,6 @@ __global__ void __launch_bounds__(T) query_prep_kernel(const uint64_t *leaves,
   }
 }
 
-// Exact sum of 60x60-bit products with 30-bit halves: for a = a1 2^30 + a0,
-// b = b1 2^30 + b0 the product is a0 b0 + (a0 b1 + a1 b0) 2^30 + a1 b1 2^60.
-// Each half-product is < 2^60, so the three 64-bit partial sums absorb 16,
-// 8 and 16 k-steps; every 8 steps they are folded into 128-bit totals.
-struct Acc3 {
-  uint64_t ll, mid, hh;
-  U128 LL, MID, HH;
-};
-
-__device__ __forceinline__ void acc3_zero(Acc3 &a) {
-  a.ll = a.mid = a.hh = 0;
-  a.LL = a.MID = a.HH = U128{0, 0};
-}
-__device__ __forceinline__ void acc3_mac(Acc3 &a, uint32_t a0, uint32_t a1, uint32_t b0,
-                                         uint32_t b1) {
-  a.ll += (uint64_t)a0 * b0;
-  a.mid += (uint64_t)a0 * b1;
-  a.mid += (uint64_t)a1 * b0;
-  a.hh += (uint64_t)a1 * b1;
-}
-__device__ __forceinline__ void acc3_flush(Acc3 &a) {
-  add_to(a.LL, U128{a.ll, 0});
-  add_to(a.MID, U128{a.mid, 0});
-  add_to(a.HH, U128{a.hh, 0});
-  a.ll = a.mid = a.hh = 0;
-}
-__device__ __forceinline__ uint64_t acc3_reduce(Acc3 &a, const Consts &C, uint64_t mu_lo,
-                                                uint64_t mu_hi) {
-  acc3_flush(a);
-  const uint64_t q = C.q;
-  const uint64_t rl = barrett128(a.LL, q, mu_lo, mu_hi);
-  const uint64_t rm = barrett128(a.MID, q, mu_lo, mu_hi);
-  const uint64_t rh = barrett128(a.HH, q, mu_lo, mu_hi);
-  uint64_t r = add_mod(rl, mul_shoup(rm, C.two30, C.two30_s, q), q);
-  return add_mod(r, mul_shoup(rh, C.two60, C.two60_s, q), q);
-}
-
-// Database x query product (naive_level_mat_mat_128 / mat_mat_128,
-// matrix.cpp:79-97,220-235, plus delay_modulus's reduction, server.cpp:178-243).
-// Thread owns R consecutive rows of one coefficient plane c and streams
-// down the n1 columns: DB[c][k][row0..row0+R) is one R*8-byte load, Q[c][k]
-// one 16-byte broadcast load.
-template <int R>
-__global__ void __launch_bounds__(256) scan_kernel(const uint64_t *__restrict__ dbs,
-                                                   const uint4 *__restrict__ qs,
-                                                   size_t qs_stride, uint64_t *out,
-                                                   size_t out_stride, int n1, int n_rest,
-                                                   Consts C, uint64_t mu_lo, uint64_t mu_hi) {
-  const int b = blockIdx.y;
-  const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int groups = n_rest / R;
-  const size_t c = g / groups;
-  if (c >= (size_t)kN) return;
-  const int row0 = (int)(g % groups) * R;
-  const uint64_t *plane = dbs + c * (size_t)n1 * n_rest + row0;
-  const uint4 *qv = qs + b * qs_stride + c * (size_t)n1;
-
-  Acc3 acc[R][2];
-#pragma unroll
-  for (int r = 0; r < R; ++r) {
-    acc3_zero(acc[r][0]);
-    acc3_zero(acc[r][1]);
-  }
-  constexpr int U = 8;
-  int k = 0;
-  for (; k + U <= n1; k += U) {
-    uint64_t a[U][R];
-    uint4 bq[U];
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const uint64_t *src = plane + (size_t)(k + u) * n_rest;
-      if constexpr (R == 2) {
-        const ulonglong2 v = __ldcs(reinterpret_cast<const ulonglong2 *>(src));
-        a[u][0] = v.x;
-        a[u][R - 1] = v.y;
-      } else {
-        a[u][0] = __ldcs(src);
-      }
-      bq[u] = __ldg(qv + k + u);
-    }
-#pragma unroll
-    for (int u = 0; u < U; ++u)
-#pragma unroll
-      for (int r = 0; r < R; ++r) {
-        const uint32_t a0 = (uint32_t)a[u][r], a1 = (uint32_t)(a[u][r] >> 32);
-        acc3_mac(acc[r][0], a0, a1, bq[u].x, bq[u].y);
-        acc3_mac(acc[r][1], a0, a1, bq[u].z, bq[u].w);
-      }
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-      acc3_flush(acc[r][0]);
-      acc3_flush(acc[r][1]);
-    }
-  }
-  for (; k < n1; ++k) {
-    const uint64_t *src = plane + (size_t)k * n_rest;
-    const uint4 bq = __ldg(qv + k);
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-      const uint64_t av = src[r];
-      const uint32_t a0 = (uint32_t)av, a1 = (uint32_t)(av >> 32);
-      acc3_mac(acc[r][0], a0, a1, bq.x, bq.y);
-      acc3_mac(acc[r][1], a0, a1, bq.z, bq.w);
-    }
-  }
-  uint64_t *o = out + b * out_stride;
-#pragma unroll
-  for (int r = 0; r < R; ++r) {
-    const size_t row = (size_t)row0 + r;
-    o[row * 2 * kN + c] = acc3_reduce(acc[r][0], C, mu_lo, mu_hi);
-    o[row * 2 * kN + kN + c] = acc3_reduce(acc[r][1], C, mu_lo, mu_hi);
-  }
-}
-
 // ---------------------------------------------------------------------------
 // mod switch (server.cpp:779-801) + response packing (server.cpp:581-633)
 // ---------------------------------------------------------------------------
@@ -588,22 +474,6 @@ void launch_query_to_gsw(const uint64_t *leaves, size_t leaves_stride, uint64_t 
 void launch_query_prep(const uint64_t *leaves, size_t leaves_stride, uint4 *qs, size_t qs_stride,
                        int n1, int batch, const ModTab &Mq, cudaStream_t s) {
   query_prep_kernel<<<dim3(n1, batch), T, 0, s>>>(leaves, leaves_stride, qs, qs_stride, n1, Mq);
-}
-
-void launch_scan(const uint64_t *dbs, const uint4 *qs, size_t qs_stride, uint64_t *out,
-                 size_t out_stride, int n1, int n_rest, int batch, const Consts &C,
-                 uint64_t mu_lo, uint64_t mu_hi, cudaStream_t s) {
-  if (n_rest % 2 == 0) {
-    const size_t threads = (size_t)kN * (n_rest / 2);
-    const unsigned blocks = (unsigned)((threads + 255) / 256);
-    scan_kernel<2><<<dim3(blocks, batch), 256, 0, s>>>(dbs, qs, qs_stride, out, out_stride, n1,
-                                                      n_rest, C, mu_lo, mu_hi);
-  } else {
-    const size_t threads = (size_t)kN * n_rest;
-    const unsigned blocks = (unsigned)((threads + 255) / 256);
-    scan_kernel<1><<<dim3(blocks, batch), 256, 0, s>>>(dbs, qs, qs_stride, out, out_stride, n1,
-                                                      n_rest, C, mu_lo, mu_hi);
-  }
 }
 
 void launch_fold(uint64_t *res, size_t res_stride, const uint64_t *gsw, size_t gsw_stride,

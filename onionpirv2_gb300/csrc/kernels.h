@@ -63,9 +63,12 @@ void launch_query_to_gsw(const uint64_t *leaves, size_t leaves_stride, uint64_t 
 void launch_query_prep(const uint64_t *leaves, size_t leaves_stride, uint4 *qs, size_t qs_stride,
                        int n1, int batch, const ModTab &Mq, cudaStream_t s);
 // out[b][row][poly][c] = sum_k DB[c][k][row] * Q[b][c][k][poly] mod q  (NTT form)
+// (bulk-copy pipelined kernel when n_rest >= 2 and 4 | n1; status collects
+// bounded-wait timeouts, see async.cuh)
 void launch_scan(const uint64_t *dbs, const uint4 *qs, size_t qs_stride, uint64_t *out,
                  size_t out_stride, int n1, int n_rest, int batch, const Consts &C,
-                 uint64_t mu_lo, uint64_t mu_hi, cudaStream_t s);
+                 uint64_t mu_lo, uint64_t mu_hi, uint32_t *status, cudaStream_t s);
+cudaError_t init_scan_attributes();
 
 // ---- one folding level (other_dim_mux): res[b][j] += INTT(RGSW x (res[j+half]-res[j]))
 void launch_fold(uint64_t *res, size_t res_stride, const uint64_t *gsw, size_t gsw_stride,

@@ -1,0 +1,392 @@
+// scan.cu -- first-dimension database x query product on sm_103a.
+//
+// Restates naive_level_mat_mat_128 / mat_mat_128 (matrix.cpp:79-97,220-235)
+// and delay_modulus's reduction (server.cpp:178-243): for every NTT slot c,
+//   out[row][poly][c] = sum_k DB[c][k][row] * Q[c][k][poly]  mod q,
+// summed exactly (the reference sums in a wrapping uint128; for the shipped
+// shapes its sums never wrap, so the results agree bit for bit).
+//
+// The database lives in HBM as dbs[c][k][row], each 60-bit residue stored as
+// lo30 | hi30 << 32, so one 8-byte load yields both 30-bit halves.  Products
+// are formed from 30x30-bit halves (IMAD.WIDE.U32), accumulated in 64-bit
+// partial sums and folded into 128-bit totals every 8 k-steps.
+//
+// scan_bulk_kernel (the production path) is a persistent, warp-specialised
+// kernel: one producer warp streams [k-block][rows] tiles of the database and
+// the matching query words into a ring of shared-memory stages with
+// cp.async.bulk (completion on mbarriers); eight consumer warps multiply out
+// of shared memory.  All waits are bounded (async.cuh).
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdlib>
+
+#include "async.cuh"
+#include "common.cuh"
+#include "kernels.h"
+
+namespace opir {
+
+namespace {
+
+struct Acc3 {
+  uint64_t ll, mid, hh;
+  U128 LL, MID, HH;
+};
+
+__device__ __forceinline__ void acc3_zero(Acc3 &a) {
+  a.ll = a.mid = a.hh = 0;
+  a.LL = a.MID = a.HH = U128{0, 0};
+}
+// a = a1 2^30 + a0, b = b1 2^30 + b0 (all halves < 2^30):
+// a b = a0 b0 + (a0 b1 + a1 b0) 2^30 + a1 b1 2^60.  Each half product is
+// < 2^60, so the 64-bit partials absorb 16, 8 and 16 k-steps.
+__device__ __forceinline__ void acc3_mac(Acc3 &a, uint32_t a0, uint32_t a1, uint32_t b0,
+                                         uint32_t b1) {
+  a.ll += (uint64_t)a0 * b0;
+  a.mid += (uint64_t)a0 * b1;
+  a.mid += (uint64_t)a1 * b0;
+  a.hh += (uint64_t)a1 * b1;
+}
+__device__ __forceinline__ void acc3_flush(Acc3 &a) {
+  add_to(a.LL, U128{a.ll, 0});
+  add_to(a.MID, U128{a.mid, 0});
+  add_to(a.HH, U128{a.hh, 0});
+  a.ll = a.mid = a.hh = 0;
+}
+__device__ __forceinline__ uint64_t acc3_reduce(Acc3 &a, const Consts &C, uint64_t mu_lo,
+                                                uint64_t mu_hi) {
+  acc3_flush(a);
+  const uint64_t q = C.q;
+  const uint64_t rl = barrett128(a.LL, q, mu_lo, mu_hi);
+  const uint64_t rm = barrett128(a.MID, q, mu_lo, mu_hi);
+  const uint64_t rh = barrett128(a.HH, q, mu_lo, mu_hi);
+  uint64_t r = add_mod(rl, mul_shoup(rm, C.two30, C.two30_s, q), q);
+  return add_mod(r, mul_shoup(rh, C.two60, C.two60_s, q), q);
+}
+
+// ---------------------------------------------------------------------------
+// generic kernel (any shape): thread owns R rows of one plane, loads straight
+// from global memory
+// ---------------------------------------------------------------------------
+template <int R>
+__global__ void __launch_bounds__(256) scan_kernel(const uint64_t *__restrict__ dbs,
+                                                   const uint4 *__restrict__ qs,
+                                                   size_t qs_stride, uint64_t *out,
+                                                   size_t out_stride, int n1, int n_rest,
+                                                   Consts C, uint64_t mu_lo, uint64_t mu_hi) {
+  const int b = blockIdx.y;
+  const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int groups = n_rest / R;
+  const size_t c = g / groups;
+  if (c >= (size_t)kN) return;
+  const int row0 = (int)(g % groups) * R;
+  const uint64_t *plane = dbs + c * (size_t)n1 * n_rest + row0;
+  const uint4 *qv = qs + b * qs_stride + c * (size_t)n1;
+
+  Acc3 acc[R][2];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    acc3_zero(acc[r][0]);
+    acc3_zero(acc[r][1]);
+  }
+  constexpr int U = 8;
+  int k = 0;
+  for (; k + U <= n1; k += U) {
+    uint64_t a[U][R];
+    uint4 bq[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const uint64_t *src = plane + (size_t)(k + u) * n_rest;
+      if constexpr (R == 2) {
+        const ulonglong2 v = __ldcs(reinterpret_cast<const ulonglong2 *>(src));
+        a[u][0] = v.x;
+        a[u][R - 1] = v.y;
+      } else {
+        a[u][0] = __ldcs(src);
+      }
+      bq[u] = __ldg(qv + k + u);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const uint32_t a0 = (uint32_t)a[u][r], a1 = (uint32_t)(a[u][r] >> 32);
+        acc3_mac(acc[r][0], a0, a1, bq[u].x, bq[u].y);
+        acc3_mac(acc[r][1], a0, a1, bq[u].z, bq[u].w);
+      }
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      acc3_flush(acc[r][0]);
+      acc3_flush(acc[r][1]);
+    }
+  }
+  for (; k < n1; ++k) {
+    const uint64_t *src = plane + (size_t)k * n_rest;
+    const uint4 bq = __ldg(qv + k);
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const uint64_t av = src[r];
+      const uint32_t a0 = (uint32_t)av, a1 = (uint32_t)(av >> 32);
+      acc3_mac(acc[r][0], a0, a1, bq.x, bq.y);
+      acc3_mac(acc[r][1], a0, a1, bq.z, bq.w);
+    }
+  }
+  uint64_t *o = out + b * out_stride;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const size_t row = (size_t)row0 + r;
+    o[row * 2 * kN + c] = acc3_reduce(acc[r][0], C, mu_lo, mu_hi);
+    o[row * 2 * kN + kN + c] = acc3_reduce(acc[r][1], C, mu_lo, mu_hi);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// bulk-copy pipelined kernel
+// ---------------------------------------------------------------------------
+constexpr int kConsumerWarps = 8;
+constexpr int kConsumers = kConsumerWarps * 32;  // 256 threads x 2 rows
+constexpr int kTileRows = 2 * kConsumers;        // 512 rows (of one or more planes) per tile
+
+struct ScanGeom {
+  int n1, n_rest;
+  int rt;       // rows of a plane per tile  (min(n_rest, 512))
+  int pc;       // planes per tile           (512 / rt)
+  int row_tiles;  // n_rest / rt
+  int nkb;      // n1 / kStepK
+  long long items;  // batch * (kN / pc) * row_tiles
+  int q_bytes;      // pc * kStepK * 16
+};
+
+// kStepK k-steps per stage, kStages stages, kMinBlocks CTAs per SM.
+template <int kStepK, int kStages, int kMinBlocks>
+__global__ void __launch_bounds__(kConsumers + 32, kMinBlocks)
+    scan_bulk_kernel(const uint64_t *__restrict__ dbs, const uint4 *__restrict__ qs,
+                     size_t qs_stride, uint64_t *out, size_t out_stride, ScanGeom G, Consts C,
+                     uint64_t mu_lo, uint64_t mu_hi, uint32_t *status) {
+  constexpr int kStageDbBytes = kStepK * kTileRows * 8;
+  constexpr int kFlushEvery = 8 / kStepK;  // stages between flushes (8 k-steps)
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const int stage_bytes = kStageDbBytes + G.q_bytes;
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem_raw + kStages * stage_bytes);
+  uint64_t *full = bars, *empty = bars + kStages;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], kConsumerWarps);
+    }
+    mbar_fence_init();
+  }
+  __syncthreads();
+
+  const size_t plane_words = (size_t)G.n1 * G.n_rest;
+  const long long per_b = (long long)(kN / G.pc) * G.row_tiles;
+
+  if (warp == kConsumerWarps) {
+    // ------------------------------ producer ------------------------------
+    long long it = 0;
+    bool ok = true;
+    for (long long item = blockIdx.x; item < G.items && ok; item += gridDim.x) {
+      const int b = (int)(item / per_b);
+      const long long rem = item % per_b;
+      const int g = (int)(rem / G.row_tiles), rt = (int)(rem % G.row_tiles);
+      const int c0 = g * G.pc;
+      for (int kb = 0; kb < G.nkb; ++kb, ++it) {
+        const int s = (int)(it % kStages);
+        const uint32_t round = (uint32_t)(it / kStages);
+        if (round > 0) {
+          bool w = true;
+          if (lane == 0) w = mbar_wait(&empty[s], (round - 1) & 1);
+          w = __shfl_sync(0xffffffffu, w, 0);
+          if (!w) {
+            if (lane == 0) report_error(status, kErrWaitEmpty);
+            ok = false;
+            break;
+          }
+        }
+        unsigned char *st = smem_raw + (size_t)s * stage_bytes;
+        uint64_t *sdb = reinterpret_cast<uint64_t *>(st);
+        uint4 *sq = reinterpret_cast<uint4 *>(st + kStageDbBytes);
+        if (lane == 0) mbar_arrive_expect_tx(&full[s], (uint32_t)stage_bytes);
+        __syncwarp();
+        const int k0 = kb * kStepK;
+        if (G.rt == G.n_rest) {
+          // one contiguous [k-block][rows] run per plane
+          for (int p = lane; p < G.pc; p += 32) {
+            const uint64_t *src = dbs + (size_t)(c0 + p) * plane_words + (size_t)k0 * G.n_rest;
+            bulk_g2s(sdb + (size_t)p * kStepK * G.rt, src, kStepK * G.rt * 8, &full[s]);
+          }
+        } else {
+          // one plane, a row tile of it: one run per k
+          for (int k = lane; k < kStepK; k += 32) {
+            const uint64_t *src = dbs + (size_t)c0 * plane_words + (size_t)(k0 + k) * G.n_rest +
+                                  (size_t)rt * G.rt;
+            bulk_g2s(sdb + (size_t)k * G.rt, src, G.rt * 8, &full[s]);
+          }
+        }
+        for (int p = lane; p < G.pc; p += 32) {
+          const uint4 *src = qs + b * qs_stride + (size_t)(c0 + p) * G.n1 + k0;
+          bulk_g2s(sq + p * kStepK, src, kStepK * 16, &full[s]);
+        }
+      }
+    }
+    // drain: never leave the CTA with copies still landing in its shared memory
+    if (lane == 0) {
+      const long long first = it > kStages ? it - kStages : 0;
+      for (long long j = first; j < it; ++j) {
+        if (!mbar_wait(&full[j % kStages], (uint32_t)((j / kStages) & 1))) {
+          report_error(status, kErrDrain);
+          break;
+        }
+      }
+    }
+    return;
+  }
+
+  // ------------------------------ consumers ------------------------------
+  const int t = threadIdx.x;
+  const int slot = 2 * t;
+  const int p = slot / G.rt, r = slot % G.rt;
+  long long it = 0;
+  for (long long item = blockIdx.x; item < G.items; item += gridDim.x) {
+    const int b = (int)(item / per_b);
+    const long long rem = item % per_b;
+    const int g = (int)(rem / G.row_tiles), rt = (int)(rem % G.row_tiles);
+    Acc3 acc[2][2];
+    acc3_zero(acc[0][0]);
+    acc3_zero(acc[0][1]);
+    acc3_zero(acc[1][0]);
+    acc3_zero(acc[1][1]);
+    for (int kb = 0; kb < G.nkb; ++kb, ++it) {
+      const int s = (int)(it % kStages);
+      if (!mbar_wait(&full[s], (uint32_t)((it / kStages) & 1))) {
+        report_error(status, kErrWaitFull);
+        return;
+      }
+      const unsigned char *st = smem_raw + (size_t)s * stage_bytes;
+      const uint64_t *sdb = reinterpret_cast<const uint64_t *>(st) + (size_t)p * kStepK * G.rt + r;
+      const uint4 *sq = reinterpret_cast<const uint4 *>(st + kStageDbBytes) + p * kStepK;
+#pragma unroll
+      for (int k = 0; k < kStepK; ++k) {
+        const ulonglong2 a = *reinterpret_cast<const ulonglong2 *>(sdb + (size_t)k * G.rt);
+        const uint4 bq = sq[k];
+        acc3_mac(acc[0][0], (uint32_t)a.x, (uint32_t)(a.x >> 32), bq.x, bq.y);
+        acc3_mac(acc[0][1], (uint32_t)a.x, (uint32_t)(a.x >> 32), bq.z, bq.w);
+        acc3_mac(acc[1][0], (uint32_t)a.y, (uint32_t)(a.y >> 32), bq.x, bq.y);
+        acc3_mac(acc[1][1], (uint32_t)a.y, (uint32_t)(a.y >> 32), bq.z, bq.w);
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[s]);
+      if (kb % kFlushEvery == kFlushEvery - 1) {  // 8 k-steps since the last flush
+        acc3_flush(acc[0][0]);
+        acc3_flush(acc[0][1]);
+        acc3_flush(acc[1][0]);
+        acc3_flush(acc[1][1]);
+      }
+    }
+    const size_t c = (size_t)g * G.pc + p;
+    uint64_t *o = out + b * out_stride;
+#pragma unroll
+    for (int rr = 0; rr < 2; ++rr) {
+      const size_t row = (size_t)rt * G.rt + r + rr;
+      o[row * 2 * kN + c] = acc3_reduce(acc[rr][0], C, mu_lo, mu_hi);
+      o[row * 2 * kN + kN + c] = acc3_reduce(acc[rr][1], C, mu_lo, mu_hi);
+    }
+  }
+}
+
+int g_num_sms = 0;
+
+struct BulkCfg {
+  int k, stages, min_blocks;
+};
+// configurations compiled in; OPIR_SCAN_CFG selects one by index (tuning)
+constexpr BulkCfg kCfgs[] = {{4, 8, 1}, {4, 6, 2}, {8, 4, 1}, {2, 12, 1}, {4, 12, 1}};
+int g_cfg = 0;
+
+template <int K, int S, int B>
+cudaError_t set_attr() {
+  const int max_smem = S * (K * kTileRows * 8 + (kTileRows / 2) * K * 16) + 2 * S * 8;
+  return cudaFuncSetAttribute(scan_bulk_kernel<K, S, B>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              max_smem > 227 * 1024 ? 227 * 1024 : max_smem);
+}
+
+template <int K, int S, int B>
+bool launch_bulk(const uint64_t *dbs, const uint4 *qs, size_t qs_stride, uint64_t *out,
+                 size_t out_stride, int n1, int n_rest, int batch, const Consts &C,
+                 uint64_t mu_lo, uint64_t mu_hi, uint32_t *status, cudaStream_t s) {
+  ScanGeom G;
+  G.n1 = n1;
+  G.n_rest = n_rest;
+  G.rt = n_rest < kTileRows ? n_rest : kTileRows;
+  G.pc = kTileRows / G.rt;
+  G.row_tiles = n_rest / G.rt;
+  G.nkb = n1 / K;
+  G.items = (long long)batch * (kN / G.pc) * G.row_tiles;
+  G.q_bytes = G.pc * K * 16;
+  const int smem = S * (K * kTileRows * 8 + G.q_bytes) + 2 * S * 8;
+  if (smem > 227 * 1024) return false;  // tiny planes: many query runs per stage
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, scan_bulk_kernel<K, S, B>, kConsumers + 32,
+                                                smem);
+  if (per_sm < 1) per_sm = 1;
+  const int sms = g_num_sms > 0 ? g_num_sms : 152;
+  long long grid = (long long)per_sm * sms;
+  if (grid > G.items) grid = G.items;
+  scan_bulk_kernel<K, S, B><<<(unsigned)grid, kConsumers + 32, smem, s>>>(
+      dbs, qs, qs_stride, out, out_stride, G, C, mu_lo, mu_hi, status);
+  return true;
+}
+
+}  // namespace
+
+cudaError_t init_scan_attributes() {
+  cudaError_t e;
+  if ((e = set_attr<4, 8, 1>()) != cudaSuccess) return e;
+  if ((e = set_attr<4, 6, 2>()) != cudaSuccess) return e;
+  if ((e = set_attr<8, 4, 1>()) != cudaSuccess) return e;
+  if ((e = set_attr<2, 12, 1>()) != cudaSuccess) return e;
+  if ((e = set_attr<4, 12, 1>()) != cudaSuccess) return e;
+  int dev;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+  if (const char *v = getenv("OPIR_SCAN_CFG")) {
+    const int i = atoi(v);
+    if (i >= 0 && i < (int)(sizeof(kCfgs) / sizeof(kCfgs[0]))) g_cfg = i;
+  }
+  return cudaSuccess;
+}
+
+void launch_scan(const uint64_t *dbs, const uint4 *qs, size_t qs_stride, uint64_t *out,
+                 size_t out_stride, int n1, int n_rest, int batch, const Consts &C,
+                 uint64_t mu_lo, uint64_t mu_hi, uint32_t *status, cudaStream_t s) {
+  const int K = kCfgs[g_cfg].k;
+  const bool bulk = n_rest >= 2 && n1 % 8 == 0 && n1 % K == 0;
+  if (bulk) {
+    bool done;
+    switch (g_cfg) {
+      case 0: done = launch_bulk<4, 8, 1>(dbs, qs, qs_stride, out, out_stride, n1, n_rest, batch, C, mu_lo, mu_hi, status, s); break;
+      case 1: done = launch_bulk<4, 6, 2>(dbs, qs, qs_stride, out, out_stride, n1, n_rest, batch, C, mu_lo, mu_hi, status, s); break;
+      case 2: done = launch_bulk<8, 4, 1>(dbs, qs, qs_stride, out, out_stride, n1, n_rest, batch, C, mu_lo, mu_hi, status, s); break;
+      case 3: done = launch_bulk<2, 12, 1>(dbs, qs, qs_stride, out, out_stride, n1, n_rest, batch, C, mu_lo, mu_hi, status, s); break;
+      default: done = launch_bulk<4, 12, 1>(dbs, qs, qs_stride, out, out_stride, n1, n_rest, batch, C, mu_lo, mu_hi, status, s); break;
+    }
+    if (done) return;
+  }
+  if (n_rest % 2 == 0) {
+    const size_t threads = (size_t)kN * (n_rest / 2);
+    const unsigned blocks = (unsigned)((threads + 255) / 256);
+    scan_kernel<2><<<dim3(blocks, batch), 256, 0, s>>>(dbs, qs, qs_stride, out, out_stride, n1,
+                                                      n_rest, C, mu_lo, mu_hi);
+  } else {
+    const size_t threads = (size_t)kN * n_rest;
+    const unsigned blocks = (unsigned)((threads + 255) / 256);
+    scan_kernel<1><<<dim3(blocks, batch), 256, 0, s>>>(dbs, qs, qs_stride, out, out_stride, n1,
+                                                      n_rest, C, mu_lo, mu_hi);
+  }
+}
+
+}  // namespace opir

@@ -151,3 +151,42 @@ def test_push_chunk_matches_reference_layout(oracle_lib, gpu_lib):
     resp = server.make_query(1, query)
     ref, _, _, _ = o.make_query_server(db, gk, o.gsw_key_to_ntt(gswk), query)
     assert np.array_equal(resp, ref)
+
+
+SHAPES = [
+    # (num_entries, max_fst_dim): n1 x n_rest
+    (4096, 256),   # 256 x 16   (32 planes per scan tile)
+    (8192, 8),     # 8 x 1024   (row tiles of 512 rows)
+    (512, 256),    # 256 x 2    (query runs exceed shared memory: generic kernel)
+    (1024, 1024),  # 1024 x 1   (single dimension, no folding)
+]
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+@pytest.mark.parametrize("cfg", [0, 1, 2, 3, 4])
+def test_scan_configs_and_shapes(oracle_lib, gpu_lib, monkeypatch, shape, cfg):
+    """Every compiled scan pipeline configuration and every tile geometry
+    gives the oracle's first-dimension result and response."""
+    if cfg and shape != (4096, 256) and shape != (8192, 8):
+        pytest.skip("configurations are swept on the two bulk-copy geometries")
+    from onionpirv2_gb300 import PirParams, PirServer
+    monkeypatch.setenv("OPIR_SCAN_CFG", str(cfg))
+    o = oracle_lib.Oracle(*shape)
+    P = o.P
+    server = PirServer(PirParams(num_entries=shape[0], max_fst_dim=shape[1]))
+    server.gen_data(31)
+    db = o.build_db(31)
+    sk, gk, gswk = make_client(o, 5)
+    server.set_client_galois_key(1, gk)
+    server.set_client_gsw_key(1, gswk)
+    idx = (P.num_entries * 2) // 3
+    query = o.make_query(sk, 17, idx)
+    tr = server.make_query_trace(1, query)
+    leaves = o.expand(query, gk)
+    fd, _ = o.first_dim(db, leaves[:P.n1])
+    assert np.array_equal(tr["first_dim"], fd)
+    resp, packed, _, _ = o.make_query_server(db, gk, o.gsw_key_to_ntt(gswk), query)
+    assert np.array_equal(tr["resp"], resp)
+    plain, _ = o.decrypt(sk, tr["resp"], 2)
+    assert np.array_equal(o.entry_from_plain(idx, plain), server.direct_get_entry(idx))
+    server.close()
