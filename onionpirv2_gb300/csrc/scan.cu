@@ -41,18 +41,27 @@ __device__ __forceinline__ void acc3_zero(Acc3 &a) {
 // a = a1 2^30 + a0, b = b1 2^30 + b0 (all halves < 2^30):
 // a b = a0 b0 + (a0 b1 + a1 b0) 2^30 + a1 b1 2^60.  Each half product is
 // < 2^60, so the 64-bit partials absorb 16, 8 and 16 k-steps.
+__device__ __forceinline__ void mad_wide(uint64_t &acc, uint32_t x, uint32_t y) {
+  asm("mad.wide.u32 %0, %1, %2, %0;" : "+l"(acc) : "r"(x), "r"(y));  // acc += x * y (one IMAD.WIDE)
+}
 __device__ __forceinline__ void acc3_mac(Acc3 &a, uint32_t a0, uint32_t a1, uint32_t b0,
                                          uint32_t b1) {
-  a.ll += (uint64_t)a0 * b0;
-  a.mid += (uint64_t)a0 * b1;
-  a.mid += (uint64_t)a1 * b0;
-  a.hh += (uint64_t)a1 * b1;
+  mad_wide(a.ll, a0, b0);
+  mad_wide(a.mid, a0, b1);
+  mad_wide(a.mid, a1, b0);
+  mad_wide(a.hh, a1, b1);
 }
 __device__ __forceinline__ void acc3_flush(Acc3 &a) {
   add_to(a.LL, U128{a.ll, 0});
   add_to(a.MID, U128{a.mid, 0});
   add_to(a.HH, U128{a.hh, 0});
   a.ll = a.mid = a.hh = 0;
+}
+// the middle partial takes two products per step: flush it every 8 steps,
+// the outer two every 16
+__device__ __forceinline__ void acc3_flush_mid(Acc3 &a) {
+  add_to(a.MID, U128{a.mid, 0});
+  a.mid = 0;
 }
 __device__ __forceinline__ uint64_t acc3_reduce(Acc3 &a, const Consts &C, uint64_t mu_lo,
                                                 uint64_t mu_hi) {
@@ -144,9 +153,7 @@ __global__ void __launch_bounds__(256) scan_kernel(const uint64_t *__restrict__ 
 // ---------------------------------------------------------------------------
 // bulk-copy pipelined kernel
 // ---------------------------------------------------------------------------
-constexpr int kConsumerWarps = 8;
-constexpr int kConsumers = kConsumerWarps * 32;  // 256 threads x 2 rows
-constexpr int kTileRows = 2 * kConsumers;        // 512 rows (of one or more planes) per tile
+constexpr int kTileRows = 512;  // rows (of one or more planes) per tile
 
 struct ScanGeom {
   int n1, n_rest;
@@ -158,14 +165,17 @@ struct ScanGeom {
   int q_bytes;      // pc * kStepK * 16
 };
 
-// kStepK k-steps per stage, kStages stages, kMinBlocks CTAs per SM.
-template <int kStepK, int kStages, int kMinBlocks>
-__global__ void __launch_bounds__(kConsumers + 32, kMinBlocks)
+// kRows rows per consumer thread, kWarps consumer warps (kRows * kWarps * 32
+// == 512), kStepK k-steps per stage, kStages stages, kMinBlocks CTAs per SM.
+template <int kRows, int kWarps, int kStepK, int kStages, int kMinBlocks>
+__global__ void __launch_bounds__(kWarps * 32 + 32, kMinBlocks)
     scan_bulk_kernel(const uint64_t *__restrict__ dbs, const uint4 *__restrict__ qs,
                      size_t qs_stride, uint64_t *out, size_t out_stride, ScanGeom G, Consts C,
                      uint64_t mu_lo, uint64_t mu_hi, uint32_t *status) {
+  static_assert(kRows * kWarps * 32 == kTileRows, "a tile is 512 rows");
+  static_assert(kStepK == 1 || kStepK == 2 || kStepK == 4 || kStepK == 8 || kStepK % 16 == 0,
+                "flush cadence: middle partial every 8 k-steps, outer ones every 16");
   constexpr int kStageDbBytes = kStepK * kTileRows * 8;
-  constexpr int kFlushEvery = 8 / kStepK;  // stages between flushes (8 k-steps)
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const int stage_bytes = kStageDbBytes + G.q_bytes;
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem_raw + kStages * stage_bytes);
@@ -175,7 +185,7 @@ __global__ void __launch_bounds__(kConsumers + 32, kMinBlocks)
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
       mbar_init(&full[s], 1);
-      mbar_init(&empty[s], kConsumerWarps);
+      mbar_init(&empty[s], kWarps);
     }
     mbar_fence_init();
   }
@@ -184,9 +194,11 @@ __global__ void __launch_bounds__(kConsumers + 32, kMinBlocks)
   const size_t plane_words = (size_t)G.n1 * G.n_rest;
   const long long per_b = (long long)(kN / G.pc) * G.row_tiles;
 
-  if (warp == kConsumerWarps) {
+  if (warp == kWarps) {
     // ------------------------------ producer ------------------------------
     long long it = 0;
+    int ps = 0;           // stage to fill next
+    uint32_t pphase = 0;  // round parity of that stage
     bool ok = true;
     for (long long item = blockIdx.x; item < G.items && ok; item += gridDim.x) {
       const int b = (int)(item / per_b);
@@ -194,11 +206,16 @@ __global__ void __launch_bounds__(kConsumers + 32, kMinBlocks)
       const int g = (int)(rem / G.row_tiles), rt = (int)(rem % G.row_tiles);
       const int c0 = g * G.pc;
       for (int kb = 0; kb < G.nkb; ++kb, ++it) {
-        const int s = (int)(it % kStages);
-        const uint32_t round = (uint32_t)(it / kStages);
-        if (round > 0) {
+        const int s = ps;
+        const bool reuse = it >= kStages;
+        const uint32_t ephase = pphase ^ 1u;  // phase of the consumers' release of the last use
+        if (++ps == kStages) {
+          ps = 0;
+          pphase ^= 1u;
+        }
+        if (reuse) {
           bool w = true;
-          if (lane == 0) w = mbar_wait(&empty[s], (round - 1) & 1);
+          if (lane == 0) w = mbar_wait(&empty[s], ephase);
           w = __shfl_sync(0xffffffffu, w, 0);
           if (!w) {
             if (lane == 0) report_error(status, kErrWaitEmpty);
@@ -246,22 +263,22 @@ __global__ void __launch_bounds__(kConsumers + 32, kMinBlocks)
   }
 
   // ------------------------------ consumers ------------------------------
-  const int t = threadIdx.x;
-  const int slot = 2 * t;
+  const int slot = kRows * threadIdx.x;
   const int p = slot / G.rt, r = slot % G.rt;
-  long long it = 0;
+  int s = 0;
+  uint32_t phase = 0;
   for (long long item = blockIdx.x; item < G.items; item += gridDim.x) {
     const int b = (int)(item / per_b);
     const long long rem = item % per_b;
     const int g = (int)(rem / G.row_tiles), rt = (int)(rem % G.row_tiles);
-    Acc3 acc[2][2];
-    acc3_zero(acc[0][0]);
-    acc3_zero(acc[0][1]);
-    acc3_zero(acc[1][0]);
-    acc3_zero(acc[1][1]);
-    for (int kb = 0; kb < G.nkb; ++kb, ++it) {
-      const int s = (int)(it % kStages);
-      if (!mbar_wait(&full[s], (uint32_t)((it / kStages) & 1))) {
+    Acc3 acc[kRows][2];
+#pragma unroll
+    for (int rr = 0; rr < kRows; ++rr) {
+      acc3_zero(acc[rr][0]);
+      acc3_zero(acc[rr][1]);
+    }
+    for (int kb = 0; kb < G.nkb; ++kb) {
+      if (!mbar_wait(&full[s], phase)) {
         report_error(status, kErrWaitFull);
         return;
       }
@@ -270,26 +287,60 @@ __global__ void __launch_bounds__(kConsumers + 32, kMinBlocks)
       const uint4 *sq = reinterpret_cast<const uint4 *>(st + kStageDbBytes) + p * kStepK;
 #pragma unroll
       for (int k = 0; k < kStepK; ++k) {
-        const ulonglong2 a = *reinterpret_cast<const ulonglong2 *>(sdb + (size_t)k * G.rt);
+        uint64_t a[kRows];
+        if constexpr (kRows == 2) {
+          const ulonglong2 v = *reinterpret_cast<const ulonglong2 *>(sdb + (size_t)k * G.rt);
+          a[0] = v.x;
+          a[kRows - 1] = v.y;
+        } else {
+          a[0] = sdb[(size_t)k * G.rt];
+        }
         const uint4 bq = sq[k];
-        acc3_mac(acc[0][0], (uint32_t)a.x, (uint32_t)(a.x >> 32), bq.x, bq.y);
-        acc3_mac(acc[0][1], (uint32_t)a.x, (uint32_t)(a.x >> 32), bq.z, bq.w);
-        acc3_mac(acc[1][0], (uint32_t)a.y, (uint32_t)(a.y >> 32), bq.x, bq.y);
-        acc3_mac(acc[1][1], (uint32_t)a.y, (uint32_t)(a.y >> 32), bq.z, bq.w);
+#pragma unroll
+        for (int rr = 0; rr < kRows; ++rr) {
+          const uint32_t a0 = (uint32_t)a[rr], a1 = (uint32_t)(a[rr] >> 32);
+          acc3_mac(acc[rr][0], a0, a1, bq.x, bq.y);
+          acc3_mac(acc[rr][1], a0, a1, bq.z, bq.w);
+        }
+        if constexpr (kStepK >= 8) {
+          // global step kb * kStepK + k; kStepK is 8 or a multiple of 16
+          const int gk = (kStepK % 16 == 0) ? k : (kb & 1) * 8 + k;
+          if ((gk & 15) == 15) {
+#pragma unroll
+            for (int rr = 0; rr < kRows; ++rr) {
+              acc3_flush(acc[rr][0]);
+              acc3_flush(acc[rr][1]);
+            }
+          } else if ((gk & 7) == 7) {
+#pragma unroll
+            for (int rr = 0; rr < kRows; ++rr) {
+              acc3_flush_mid(acc[rr][0]);
+              acc3_flush_mid(acc[rr][1]);
+            }
+          }
+        }
       }
       __syncwarp();
       if (lane == 0) mbar_arrive(&empty[s]);
-      if (kb % kFlushEvery == kFlushEvery - 1) {  // 8 k-steps since the last flush
-        acc3_flush(acc[0][0]);
-        acc3_flush(acc[0][1]);
-        acc3_flush(acc[1][0]);
-        acc3_flush(acc[1][1]);
+      if (++s == kStages) {
+        s = 0;
+        phase ^= 1u;
+      }
+      if constexpr (kStepK < 8) {
+        constexpr int kEvery = 8 / kStepK;  // stages per 8 k-steps
+        if (kb % kEvery == kEvery - 1) {
+#pragma unroll
+          for (int rr = 0; rr < kRows; ++rr) {
+            acc3_flush(acc[rr][0]);
+            acc3_flush(acc[rr][1]);
+          }
+        }
       }
     }
     const size_t c = (size_t)g * G.pc + p;
     uint64_t *o = out + b * out_stride;
 #pragma unroll
-    for (int rr = 0; rr < 2; ++rr) {
+    for (int rr = 0; rr < kRows; ++rr) {
       const size_t row = (size_t)rt * G.rt + r + rr;
       o[row * 2 * kN + c] = acc3_reduce(acc[rr][0], C, mu_lo, mu_hi);
       o[row * 2 * kN + kN + c] = acc3_reduce(acc[rr][1], C, mu_lo, mu_hi);
@@ -298,31 +349,27 @@ __global__ void __launch_bounds__(kConsumers + 32, kMinBlocks)
 }
 
 int g_num_sms = 0;
-
-struct BulkCfg {
-  int k, stages, min_blocks;
-};
-// configurations compiled in; OPIR_SCAN_CFG selects one by index (tuning)
-constexpr BulkCfg kCfgs[] = {{4, 8, 1}, {4, 6, 2}, {8, 4, 1}, {2, 12, 1}, {4, 12, 1}};
 int g_cfg = 0;
 
-template <int K, int S, int B>
+template <int R, int W, int K, int S, int B>
 cudaError_t set_attr() {
   const int max_smem = S * (K * kTileRows * 8 + (kTileRows / 2) * K * 16) + 2 * S * 8;
-  return cudaFuncSetAttribute(scan_bulk_kernel<K, S, B>,
+  return cudaFuncSetAttribute(scan_bulk_kernel<R, W, K, S, B>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize,
                               max_smem > 227 * 1024 ? 227 * 1024 : max_smem);
 }
 
-template <int K, int S, int B>
+template <int R, int W, int K, int S, int B>
 bool launch_bulk(const uint64_t *dbs, const uint4 *qs, size_t qs_stride, uint64_t *out,
                  size_t out_stride, int n1, int n_rest, int batch, const Consts &C,
                  uint64_t mu_lo, uint64_t mu_hi, uint32_t *status, cudaStream_t s) {
+  if (n1 % K != 0) return false;
   ScanGeom G;
   G.n1 = n1;
   G.n_rest = n_rest;
   G.rt = n_rest < kTileRows ? n_rest : kTileRows;
   G.pc = kTileRows / G.rt;
+  if (G.rt < R) return false;
   G.row_tiles = n_rest / G.rt;
   G.nkb = n1 / K;
   G.items = (long long)batch * (kN / G.pc) * G.row_tiles;
@@ -330,32 +377,44 @@ bool launch_bulk(const uint64_t *dbs, const uint4 *qs, size_t qs_stride, uint64_
   const int smem = S * (K * kTileRows * 8 + G.q_bytes) + 2 * S * 8;
   if (smem > 227 * 1024) return false;  // tiny planes: many query runs per stage
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, scan_bulk_kernel<K, S, B>, kConsumers + 32,
-                                                smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, scan_bulk_kernel<R, W, K, S, B>,
+                                                W * 32 + 32, smem);
   if (per_sm < 1) per_sm = 1;
   const int sms = g_num_sms > 0 ? g_num_sms : 152;
   long long grid = (long long)per_sm * sms;
   if (grid > G.items) grid = G.items;
-  scan_bulk_kernel<K, S, B><<<(unsigned)grid, kConsumers + 32, smem, s>>>(
+  scan_bulk_kernel<R, W, K, S, B><<<(unsigned)grid, W * 32 + 32, smem, s>>>(
       dbs, qs, qs_stride, out, out_stride, G, C, mu_lo, mu_hi, status);
   return true;
 }
 
+// compiled configurations {rows, warps, k-steps, stages, CTAs/SM};
+// OPIR_SCAN_CFG selects one by index (tuning sweeps)
+#define OPIR_SCAN_CONFIGS(X) \
+  X(0, 1, 16, 16, 3, 1)      \
+  X(1, 1, 16, 8, 6, 1)       \
+  X(2, 1, 16, 16, 2, 1)      \
+  X(3, 1, 16, 8, 5, 1)       \
+  X(4, 1, 16, 4, 12, 1)      \
+  X(5, 2, 8, 16, 3, 1)
+constexpr int kNumCfgs = 6;
+
 }  // namespace
 
 cudaError_t init_scan_attributes() {
-  cudaError_t e;
-  if ((e = set_attr<4, 8, 1>()) != cudaSuccess) return e;
-  if ((e = set_attr<4, 6, 2>()) != cudaSuccess) return e;
-  if ((e = set_attr<8, 4, 1>()) != cudaSuccess) return e;
-  if ((e = set_attr<2, 12, 1>()) != cudaSuccess) return e;
-  if ((e = set_attr<4, 12, 1>()) != cudaSuccess) return e;
+  cudaError_t e = cudaSuccess;
+#define OPIR_SET(i, R, W, K, S, B) \
+  if (e == cudaSuccess) e = set_attr<R, W, K, S, B>();
+  OPIR_SCAN_CONFIGS(OPIR_SET)
+#undef OPIR_SET
+  if (e != cudaSuccess) return e;
   int dev;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+  g_cfg = 0;
   if (const char *v = getenv("OPIR_SCAN_CFG")) {
     const int i = atoi(v);
-    if (i >= 0 && i < (int)(sizeof(kCfgs) / sizeof(kCfgs[0]))) g_cfg = i;
+    if (i >= 0 && i < kNumCfgs) g_cfg = i;
   }
   return cudaSuccess;
 }
@@ -363,16 +422,16 @@ cudaError_t init_scan_attributes() {
 void launch_scan(const uint64_t *dbs, const uint4 *qs, size_t qs_stride, uint64_t *out,
                  size_t out_stride, int n1, int n_rest, int batch, const Consts &C,
                  uint64_t mu_lo, uint64_t mu_hi, uint32_t *status, cudaStream_t s) {
-  const int K = kCfgs[g_cfg].k;
-  const bool bulk = n_rest >= 2 && n1 % 8 == 0 && n1 % K == 0;
-  if (bulk) {
-    bool done;
+  if (n_rest >= 2 && n1 % 8 == 0) {
+    bool done = false;
     switch (g_cfg) {
-      case 0: done = launch_bulk<4, 8, 1>(dbs, qs, qs_stride, out, out_stride, n1, n_rest, batch, C, mu_lo, mu_hi, status, s); break;
-      case 1: done = launch_bulk<4, 6, 2>(dbs, qs, qs_stride, out, out_stride, n1, n_rest, batch, C, mu_lo, mu_hi, status, s); break;
-      case 2: done = launch_bulk<8, 4, 1>(dbs, qs, qs_stride, out, out_stride, n1, n_rest, batch, C, mu_lo, mu_hi, status, s); break;
-      case 3: done = launch_bulk<2, 12, 1>(dbs, qs, qs_stride, out, out_stride, n1, n_rest, batch, C, mu_lo, mu_hi, status, s); break;
-      default: done = launch_bulk<4, 12, 1>(dbs, qs, qs_stride, out, out_stride, n1, n_rest, batch, C, mu_lo, mu_hi, status, s); break;
+#define OPIR_CASE(i, R, W, K, S, B)                                                            \
+  case i:                                                                                      \
+    done = launch_bulk<R, W, K, S, B>(dbs, qs, qs_stride, out, out_stride, n1, n_rest, batch, \
+                                      C, mu_lo, mu_hi, status, s);                             \
+    break;
+      OPIR_SCAN_CONFIGS(OPIR_CASE)
+#undef OPIR_CASE
     }
     if (done) return;
   }

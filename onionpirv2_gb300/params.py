@@ -101,6 +101,10 @@ WORKLOADS: Dict[str, dict] = {
     "db4096": dict(max_fst_dim=256, num_entries=4096),
     # 512 x 2^6 = 32,768 plaintexts, 537 MB NTT form (small profiling case, > L2)
     "db32768": dict(max_fst_dim=512, num_entries=1 << 15),
+    # 128 x 2^9 = 65,536 plaintexts, 1.07 GB NTT form: the scan's tile and
+    # work split of the 262,144-plaintext case at a quarter of the size
+    # (profiling case)
+    "db65536": dict(max_fst_dim=128, num_entries=1 << 16),
     # 512 x 2^9 = 262,144 plaintexts, ~1 GB raw entries, 4.29 GB NTT form
     "db262144": dict(max_fst_dim=512, num_entries=1 << 18),
     # 1024 x 2^11 = 2,097,152 plaintexts, ~8 GB raw entries, 34.4 GB NTT form
