@@ -41,213 +41,6 @@ __global__ void __launch_bounds__(T) ntt_kernel(ModTab M, uint64_t *polys, int i
 }
 
 // ---------------------------------------------------------------------------
-// expansion: one level of fast_expand_qry (server.cpp:383-428)
-//   c' = apply_galois(c_i, N/k + 1)   (automorphism + key switch with p)
-//   c_2i = c_i + c';  c_2i+1 = (c_i - c') * x^-k
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(T) expand_level_kernel(const uint64_t *cur, uint64_t *nxt,
-                                                         size_t in_stride, size_t out_stride,
-                                                         const __grid_constant__ KeyBatch kb,
-                                                         int level, ModTab Mq, ModTab Mp,
-                                                         Consts C) {
-  extern __shared__ uint64_t smem[];
-  uint64_t *sa = smem, *sb = smem + kSmemPoly;
-  uint64_t *s_sig0 = smem + 2 * kSmemPoly;  // sigma(c0), natural index
-  uint64_t *s_sig1 = s_sig0 + kN;           // sigma(c1)
-  const int tid = threadIdx.x;
-  const int node = blockIdx.x, b = blockIdx.y;
-  const int k = 1 << level;
-  const uint64_t g = (uint64_t)(kN / k + 1);
-  const uint64_t q = C.q, p = C.p;
-  const uint64_t *ci = cur + b * in_stride + (size_t)node * 2 * kN;
-
-  // automorphism x -> x^g on both polynomials (scatter to shared memory)
-#pragma unroll
-  for (int e = 0; e < 8; ++e) {
-    const int i = strided_idx(tid, e);
-    const uint32_t j = (uint32_t)(((uint64_t)i * g) & (2 * kN - 1));
-    const uint64_t v0 = ci[i], v1 = ci[kN + i];
-    if (j < (uint32_t)kN) {
-      s_sig0[j] = v0;
-      s_sig1[j] = v1;
-    } else {
-      s_sig0[j - kN] = neg_mod(v0, q);
-      s_sig1[j - kN] = neg_mod(v1, q);
-    }
-  }
-  __syncthreads();
-
-  // T = sigma(c1) in NTT form mod q and mod p
-  uint64_t tq[8], tp[8];
-#pragma unroll
-  for (int e = 0; e < 8; ++e) {
-    const uint64_t v = s_sig1[strided_idx(tid, e)];
-    tq[e] = v;
-    tp[e] = v >= p ? v - p : v;  // q < 2p
-  }
-  ntt_fwd(tq, sa, sb, Mq);
-  ntt_fwd(tp, sa, sb, Mp);
-
-  const uint64_t *key = kb.q[b].galois + (size_t)level * 4 * kN;
-  uint64_t out[2][8];
-#pragma unroll
-  for (int kk = 0; kk < 2; ++kk) {
-    const uint64_t *kq = key + (2 * kk + 0) * kN, *kp = key + (2 * kk + 1) * kN;
-    uint64_t aq[8], ap[8];
-#pragma unroll
-    for (int e = 0; e < 8; ++e) {
-      const int si = slot_idx(tid, e);
-      aq[e] = mul_mod(tq[e], __ldg(kq + si), Mq);
-      ap[e] = mul_mod(tp[e], __ldg(kp + si), Mp);
-    }
-    ntt_inv(aq, sa, sb, Mq);
-    ntt_inv(ap, sa, sb, Mp);
-    // round(X / p) mod q = (x_q + p/2 - ((x_p + p/2) mod p)) * p^-1 mod q
-#pragma unroll
-    for (int e = 0; e < 8; ++e) {
-      const uint64_t rr = add_mod(ap[e], C.p_half, p);
-      const uint64_t v = sub_mod(add_mod(aq[e], C.p_half_mod_q, q), rr, q);
-      out[kk][e] = mul_shoup(v, C.p_inv_q, C.p_inv_q_s, q);
-    }
-  }
-
-  uint64_t *ce = nxt + b * out_stride + (size_t)(2 * node) * 2 * kN;
-  uint64_t *co = ce + 2 * kN;
-#pragma unroll
-  for (int e = 0; e < 8; ++e) {
-    const int i = strided_idx(tid, e);
-    const uint64_t cp0 = add_mod(s_sig0[i], out[0][e], q);
-    const uint64_t cp1 = out[1][e];
-    const uint64_t x0 = ci[i], x1 = ci[kN + i];
-    ce[i] = add_mod(x0, cp0, q);
-    ce[kN + i] = add_mod(x1, cp1, q);
-    const uint64_t d0 = sub_mod(x0, cp0, q), d1 = sub_mod(x1, cp1, q);
-    // multiply by x^-k (utils.cpp:6-26): coefficient i moves to i - k, wrapping
-    // ones are negated (zero stays zero)
-    if (i >= k) {
-      co[i - k] = d0;
-      co[kN + i - k] = d1;
-    } else {
-      co[kN - k + i] = neg_mod(d0, q);
-      co[2 * kN - k + i] = neg_mod(d1, q);
-    }
-  }
-}
-
-// ---------------------------------------------------------------------------
-// RGSW external product core (gsw_eval.cpp:33-106, 184-252):
-// decompose both polynomials of ct (coefficient form, given in the strided
-// distribution) into l digits of base_log2 bits each, NTT every digit, and
-// accumulate digit_j * gsw[j][k] in 128 bits; reduce mod q.  Output: NTT
-// form, slot distribution.
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ void ext_product_core(const uint64_t x[2][8], const uint64_t *gsw,
-                                                 int l, int base_log2, uint64_t *sa,
-                                                 uint64_t *sb, const ModTab &M,
-                                                 uint64_t out[2][8]) {
-  const int tid = threadIdx.x;
-  const uint64_t mask = (1ULL << base_log2) - 1;
-  U128 acc0[8], acc1[8];
-#pragma unroll
-  for (int e = 0; e < 8; ++e) acc0[e] = acc1[e] = U128{0, 0};
-#pragma unroll
-  for (int poly = 0; poly < 2; ++poly) {
-    for (int pp = l - 1; pp >= 0; --pp) {
-      const int j = poly * l + (l - 1 - pp);
-      const int sh = pp * base_log2;
-      uint64_t d[8];
-#pragma unroll
-      for (int e = 0; e < 8; ++e) d[e] = (x[poly][e] >> sh) & mask;
-      ntt_fwd(d, sa, sb, M);
-      const uint64_t *g0 = gsw + (size_t)j * 2 * kN, *g1 = g0 + kN;
-#pragma unroll
-      for (int e = 0; e < 8; ++e) {
-        const int si = slot_idx(tid, e);
-        mac_to(acc0[e], d[e], __ldg(g0 + si));
-        mac_to(acc1[e], d[e], __ldg(g1 + si));
-      }
-    }
-  }
-#pragma unroll
-  for (int e = 0; e < 8; ++e) {
-    out[0][e] = barrett128(acc0[e], M.q, M.mu_lo, M.mu_hi);
-    out[1][e] = barrett128(acc1[e], M.q, M.mu_lo, M.mu_hi);
-  }
-}
-
-// query_to_gsw (gsw_eval.cpp:254-286) for every leaf n1 + j, j < num_cts:
-// row (j % l) of RGSW (j / l) = NTT(ct); row l + (j % l) = RGSW(sk) x ct.
-__global__ void __launch_bounds__(T) query_to_gsw_kernel(const uint64_t *leaves,
-                                                         size_t leaves_stride, uint64_t *gsw_out,
-                                                         size_t gsw_stride,
-                                                         const __grid_constant__ KeyBatch kb,
-                                                         int n1, ModTab M, Consts C) {
-  __shared__ uint64_t sa[kSmemPoly], sb[kSmemPoly];
-  const int tid = threadIdx.x;
-  const int j = blockIdx.x, b = blockIdx.y;
-  const int l = C.l;
-  const int dim = j / l, kk = j % l;
-  const uint64_t *ct = leaves + b * leaves_stride + (size_t)(n1 + j) * 2 * kN;
-  uint64_t *rgsw = gsw_out + b * gsw_stride + (size_t)dim * 2 * l * 2 * kN;
-  uint64_t x[2][8];
-#pragma unroll
-  for (int poly = 0; poly < 2; ++poly)
-#pragma unroll
-    for (int e = 0; e < 8; ++e) x[poly][e] = ct[poly * kN + strided_idx(tid, e)];
-  // first half: the ciphertext itself in NTT form
-  uint64_t *row0 = rgsw + (size_t)kk * 2 * kN;
-#pragma unroll
-  for (int poly = 0; poly < 2; ++poly) {
-    uint64_t r[8];
-#pragma unroll
-    for (int e = 0; e < 8; ++e) r[e] = x[poly][e];
-    ntt_fwd(r, sa, sb, M);
-#pragma unroll
-    for (int e = 0; e < 8; ++e) row0[poly * kN + slot_idx(tid, e)] = r[e];
-  }
-  // second half: external product with RGSW(sk) under the key gadget
-  uint64_t out[2][8];
-  ext_product_core(x, kb.q[b].gsw_key, C.l_key, C.base_log2_key, sa, sb, M, out);
-  uint64_t *row1 = rgsw + (size_t)(l + kk) * 2 * kN;
-#pragma unroll
-  for (int poly = 0; poly < 2; ++poly)
-#pragma unroll
-    for (int e = 0; e < 8; ++e) row1[poly * kN + slot_idx(tid, e)] = out[poly][e];
-}
-
-// other_dim_mux (server.cpp:295-334) for pair j: y -= x; y = RGSW x y; y =
-// INTT(y); x += y.
-__global__ void __launch_bounds__(T) fold_kernel(uint64_t *res, size_t res_stride,
-                                                 const uint64_t *gsw, size_t gsw_stride, int half,
-                                                 ModTab M, Consts C) {
-  __shared__ uint64_t sa[kSmemPoly], sb[kSmemPoly];
-  const int tid = threadIdx.x;
-  const int j = blockIdx.x, b = blockIdx.y;
-  const uint64_t q = C.q;
-  uint64_t *xp = res + b * res_stride + (size_t)j * 2 * kN;
-  const uint64_t *yp = res + b * res_stride + (size_t)(j + half) * 2 * kN;
-  uint64_t d[2][8];
-#pragma unroll
-  for (int poly = 0; poly < 2; ++poly)
-#pragma unroll
-    for (int e = 0; e < 8; ++e) {
-      const int i = poly * kN + strided_idx(tid, e);
-      d[poly][e] = sub_mod(yp[i], xp[i], q);
-    }
-  uint64_t out[2][8];
-  ext_product_core(d, gsw + b * gsw_stride, C.l, C.base_log2, sa, sb, M, out);
-#pragma unroll
-  for (int poly = 0; poly < 2; ++poly) {
-    ntt_inv(out[poly], sa, sb, M);
-#pragma unroll
-    for (int e = 0; e < 8; ++e) {
-      const int i = poly * kN + strided_idx(tid, e);
-      xp[i] = add_mod(xp[i], out[poly][e], q);
-    }
-  }
-}
-
-// ---------------------------------------------------------------------------
 // first dimension
 // ---------------------------------------------------------------------------
 
@@ -433,52 +226,14 @@ __global__ void db_from_aligned_kernel(const uint64_t *aligned, uint64_t *dbs, i
 // launchers
 // ---------------------------------------------------------------------------
 
-constexpr size_t kExpandSmem = (2 * kSmemPoly + 2 * kN) * sizeof(uint64_t);
-
-cudaError_t init_kernel_attributes() {
-  return cudaFuncSetAttribute(expand_level_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)kExpandSmem);
-}
-
 void launch_ntt(const ModTab &M, uint64_t *polys, size_t count, bool inverse, cudaStream_t s) {
   if (!count) return;
   ntt_kernel<<<(unsigned)count, T, 0, s>>>(M, polys, inverse ? 1 : 0);
 }
 
-void launch_expand_level(const uint64_t *cur, uint64_t *nxt, size_t in_stride, size_t out_stride,
-                         const QueryDesc *qd, int level, int live_nodes, int batch,
-                         const ModTab &Mq, const ModTab &Mp, const Consts &C, cudaStream_t s) {
-  for (int b0 = 0; b0 < batch; b0 += kMaxKeyBatch) {
-    const int nb = batch - b0 < kMaxKeyBatch ? batch - b0 : kMaxKeyBatch;
-    KeyBatch kb;
-    for (int i = 0; i < nb; ++i) kb.q[i] = qd[b0 + i];
-    expand_level_kernel<<<dim3(live_nodes, nb), T, kExpandSmem, s>>>(
-        cur + b0 * in_stride, nxt + b0 * out_stride, in_stride, out_stride, kb, level, Mq, Mp, C);
-  }
-}
-
-void launch_query_to_gsw(const uint64_t *leaves, size_t leaves_stride, uint64_t *gsw_out,
-                         size_t gsw_stride, const QueryDesc *qd, int n1, int num_cts, int batch,
-                         const ModTab &Mq, const Consts &C, cudaStream_t s) {
-  if (num_cts <= 0) return;
-  for (int b0 = 0; b0 < batch; b0 += kMaxKeyBatch) {
-    const int nb = batch - b0 < kMaxKeyBatch ? batch - b0 : kMaxKeyBatch;
-    KeyBatch kb;
-    for (int i = 0; i < nb; ++i) kb.q[i] = qd[b0 + i];
-    query_to_gsw_kernel<<<dim3(num_cts, nb), T, 0, s>>>(
-        leaves + b0 * leaves_stride, leaves_stride, gsw_out + b0 * gsw_stride, gsw_stride, kb, n1,
-        Mq, C);
-  }
-}
-
 void launch_query_prep(const uint64_t *leaves, size_t leaves_stride, uint4 *qs, size_t qs_stride,
                        int n1, int batch, const ModTab &Mq, cudaStream_t s) {
   query_prep_kernel<<<dim3(n1, batch), T, 0, s>>>(leaves, leaves_stride, qs, qs_stride, n1, Mq);
-}
-
-void launch_fold(uint64_t *res, size_t res_stride, const uint64_t *gsw, size_t gsw_stride,
-                 int half, int batch, const ModTab &Mq, const Consts &C, cudaStream_t s) {
-  fold_kernel<<<dim3(half, batch), T, 0, s>>>(res, res_stride, gsw, gsw_stride, half, Mq, C);
 }
 
 void launch_modswitch_pack(const uint64_t *res, size_t res_stride, uint64_t *resp,

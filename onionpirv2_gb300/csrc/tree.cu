@@ -1,0 +1,551 @@
+// tree.cu -- the tree-shaped stages of PirServer::make_query on sm_103a:
+// query expansion (fast_expand_qry, server.cpp:383-428), RGSW
+// reconstruction (query_to_gsw, gsw_eval.cpp:254-286) and folding of the
+// further dimensions (other_dim_mux, server.cpp:295-334).
+//
+// Each stage has two forms.  The one-CTA form gives a whole ciphertext to one
+// CTA of 256 threads (least total work; used when a launch has many
+// ciphertexts).  The cluster form splits one ciphertext's independent NTTs
+// over a thread-block cluster and combines the partial results through
+// distributed shared memory, which shortens the dependent chain of NTTs per
+// tree level (used for the narrow levels, where latency dominates).
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdlib>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace cg = cooperative_groups;
+
+namespace opir {
+
+namespace {
+
+constexpr int T = kNttThreads;
+
+// ---------------------------------------------------------------------------
+// expansion: one level of fast_expand_qry (server.cpp:383-428)
+//   c' = apply_galois(c_i, N/k + 1)   (automorphism + key switch with p)
+//   c_2i = c_i + c';  c_2i+1 = (c_i - c') * x^-k
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(T) expand_level_kernel(const uint64_t *cur, uint64_t *nxt,
+                                                         size_t in_stride, size_t out_stride,
+                                                         const __grid_constant__ KeyBatch kb,
+                                                         int level, ModTab Mq, ModTab Mp,
+                                                         Consts C) {
+  extern __shared__ uint64_t smem[];
+  uint64_t *sa = smem, *sb = smem + kSmemPoly;
+  uint64_t *s_sig0 = smem + 2 * kSmemPoly;  // sigma(c0), natural index
+  uint64_t *s_sig1 = s_sig0 + kN;           // sigma(c1)
+  const int tid = threadIdx.x;
+  const int node = blockIdx.x, b = blockIdx.y;
+  const int k = 1 << level;
+  const uint64_t g = (uint64_t)(kN / k + 1);
+  const uint64_t q = C.q, p = C.p;
+  const uint64_t *ci = cur + b * in_stride + (size_t)node * 2 * kN;
+
+  // automorphism x -> x^g on both polynomials (scatter to shared memory)
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const int i = strided_idx(tid, e);
+    const uint32_t j = (uint32_t)(((uint64_t)i * g) & (2 * kN - 1));
+    const uint64_t v0 = ci[i], v1 = ci[kN + i];
+    if (j < (uint32_t)kN) {
+      s_sig0[j] = v0;
+      s_sig1[j] = v1;
+    } else {
+      s_sig0[j - kN] = neg_mod(v0, q);
+      s_sig1[j - kN] = neg_mod(v1, q);
+    }
+  }
+  __syncthreads();
+
+  // T = sigma(c1) in NTT form mod q and mod p
+  uint64_t tq[8], tp[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const uint64_t v = s_sig1[strided_idx(tid, e)];
+    tq[e] = v;
+    tp[e] = v >= p ? v - p : v;  // q < 2p
+  }
+  ntt_fwd(tq, sa, sb, Mq);
+  ntt_fwd(tp, sa, sb, Mp);
+
+  const uint64_t *key = kb.q[b].galois + (size_t)level * 4 * kN;
+  uint64_t out[2][8];
+#pragma unroll
+  for (int kk = 0; kk < 2; ++kk) {
+    const uint64_t *kq = key + (2 * kk + 0) * kN, *kp = key + (2 * kk + 1) * kN;
+    uint64_t aq[8], ap[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const int si = slot_idx(tid, e);
+      aq[e] = mul_mod(tq[e], __ldg(kq + si), Mq);
+      ap[e] = mul_mod(tp[e], __ldg(kp + si), Mp);
+    }
+    ntt_inv(aq, sa, sb, Mq);
+    ntt_inv(ap, sa, sb, Mp);
+    // round(X / p) mod q = (x_q + p/2 - ((x_p + p/2) mod p)) * p^-1 mod q
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const uint64_t rr = add_mod(ap[e], C.p_half, p);
+      const uint64_t v = sub_mod(add_mod(aq[e], C.p_half_mod_q, q), rr, q);
+      out[kk][e] = mul_shoup(v, C.p_inv_q, C.p_inv_q_s, q);
+    }
+  }
+
+  uint64_t *ce = nxt + b * out_stride + (size_t)(2 * node) * 2 * kN;
+  uint64_t *co = ce + 2 * kN;
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const int i = strided_idx(tid, e);
+    const uint64_t cp0 = add_mod(s_sig0[i], out[0][e], q);
+    const uint64_t cp1 = out[1][e];
+    const uint64_t x0 = ci[i], x1 = ci[kN + i];
+    ce[i] = add_mod(x0, cp0, q);
+    ce[kN + i] = add_mod(x1, cp1, q);
+    const uint64_t d0 = sub_mod(x0, cp0, q), d1 = sub_mod(x1, cp1, q);
+    // multiply by x^-k (utils.cpp:6-26): coefficient i moves to i - k, wrapping
+    // ones are negated (zero stays zero)
+    if (i >= k) {
+      co[i - k] = d0;
+      co[kN + i - k] = d1;
+    } else {
+      co[kN - k + i] = neg_mod(d0, q);
+      co[2 * kN - k + i] = neg_mod(d1, q);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// RGSW external product core (gsw_eval.cpp:33-106, 184-252):
+// decompose both polynomials of ct (coefficient form, given in the strided
+// distribution) into l digits of base_log2 bits each, NTT every digit, and
+// accumulate digit_j * gsw[j][k] in 128 bits; reduce mod q.  Output: NTT
+// form, slot distribution.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void ext_product_core(const uint64_t x[2][8], const uint64_t *gsw,
+                                                 int l, int base_log2, uint64_t *sa,
+                                                 uint64_t *sb, const ModTab &M,
+                                                 uint64_t out[2][8]) {
+  const int tid = threadIdx.x;
+  const uint64_t mask = (1ULL << base_log2) - 1;
+  U128 acc0[8], acc1[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) acc0[e] = acc1[e] = U128{0, 0};
+#pragma unroll
+  for (int poly = 0; poly < 2; ++poly) {
+    for (int pp = l - 1; pp >= 0; --pp) {
+      const int j = poly * l + (l - 1 - pp);
+      const int sh = pp * base_log2;
+      uint64_t d[8];
+#pragma unroll
+      for (int e = 0; e < 8; ++e) d[e] = (x[poly][e] >> sh) & mask;
+      ntt_fwd(d, sa, sb, M);
+      const uint64_t *g0 = gsw + (size_t)j * 2 * kN, *g1 = g0 + kN;
+#pragma unroll
+      for (int e = 0; e < 8; ++e) {
+        const int si = slot_idx(tid, e);
+        mac_to(acc0[e], d[e], __ldg(g0 + si));
+        mac_to(acc1[e], d[e], __ldg(g1 + si));
+      }
+    }
+  }
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    out[0][e] = barrett128(acc0[e], M.q, M.mu_lo, M.mu_hi);
+    out[1][e] = barrett128(acc1[e], M.q, M.mu_lo, M.mu_hi);
+  }
+}
+
+// query_to_gsw (gsw_eval.cpp:254-286) for every leaf n1 + j, j < num_cts:
+// row (j % l) of RGSW (j / l) = NTT(ct); row l + (j % l) = RGSW(sk) x ct.
+__global__ void __launch_bounds__(T) query_to_gsw_kernel(const uint64_t *leaves,
+                                                         size_t leaves_stride, uint64_t *gsw_out,
+                                                         size_t gsw_stride,
+                                                         const __grid_constant__ KeyBatch kb,
+                                                         int n1, ModTab M, Consts C) {
+  __shared__ uint64_t sa[kSmemPoly], sb[kSmemPoly];
+  const int tid = threadIdx.x;
+  const int j = blockIdx.x, b = blockIdx.y;
+  const int l = C.l;
+  const int dim = j / l, kk = j % l;
+  const uint64_t *ct = leaves + b * leaves_stride + (size_t)(n1 + j) * 2 * kN;
+  uint64_t *rgsw = gsw_out + b * gsw_stride + (size_t)dim * 2 * l * 2 * kN;
+  uint64_t x[2][8];
+#pragma unroll
+  for (int poly = 0; poly < 2; ++poly)
+#pragma unroll
+    for (int e = 0; e < 8; ++e) x[poly][e] = ct[poly * kN + strided_idx(tid, e)];
+  // first half: the ciphertext itself in NTT form
+  uint64_t *row0 = rgsw + (size_t)kk * 2 * kN;
+#pragma unroll
+  for (int poly = 0; poly < 2; ++poly) {
+    uint64_t r[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) r[e] = x[poly][e];
+    ntt_fwd(r, sa, sb, M);
+#pragma unroll
+    for (int e = 0; e < 8; ++e) row0[poly * kN + slot_idx(tid, e)] = r[e];
+  }
+  // second half: external product with RGSW(sk) under the key gadget
+  uint64_t out[2][8];
+  ext_product_core(x, kb.q[b].gsw_key, C.l_key, C.base_log2_key, sa, sb, M, out);
+  uint64_t *row1 = rgsw + (size_t)(l + kk) * 2 * kN;
+#pragma unroll
+  for (int poly = 0; poly < 2; ++poly)
+#pragma unroll
+    for (int e = 0; e < 8; ++e) row1[poly * kN + slot_idx(tid, e)] = out[poly][e];
+}
+
+// other_dim_mux (server.cpp:295-334) for pair j: y -= x; y = RGSW x y; y =
+// INTT(y); x += y.
+__global__ void __launch_bounds__(T) fold_kernel(uint64_t *res, size_t res_stride,
+                                                 const uint64_t *gsw, size_t gsw_stride, int half,
+                                                 ModTab M, Consts C) {
+  __shared__ uint64_t sa[kSmemPoly], sb[kSmemPoly];
+  const int tid = threadIdx.x;
+  const int j = blockIdx.x, b = blockIdx.y;
+  const uint64_t q = C.q;
+  uint64_t *xp = res + b * res_stride + (size_t)j * 2 * kN;
+  const uint64_t *yp = res + b * res_stride + (size_t)(j + half) * 2 * kN;
+  uint64_t d[2][8];
+#pragma unroll
+  for (int poly = 0; poly < 2; ++poly)
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const int i = poly * kN + strided_idx(tid, e);
+      d[poly][e] = sub_mod(yp[i], xp[i], q);
+    }
+  uint64_t out[2][8];
+  ext_product_core(d, gsw + b * gsw_stride, C.l, C.base_log2, sa, sb, M, out);
+#pragma unroll
+  for (int poly = 0; poly < 2; ++poly) {
+    ntt_inv(out[poly], sa, sb, M);
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const int i = poly * kN + strided_idx(tid, e);
+      xp[i] = add_mod(xp[i], out[poly][e], q);
+    }
+  }
+}
+
+
+// ---------------------------------------------------------------------------
+// cluster forms
+// ---------------------------------------------------------------------------
+
+// Expansion, 4 CTAs per tree node; CTA rank = 2 m + kk handles modulus m
+// (0 = q, 1 = p) and key polynomial kk: NTT_m(sigma(c1)) * K[kk][m], INTT.
+// The q-CTA kk then combines with the p-CTA kk through distributed shared
+// memory and writes polynomial kk of both children (polynomial kk of c'
+// depends on key polynomial kk only).
+__global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(T)
+    expand_cluster_kernel(const uint64_t *cur, uint64_t *nxt, size_t in_stride, size_t out_stride,
+                          const __grid_constant__ KeyBatch kb, int level, ModTab Mq, ModTab Mp,
+                          Consts C) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const int m = rank >> 1, kk = rank & 1;
+  extern __shared__ uint64_t smem[];
+  uint64_t *sa = smem, *sb = smem + kSmemPoly;
+  uint64_t *s_sig = smem + 2 * kSmemPoly;  // sigma(c1), then sigma(c0) (natural index)
+  uint64_t *s_out = s_sig + kN;            // p-CTAs: their inverse transform (natural index)
+  const int tid = threadIdx.x;
+  const int node = blockIdx.x >> 2, b = blockIdx.y;
+  const int k = 1 << level;
+  const uint64_t g = (uint64_t)(kN / k + 1);
+  const uint64_t q = C.q, p = C.p;
+  const uint64_t *ci = cur + b * in_stride + (size_t)node * 2 * kN;
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const int i = strided_idx(tid, e);
+    const uint32_t j = (uint32_t)(((uint64_t)i * g) & (2 * kN - 1));
+    const uint64_t v = ci[kN + i];
+    if (j < (uint32_t)kN)
+      s_sig[j] = v;
+    else
+      s_sig[j - kN] = neg_mod(v, q);
+  }
+  __syncthreads();
+  const ModTab &M = m ? Mp : Mq;
+  uint64_t t[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const uint64_t v = s_sig[strided_idx(tid, e)];
+    t[e] = (m && v >= p) ? v - p : v;  // q < 2p
+  }
+  ntt_fwd(t, sa, sb, M);
+  const uint64_t *key = kb.q[b].galois + (size_t)level * 4 * kN + (size_t)(2 * kk + m) * kN;
+#pragma unroll
+  for (int e = 0; e < 8; ++e) t[e] = mul_mod(t[e], __ldg(key + slot_idx(tid, e)), M);
+  ntt_inv(t, sa, sb, M);
+  if (m == 1) {
+#pragma unroll
+    for (int e = 0; e < 8; ++e) s_out[strided_idx(tid, e)] = t[e];
+  } else if (kk == 0) {
+    // sigma(c0) into s_sig (its last reads were before the transforms' barriers)
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const int i = strided_idx(tid, e);
+      const uint32_t j = (uint32_t)(((uint64_t)i * g) & (2 * kN - 1));
+      const uint64_t v = ci[i];
+      if (j < (uint32_t)kN)
+        s_sig[j] = v;
+      else
+        s_sig[j - kN] = neg_mod(v, q);
+    }
+  }
+  cluster.sync();
+  if (m == 0) {
+    const uint64_t *rp = cluster.map_shared_rank(s_out, 2 + kk);
+    uint64_t *ce = nxt + b * out_stride + (size_t)(2 * node) * 2 * kN + (size_t)kk * kN;
+    uint64_t *co = ce + 2 * kN;
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const int i = strided_idx(tid, e);
+      const uint64_t rr = add_mod(rp[i], C.p_half, p);
+      const uint64_t v = mul_shoup(sub_mod(add_mod(t[e], C.p_half_mod_q, q), rr, q), C.p_inv_q,
+                                   C.p_inv_q_s, q);
+      const uint64_t cp = kk == 0 ? add_mod(s_sig[i], v, q) : v;
+      const uint64_t x = ci[(size_t)kk * kN + i];
+      ce[i] = add_mod(x, cp, q);
+      const uint64_t d = sub_mod(x, cp, q);
+      if (i >= k)
+        co[i - k] = d;
+      else
+        co[kN - k + i] = neg_mod(d, q);
+    }
+  }
+  cluster.sync();
+}
+
+// MAC of digit polynomials (coefficient form, strided distribution, NTT'd
+// here) with RGSW rows, for both output polynomials; 128-bit sums.
+__device__ __forceinline__ void digit_mac(uint64_t d[8], const uint64_t *row, uint64_t *sa,
+                                          uint64_t *sb, const ModTab &M, U128 acc0[8],
+                                          U128 acc1[8]) {
+  const int tid = threadIdx.x;
+  ntt_fwd(d, sa, sb, M);
+  const uint64_t *g0 = row, *g1 = row + kN;
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const int si = slot_idx(tid, e);
+    mac_to(acc0[e], d[e], __ldg(g0 + si));
+    mac_to(acc1[e], d[e], __ldg(g1 + si));
+  }
+}
+
+// Folding (other_dim_mux), 5 CTAs per ciphertext pair (l = 5): CTA r
+// decomposes y - x at digit level l-1-r for both polynomials, transforms and
+// multiplies them with RGSW rows r and l + r, and leaves its partial sums
+// (reduced mod q) in shared memory; CTAs 0 and 1 add the five partials of
+// output polynomial 0 / 1, transform back and add x.
+constexpr int kFoldCluster = 5;
+__global__ void __cluster_dims__(kFoldCluster, 1, 1) __launch_bounds__(T)
+    fold_cluster_kernel(uint64_t *res, size_t res_stride, const uint64_t *gsw, size_t gsw_stride,
+                        int half, ModTab M, Consts C) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int r = (int)cluster.block_rank();
+  extern __shared__ uint64_t smem[];
+  uint64_t *sa = smem, *sb = smem + kSmemPoly;
+  uint64_t *part = smem + 2 * kSmemPoly;  // [kk][slot]
+  const int tid = threadIdx.x;
+  const int j = blockIdx.x / kFoldCluster, b = blockIdx.y;
+  const uint64_t q = C.q;
+  const int l = kFoldCluster;
+  uint64_t *xp = res + b * res_stride + (size_t)j * 2 * kN;
+  const uint64_t *yp = res + b * res_stride + (size_t)(j + half) * 2 * kN;
+  const uint64_t *rgsw = gsw + b * gsw_stride;
+  const int sh = (l - 1 - r) * C.base_log2;
+  const uint64_t mask = (1ULL << C.base_log2) - 1;
+  U128 acc0[8], acc1[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) acc0[e] = acc1[e] = U128{0, 0};
+#pragma unroll
+  for (int poly = 0; poly < 2; ++poly) {
+    uint64_t d[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const int i = poly * kN + strided_idx(tid, e);
+      d[e] = (sub_mod(yp[i], xp[i], q) >> sh) & mask;
+    }
+    digit_mac(d, rgsw + (size_t)(poly * l + r) * 2 * kN, sa, sb, M, acc0, acc1);
+  }
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const int si = slot_idx(tid, e);
+    part[si] = barrett128(acc0[e], q, M.mu_lo, M.mu_hi);
+    part[kN + si] = barrett128(acc1[e], q, M.mu_lo, M.mu_hi);
+  }
+  cluster.sync();
+  if (r < 2) {
+    uint64_t sum[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) sum[e] = 0;
+    for (int rr = 0; rr < kFoldCluster; ++rr) {
+      const uint64_t *pr = cluster.map_shared_rank(part, rr) + (size_t)r * kN;
+#pragma unroll
+      for (int e = 0; e < 8; ++e) sum[e] = add_mod(sum[e], pr[slot_idx(tid, e)], q);
+    }
+    ntt_inv(sum, sa, sb, M);
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const int i = r * kN + strided_idx(tid, e);
+      xp[i] = add_mod(xp[i], sum[e], q);
+    }
+  }
+  cluster.sync();
+}
+
+// RGSW reconstruction (query_to_gsw), 6 CTAs per ciphertext (l_key = 10):
+// CTA 5 writes the first-half row (the ciphertext in NTT form); CTA r < 5
+// handles key digit levels 2r and 2r+1 of both polynomials; CTAs 0 and 1 add
+// the partials of output polynomial 0 / 1 into the second-half row.
+constexpr int kQtgCluster = 6;
+__global__ void __cluster_dims__(kQtgCluster, 1, 1) __launch_bounds__(T)
+    query_to_gsw_cluster_kernel(const uint64_t *leaves, size_t leaves_stride, uint64_t *gsw_out,
+                                size_t gsw_stride, const __grid_constant__ KeyBatch kb, int n1,
+                                ModTab M, Consts C) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int r = (int)cluster.block_rank();
+  extern __shared__ uint64_t smem[];
+  uint64_t *sa = smem, *sb = smem + kSmemPoly;
+  uint64_t *part = smem + 2 * kSmemPoly;
+  const int tid = threadIdx.x;
+  const int jct = blockIdx.x / kQtgCluster, b = blockIdx.y;
+  const int l = C.l, lk = C.l_key;
+  const int dim = jct / l, kk = jct % l;
+  const uint64_t q = C.q;
+  const uint64_t *ct = leaves + b * leaves_stride + (size_t)(n1 + jct) * 2 * kN;
+  uint64_t *rgsw = gsw_out + b * gsw_stride + (size_t)dim * 2 * l * 2 * kN;
+  if (r == kQtgCluster - 1) {
+    uint64_t *row0 = rgsw + (size_t)kk * 2 * kN;
+#pragma unroll
+    for (int poly = 0; poly < 2; ++poly) {
+      uint64_t v[8];
+#pragma unroll
+      for (int e = 0; e < 8; ++e) v[e] = ct[poly * kN + strided_idx(tid, e)];
+      ntt_fwd(v, sa, sb, M);
+#pragma unroll
+      for (int e = 0; e < 8; ++e) row0[poly * kN + slot_idx(tid, e)] = v[e];
+    }
+  } else {
+    const uint64_t *key = kb.q[b].gsw_key;
+    const uint64_t mask = (1ULL << C.base_log2_key) - 1;
+    U128 acc0[8], acc1[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) acc0[e] = acc1[e] = U128{0, 0};
+#pragma unroll
+    for (int poly = 0; poly < 2; ++poly) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int level = 2 * r + h;          // row index within the poly's l_key rows
+        const int sh = (lk - 1 - level) * C.base_log2_key;
+        uint64_t d[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) d[e] = (ct[poly * kN + strided_idx(tid, e)] >> sh) & mask;
+        digit_mac(d, key + (size_t)(poly * lk + level) * 2 * kN, sa, sb, M, acc0, acc1);
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const int si = slot_idx(tid, e);
+      part[si] = barrett128(acc0[e], q, M.mu_lo, M.mu_hi);
+      part[kN + si] = barrett128(acc1[e], q, M.mu_lo, M.mu_hi);
+    }
+  }
+  cluster.sync();
+  if (r < 2) {
+    uint64_t *row1 = rgsw + (size_t)(l + kk) * 2 * kN + (size_t)r * kN;
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const int si = slot_idx(tid, e);
+      uint64_t sum = 0;
+      for (int rr = 0; rr < kQtgCluster - 1; ++rr)
+        sum = add_mod(sum, cluster.map_shared_rank(part, rr)[(size_t)r * kN + si], q);
+      row1[si] = sum;
+    }
+  }
+  cluster.sync();
+}
+
+int g_cluster_threshold = 304;  // use the cluster form below this many CTA-sized items
+
+}  // namespace
+
+constexpr size_t kExpandSmem = (2 * kSmemPoly + 2 * kN) * sizeof(uint64_t);
+
+constexpr size_t kClusterSmem = (2 * kSmemPoly + 2 * kN) * sizeof(uint64_t);
+
+cudaError_t init_kernel_attributes() {
+  cudaError_t e;
+  if ((e = cudaFuncSetAttribute(expand_level_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)kExpandSmem)) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(expand_cluster_kernel,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)kClusterSmem)) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(fold_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)kClusterSmem)) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(query_to_gsw_cluster_kernel,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)kClusterSmem)) != cudaSuccess)
+    return e;
+  g_cluster_threshold = 304;
+  if (const char *v = getenv("OPIR_CLUSTER_THRESHOLD")) g_cluster_threshold = atoi(v);
+  return cudaSuccess;
+}
+
+void launch_expand_level(const uint64_t *cur, uint64_t *nxt, size_t in_stride, size_t out_stride,
+                         const QueryDesc *qd, int level, int live_nodes, int batch,
+                         const ModTab &Mq, const ModTab &Mp, const Consts &C, cudaStream_t s) {
+  for (int b0 = 0; b0 < batch; b0 += kMaxKeyBatch) {
+    const int nb = batch - b0 < kMaxKeyBatch ? batch - b0 : kMaxKeyBatch;
+    KeyBatch kb;
+    for (int i = 0; i < nb; ++i) kb.q[i] = qd[b0 + i];
+    if (live_nodes * nb < g_cluster_threshold)
+      expand_cluster_kernel<<<dim3(4 * live_nodes, nb), T, kClusterSmem, s>>>(
+          cur + b0 * in_stride, nxt + b0 * out_stride, in_stride, out_stride, kb, level, Mq, Mp,
+          C);
+    else
+      expand_level_kernel<<<dim3(live_nodes, nb), T, kExpandSmem, s>>>(
+          cur + b0 * in_stride, nxt + b0 * out_stride, in_stride, out_stride, kb, level, Mq, Mp,
+          C);
+  }
+}
+
+void launch_query_to_gsw(const uint64_t *leaves, size_t leaves_stride, uint64_t *gsw_out,
+                         size_t gsw_stride, const QueryDesc *qd, int n1, int num_cts, int batch,
+                         const ModTab &Mq, const Consts &C, cudaStream_t s) {
+  if (num_cts <= 0) return;
+  for (int b0 = 0; b0 < batch; b0 += kMaxKeyBatch) {
+    const int nb = batch - b0 < kMaxKeyBatch ? batch - b0 : kMaxKeyBatch;
+    KeyBatch kb;
+    for (int i = 0; i < nb; ++i) kb.q[i] = qd[b0 + i];
+    if (C.l_key == 2 * (kQtgCluster - 1) && num_cts * nb < g_cluster_threshold)
+      query_to_gsw_cluster_kernel<<<dim3(kQtgCluster * num_cts, nb), T, kClusterSmem, s>>>(
+          leaves + b0 * leaves_stride, leaves_stride, gsw_out + b0 * gsw_stride, gsw_stride, kb,
+          n1, Mq, C);
+    else
+      query_to_gsw_kernel<<<dim3(num_cts, nb), T, 0, s>>>(
+          leaves + b0 * leaves_stride, leaves_stride, gsw_out + b0 * gsw_stride, gsw_stride, kb,
+          n1, Mq, C);
+  }
+}
+
+void launch_fold(uint64_t *res, size_t res_stride, const uint64_t *gsw, size_t gsw_stride,
+                 int half, int batch, const ModTab &Mq, const Consts &C, cudaStream_t s) {
+  if (C.l == kFoldCluster && half * batch < g_cluster_threshold)
+    fold_cluster_kernel<<<dim3(kFoldCluster * half, batch), T, kClusterSmem, s>>>(
+        res, res_stride, gsw, gsw_stride, half, Mq, C);
+  else
+    fold_kernel<<<dim3(half, batch), T, 0, s>>>(res, res_stride, gsw, gsw_stride, half, Mq, C);
+}
+
+}  // namespace opir

@@ -190,3 +190,37 @@ def test_scan_configs_and_shapes(oracle_lib, gpu_lib, monkeypatch, shape, cfg):
     plain, _ = o.decrypt(sk, tr["resp"], 2)
     assert np.array_equal(o.entry_from_plain(idx, plain), server.direct_get_entry(idx))
     server.close()
+
+
+@pytest.mark.parametrize("threshold", [0, 1 << 30])
+def test_one_cta_and_cluster_tree_forms(oracle_lib, gpu_lib, monkeypatch, threshold):
+    """Expansion, RGSW reconstruction and folding give the oracle's results
+    in both kernel forms (one CTA per ciphertext, or a cluster of CTAs)."""
+    from onionpirv2_gb300 import PirParams, PirServer
+    monkeypatch.setenv("OPIR_CLUSTER_THRESHOLD", str(threshold))
+    o = oracle_lib.Oracle(4096, 256)
+    P = o.P
+    server = PirServer(PirParams(num_entries=4096, max_fst_dim=256))
+    server.gen_data(8)
+    db = o.build_db(8)
+    ids, queries, refs = [], [], []
+    for j in range(3):
+        sk, gk, gswk = make_client(o, 40 + j)
+        server.set_client_galois_key(j, gk)
+        server.set_client_gsw_key(j, gswk)
+        qry = o.make_query(sk, 60 + j, 1000 * j + 7)
+        ids.append(j)
+        queries.append(qry)
+        refs.append(o.make_query_server(db, gk, o.gsw_key_to_ntt(gswk), qry)[0])
+        tr = server.make_query_trace(j, qry)
+        leaves = o.expand(qry, gk)
+        assert np.array_equal(tr["leaves"], leaves)
+        gsw_ntt = o.gsw_key_to_ntt(gswk)
+        for i in range(1, P.ndim):
+            s = P.n1 + (i - 1) * P.l
+            assert np.array_equal(tr["gsw"][i - 1], o.query_to_gsw(leaves[s:s + P.l], gsw_ntt))
+        assert np.array_equal(tr["resp"], refs[-1])
+    resp, _ = server.make_query_batch(ids, np.stack(queries))
+    for j in range(3):
+        assert np.array_equal(resp[j], refs[j])
+    server.close()
