@@ -87,26 +87,27 @@ __device__ __forceinline__ uint64_t mul_mod(uint64_t a, uint64_t b, const ModTab
 //   (the transform SEAL's ntt_negacyclic_harvey computes).
 // Inverse: Gentleman-Sande, the exact inverse, scaled by N^-1.
 //
-// The 11 radix-2 stages run as: bits 10-8 in registers, exchange through
-// shared memory, bits 7-5 in registers, exchange, bits 4-2 in registers,
-// then bits 1-0 with warp shuffles (after the second exchange those index
-// bits are lane bits).  Two distributions of coefficients over threads:
-//   strided:  r[e] <-> index tid + 256 e          (coalesced global access)
-//   slot:     r[e] <-> index (tid>>2)<<5 | e<<2 | (tid&3)
+// Butterflies are Harvey's lazy ones: forward values live in [0, 4q),
+// inverse values in [0, 2q) (q < 2^60, so 4q < 2^62); both transforms end
+// with a full reduction, so every output is in [0, q).
+//
+// The 11 radix-2 stages run as four register passes -- index bits 10-8,
+// 7-5, 4-2 and 1-0 -- separated by three shared-memory exchanges.  Two
+// distributions of coefficients over threads:
+//   strided:  r[e] <-> index tid + 256 e      (coalesced global access)
+//   slot:     r[e] <-> index 8 tid + e        (8 consecutive NTT slots)
 // The forward transform maps strided -> slot, the inverse slot -> strided.
-// Pointwise work between them stays in the slot distribution, reading
-// operands from global memory at slot_idx() (full 32-byte sectors).
+// Pointwise work between them stays in the slot distribution and reads its
+// operands with 16-byte vector loads (ldg_slot8).
 // ---------------------------------------------------------------------------
 
-// shared-memory index with 4 pad words per 32: conflict-free for every
-// exchange pattern used here
-__device__ __forceinline__ int spad(int i) { return i + ((i >> 5) << 2); }
-constexpr int kSmemPoly = kN + (kN / 32) * 4;  // padded polynomial footprint (u64 words)
+// shared-memory index with 2 pad words per 16: every exchange pattern below
+// is bank-conflict free (the slot exchange uses 16-byte accesses)
+__device__ __forceinline__ int spad(int i) { return i + ((i >> 4) << 1); }
+constexpr int kSmemPoly = kN + (kN / 16) * 2;  // padded polynomial footprint (u64 words)
 
 __device__ __forceinline__ int strided_idx(int tid, int e) { return tid + kNttThreads * e; }
-__device__ __forceinline__ int slot_idx(int tid, int e) {
-  return ((tid >> 2) << 5) | (e << 2) | (tid & 3);
-}
+__device__ __forceinline__ int slot_idx(int tid, int e) { return 8 * tid + e; }
 // index of element e of thread tid in the register pass whose 3 bits start at lo
 __device__ __forceinline__ int pass_index(int tid, int e, int lo) {
   const int low = tid & ((1 << lo) - 1);
@@ -114,20 +115,32 @@ __device__ __forceinline__ int pass_index(int tid, int e, int lo) {
   return (high << (lo + 3)) | (e << lo) | low;
 }
 
-__device__ __forceinline__ void ct_bf(uint64_t &x, uint64_t &y, ulonglong2 w, uint64_t q) {
-  const uint64_t v = mul_shoup(y, w.x, w.y, q);
-  const uint64_t u = x;
-  x = add_mod(u, v, q);
-  y = sub_mod(u, v, q);
+// x * w mod q up to one extra q: result in [0, 2q) for any x < 2^64
+__device__ __forceinline__ uint64_t mul_shoup_lazy(uint64_t x, uint64_t w, uint64_t ws, uint64_t q) {
+  const uint64_t hq = __umul64hi(x, ws);
+  return x * w - hq * q;
 }
-__device__ __forceinline__ void gs_bf(uint64_t &x, uint64_t &y, ulonglong2 w, uint64_t q) {
+
+// lazy CT butterfly: inputs and outputs in [0, 4q)
+__device__ __forceinline__ void ct_bf(uint64_t &x, uint64_t &y, ulonglong2 w, uint64_t q,
+                                      uint64_t q2) {
+  const uint64_t u = x >= q2 ? x - q2 : x;
+  const uint64_t t = mul_shoup_lazy(y, w.x, w.y, q);
+  x = u + t;
+  y = u - t + q2;
+}
+// lazy GS butterfly: inputs and outputs in [0, 2q)
+__device__ __forceinline__ void gs_bf(uint64_t &x, uint64_t &y, ulonglong2 w, uint64_t q,
+                                      uint64_t q2) {
   const uint64_t u = x, v = y;
-  x = add_mod(u, v, q);
-  y = mul_shoup(sub_mod(u, v, q), w.x, w.y, q);
+  const uint64_t s = u + v;
+  x = s >= q2 ? s - q2 : s;
+  y = mul_shoup_lazy(u - v + q2, w.x, w.y, q);
 }
 
 // Three CT stages (bits lo+2, lo+1, lo).  Stage on bit b: twiddle m + (idx >> (b+1)), m = 2^(10-b).
-__device__ __forceinline__ void ct_pass3(uint64_t r[8], int tid, int lo, const ulonglong2 *tw, uint64_t q) {
+__device__ __forceinline__ void ct_pass3(uint64_t r[8], int tid, int lo, const ulonglong2 *tw,
+                                         uint64_t q, uint64_t q2) {
   const int base = pass_index(tid, 0, lo);
 #pragma unroll
   for (int s = 2; s >= 0; --s) {
@@ -138,11 +151,12 @@ __device__ __forceinline__ void ct_pass3(uint64_t r[8], int tid, int lo, const u
     for (int e = 0; e < 8; ++e) {
       if (e & half) continue;
       const int idx = base | (e << lo);
-      ct_bf(r[e], r[e | half], __ldg(tw + m + (idx >> (b + 1))), q);
+      ct_bf(r[e], r[e | half], __ldg(tw + m + (idx >> (b + 1))), q, q2);
     }
   }
 }
-__device__ __forceinline__ void gs_pass3(uint64_t r[8], int tid, int lo, const ulonglong2 *tw, uint64_t q) {
+__device__ __forceinline__ void gs_pass3(uint64_t r[8], int tid, int lo, const ulonglong2 *tw,
+                                         uint64_t q, uint64_t q2) {
   const int base = pass_index(tid, 0, lo);
 #pragma unroll
   for (int s = 0; s <= 2; ++s) {
@@ -153,43 +167,36 @@ __device__ __forceinline__ void gs_pass3(uint64_t r[8], int tid, int lo, const u
     for (int e = 0; e < 8; ++e) {
       if (e & half) continue;
       const int idx = base | (e << lo);
-      gs_bf(r[e], r[e | half], __ldg(tw + m + (idx >> (b + 1))), q);
+      gs_bf(r[e], r[e | half], __ldg(tw + m + (idx >> (b + 1))), q, q2);
     }
   }
 }
-
-__device__ __forceinline__ uint64_t shfl_xor64(uint64_t v, int mask) {
-  return __shfl_xor_sync(0xffffffffu, v, mask);
-}
-
-// CT stage on index bit b in {0, 1} (== lane bit b in the slot distribution).
-__device__ __forceinline__ void ct_lane_stage(uint64_t r[8], int tid, int b, const ulonglong2 *tw, uint64_t q) {
-  const int m = 1 << (10 - b);
-  const bool hi = (tid >> b) & 1;
+// Stages on bits 1 and 0: the thread's slots 8 tid .. 8 tid + 7 form the
+// radix-4 groups g = 2 tid and 2 tid + 1.
+__device__ __forceinline__ void ct_pass2(uint64_t r[8], int tid, const ulonglong2 *tw, uint64_t q,
+                                         uint64_t q2) {
 #pragma unroll
-  for (int e = 0; e < 8; ++e) {
-    const int idx = slot_idx(tid, e);
-    const ulonglong2 w = __ldg(tw + m + (idx >> (b + 1)));
-    const uint64_t own = r[e];
-    const uint64_t send = hi ? mul_shoup(own, w.x, w.y, q) : own;
-    const uint64_t recv = shfl_xor64(send, 1 << b);
-    r[e] = hi ? sub_mod(recv, send, q) : add_mod(own, recv, q);
+  for (int gsub = 0; gsub < 2; ++gsub) {
+    const int g = 2 * tid + gsub;
+    uint64_t *x = r + 4 * gsub;
+    const ulonglong2 w1 = __ldg(tw + 512 + g);
+    ct_bf(x[0], x[2], w1, q, q2);
+    ct_bf(x[1], x[3], w1, q, q2);
+    ct_bf(x[0], x[1], __ldg(tw + 1024 + 2 * g), q, q2);
+    ct_bf(x[2], x[3], __ldg(tw + 1024 + 2 * g + 1), q, q2);
   }
 }
-__device__ __forceinline__ void gs_lane_stage(uint64_t r[8], int tid, int b, const ulonglong2 *tw, uint64_t q) {
-  const int m = 1 << (10 - b);
-  const bool hi = (tid >> b) & 1;
+__device__ __forceinline__ void gs_pass2(uint64_t r[8], int tid, const ulonglong2 *tw, uint64_t q,
+                                         uint64_t q2) {
 #pragma unroll
-  for (int e = 0; e < 8; ++e) {
-    const int idx = slot_idx(tid, e);
-    const uint64_t own = r[e];
-    const uint64_t recv = shfl_xor64(own, 1 << b);
-    if (hi) {
-      const ulonglong2 w = __ldg(tw + m + (idx >> (b + 1)));
-      r[e] = mul_shoup(sub_mod(recv, own, q), w.x, w.y, q);
-    } else {
-      r[e] = add_mod(own, recv, q);
-    }
+  for (int gsub = 0; gsub < 2; ++gsub) {
+    const int g = 2 * tid + gsub;
+    uint64_t *x = r + 4 * gsub;
+    gs_bf(x[0], x[1], __ldg(tw + 1024 + 2 * g), q, q2);
+    gs_bf(x[2], x[3], __ldg(tw + 1024 + 2 * g + 1), q, q2);
+    const ulonglong2 w1 = __ldg(tw + 512 + g);
+    gs_bf(x[0], x[2], w1, q, q2);
+    gs_bf(x[1], x[3], w1, q, q2);
   }
 }
 
@@ -201,44 +208,89 @@ __device__ __forceinline__ void load_pass(const uint64_t *s, uint64_t r[8], int 
 #pragma unroll
   for (int e = 0; e < 8; ++e) r[e] = s[spad(pass_index(tid, e, lo))];
 }
+__device__ __forceinline__ void store_slots(uint64_t *s, const uint64_t r[8], int tid) {
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+    *reinterpret_cast<ulonglong2 *>(s + spad(8 * tid + 2 * j)) = make_ulonglong2(r[2 * j], r[2 * j + 1]);
+}
+__device__ __forceinline__ void load_slots(const uint64_t *s, uint64_t r[8], int tid) {
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const ulonglong2 v = *reinterpret_cast<const ulonglong2 *>(s + spad(8 * tid + 2 * j));
+    r[2 * j] = v.x;
+    r[2 * j + 1] = v.y;
+  }
+}
 
-// Forward NTT: r strided -> r slot.  sa, sb: two shared buffers of
-// kSmemPoly words each (double buffering: two barriers per transform).
-// All 256 threads of the calling group must participate.
+// 8 consecutive slots of a global array (16-byte aligned) for this thread
+__device__ __forceinline__ void ldg_slot8(const uint64_t *base, uint64_t v[8]) {
+  const ulonglong2 *p = reinterpret_cast<const ulonglong2 *>(base) + 4 * (threadIdx.x & (kNttThreads - 1));
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const ulonglong2 t = __ldg(p + j);
+    v[2 * j] = t.x;
+    v[2 * j + 1] = t.y;
+  }
+}
+__device__ __forceinline__ void stg_slot8(uint64_t *base, const uint64_t v[8]) {
+  ulonglong2 *p = reinterpret_cast<ulonglong2 *>(base) + 4 * (threadIdx.x & (kNttThreads - 1));
+#pragma unroll
+  for (int j = 0; j < 4; ++j) p[j] = make_ulonglong2(v[2 * j], v[2 * j + 1]);
+}
+
+// Forward NTT: r strided (values < 4q) -> r slot (fully reduced).  sa, sb:
+// two shared buffers of kSmemPoly words; all 256 threads of the group take
+// part; ends with a barrier so sa/sb may be reused at once.
 __device__ __forceinline__ void ntt_fwd(uint64_t r[8], uint64_t *sa, uint64_t *sb,
                                         const ulonglong2 *tw, uint64_t q) {
   const int tid = threadIdx.x & (kNttThreads - 1);
-  ct_pass3(r, tid, 8, tw, q);
+  const uint64_t q2 = 2 * q;
+  ct_pass3(r, tid, 8, tw, q, q2);
   store_pass(sa, r, tid, 8);
   __syncthreads();
   load_pass(sa, r, tid, 5);
-  ct_pass3(r, tid, 5, tw, q);
+  ct_pass3(r, tid, 5, tw, q, q2);
   store_pass(sb, r, tid, 5);
   __syncthreads();
   load_pass(sb, r, tid, 2);
-  ct_pass3(r, tid, 2, tw, q);
-  ct_lane_stage(r, tid, 1, tw, q);
-  ct_lane_stage(r, tid, 0, tw, q);
+  ct_pass3(r, tid, 2, tw, q, q2);
+  store_pass(sa, r, tid, 2);
+  __syncthreads();
+  load_slots(sa, r, tid);
+  ct_pass2(r, tid, tw, q, q2);
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    uint64_t v = r[e] >= q2 ? r[e] - q2 : r[e];
+    r[e] = v >= q ? v - q : v;
+  }
+  __syncthreads();
 }
 
-// Inverse NTT: r slot -> r strided, scaled by N^-1.
+// Inverse NTT: r slot (values < 2q) -> r strided (fully reduced), scaled by N^-1.
 __device__ __forceinline__ void ntt_inv(uint64_t r[8], uint64_t *sa, uint64_t *sb,
                                         const ulonglong2 *tw, uint64_t q, uint64_t n_inv,
                                         uint64_t n_inv_s) {
   const int tid = threadIdx.x & (kNttThreads - 1);
-  gs_lane_stage(r, tid, 0, tw, q);
-  gs_lane_stage(r, tid, 1, tw, q);
-  gs_pass3(r, tid, 2, tw, q);
-  store_pass(sa, r, tid, 2);
+  const uint64_t q2 = 2 * q;
+  gs_pass2(r, tid, tw, q, q2);
+  store_slots(sa, r, tid);
   __syncthreads();
-  load_pass(sa, r, tid, 5);
-  gs_pass3(r, tid, 5, tw, q);
-  store_pass(sb, r, tid, 5);
+  load_pass(sa, r, tid, 2);
+  gs_pass3(r, tid, 2, tw, q, q2);
+  store_pass(sb, r, tid, 2);
   __syncthreads();
-  load_pass(sb, r, tid, 8);
-  gs_pass3(r, tid, 8, tw, q);
+  load_pass(sb, r, tid, 5);
+  gs_pass3(r, tid, 5, tw, q, q2);
+  store_pass(sa, r, tid, 5);
+  __syncthreads();
+  load_pass(sa, r, tid, 8);
+  gs_pass3(r, tid, 8, tw, q, q2);
 #pragma unroll
-  for (int e = 0; e < 8; ++e) r[e] = mul_shoup(r[e], n_inv, n_inv_s, q);
+  for (int e = 0; e < 8; ++e) {
+    const uint64_t v = mul_shoup_lazy(r[e], n_inv, n_inv_s, q);
+    r[e] = v >= q ? v - q : v;
+  }
+  __syncthreads();
 }
 
 __device__ __forceinline__ void ntt_fwd(uint64_t r[8], uint64_t *sa, uint64_t *sb, const ModTab &M) {

@@ -29,11 +29,9 @@ __global__ void __launch_bounds__(T) ntt_kernel(ModTab M, uint64_t *polys, int i
 #pragma unroll
     for (int e = 0; e < 8; ++e) r[e] = p[strided_idx(tid, e)];
     ntt_fwd(r, sa, sb, M);
-#pragma unroll
-    for (int e = 0; e < 8; ++e) p[slot_idx(tid, e)] = r[e];
+    stg_slot8(p, r);
   } else {
-#pragma unroll
-    for (int e = 0; e < 8; ++e) r[e] = p[slot_idx(tid, e)];
+    ldg_slot8(p, r);
     ntt_inv(r, sa, sb, M);
 #pragma unroll
     for (int e = 0; e < 8; ++e) p[strided_idx(tid, e)] = r[e];

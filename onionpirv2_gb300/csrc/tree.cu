@@ -80,11 +80,12 @@ __global__ void __launch_bounds__(T) expand_level_kernel(const uint64_t *cur, ui
   for (int kk = 0; kk < 2; ++kk) {
     const uint64_t *kq = key + (2 * kk + 0) * kN, *kp = key + (2 * kk + 1) * kN;
     uint64_t aq[8], ap[8];
+    ldg_slot8(kq, aq);
+    ldg_slot8(kp, ap);
 #pragma unroll
     for (int e = 0; e < 8; ++e) {
-      const int si = slot_idx(tid, e);
-      aq[e] = mul_mod(tq[e], __ldg(kq + si), Mq);
-      ap[e] = mul_mod(tp[e], __ldg(kp + si), Mp);
+      aq[e] = mul_mod(tq[e], aq[e], Mq);
+      ap[e] = mul_mod(tp[e], ap[e], Mp);
     }
     ntt_inv(aq, sa, sb, Mq);
     ntt_inv(ap, sa, sb, Mp);
@@ -146,11 +147,13 @@ __device__ __forceinline__ void ext_product_core(const uint64_t x[2][8], const u
       for (int e = 0; e < 8; ++e) d[e] = (x[poly][e] >> sh) & mask;
       ntt_fwd(d, sa, sb, M);
       const uint64_t *g0 = gsw + (size_t)j * 2 * kN, *g1 = g0 + kN;
+      uint64_t w0[8], w1[8];
+      ldg_slot8(g0, w0);
+      ldg_slot8(g1, w1);
 #pragma unroll
       for (int e = 0; e < 8; ++e) {
-        const int si = slot_idx(tid, e);
-        mac_to(acc0[e], d[e], __ldg(g0 + si));
-        mac_to(acc1[e], d[e], __ldg(g1 + si));
+        mac_to(acc0[e], d[e], w0[e]);
+        mac_to(acc1[e], d[e], w1[e]);
       }
     }
   }
@@ -189,7 +192,7 @@ __global__ void __launch_bounds__(T) query_to_gsw_kernel(const uint64_t *leaves,
     for (int e = 0; e < 8; ++e) r[e] = x[poly][e];
     ntt_fwd(r, sa, sb, M);
 #pragma unroll
-    for (int e = 0; e < 8; ++e) row0[poly * kN + slot_idx(tid, e)] = r[e];
+    stg_slot8(row0 + poly * kN, r);
   }
   // second half: external product with RGSW(sk) under the key gadget
   uint64_t out[2][8];
@@ -198,7 +201,7 @@ __global__ void __launch_bounds__(T) query_to_gsw_kernel(const uint64_t *leaves,
 #pragma unroll
   for (int poly = 0; poly < 2; ++poly)
 #pragma unroll
-    for (int e = 0; e < 8; ++e) row1[poly * kN + slot_idx(tid, e)] = out[poly][e];
+    stg_slot8(row1 + poly * kN, out[poly]);
 }
 
 // other_dim_mux (server.cpp:295-334) for pair j: y -= x; y = RGSW x y; y =
@@ -281,7 +284,12 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(T)
   ntt_fwd(t, sa, sb, M);
   const uint64_t *key = kb.q[b].galois + (size_t)level * 4 * kN + (size_t)(2 * kk + m) * kN;
 #pragma unroll
-  for (int e = 0; e < 8; ++e) t[e] = mul_mod(t[e], __ldg(key + slot_idx(tid, e)), M);
+  {
+    uint64_t kv[8];
+    ldg_slot8(key, kv);
+#pragma unroll
+    for (int e = 0; e < 8; ++e) t[e] = mul_mod(t[e], kv[e], M);
+  }
   ntt_inv(t, sa, sb, M);
   if (m == 1) {
 #pragma unroll
@@ -330,12 +338,13 @@ __device__ __forceinline__ void digit_mac(uint64_t d[8], const uint64_t *row, ui
                                           U128 acc1[8]) {
   const int tid = threadIdx.x;
   ntt_fwd(d, sa, sb, M);
-  const uint64_t *g0 = row, *g1 = row + kN;
+  uint64_t w0[8], w1[8];
+  ldg_slot8(row, w0);
+  ldg_slot8(row + kN, w1);
 #pragma unroll
   for (int e = 0; e < 8; ++e) {
-    const int si = slot_idx(tid, e);
-    mac_to(acc0[e], d[e], __ldg(g0 + si));
-    mac_to(acc1[e], d[e], __ldg(g1 + si));
+    mac_to(acc0[e], d[e], w0[e]);
+    mac_to(acc1[e], d[e], w1[e]);
   }
 }
 
@@ -431,7 +440,7 @@ __global__ void __cluster_dims__(kQtgCluster, 1, 1) __launch_bounds__(T)
       for (int e = 0; e < 8; ++e) v[e] = ct[poly * kN + strided_idx(tid, e)];
       ntt_fwd(v, sa, sb, M);
 #pragma unroll
-      for (int e = 0; e < 8; ++e) row0[poly * kN + slot_idx(tid, e)] = v[e];
+      stg_slot8(row0 + poly * kN, v);
     }
   } else {
     const uint64_t *key = kb.q[b].gsw_key;
