@@ -482,7 +482,13 @@ __global__ void __cluster_dims__(kQtgCluster, 1, 1) __launch_bounds__(T)
   cluster.sync();
 }
 
-int g_cluster_threshold = 304;  // use the cluster form below this many CTA-sized items
+// Cluster form below these many ciphertexts per launch (batch included);
+// one-CTA form at or above.  From per-launch timings on GB300: the cluster
+// expansion wins at every level of a single query, the cluster fold only on
+// the narrow levels (<= 32 pairs), RGSW reconstruction is even.
+int g_expand_threshold = 1024;
+int g_fold_threshold = 48;
+int g_qtg_threshold = 40;
 
 }  // namespace
 
@@ -506,8 +512,11 @@ cudaError_t init_kernel_attributes() {
                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)kClusterSmem)) != cudaSuccess)
     return e;
-  g_cluster_threshold = 304;
-  if (const char *v = getenv("OPIR_CLUSTER_THRESHOLD")) g_cluster_threshold = atoi(v);
+  g_expand_threshold = 1024;
+  g_fold_threshold = 48;
+  g_qtg_threshold = 40;
+  if (const char *v = getenv("OPIR_CLUSTER_THRESHOLD"))  // one threshold for all (tests, sweeps)
+    g_expand_threshold = g_fold_threshold = g_qtg_threshold = atoi(v);
   return cudaSuccess;
 }
 
@@ -518,7 +527,7 @@ void launch_expand_level(const uint64_t *cur, uint64_t *nxt, size_t in_stride, s
     const int nb = batch - b0 < kMaxKeyBatch ? batch - b0 : kMaxKeyBatch;
     KeyBatch kb;
     for (int i = 0; i < nb; ++i) kb.q[i] = qd[b0 + i];
-    if (live_nodes * nb < g_cluster_threshold)
+    if (live_nodes * nb < g_expand_threshold)
       expand_cluster_kernel<<<dim3(4 * live_nodes, nb), T, kClusterSmem, s>>>(
           cur + b0 * in_stride, nxt + b0 * out_stride, in_stride, out_stride, kb, level, Mq, Mp,
           C);
@@ -537,7 +546,7 @@ void launch_query_to_gsw(const uint64_t *leaves, size_t leaves_stride, uint64_t 
     const int nb = batch - b0 < kMaxKeyBatch ? batch - b0 : kMaxKeyBatch;
     KeyBatch kb;
     for (int i = 0; i < nb; ++i) kb.q[i] = qd[b0 + i];
-    if (C.l_key == 2 * (kQtgCluster - 1) && num_cts * nb < g_cluster_threshold)
+    if (C.l_key == 2 * (kQtgCluster - 1) && num_cts * nb < g_qtg_threshold)
       query_to_gsw_cluster_kernel<<<dim3(kQtgCluster * num_cts, nb), T, kClusterSmem, s>>>(
           leaves + b0 * leaves_stride, leaves_stride, gsw_out + b0 * gsw_stride, gsw_stride, kb,
           n1, Mq, C);
@@ -550,7 +559,7 @@ void launch_query_to_gsw(const uint64_t *leaves, size_t leaves_stride, uint64_t 
 
 void launch_fold(uint64_t *res, size_t res_stride, const uint64_t *gsw, size_t gsw_stride,
                  int half, int batch, const ModTab &Mq, const Consts &C, cudaStream_t s) {
-  if (C.l == kFoldCluster && half * batch < g_cluster_threshold)
+  if (C.l == kFoldCluster && half * batch < g_fold_threshold)
     fold_cluster_kernel<<<dim3(kFoldCluster * half, batch), T, kClusterSmem, s>>>(
         res, res_stride, gsw, gsw_stride, half, Mq, C);
   else
