@@ -122,6 +122,19 @@ int opir_make_query_trace(opir_ctx *ctx, uint32_t db_id, uint64_t client_id,
                           const uint64_t *query, uint64_t *leaves, uint64_t *gsw,
                           uint64_t *first_dim, uint64_t *resp, uint8_t *packed);
 
+/* First dimension only, without allocating device memory (no counterpart
+ * in the reference; there it is the inside of evaluate_first_dim,
+ * server.cpp:124-175).  d_fst_cts: the n1 expanded selection ciphertexts
+ * [n1][2][N] (device, coefficient form); d_out: the n_rest results
+ * [n_rest][2][N] (device, coefficient form).  For callers that cannot call
+ * cudaMalloc: the scan's query operand lives in a 16 MiB static device
+ * array, so n1 <= 512 (larger databases get OPIR_ERR_ARG).  The first call
+ * on a device looks up that array's address (cudaGetSymbolAddress), so make
+ * it before any stream capture.  Asynchronous on the context stream; all
+ * calls share the array, so calls that overlap on the GPU race. */
+int opir_first_dim_noalloc(opir_ctx *ctx, uint32_t db_id, const uint64_t *d_fst_cts,
+                           uint64_t *d_out);
+
 /* ---- timing and accounting ---- */
 /* Enable per-stage CUDA-event timing of subsequent queries. */
 int opir_set_timing(opir_ctx *ctx, int enable);

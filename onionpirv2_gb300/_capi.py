@@ -34,7 +34,8 @@ EXPORTS = (
     "opir_response_bytes", "opir_db_create", "opir_db_destroy", "opir_db_push_chunk",
     "opir_db_fill_synthetic", "opir_db_upload_aligned", "opir_set_galois_key",
     "opir_set_gsw_key", "opir_erase_client", "opir_make_query", "opir_make_query_batch",
-    "opir_make_query_device", "opir_make_query_trace", "opir_set_timing", "opir_stage_times",
+    "opir_make_query_device", "opir_make_query_trace", "opir_first_dim_noalloc",
+    "opir_set_timing", "opir_stage_times",
     "opir_launch_count", "opir_sync", "opir_ntt",
 )
 
@@ -109,6 +110,7 @@ def load(path: str = LIB):
                                          _vp]
     L.opir_make_query_trace.argtypes = [_vp, ctypes.c_uint32, ctypes.c_uint64, _u64p, _u64p, _u64p,
                                         _u64p, _u64p, _u8p]
+    L.opir_first_dim_noalloc.argtypes = [_vp, ctypes.c_uint32, _vp, _vp]
     L.opir_set_timing.argtypes = [_vp, ctypes.c_int]
     L.opir_stage_times.argtypes = [_vp, ctypes.POINTER(ctypes.c_float)]
     L.opir_launch_count.argtypes = [_vp]

@@ -781,3 +781,69 @@ int opir_ntt(opir_ctx *ctx, int mod, int inverse, uint64_t *polys, uint64_t coun
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// First dimension without allocation
+//
+// For callers that must not allocate device memory during a call: a request
+// thread with a latency budget (cudaMalloc/cudaFree synchronise the device),
+// a host process whose device memory is pre-reserved by another allocator,
+// or code that later records the work into a CUDA graph.  The query operand
+// of the scan lives in the file-scope array below instead of context
+// workspace.  Every GPU that loads this library holds the array until the
+// process exits.
+// ===========================================================================
+
+// Room for the transposed query operand: n1 * N * 16 bytes, so n1 <= 512.
+constexpr size_t kNoAllocScratchBytes = size_t(16) << 20;  // 16 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace {
+std::mutex g_noalloc_mu;
+constexpr int kMaxDevices = 64;
+void *g_noalloc_ptr[kMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on the current device (looked up once
+// per device; the host-side symbol is not a device address).
+cudaError_t noalloc_scratch(int device, void **out) {
+  std::lock_guard<std::mutex> g(g_noalloc_mu);
+  if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
+  if (!g_noalloc_ptr[device]) {
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    g_noalloc_ptr[device] = p;
+  }
+  *out = g_noalloc_ptr[device];
+  return cudaSuccess;
+}
+}  // namespace
+
+extern "C" int opir_first_dim_noalloc(opir_ctx *ctx, uint32_t db_id, const uint64_t *d_fst_cts,
+                                      uint64_t *d_out) {
+  if (!ctx || !d_fst_cts || !d_out) return OPIR_ERR_ARG;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  Db *db = find_db(ctx, db_id);
+  if (!db) return ctx->fail(OPIR_ERR_UNKNOWN_DB, "unknown database %u", db_id);
+  const size_t n1 = db->shape.fst_dim_sz, nr = db->shape.other_dim_sz;
+  const size_t need = n1 * (size_t)kN * sizeof(uint4);
+  if (need > kNoAllocScratchBytes)
+    return ctx->fail(OPIR_ERR_ARG,
+                     "first dimension %zu needs %zu bytes of scratch; the static scratch holds "
+                     "%zu (first dimension <= %zu)",
+                     n1, need, kNoAllocScratchBytes, kNoAllocScratchBytes / (kN * sizeof(uint4)));
+  CK(cudaSetDevice(ctx->device), "set device");
+  void *scratch = nullptr;
+  CK(noalloc_scratch(ctx->device, &scratch), "cudaGetSymbolAddress(static scratch)");
+  uint4 *qs = static_cast<uint4 *>(scratch);
+  cudaStream_t s = ctx->stream;
+  const size_t CTW = 2 * (size_t)kN;
+  // the operand is fully rewritten before the scan reads it: nothing to clear
+  launch_query_prep(d_fst_cts, n1 * CTW, qs, (size_t)kN * n1, (int)n1, 1, ctx->Mq.tab, s);
+  launch_scan(db->dbs.as<uint64_t>(), qs, (size_t)kN * n1, d_out, nr * CTW, (int)n1, (int)nr, 1,
+              ctx->C, ctx->Mq.tab.mu_lo, ctx->Mq.tab.mu_hi, ctx->status.as<uint32_t>(), s);
+  launch_ntt(ctx->Mq.tab, d_out, nr * 2, true, s);
+  ctx->launches += 3;
+  CK(cudaGetLastError(), "first dimension launch");
+  return OPIR_OK;
+}
