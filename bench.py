@@ -60,6 +60,9 @@ def parse():
     ap.add_argument("--workload", default="db262144")
     ap.add_argument("--cpu-queries", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch", type=int, default=32,
+                    help="batch size of the batched measurement (0 = skip)")
+    ap.add_argument("--batch-steps", type=int, default=10)
     return ap.parse_args()
 
 
@@ -261,14 +264,16 @@ def main():
     server.gen_data(DB_SEED)
     ingest_s = time.perf_counter() - t_ingest
     total = args.warmup + args.steps
-    clients, queries = make_inputs(params, total)
+    nbatchq = args.batch * (args.batch_steps + 3) if args.batch > 1 else 0
+    clients, queries = make_inputs(params, max(total, nbatchq))
     for cid, (gk, gsw) in enumerate(clients):
         server.set_client_galois_key(cid, gk)
         server.set_client_gsw_key(cid, gsw)
     rb = server.resp_bytes
+    nq = queries.shape[0]
     dq = torch.from_numpy(queries.view(np.int64)).to(f"cuda:{local}")
-    dresp = torch.empty((total, 2, N), dtype=torch.int64, device=f"cuda:{local}")
-    dpack = torch.empty((total, rb), dtype=torch.uint8, device=f"cuda:{local}")
+    dresp = torch.empty((nq, 2, N), dtype=torch.int64, device=f"cuda:{local}")
+    dpack = torch.empty((nq, rb), dtype=torch.uint8, device=f"cuda:{local}")
     torch.cuda.synchronize()
     qbytes = 2 * N * 8
 
@@ -332,6 +337,39 @@ def main():
         e1.record(stream)
         e1.synchronize()
     e2e_ms = e0.elapsed_time(e1)
+
+    # ---- batched: B queries per step share one pass over the database
+    batched = None
+    if args.batch > 1:
+        B = args.batch
+
+        def bstep(i):
+            ids = [(i * B + j) % NUM_CLIENTS for j in range(B)]
+            server.make_query_device(ids, dq.data_ptr() + i * B * qbytes,
+                                     dresp.data_ptr() + i * B * qbytes, dpack.data_ptr() + i * B * rb)
+
+        with torch.cuda.stream(stream):
+            for i in range(3):
+                bstep(i)
+            stream.synchronize()
+            b0, b1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            b0.record(stream)
+            for i in range(args.batch_steps):
+                bstep(i % (args.batch_steps + 3))
+            b1.record(stream)
+            b1.synchronize()
+            bms = b0.elapsed_time(b1) / args.batch_steps
+            server.set_timing(True)
+            bst = []
+            for i in range(min(args.batch_steps, 5)):
+                bstep(i)
+                stream.synchronize()
+                bst.append(server.stage_times())
+            server.set_timing(False)
+        bqps = B * world / (bms / 1e3)
+        batched = {"batch": B, "value": bqps, "unit": "queries/s", "ms_per_batch": bms,
+                   "speedup_vs_single": bqps / qps, "path": "imad batched GEMM",
+                   "stages_ms": {k: statistics.mean(x[k] for x in bst) for k in bst[0]}}
     clocks.stop()
     e2e_qps = e2e_steps * world / (e2e_ms / 1e3)
 
@@ -361,6 +399,7 @@ def main():
         "gpu_launches": launches,
         "clocks": clocks.summary(t0, t1),
         "ingest_s": ingest_s,
+        "batched": batched,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cb, match = cpu_baseline(params, args.workload, clients, queries, gpu_resps,

@@ -152,6 +152,9 @@ int opir_sync(opir_ctx *ctx);
 /* Negacyclic NTT of `count` polynomials mod q (mod = 0) or p (mod = 1),
  * host buffers, in place. */
 int opir_ntt(opir_ctx *ctx, int mod, int inverse, uint64_t *polys, uint64_t count);
+/* The same on device memory, asynchronous on the context stream
+ * (forward: natural order in, NTT slot order out; inverse: the reverse). */
+int opir_ntt_device(opir_ctx *ctx, int mod, int inverse, uint64_t *d_polys, uint64_t count);
 
 #ifdef __cplusplus
 }

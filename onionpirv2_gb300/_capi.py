@@ -36,7 +36,7 @@ EXPORTS = (
     "opir_set_gsw_key", "opir_erase_client", "opir_make_query", "opir_make_query_batch",
     "opir_make_query_device", "opir_make_query_trace", "opir_first_dim_noalloc",
     "opir_set_timing", "opir_stage_times",
-    "opir_launch_count", "opir_sync", "opir_ntt",
+    "opir_launch_count", "opir_sync", "opir_ntt", "opir_ntt_device",
 )
 
 
@@ -116,6 +116,7 @@ def load(path: str = LIB):
     L.opir_launch_count.argtypes = [_vp]
     L.opir_launch_count.restype = ctypes.c_uint64
     L.opir_sync.argtypes = [_vp]
+    L.opir_ntt_device.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _vp, ctypes.c_uint64]
     L.opir_ntt.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _u64p, ctypes.c_uint64]
     _lib = L
     return L

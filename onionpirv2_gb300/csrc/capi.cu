@@ -14,6 +14,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -175,6 +176,7 @@ struct opir_ctx {
   std::map<uint64_t, std::unique_ptr<Client>> clients;
   Workspace ws;
   DevBuf status;  // device status word: bounded-wait timeouts (async.cuh)
+  bool batch_scan = true;  // batched GEMM for batches >= 2 (OPIR_BATCH_SCAN=0 turns it off)
   bool timing = false;
   cudaEvent_t ev[8] = {};
   float stage_ms[6] = {};
@@ -327,12 +329,24 @@ int run_pipeline(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
   // ---- first dimension
   const size_t qs_stride = (size_t)kN * n1;
   const size_t res_stride = nr * CTW;
-  launch_query_prep(leaves, leaves_stride, W.qs.as<uint4>(), qs_stride, (int)n1, batch,
-                    ctx->Mq.tab, s);
-  record(ctx, 6);
-  launch_scan(db.dbs.as<uint64_t>(), W.qs.as<uint4>(), qs_stride, W.res.as<uint64_t>(),
-              res_stride, (int)n1, (int)nr, batch, ctx->C, ctx->Mq.tab.mu_lo, ctx->Mq.tab.mu_hi,
-              ctx->status.as<uint32_t>(), s);
+  // a batch of queries shares one pass over the database (batched GEMM);
+  // a single query (or an unsupported shape) streams it once per query
+  const bool batched = batch >= 2 && ctx->batch_scan && nr % 32 == 0 && n1 % 16 == 0;
+  if (batched) {
+    launch_query_prep_batched(leaves, leaves_stride, W.qs.as<uint4>(), (int)n1, batch,
+                              ctx->Mq.tab, s);
+    record(ctx, 6);
+    launch_scan_batched(db.dbs.as<uint64_t>(), W.qs.as<uint4>(), W.res.as<uint64_t>(), res_stride,
+                        (int)n1, (int)nr, batch, ctx->C, ctx->Mq.tab.mu_lo, ctx->Mq.tab.mu_hi,
+                        ctx->status.as<uint32_t>(), s);
+  } else {
+    launch_query_prep(leaves, leaves_stride, W.qs.as<uint4>(), qs_stride, (int)n1, batch,
+                      ctx->Mq.tab, s);
+    record(ctx, 6);
+    launch_scan(db.dbs.as<uint64_t>(), W.qs.as<uint4>(), qs_stride, W.res.as<uint64_t>(),
+                res_stride, (int)n1, (int)nr, batch, ctx->C, ctx->Mq.tab.mu_lo,
+                ctx->Mq.tab.mu_hi, ctx->status.as<uint32_t>(), s);
+  }
   record(ctx, 7);
   launch_ntt(ctx->Mq.tab, W.res.as<uint64_t>(), (size_t)batch * nr * 2, true, s);
   ctx->launches += 3;
@@ -455,6 +469,7 @@ int opir_ctx_create(const opir_params *P, int device, opir_ctx **out) {
   if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess)
     return OPIR_ERR_CUDA;
   c->stream = c->own_stream;
+  if (const char *v = getenv("OPIR_BATCH_SCAN")) c->batch_scan = atoi(v) != 0;
   for (auto &e : c->ev)
     if (cudaEventCreate(&e) != cudaSuccess) return OPIR_ERR_CUDA;
   Consts &C = c->C;
@@ -777,6 +792,16 @@ int opir_ntt(opir_ctx *ctx, int mod, int inverse, uint64_t *polys, uint64_t coun
   CK(cudaGetLastError(), "ntt launch");
   CK(cudaMemcpyAsync(polys, d.p, bytes, cudaMemcpyDeviceToHost, ctx->stream), "download");
   CK(cudaStreamSynchronize(ctx->stream), "ntt");
+  return OPIR_OK;
+}
+
+int opir_ntt_device(opir_ctx *ctx, int mod, int inverse, uint64_t *d_polys, uint64_t count) {
+  if (!ctx || !d_polys || (mod != 0 && mod != 1)) return OPIR_ERR_ARG;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  cudaSetDevice(ctx->device);
+  launch_ntt(mod ? ctx->Mp.tab : ctx->Mq.tab, d_polys, count, inverse != 0, ctx->stream);
+  ctx->launches++;
+  CK(cudaGetLastError(), "ntt launch");
   return OPIR_OK;
 }
 

@@ -47,7 +47,8 @@ __global__ void __launch_bounds__(T) ntt_kernel(ModTab M, uint64_t *polys, int i
 // qs[c * n1 + k] = {lo30(Q0), hi30(Q0), lo30(Q1), hi30(Q1)} of leaf k.
 __global__ void __launch_bounds__(T) query_prep_kernel(const uint64_t *leaves,
                                                        size_t leaves_stride, uint4 *qs,
-                                                       size_t qs_stride, int n1, ModTab M) {
+                                                       size_t stride_b, size_t stride_c,
+                                                       size_t stride_k, ModTab M) {
   __shared__ uint64_t sa[kSmemPoly], sb[kSmemPoly];
   const int tid = threadIdx.x;
   const int k = blockIdx.x, b = blockIdx.y;
@@ -60,7 +61,7 @@ __global__ void __launch_bounds__(T) query_prep_kernel(const uint64_t *leaves,
   }
   ntt_fwd(r0, sa, sb, M);
   ntt_fwd(r1, sa, sb, M);
-  uint4 *dst = qs + b * qs_stride;
+  uint4 *dst = qs + b * stride_b + k * stride_k;
 #pragma unroll
   for (int e = 0; e < 8; ++e) {
     const int c = slot_idx(tid, e);
@@ -69,7 +70,7 @@ __global__ void __launch_bounds__(T) query_prep_kernel(const uint64_t *leaves,
     v.y = (uint32_t)(r0[e] >> 30);
     v.z = (uint32_t)(r1[e] & 0x3FFFFFFFu);
     v.w = (uint32_t)(r1[e] >> 30);
-    dst[(size_t)c * n1 + k] = v;
+    dst[(size_t)c * stride_c] = v;
   }
 }
 
@@ -231,7 +232,14 @@ void launch_ntt(const ModTab &M, uint64_t *polys, size_t count, bool inverse, cu
 
 void launch_query_prep(const uint64_t *leaves, size_t leaves_stride, uint4 *qs, size_t qs_stride,
                        int n1, int batch, const ModTab &Mq, cudaStream_t s) {
-  query_prep_kernel<<<dim3(n1, batch), T, 0, s>>>(leaves, leaves_stride, qs, qs_stride, n1, Mq);
+  query_prep_kernel<<<dim3(n1, batch), T, 0, s>>>(leaves, leaves_stride, qs, qs_stride,
+                                                   (size_t)n1, 1, Mq);
+}
+
+void launch_query_prep_batched(const uint64_t *leaves, size_t leaves_stride, uint4 *qsb, int n1,
+                               int batch, const ModTab &Mq, cudaStream_t s) {
+  query_prep_kernel<<<dim3(n1, batch), T, 0, s>>>(leaves, leaves_stride, qsb, 1,
+                                                   (size_t)n1 * batch, (size_t)batch, Mq);
 }
 
 void launch_modswitch_pack(const uint64_t *res, size_t res_stride, uint64_t *resp,

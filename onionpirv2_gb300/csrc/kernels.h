@@ -62,6 +62,9 @@ void launch_query_to_gsw(const uint64_t *leaves, size_t leaves_stride, uint64_t 
 // NTT the first n1 leaves and transpose to the scan operand Qs[b][c][k]
 void launch_query_prep(const uint64_t *leaves, size_t leaves_stride, uint4 *qs, size_t qs_stride,
                        int n1, int batch, const ModTab &Mq, cudaStream_t s);
+// the same into the batched operand layout qsb[c][k][b]
+void launch_query_prep_batched(const uint64_t *leaves, size_t leaves_stride, uint4 *qsb, int n1,
+                               int batch, const ModTab &Mq, cudaStream_t s);
 // out[b][row][poly][c] = sum_k DB[c][k][row] * Q[b][c][k][poly] mod q  (NTT form)
 // (bulk-copy pipelined kernel when n_rest >= 2 and 4 | n1; status collects
 // bounded-wait timeouts, see async.cuh)
@@ -69,6 +72,12 @@ void launch_scan(const uint64_t *dbs, const uint4 *qs, size_t qs_stride, uint64_
                  size_t out_stride, int n1, int n_rest, int batch, const Consts &C,
                  uint64_t mu_lo, uint64_t mu_hi, uint32_t *status, cudaStream_t s);
 cudaError_t init_scan_attributes();
+// Batched product: one pass over the database for up to 32 queries at a time
+// (qsb[c][k][b], out as launch_scan).  Returns false if the shape is not
+// supported (caller falls back to launch_scan).
+bool launch_scan_batched(const uint64_t *dbs, const uint4 *qsb, uint64_t *out, size_t out_stride,
+                         int n1, int n_rest, int batch, const Consts &C, uint64_t mu_lo,
+                         uint64_t mu_hi, uint32_t *status, cudaStream_t s);
 
 // ---- one folding level (other_dim_mux): res[b][j] += INTT(RGSW x (res[j+half]-res[j]))
 void launch_fold(uint64_t *res, size_t res_stride, const uint64_t *gsw, size_t gsw_stride,

@@ -348,6 +348,244 @@ __global__ void __launch_bounds__(kWarps * 32 + 32, kMinBlocks)
   }
 }
 
+// ---------------------------------------------------------------------------
+// batched product (many queries, one pass over the database)
+//
+// Per NTT slot c the first dimension of B queries is the integer GEMM
+// (n_rest x n1) . (n1 x 2B).  A CTA computes a 32-row x 32-query tile (64
+// output columns) of one slot; each consumer thread owns two rows and two
+// queries (8 outputs).  A 60x60-bit product uses Karatsuba on the 30-bit
+// halves: a b = a0 b0 + ((a0 + a1)(b0 + b1) - a0 b0 - a1 b1) 2^30 + a1 b1 2^60,
+// three IMAD.WIDE per MAC.  The (a0+a1)(b0+b1) partial (< 2^62) is folded into
+// its 96-bit total every 4 k-steps, the outer ones every 16.
+// ---------------------------------------------------------------------------
+constexpr int kBQ = 32;       // queries per tile
+constexpr int kBRows = 32;    // rows per tile
+constexpr int kBWarps = 8;    // consumer warps (256 threads: 16 row pairs x 16 query pairs)
+constexpr int kBK = 16;       // k-steps per stage
+constexpr int kBStages = 4;
+
+struct A96 {
+  uint64_t lo;
+  uint32_t hi;
+};
+__device__ __forceinline__ void add96(A96 &a, uint64_t v) {
+  asm("add.cc.u64 %0, %0, %2;\n\taddc.u32 %1, %1, 0;" : "+l"(a.lo), "+r"(a.hi) : "l"(v));
+}
+struct KAcc {
+  uint64_t ll, hh, ss;
+  A96 LL, HH, SS;
+};
+__device__ __forceinline__ void kacc_zero(KAcc &a) {
+  a.ll = a.hh = a.ss = 0;
+  a.LL = a.HH = a.SS = A96{0, 0};
+}
+__device__ __forceinline__ uint64_t kacc_reduce(KAcc &a, const Consts &C, uint64_t mu_lo,
+                                                uint64_t mu_hi) {
+  add96(a.LL, a.ll);
+  add96(a.HH, a.hh);
+  add96(a.SS, a.ss);
+  // mid = SS - LL - HH  (exact, >= 0)
+  U128 mid{a.SS.lo, a.SS.hi};
+  asm("sub.cc.u64 %0, %0, %2;\n\tsubc.u64 %1, %1, %3;" : "+l"(mid.lo), "+l"(mid.hi)
+      : "l"(a.LL.lo), "l"((uint64_t)a.LL.hi));
+  asm("sub.cc.u64 %0, %0, %2;\n\tsubc.u64 %1, %1, %3;" : "+l"(mid.lo), "+l"(mid.hi)
+      : "l"(a.HH.lo), "l"((uint64_t)a.HH.hi));
+  const uint64_t q = C.q;
+  const uint64_t rl = barrett128(U128{a.LL.lo, a.LL.hi}, q, mu_lo, mu_hi);
+  const uint64_t rm = barrett128(mid, q, mu_lo, mu_hi);
+  const uint64_t rh = barrett128(U128{a.HH.lo, a.HH.hi}, q, mu_lo, mu_hi);
+  uint64_t r = add_mod(rl, mul_shoup(rm, C.two30, C.two30_s, q), q);
+  return add_mod(r, mul_shoup(rh, C.two60, C.two60_s, q), q);
+}
+
+struct BatchGeom {
+  int n1, n_rest, batch;
+  int row_tiles;     // n_rest / 32
+  int groups;        // ceil(batch / 32)
+  int nkb;           // n1 / kBK
+  long long items;   // groups * kN * row_tiles
+};
+
+__global__ void __launch_bounds__(kBWarps * 32 + 32, 1)
+    scan_batch_kernel(const uint64_t *__restrict__ dbs, const uint4 *__restrict__ qsb,
+                      uint64_t *out, size_t out_stride, BatchGeom G, Consts C, uint64_t mu_lo,
+                      uint64_t mu_hi, uint32_t *status) {
+  constexpr int kDbBytes = kBK * kBRows * 8;  // 4 KB
+  constexpr int kQBytes = kBK * kBQ * 16;     // 8 KB
+  constexpr int kStage = kDbBytes + kQBytes;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw + kBStages * kStage);
+  uint64_t *empty = full + kBStages;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kBStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], kBWarps);
+    }
+    mbar_fence_init();
+  }
+  __syncthreads();
+  const size_t plane_words = (size_t)G.n1 * G.n_rest;
+  const long long per_group = (long long)kN * G.row_tiles;
+
+  if (warp == kBWarps) {
+    // ------------------------------ producer ------------------------------
+    int ps = 0;
+    uint32_t pphase = 0;
+    long long it = 0;
+    bool ok = true;
+    for (long long item = blockIdx.x; item < G.items && ok; item += gridDim.x) {
+      const int grp = (int)(item / per_group);
+      const long long rem = item % per_group;
+      const int c = (int)(rem / G.row_tiles), rt = (int)(rem % G.row_tiles);
+      const int b0 = grp * kBQ;
+      const int nq = G.batch - b0 < kBQ ? G.batch - b0 : kBQ;
+      for (int kb = 0; kb < G.nkb; ++kb, ++it) {
+        const int s = ps;
+        const bool reuse = it >= kBStages;
+        const uint32_t ephase = pphase ^ 1u;
+        if (++ps == kBStages) {
+          ps = 0;
+          pphase ^= 1u;
+        }
+        if (reuse) {
+          bool w = true;
+          if (lane == 0) w = mbar_wait(&empty[s], ephase);
+          w = __shfl_sync(0xffffffffu, w, 0);
+          if (!w) {
+            if (lane == 0) report_error(status, kErrWaitEmpty);
+            ok = false;
+            break;
+          }
+        }
+        unsigned char *st = smem_raw + (size_t)s * kStage;
+        uint64_t *sdb = reinterpret_cast<uint64_t *>(st);
+        uint4 *sq = reinterpret_cast<uint4 *>(st + kDbBytes);
+        const uint32_t bytes = (uint32_t)(kDbBytes + kBK * nq * 16);
+        if (lane == 0) mbar_arrive_expect_tx(&full[s], bytes);
+        __syncwarp();
+        const int k0 = kb * kBK;
+        const uint64_t *plane = dbs + (size_t)c * plane_words + (size_t)rt * kBRows;
+        if (G.n_rest == kBRows) {
+          if (lane == 0) bulk_g2s(sdb, plane + (size_t)k0 * G.n_rest, kDbBytes, &full[s]);
+        } else if (lane < kBK) {
+          bulk_g2s(sdb + lane * kBRows, plane + (size_t)(k0 + lane) * G.n_rest, kBRows * 8,
+                   &full[s]);
+        }
+        const uint4 *qsrc = qsb + ((size_t)c * G.n1 + k0) * G.batch + b0;
+        if (nq == G.batch && nq == kBQ) {
+          if (lane == 0) bulk_g2s(sq, qsrc, kQBytes, &full[s]);
+        } else if (lane < kBK) {
+          bulk_g2s(sq + lane * kBQ, qsrc + (size_t)lane * G.batch, nq * 16, &full[s]);
+        }
+      }
+    }
+    if (lane == 0) {
+      const long long first = it > kBStages ? it - kBStages : 0;
+      for (long long j = first; j < it; ++j)
+        if (!mbar_wait(&full[j % kBStages], (uint32_t)((j / kBStages) & 1))) {
+          report_error(status, kErrDrain);
+          break;
+        }
+    }
+    return;
+  }
+
+  // ------------------------------ consumers ------------------------------
+  const int r = (threadIdx.x >> 4) * 2;  // first of the thread's two rows
+  const int jq = (threadIdx.x & 15) * 2; // first of the thread's two queries
+  int s = 0;
+  uint32_t phase = 0;
+  for (long long item = blockIdx.x; item < G.items; item += gridDim.x) {
+    const int grp = (int)(item / per_group);
+    const long long rem = item % per_group;
+    const int c = (int)(rem / G.row_tiles), rt = (int)(rem % G.row_tiles);
+    KAcc acc[2][2][2];  // [row][query][poly]
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        kacc_zero(acc[i][j][0]);
+        kacc_zero(acc[i][j][1]);
+      }
+    for (int kb = 0; kb < G.nkb; ++kb) {
+      if (!mbar_wait(&full[s], phase)) {
+        report_error(status, kErrWaitFull);
+        return;
+      }
+      const unsigned char *st = smem_raw + (size_t)s * kStage;
+      const uint64_t *sdb = reinterpret_cast<const uint64_t *>(st) + r;
+      const uint4 *sq = reinterpret_cast<const uint4 *>(st + kDbBytes) + jq;
+#pragma unroll 1
+      for (int k4 = 0; k4 < kBK; k4 += 4) {
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) {
+          const int k = k4 + kk;
+          const ulonglong2 av = *reinterpret_cast<const ulonglong2 *>(sdb + k * kBRows);
+          const uint4 q0 = sq[k * kBQ], q1 = sq[k * kBQ + 1];
+          const uint32_t bs[2][2] = {{q0.x + q0.y, q0.z + q0.w}, {q1.x + q1.y, q1.z + q1.w}};
+          const uint4 bq[2] = {q0, q1};
+#pragma unroll
+          for (int i = 0; i < 2; ++i) {
+            const uint64_t a = i ? av.y : av.x;
+            const uint32_t a0 = (uint32_t)a, a1 = (uint32_t)(a >> 32), sa = a0 + a1;
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+              mad_wide(acc[i][j][0].ll, a0, bq[j].x);
+              mad_wide(acc[i][j][0].hh, a1, bq[j].y);
+              mad_wide(acc[i][j][0].ss, sa, bs[j][0]);
+              mad_wide(acc[i][j][1].ll, a0, bq[j].z);
+              mad_wide(acc[i][j][1].hh, a1, bq[j].w);
+              mad_wide(acc[i][j][1].ss, sa, bs[j][1]);
+            }
+          }
+        }
+        // the (a0+a1)(b0+b1) partial holds 4 steps
+#pragma unroll
+        for (int i = 0; i < 2; ++i)
+#pragma unroll
+          for (int j = 0; j < 2; ++j)
+#pragma unroll
+            for (int pl = 0; pl < 2; ++pl) {
+              add96(acc[i][j][pl].SS, acc[i][j][pl].ss);
+              acc[i][j][pl].ss = 0;
+            }
+      }
+      // the outer partials hold 16 steps: one stage
+#pragma unroll
+      for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+#pragma unroll
+          for (int pl = 0; pl < 2; ++pl) {
+            add96(acc[i][j][pl].LL, acc[i][j][pl].ll);
+            add96(acc[i][j][pl].HH, acc[i][j][pl].hh);
+            acc[i][j][pl].ll = acc[i][j][pl].hh = 0;
+          }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[s]);
+      if (++s == kBStages) {
+        s = 0;
+        phase ^= 1u;
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      const size_t row = (size_t)rt * kBRows + r + i;
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        const int b = grp * kBQ + jq + j;
+        if (b < G.batch) {
+          uint64_t *o = out + (size_t)b * out_stride + row * 2 * kN + c;
+          o[0] = kacc_reduce(acc[i][j][0], C, mu_lo, mu_hi);
+          o[kN] = kacc_reduce(acc[i][j][1], C, mu_lo, mu_hi);
+        }
+      }
+    }
+  }
+}
+
 int g_num_sms = 0;
 int g_cfg = 0;
 
@@ -411,12 +649,38 @@ cudaError_t init_scan_attributes() {
   int dev;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+  {
+    const int smem = kBStages * (kBK * kBRows * 8 + kBK * kBQ * 16) + 2 * kBStages * 8;
+    e = cudaFuncSetAttribute(scan_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+  }
   g_cfg = 0;
   if (const char *v = getenv("OPIR_SCAN_CFG")) {
     const int i = atoi(v);
     if (i >= 0 && i < kNumCfgs) g_cfg = i;
   }
   return cudaSuccess;
+}
+
+bool launch_scan_batched(const uint64_t *dbs, const uint4 *qsb, uint64_t *out, size_t out_stride,
+                         int n1, int n_rest, int batch, const Consts &C, uint64_t mu_lo,
+                         uint64_t mu_hi, uint32_t *status, cudaStream_t s) {
+  if (n_rest % kBRows != 0 || n1 % kBK != 0 || batch < 1) return false;
+  BatchGeom G;
+  G.n1 = n1;
+  G.n_rest = n_rest;
+  G.batch = batch;
+  G.row_tiles = n_rest / kBRows;
+  G.groups = (batch + kBQ - 1) / kBQ;
+  G.nkb = n1 / kBK;
+  G.items = (long long)G.groups * kN * G.row_tiles;
+  const int smem = kBStages * (kBK * kBRows * 8 + kBK * kBQ * 16) + 2 * kBStages * 8;
+  const int sms = g_num_sms > 0 ? g_num_sms : 152;
+  long long grid = sms;
+  if (grid > G.items) grid = G.items;
+  scan_batch_kernel<<<(unsigned)grid, kBWarps * 32 + 32, smem, s>>>(dbs, qsb, out, out_stride, G, C,
+                                                                     mu_lo, mu_hi, status);
+  return true;
 }
 
 void launch_scan(const uint64_t *dbs, const uint4 *qs, size_t qs_stride, uint64_t *out,

@@ -224,3 +224,49 @@ def test_one_cta_and_cluster_tree_forms(oracle_lib, gpu_lib, monkeypatch, thresh
     for j in range(3):
         assert np.array_equal(resp[j], refs[j])
     server.close()
+
+
+@pytest.mark.parametrize("batch", [3, 33])
+def test_batched_scan_matches_single_and_oracle(oracle_lib, gpu_lib, monkeypatch, batch):
+    """Batched GEMM (one pass over the database for up to 32 queries) equals
+    the per-query scan and the oracle, also for a partial second group."""
+    from onionpirv2_gb300 import PirParams, PirServer
+    o = oracle_lib.Oracle(1 << 13, 64)  # 64 x 128
+    P = o.P
+    assert (P.n1, P.n_rest) == (64, 128)
+    server = PirServer(PirParams(num_entries=1 << 13, max_fst_dim=64))
+    server.gen_data(77)
+    db = o.build_db(77)
+    ids, queries, keys, idxs = [], [], [], []
+    for j in range(batch):
+        sk, gk, gswk = make_client(o, 500 + 3 * j)
+        cid = 100 + (j % 7)  # clients repeat inside the batch
+        if j < 7:
+            server.set_client_galois_key(cid, gk)
+            server.set_client_gsw_key(cid, gswk)
+            keys.append((sk, gk, gswk))
+        sk, gk, gswk = keys[j % 7]
+        idx = (j * 2311 + 5) % P.num_entries
+        ids.append(cid)
+        idxs.append(idx)
+        queries.append(o.make_query(sk, 900 + j, idx))
+    resp, packed = server.make_query_batch(ids, np.stack(queries))
+    for j in (0, 1, batch - 1):
+        sk, gk, gswk = keys[j % 7]
+        ref, ref_packed, _, _ = o.make_query_server(db, gk, o.gsw_key_to_ntt(gswk), queries[j])
+        assert np.array_equal(resp[j], ref), j
+        assert packed[j].tobytes() == ref_packed.tobytes()
+    for j in range(batch):
+        plain, _ = o.decrypt(keys[j % 7][0], resp[j], 2)
+        assert np.array_equal(o.entry_from_plain(idxs[j], plain), server.direct_get_entry(idxs[j]))
+    # the same batch through the per-query scan
+    monkeypatch.setenv("OPIR_BATCH_SCAN", "0")
+    server2 = PirServer(PirParams(num_entries=1 << 13, max_fst_dim=64))
+    server2.gen_data(77)
+    for j in range(len(keys)):
+        server2.set_client_galois_key(100 + j, keys[j][1])
+        server2.set_client_gsw_key(100 + j, keys[j][2])
+    resp2, _ = server2.make_query_batch(ids, np.stack(queries))
+    assert np.array_equal(resp, resp2)
+    server.close()
+    server2.close()
