@@ -1,0 +1,128 @@
+// onionpir_server.hpp -- header-only C++ PirServer over the GB300 C ABI.
+//
+// Keeps the method names and meaning of the reference class
+// (src/includes/server.h:13-51): the constructor takes the parameter set,
+// gen_data / push_database_chunk fill the database, set_client_galois_key /
+// set_client_gsw_key register a client, make_query answers a query and
+// save_resp_to_stream writes the packed response.  Errors are thrown as the
+// reference's exception types: std::invalid_argument for bad arguments,
+// std::out_of_range for an unknown client (std::map::at in the reference),
+// std::runtime_error for device failures.  SEAL objects are replaced by plain
+// arrays (ciphertext = uint64_t[2][N], coefficient form, mod q); SEAL wire
+// decoding is not part of this header.
+#pragma once
+
+#include <cstdint>
+#include <ostream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "onionpir_gpu.h"
+
+namespace onionpir {
+
+struct PirParams {
+  uint64_t q = 0, p = 0, t = 0, small_q = 0;  // CoeffModulus::Create / generate_prime results
+  uint32_t poly_degree = 2048;
+  uint32_t l = 5, base_log2 = 12, l_key = 10, base_log2_key = 6;
+  uint32_t fst_dim_sz = 0, other_dim_sz = 0;  // PirParams::get_dims()
+  uint32_t entry_size = 0, entries_per_pt = 1, bits_per_coeff = 15;
+};
+
+using Ciphertext = std::vector<uint64_t>;  // [2][N]
+using Entry = std::vector<uint8_t>;
+
+class PirServer {
+ public:
+  explicit PirServer(const PirParams &p, int device = 0) : params_(p) {
+    opir_params gp{};
+    gp.poly_degree = p.poly_degree;
+    gp.coeff_modulus = p.q;
+    gp.special_modulus = p.p;
+    gp.plain_modulus = p.t;
+    gp.small_modulus = p.small_q;
+    gp.gsw_l = p.l;
+    gp.gsw_base_log2 = p.base_log2;
+    gp.gsw_l_key = p.l_key;
+    gp.gsw_base_log2_key = p.base_log2_key;
+    const int rc = opir_ctx_create(&gp, device, &ctx_);
+    if (rc != OPIR_OK) throw std::invalid_argument("opir_ctx_create failed: " + std::to_string(rc));
+    opir_db_shape sh{p.fst_dim_sz, p.other_dim_sz, p.entry_size, p.entries_per_pt,
+                     p.bits_per_coeff};
+    check(opir_db_create(ctx_, &sh, &db_));
+    resp_bytes_ = opir_response_bytes(ctx_);
+  }
+  ~PirServer() { opir_ctx_destroy(ctx_); }
+  PirServer(const PirServer &) = delete;
+  PirServer &operator=(const PirServer &) = delete;
+
+  // server.cpp:47-78 (entries derived from `seed` instead of /dev/urandom)
+  void gen_data(uint64_t seed) { check(opir_db_fill_synthetic(ctx_, db_, seed)); }
+
+  // server.cpp:635-701: fst_dim_sz * entries_per_pt entries of at most
+  // entry_size bytes (shorter ones are zero-padded)
+  void push_database_chunk(const std::vector<Entry> &chunk, size_t chunk_idx) {
+    const size_t n = (size_t)params_.fst_dim_sz * params_.entries_per_pt;
+    if (chunk.size() != n) throw std::invalid_argument("chunk must hold fst_dim_sz entries");
+    std::vector<uint8_t> flat(n * params_.entry_size, 0);
+    for (size_t i = 0; i < n; ++i) {
+      if (chunk[i].size() > params_.entry_size)
+        throw std::invalid_argument("Entry size is too large");
+      std::copy(chunk[i].begin(), chunk[i].end(), flat.begin() + i * params_.entry_size);
+    }
+    check(opir_db_push_chunk(ctx_, db_, flat.data(), n, chunk_idx));
+  }
+
+  // server.cpp:480-484; keys [levels][2][2][N] in NTT form
+  void set_client_galois_key(size_t client_id, const std::vector<uint64_t> &keys) {
+    const size_t per = 4 * (size_t)params_.poly_degree;
+    if (keys.empty() || keys.size() % per) throw std::invalid_argument("bad Galois key size");
+    check(opir_set_galois_key(ctx_, client_id, keys.data(), (uint32_t)(keys.size() / per)));
+  }
+  // server.cpp:486-500; rows [2 l_key][2][N] in coefficient form
+  void set_client_gsw_key(size_t client_id, const std::vector<uint64_t> &rows) {
+    if (rows.size() != 2 * (size_t)params_.l_key * 2 * params_.poly_degree)
+      throw std::invalid_argument("bad RGSW key size");
+    check(opir_set_gsw_key(ctx_, client_id, rows.data()));
+  }
+
+  // server.cpp:520-579: the response mod small_q
+  Ciphertext make_query(size_t client_id, const Ciphertext &query) {
+    if (query.size() != 2 * (size_t)params_.poly_degree)
+      throw std::invalid_argument("query must be one ciphertext");
+    Ciphertext resp(query.size());
+    last_packed_.assign(resp_bytes_, 0);
+    check(opir_make_query(ctx_, db_, client_id, query.data(), resp.data(), last_packed_.data()));
+    last_resp_ = resp;
+    return resp;
+  }
+
+  // server.cpp:581-633: writes the packed response; returns its size
+  size_t save_resp_to_stream(const Ciphertext &response, std::ostream &stream) {
+    if (response != last_resp_) throw std::invalid_argument("not the last response of make_query");
+    stream.write(reinterpret_cast<const char *>(last_packed_.data()),
+                 (std::streamsize)last_packed_.size());
+    return last_packed_.size();
+  }
+
+  opir_ctx *ctx() const { return ctx_; }
+  uint32_t db_id() const { return db_; }
+
+ private:
+  void check(int rc) {
+    if (rc == OPIR_OK) return;
+    const std::string msg = opir_last_error(ctx_);
+    if (rc == OPIR_ERR_UNKNOWN_CLIENT) throw std::out_of_range(msg);
+    if (rc == OPIR_ERR_ARG || rc == OPIR_ERR_UNKNOWN_DB) throw std::invalid_argument(msg);
+    throw std::runtime_error(msg);
+  }
+  PirParams params_;
+  opir_ctx *ctx_ = nullptr;
+  uint32_t db_ = 0;
+  uint64_t resp_bytes_ = 0;
+  Ciphertext last_resp_;
+  std::vector<uint8_t> last_packed_;
+};
+
+}  // namespace onionpir

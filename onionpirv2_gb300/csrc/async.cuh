@@ -16,6 +16,7 @@ constexpr uint32_t kErrWaitEmpty = 2u;  // producer gave up waiting for a free s
 constexpr uint32_t kErrDrain = 4u;      // producer gave up draining its copies
 
 constexpr uint32_t kSpinLimit = 1u << 22;
+constexpr uint32_t kSuspendHintNs = 2000;  // per try_wait; the wait stays bounded by kSpinLimit tries
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -52,10 +53,31 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   return ok != 0;
 }
 
+// try_wait with a suspend-time hint: a waiting warp sleeps (up to the hint)
+// instead of spinning, leaving issue slots to the warps that have work.
+__device__ __forceinline__ bool mbar_try_wait_hint(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(kSuspendHintNs)
+      : "memory");
+  return ok != 0;
+}
+
 // Bounded wait for the phase with the given parity to complete.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
   for (uint32_t i = 0; i < kSpinLimit; ++i)
     if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+// Bounded wait that sleeps between polls (consumer side of a pipeline).
+__device__ __forceinline__ bool mbar_wait_sleep(uint64_t *bar, uint32_t parity) {
+  for (uint32_t i = 0; i < kSpinLimit; ++i)
+    if (mbar_try_wait_hint(bar, parity)) return true;
   return false;
 }
 

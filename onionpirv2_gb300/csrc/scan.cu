@@ -41,8 +41,21 @@ __device__ __forceinline__ void acc3_zero(Acc3 &a) {
 // a = a1 2^30 + a0, b = b1 2^30 + b0 (all halves < 2^30):
 // a b = a0 b0 + (a0 b1 + a1 b0) 2^30 + a1 b1 2^60.  Each half product is
 // < 2^60, so the 64-bit partials absorb 16, 8 and 16 k-steps.
+// acc += x * y, 32x32 -> 64 (IMAD.WIDE.U32).  Two spellings: ptxas fuses the
+// 64-bit add into the multiply differently depending on the context, so the
+// kernels pick the one measured faster.
 __device__ __forceinline__ void mad_wide(uint64_t &acc, uint32_t x, uint32_t y) {
-  asm("mad.wide.u32 %0, %1, %2, %0;" : "+l"(acc) : "r"(x), "r"(y));  // acc += x * y (one IMAD.WIDE)
+  asm("mad.wide.u32 %0, %1, %2, %0;" : "+l"(acc) : "r"(x), "r"(y));
+}
+__device__ __forceinline__ void mad_wide_c(uint64_t &acc, uint32_t x, uint32_t y) {
+  acc += (uint64_t)x * y;
+}
+template <bool kPtx>
+__device__ __forceinline__ void madw(uint64_t &acc, uint32_t x, uint32_t y) {
+  if constexpr (kPtx)
+    mad_wide(acc, x, y);
+  else
+    mad_wide_c(acc, x, y);
 }
 __device__ __forceinline__ void acc3_mac(Acc3 &a, uint32_t a0, uint32_t a1, uint32_t b0,
                                          uint32_t b1) {
@@ -278,7 +291,7 @@ __global__ void __launch_bounds__(kWarps * 32 + 32, kMinBlocks)
       acc3_zero(acc[rr][1]);
     }
     for (int kb = 0; kb < G.nkb; ++kb) {
-      if (!mbar_wait(&full[s], phase)) {
+      if (!mbar_wait_sleep(&full[s], phase)) {
         report_error(status, kErrWaitFull);
         return;
       }
@@ -363,7 +376,7 @@ constexpr int kBQ = 32;       // queries per tile
 constexpr int kBRows = 32;    // rows per tile
 constexpr int kBWarps = 8;    // consumer warps (256 threads: 16 row pairs x 16 query pairs)
 constexpr int kBK = 16;       // k-steps per stage
-constexpr int kBStages = 4;
+constexpr int kBStages = 6;
 
 struct A96 {
   uint64_t lo;
@@ -407,6 +420,7 @@ struct BatchGeom {
   long long items;   // groups * kN * row_tiles
 };
 
+template <bool kPtx>
 __global__ void __launch_bounds__(kBWarps * 32 + 32, 1)
     scan_batch_kernel(const uint64_t *__restrict__ dbs, const uint4 *__restrict__ qsb,
                       uint64_t *out, size_t out_stride, BatchGeom G, Consts C, uint64_t mu_lo,
@@ -510,7 +524,7 @@ __global__ void __launch_bounds__(kBWarps * 32 + 32, 1)
         kacc_zero(acc[i][j][1]);
       }
     for (int kb = 0; kb < G.nkb; ++kb) {
-      if (!mbar_wait(&full[s], phase)) {
+      if (!mbar_wait_sleep(&full[s], phase)) {
         report_error(status, kErrWaitFull);
         return;
       }
@@ -532,12 +546,12 @@ __global__ void __launch_bounds__(kBWarps * 32 + 32, 1)
             const uint32_t a0 = (uint32_t)a, a1 = (uint32_t)(a >> 32), sa = a0 + a1;
 #pragma unroll
             for (int j = 0; j < 2; ++j) {
-              mad_wide(acc[i][j][0].ll, a0, bq[j].x);
-              mad_wide(acc[i][j][0].hh, a1, bq[j].y);
-              mad_wide(acc[i][j][0].ss, sa, bs[j][0]);
-              mad_wide(acc[i][j][1].ll, a0, bq[j].z);
-              mad_wide(acc[i][j][1].hh, a1, bq[j].w);
-              mad_wide(acc[i][j][1].ss, sa, bs[j][1]);
+              madw<kPtx>(acc[i][j][0].ll, a0, bq[j].x);
+              madw<kPtx>(acc[i][j][0].hh, a1, bq[j].y);
+              madw<kPtx>(acc[i][j][0].ss, sa, bs[j][0]);
+              madw<kPtx>(acc[i][j][1].ll, a0, bq[j].z);
+              madw<kPtx>(acc[i][j][1].hh, a1, bq[j].w);
+              madw<kPtx>(acc[i][j][1].ss, sa, bs[j][1]);
             }
           }
         }
@@ -588,6 +602,7 @@ __global__ void __launch_bounds__(kBWarps * 32 + 32, 1)
 
 int g_num_sms = 0;
 int g_cfg = 0;
+bool g_batch_ptx = true;
 
 template <int R, int W, int K, int S, int B>
 cudaError_t set_attr() {
@@ -651,8 +666,14 @@ cudaError_t init_scan_attributes() {
   cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
   {
     const int smem = kBStages * (kBK * kBRows * 8 + kBK * kBQ * 16) + 2 * kBStages * 8;
-    e = cudaFuncSetAttribute(scan_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    e = cudaFuncSetAttribute(scan_batch_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem);
     if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(scan_batch_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem);
+    if (e != cudaSuccess) return e;
+    g_batch_ptx = true;
+    if (const char *v = getenv("OPIR_BATCH_MAC")) g_batch_ptx = atoi(v) != 0;
   }
   g_cfg = 0;
   if (const char *v = getenv("OPIR_SCAN_CFG")) {
@@ -678,8 +699,12 @@ bool launch_scan_batched(const uint64_t *dbs, const uint4 *qsb, uint64_t *out, s
   const int sms = g_num_sms > 0 ? g_num_sms : 152;
   long long grid = sms;
   if (grid > G.items) grid = G.items;
-  scan_batch_kernel<<<(unsigned)grid, kBWarps * 32 + 32, smem, s>>>(dbs, qsb, out, out_stride, G, C,
-                                                                     mu_lo, mu_hi, status);
+  if (g_batch_ptx)
+    scan_batch_kernel<true><<<(unsigned)grid, kBWarps * 32 + 32, smem, s>>>(
+        dbs, qsb, out, out_stride, G, C, mu_lo, mu_hi, status);
+  else
+    scan_batch_kernel<false><<<(unsigned)grid, kBWarps * 32 + 32, smem, s>>>(
+        dbs, qsb, out, out_stride, G, C, mu_lo, mu_hi, status);
   return true;
 }
 
