@@ -63,6 +63,9 @@ def parse():
     ap.add_argument("--batch", type=int, default=32,
                     help="batch size of the batched measurement (0 = skip)")
     ap.add_argument("--batch-steps", type=int, default=10)
+    ap.add_argument("--micro", choices=["ntt"], default=None,
+                    help="kernel micro-benchmark instead of the query benchmark")
+    ap.add_argument("--count", type=int, default=152 * 64, help="polynomials for --micro ntt")
     return ap.parse_args()
 
 
@@ -240,10 +243,42 @@ def run_reference(args):
     return 0
 
 
+def run_micro_ntt(args):
+    """Throughput of the batched 2048-point NTT kernel (device buffers)."""
+    import ctypes
+
+    import torch
+    from onionpirv2_gb300 import PirParams, PirServer, _capi
+    L = _capi.load()
+    server = PirServer(PirParams.preset("db4096"))
+    stream = torch.cuda.Stream()
+    server.set_stream(stream.cuda_stream)
+    q = server.pir_params.coeff_modulus[0]
+    x = torch.randint(0, 2**62, (args.count, N), dtype=torch.int64, device="cuda") % q
+    torch.cuda.synchronize()
+    out = {"micro": "ntt", "count": args.count}
+    for inv in (0, 1):
+        with torch.cuda.stream(stream):
+            for _ in range(args.warmup):
+                L.opir_ntt_device(server.ctx, 0, inv, ctypes.c_void_p(x.data_ptr()), args.count)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(args.steps):
+                L.opir_ntt_device(server.ctx, 0, inv, ctypes.c_void_p(x.data_ptr()), args.count)
+            e1.record(stream)
+            e1.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        out["inverse" if inv else "forward"] = {"us": ms * 1e3, "ntt_per_us": args.count / (ms * 1e3)}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.micro == "ntt":
+        return run_micro_ntt(args)
     rank, world, local = dist_env()
     import torch
     if not torch.cuda.is_available():
