@@ -29,6 +29,23 @@ namespace opir {
 
 namespace {
 
+// acc += x * y, 32x32 -> 64 (IMAD.WIDE.U32).  Two spellings: ptxas fuses the
+// 64-bit add into the multiply differently depending on the context, so the
+// kernels pick the one measured faster.
+__device__ __forceinline__ void mad_wide(uint64_t &acc, uint32_t x, uint32_t y) {
+  asm("mad.wide.u32 %0, %1, %2, %0;" : "+l"(acc) : "r"(x), "r"(y));
+}
+__device__ __forceinline__ void mad_wide_c(uint64_t &acc, uint32_t x, uint32_t y) {
+  acc += (uint64_t)x * y;
+}
+// acc += x * y as two 32-bit multiply-adds chained through the carry flag
+__device__ __forceinline__ void mad_cc(uint64_t &acc, uint32_t x, uint32_t y) {
+  uint32_t lo = (uint32_t)acc, hi = (uint32_t)(acc >> 32);
+  asm("mad.lo.cc.u32 %0, %2, %3, %0;\n\tmadc.hi.u32 %1, %2, %3, %1;"
+      : "+r"(lo), "+r"(hi)
+      : "r"(x), "r"(y));
+  acc = ((uint64_t)hi << 32) | lo;
+}
 struct Acc3 {
   uint64_t ll, mid, hh;
   U128 LL, MID, HH;
@@ -41,28 +58,21 @@ __device__ __forceinline__ void acc3_zero(Acc3 &a) {
 // a = a1 2^30 + a0, b = b1 2^30 + b0 (all halves < 2^30):
 // a b = a0 b0 + (a0 b1 + a1 b0) 2^30 + a1 b1 2^60.  Each half product is
 // < 2^60, so the 64-bit partials absorb 16, 8 and 16 k-steps.
-// acc += x * y, 32x32 -> 64 (IMAD.WIDE.U32).  Two spellings: ptxas fuses the
-// 64-bit add into the multiply differently depending on the context, so the
-// kernels pick the one measured faster.
-__device__ __forceinline__ void mad_wide(uint64_t &acc, uint32_t x, uint32_t y) {
-  asm("mad.wide.u32 %0, %1, %2, %0;" : "+l"(acc) : "r"(x), "r"(y));
-}
-__device__ __forceinline__ void mad_wide_c(uint64_t &acc, uint32_t x, uint32_t y) {
-  acc += (uint64_t)x * y;
-}
-template <bool kPtx>
+template <int kForm>
 __device__ __forceinline__ void madw(uint64_t &acc, uint32_t x, uint32_t y) {
-  if constexpr (kPtx)
+  if constexpr (kForm == 1)
     mad_wide(acc, x, y);
+  else if constexpr (kForm == 3)
+    mad_cc(acc, x, y);
   else
     mad_wide_c(acc, x, y);
 }
 __device__ __forceinline__ void acc3_mac(Acc3 &a, uint32_t a0, uint32_t a1, uint32_t b0,
                                          uint32_t b1) {
-  mad_wide(a.ll, a0, b0);
-  mad_wide(a.mid, a0, b1);
-  mad_wide(a.mid, a1, b0);
-  mad_wide(a.hh, a1, b1);
+  mad_cc(a.ll, a0, b0);
+  mad_cc(a.mid, a0, b1);
+  mad_cc(a.mid, a1, b0);
+  mad_cc(a.hh, a1, b1);
 }
 __device__ __forceinline__ void acc3_flush(Acc3 &a) {
   add_to(a.LL, U128{a.ll, 0});
@@ -393,6 +403,9 @@ __device__ __forceinline__ void kacc_zero(KAcc &a) {
   a.ll = a.hh = a.ss = 0;
   a.LL = a.HH = a.SS = A96{0, 0};
 }
+// kKaratsuba: SS holds (a0+a1)(b0+b1) (mid = SS - LL - HH); otherwise SS
+// already holds the cross terms a0 b1 + a1 b0.
+template <bool kKaratsuba>
 __device__ __forceinline__ uint64_t kacc_reduce(KAcc &a, const Consts &C, uint64_t mu_lo,
                                                 uint64_t mu_hi) {
   add96(a.LL, a.ll);
@@ -400,10 +413,12 @@ __device__ __forceinline__ uint64_t kacc_reduce(KAcc &a, const Consts &C, uint64
   add96(a.SS, a.ss);
   // mid = SS - LL - HH  (exact, >= 0)
   U128 mid{a.SS.lo, a.SS.hi};
-  asm("sub.cc.u64 %0, %0, %2;\n\tsubc.u64 %1, %1, %3;" : "+l"(mid.lo), "+l"(mid.hi)
-      : "l"(a.LL.lo), "l"((uint64_t)a.LL.hi));
-  asm("sub.cc.u64 %0, %0, %2;\n\tsubc.u64 %1, %1, %3;" : "+l"(mid.lo), "+l"(mid.hi)
-      : "l"(a.HH.lo), "l"((uint64_t)a.HH.hi));
+  if (kKaratsuba) {
+    asm("sub.cc.u64 %0, %0, %2;\n\tsubc.u64 %1, %1, %3;" : "+l"(mid.lo), "+l"(mid.hi)
+        : "l"(a.LL.lo), "l"((uint64_t)a.LL.hi));
+    asm("sub.cc.u64 %0, %0, %2;\n\tsubc.u64 %1, %1, %3;" : "+l"(mid.lo), "+l"(mid.hi)
+        : "l"(a.HH.lo), "l"((uint64_t)a.HH.hi));
+  }
   const uint64_t q = C.q;
   const uint64_t rl = barrett128(U128{a.LL.lo, a.LL.hi}, q, mu_lo, mu_hi);
   const uint64_t rm = barrett128(mid, q, mu_lo, mu_hi);
@@ -420,7 +435,7 @@ struct BatchGeom {
   long long items;   // groups * kN * row_tiles
 };
 
-template <bool kPtx>
+template <int kForm>
 __global__ void __launch_bounds__(kBWarps * 32 + 32, 1)
     scan_batch_kernel(const uint64_t *__restrict__ dbs, const uint4 *__restrict__ qsb,
                       uint64_t *out, size_t out_stride, BatchGeom G, Consts C, uint64_t mu_lo,
@@ -546,12 +561,24 @@ __global__ void __launch_bounds__(kBWarps * 32 + 32, 1)
             const uint32_t a0 = (uint32_t)a, a1 = (uint32_t)(a >> 32), sa = a0 + a1;
 #pragma unroll
             for (int j = 0; j < 2; ++j) {
-              madw<kPtx>(acc[i][j][0].ll, a0, bq[j].x);
-              madw<kPtx>(acc[i][j][0].hh, a1, bq[j].y);
-              madw<kPtx>(acc[i][j][0].ss, sa, bs[j][0]);
-              madw<kPtx>(acc[i][j][1].ll, a0, bq[j].z);
-              madw<kPtx>(acc[i][j][1].hh, a1, bq[j].w);
-              madw<kPtx>(acc[i][j][1].ss, sa, bs[j][1]);
+              if constexpr (kForm == 2) {
+                // four products: ss holds the cross terms a0 b1 + a1 b0 (flushed every 4 steps)
+                madw<kForm>(acc[i][j][0].ll, a0, bq[j].x);
+                madw<kForm>(acc[i][j][0].ss, a0, bq[j].y);
+                madw<kForm>(acc[i][j][0].ss, a1, bq[j].x);
+                madw<kForm>(acc[i][j][0].hh, a1, bq[j].y);
+                madw<kForm>(acc[i][j][1].ll, a0, bq[j].z);
+                madw<kForm>(acc[i][j][1].ss, a0, bq[j].w);
+                madw<kForm>(acc[i][j][1].ss, a1, bq[j].z);
+                madw<kForm>(acc[i][j][1].hh, a1, bq[j].w);
+              } else {
+                madw<kForm>(acc[i][j][0].ll, a0, bq[j].x);
+                madw<kForm>(acc[i][j][0].hh, a1, bq[j].y);
+                madw<kForm>(acc[i][j][0].ss, sa, bs[j][0]);
+                madw<kForm>(acc[i][j][1].ll, a0, bq[j].z);
+                madw<kForm>(acc[i][j][1].hh, a1, bq[j].w);
+                madw<kForm>(acc[i][j][1].ss, sa, bs[j][1]);
+              }
             }
           }
         }
@@ -592,8 +619,8 @@ __global__ void __launch_bounds__(kBWarps * 32 + 32, 1)
         const int b = grp * kBQ + jq + j;
         if (b < G.batch) {
           uint64_t *o = out + (size_t)b * out_stride + row * 2 * kN + c;
-          o[0] = kacc_reduce(acc[i][j][0], C, mu_lo, mu_hi);
-          o[kN] = kacc_reduce(acc[i][j][1], C, mu_lo, mu_hi);
+          o[0] = kacc_reduce<kForm != 2>(acc[i][j][0], C, mu_lo, mu_hi);
+          o[kN] = kacc_reduce<kForm != 2>(acc[i][j][1], C, mu_lo, mu_hi);
         }
       }
     }
@@ -602,7 +629,7 @@ __global__ void __launch_bounds__(kBWarps * 32 + 32, 1)
 
 int g_num_sms = 0;
 int g_cfg = 0;
-bool g_batch_ptx = true;
+int g_batch_form = 3;  // accumulate spelling of scan_batch_kernel (OPIR_BATCH_MAC)
 
 template <int R, int W, int K, int S, int B>
 cudaError_t set_attr() {
@@ -666,14 +693,14 @@ cudaError_t init_scan_attributes() {
   cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
   {
     const int smem = kBStages * (kBK * kBRows * 8 + kBK * kBQ * 16) + 2 * kBStages * 8;
-    e = cudaFuncSetAttribute(scan_batch_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             smem);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(scan_batch_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             smem);
-    if (e != cudaSuccess) return e;
-    g_batch_ptx = true;
-    if (const char *v = getenv("OPIR_BATCH_MAC")) g_batch_ptx = atoi(v) != 0;
+    const void *fns[] = {(const void *)scan_batch_kernel<0>, (const void *)scan_batch_kernel<1>,
+                         (const void *)scan_batch_kernel<2>, (const void *)scan_batch_kernel<3>};
+    for (const void *f : fns) {
+      e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+      if (e != cudaSuccess) return e;
+    }
+    g_batch_form = 3;  // measured fastest: carry-chained 32-bit multiply-adds
+    if (const char *v = getenv("OPIR_BATCH_MAC")) g_batch_form = atoi(v) & 3;
   }
   g_cfg = 0;
   if (const char *v = getenv("OPIR_SCAN_CFG")) {
@@ -699,12 +726,18 @@ bool launch_scan_batched(const uint64_t *dbs, const uint4 *qsb, uint64_t *out, s
   const int sms = g_num_sms > 0 ? g_num_sms : 152;
   long long grid = sms;
   if (grid > G.items) grid = G.items;
-  if (g_batch_ptx)
-    scan_batch_kernel<true><<<(unsigned)grid, kBWarps * 32 + 32, smem, s>>>(
-        dbs, qsb, out, out_stride, G, C, mu_lo, mu_hi, status);
-  else
-    scan_batch_kernel<false><<<(unsigned)grid, kBWarps * 32 + 32, smem, s>>>(
-        dbs, qsb, out, out_stride, G, C, mu_lo, mu_hi, status);
+  switch (g_batch_form) {
+#define OPIR_BATCH(F)                                                        \
+  case F:                                                                    \
+    scan_batch_kernel<F><<<(unsigned)grid, kBWarps * 32 + 32, smem, s>>>(   \
+        dbs, qsb, out, out_stride, G, C, mu_lo, mu_hi, status);             \
+    break;
+    OPIR_BATCH(0)
+    OPIR_BATCH(1)
+    OPIR_BATCH(2)
+    OPIR_BATCH(3)
+#undef OPIR_BATCH
+  }
   return true;
 }
 
