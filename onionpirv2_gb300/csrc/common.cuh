@@ -121,26 +121,37 @@ __device__ __forceinline__ uint64_t mul_shoup_lazy(uint64_t x, uint64_t w, uint6
   return x * w - hq * q;
 }
 
-// lazy CT butterfly: inputs and outputs in [0, 4q)
-__device__ __forceinline__ void ct_bf(uint64_t &x, uint64_t &y, ulonglong2 w, uint64_t q,
-                                      uint64_t q2) {
-  const uint64_t u = x >= q2 ? x - q2 : x;
-  const uint64_t t = mul_shoup_lazy(y, w.x, w.y, q);
-  x = u + t;
-  y = u - t + q2;
+// x * w mod q up to three extra q: result in [0, 4q) for any x < 2^64.  The
+// Shoup quotient x * ws / 2^64 is taken from three of the four 32x32 partial
+// products (the low one and the carries out of the middle ones are dropped),
+// which undercounts it by at most 2.
+__device__ __forceinline__ uint64_t mul_shoup_lazy4(uint64_t x, uint64_t w, uint64_t ws, uint64_t q) {
+  const uint32_t x0 = (uint32_t)x, x1 = (uint32_t)(x >> 32);
+  const uint32_t s0 = (uint32_t)ws, s1 = (uint32_t)(ws >> 32);
+  const uint64_t hq = (uint64_t)x1 * s1 + __umulhi(x1, s0) + __umulhi(x0, s1);
+  return x * w - hq * q;
 }
-// lazy GS butterfly: inputs and outputs in [0, 2q)
+
+// lazy CT butterfly: inputs and outputs in [0, 8q) (q4 = 4q; q < 2^60)
+__device__ __forceinline__ void ct_bf(uint64_t &x, uint64_t &y, ulonglong2 w, uint64_t q,
+                                      uint64_t q4) {
+  const uint64_t u = x >= q4 ? x - q4 : x;
+  const uint64_t t = mul_shoup_lazy4(y, w.x, w.y, q);
+  x = u + t;
+  y = u - t + q4;
+}
+// lazy GS butterfly: inputs and outputs in [0, 4q)
 __device__ __forceinline__ void gs_bf(uint64_t &x, uint64_t &y, ulonglong2 w, uint64_t q,
-                                      uint64_t q2) {
+                                      uint64_t q4) {
   const uint64_t u = x, v = y;
   const uint64_t s = u + v;
-  x = s >= q2 ? s - q2 : s;
-  y = mul_shoup_lazy(u - v + q2, w.x, w.y, q);
+  x = s >= q4 ? s - q4 : s;
+  y = mul_shoup_lazy4(u - v + q4, w.x, w.y, q);
 }
 
 // Three CT stages (bits lo+2, lo+1, lo).  Stage on bit b: twiddle m + (idx >> (b+1)), m = 2^(10-b).
 __device__ __forceinline__ void ct_pass3(uint64_t r[8], int tid, int lo, const ulonglong2 *tw,
-                                         uint64_t q, uint64_t q2) {
+                                         uint64_t q, uint64_t q4) {
   const int base = pass_index(tid, 0, lo);
 #pragma unroll
   for (int s = 2; s >= 0; --s) {
@@ -151,12 +162,12 @@ __device__ __forceinline__ void ct_pass3(uint64_t r[8], int tid, int lo, const u
     for (int e = 0; e < 8; ++e) {
       if (e & half) continue;
       const int idx = base | (e << lo);
-      ct_bf(r[e], r[e | half], __ldg(tw + m + (idx >> (b + 1))), q, q2);
+      ct_bf(r[e], r[e | half], __ldg(tw + m + (idx >> (b + 1))), q, q4);
     }
   }
 }
 __device__ __forceinline__ void gs_pass3(uint64_t r[8], int tid, int lo, const ulonglong2 *tw,
-                                         uint64_t q, uint64_t q2) {
+                                         uint64_t q, uint64_t q4) {
   const int base = pass_index(tid, 0, lo);
 #pragma unroll
   for (int s = 0; s <= 2; ++s) {
@@ -167,36 +178,36 @@ __device__ __forceinline__ void gs_pass3(uint64_t r[8], int tid, int lo, const u
     for (int e = 0; e < 8; ++e) {
       if (e & half) continue;
       const int idx = base | (e << lo);
-      gs_bf(r[e], r[e | half], __ldg(tw + m + (idx >> (b + 1))), q, q2);
+      gs_bf(r[e], r[e | half], __ldg(tw + m + (idx >> (b + 1))), q, q4);
     }
   }
 }
 // Stages on bits 1 and 0: the thread's slots 8 tid .. 8 tid + 7 form the
 // radix-4 groups g = 2 tid and 2 tid + 1.
 __device__ __forceinline__ void ct_pass2(uint64_t r[8], int tid, const ulonglong2 *tw, uint64_t q,
-                                         uint64_t q2) {
+                                         uint64_t q4) {
 #pragma unroll
   for (int gsub = 0; gsub < 2; ++gsub) {
     const int g = 2 * tid + gsub;
     uint64_t *x = r + 4 * gsub;
     const ulonglong2 w1 = __ldg(tw + 512 + g);
-    ct_bf(x[0], x[2], w1, q, q2);
-    ct_bf(x[1], x[3], w1, q, q2);
-    ct_bf(x[0], x[1], __ldg(tw + 1024 + 2 * g), q, q2);
-    ct_bf(x[2], x[3], __ldg(tw + 1024 + 2 * g + 1), q, q2);
+    ct_bf(x[0], x[2], w1, q, q4);
+    ct_bf(x[1], x[3], w1, q, q4);
+    ct_bf(x[0], x[1], __ldg(tw + 1024 + 2 * g), q, q4);
+    ct_bf(x[2], x[3], __ldg(tw + 1024 + 2 * g + 1), q, q4);
   }
 }
 __device__ __forceinline__ void gs_pass2(uint64_t r[8], int tid, const ulonglong2 *tw, uint64_t q,
-                                         uint64_t q2) {
+                                         uint64_t q4) {
 #pragma unroll
   for (int gsub = 0; gsub < 2; ++gsub) {
     const int g = 2 * tid + gsub;
     uint64_t *x = r + 4 * gsub;
-    gs_bf(x[0], x[1], __ldg(tw + 1024 + 2 * g), q, q2);
-    gs_bf(x[2], x[3], __ldg(tw + 1024 + 2 * g + 1), q, q2);
+    gs_bf(x[0], x[1], __ldg(tw + 1024 + 2 * g), q, q4);
+    gs_bf(x[2], x[3], __ldg(tw + 1024 + 2 * g + 1), q, q4);
     const ulonglong2 w1 = __ldg(tw + 512 + g);
-    gs_bf(x[0], x[2], w1, q, q2);
-    gs_bf(x[1], x[3], w1, q, q2);
+    gs_bf(x[0], x[2], w1, q, q4);
+    gs_bf(x[1], x[3], w1, q, q4);
   }
 }
 
@@ -238,56 +249,58 @@ __device__ __forceinline__ void stg_slot8(uint64_t *base, const uint64_t v[8]) {
   for (int j = 0; j < 4; ++j) p[j] = make_ulonglong2(v[2 * j], v[2 * j + 1]);
 }
 
-// Forward NTT: r strided (values < 4q) -> r slot (fully reduced).  sa, sb:
+// Forward NTT: r strided (values < 8q) -> r slot (fully reduced).  sa, sb:
 // two shared buffers of kSmemPoly words; all 256 threads of the group take
 // part; ends with a barrier so sa/sb may be reused at once.
 __device__ __forceinline__ void ntt_fwd(uint64_t r[8], uint64_t *sa, uint64_t *sb,
                                         const ulonglong2 *tw, uint64_t q) {
   const int tid = threadIdx.x & (kNttThreads - 1);
-  const uint64_t q2 = 2 * q;
-  ct_pass3(r, tid, 8, tw, q, q2);
+  const uint64_t q2 = 2 * q, q4 = 4 * q;
+  ct_pass3(r, tid, 8, tw, q, q4);
   store_pass(sa, r, tid, 8);
   __syncthreads();
   load_pass(sa, r, tid, 5);
-  ct_pass3(r, tid, 5, tw, q, q2);
+  ct_pass3(r, tid, 5, tw, q, q4);
   store_pass(sb, r, tid, 5);
   __syncthreads();
   load_pass(sb, r, tid, 2);
-  ct_pass3(r, tid, 2, tw, q, q2);
+  ct_pass3(r, tid, 2, tw, q, q4);
   store_pass(sa, r, tid, 2);
   __syncthreads();
   load_slots(sa, r, tid);
-  ct_pass2(r, tid, tw, q, q2);
+  ct_pass2(r, tid, tw, q, q4);
 #pragma unroll
   for (int e = 0; e < 8; ++e) {
-    uint64_t v = r[e] >= q2 ? r[e] - q2 : r[e];
+    uint64_t v = r[e] >= q4 ? r[e] - q4 : r[e];
+    v = v >= q2 ? v - q2 : v;
     r[e] = v >= q ? v - q : v;
   }
   __syncthreads();
 }
 
-// Inverse NTT: r slot (values < 2q) -> r strided (fully reduced), scaled by N^-1.
+// Inverse NTT: r slot (values < 4q) -> r strided (fully reduced), scaled by N^-1.
 __device__ __forceinline__ void ntt_inv(uint64_t r[8], uint64_t *sa, uint64_t *sb,
                                         const ulonglong2 *tw, uint64_t q, uint64_t n_inv,
                                         uint64_t n_inv_s) {
   const int tid = threadIdx.x & (kNttThreads - 1);
-  const uint64_t q2 = 2 * q;
-  gs_pass2(r, tid, tw, q, q2);
+  const uint64_t q2 = 2 * q, q4 = 4 * q;
+  gs_pass2(r, tid, tw, q, q4);
   store_slots(sa, r, tid);
   __syncthreads();
   load_pass(sa, r, tid, 2);
-  gs_pass3(r, tid, 2, tw, q, q2);
+  gs_pass3(r, tid, 2, tw, q, q4);
   store_pass(sb, r, tid, 2);
   __syncthreads();
   load_pass(sb, r, tid, 5);
-  gs_pass3(r, tid, 5, tw, q, q2);
+  gs_pass3(r, tid, 5, tw, q, q4);
   store_pass(sa, r, tid, 5);
   __syncthreads();
   load_pass(sa, r, tid, 8);
-  gs_pass3(r, tid, 8, tw, q, q2);
+  gs_pass3(r, tid, 8, tw, q, q4);
 #pragma unroll
   for (int e = 0; e < 8; ++e) {
-    const uint64_t v = mul_shoup_lazy(r[e], n_inv, n_inv_s, q);
+    uint64_t v = mul_shoup_lazy4(r[e], n_inv, n_inv_s, q);
+    v = v >= q2 ? v - q2 : v;
     r[e] = v >= q ? v - q : v;
   }
   __syncthreads();
