@@ -141,6 +141,8 @@ struct Db {
   uint64_t num_pt = 0;
   int ndim = 1, u = 1, h = 0;
   DevBuf dbs;
+  DevBuf dbl;              // bf16 limb plane of dbs for the tensor-core product (built on demand)
+  bool dbl_valid = false;  // cleared whenever dbs changes
 };
 
 struct Client {
@@ -152,7 +154,7 @@ struct Client {
 
 struct Workspace {
   // sized for (batch, shape); grown on demand
-  DevBuf exp0, exp1, gsw, qs, res, resp, packed, queries, ingest, coeffs;
+  DevBuf exp0, exp1, gsw, qs, ql, res, resp, packed, queries, ingest, coeffs;
   PinnedBuf h_in, h_out;
 };
 
@@ -177,6 +179,11 @@ struct opir_ctx {
   Workspace ws;
   DevBuf status;  // device status word: bounded-wait timeouts (async.cuh)
   bool batch_scan = true;  // batched GEMM for batches >= 2 (OPIR_BATCH_SCAN=0 turns it off)
+  // batched GEMM engine: 0 = integer multiply-add kernel, 1 = tensor cores
+  // from tc_min_batch queries on (OPIR_TC, OPIR_TC_MIN_BATCH)
+  int tc_mode = 1;
+  int tc_min_batch = 2;
+  uint64_t r64 = 0, r128 = 0;  // 2^64 and 2^128 mod q
   bool timing = false;
   cudaEvent_t ev[8] = {};
   float stage_ms[6] = {};
@@ -332,7 +339,24 @@ int run_pipeline(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
   // a batch of queries shares one pass over the database (batched GEMM);
   // a single query (or an unsupported shape) streams it once per query
   const bool batched = batch >= 2 && ctx->batch_scan && nr % 32 == 0 && n1 % 16 == 0;
-  if (batched) {
+  const bool tensor = batch >= 2 && ctx->batch_scan && ctx->tc_mode == 1 &&
+                      batch >= ctx->tc_min_batch && tc_scan_supported((int)n1, (int)nr);
+  if (tensor) {
+    if (!db.dbl_valid) {
+      CK(db.dbl.alloc(tc_db_limb_bytes((int)n1, (int)nr)), "alloc database limb plane");
+      launch_db_limbs(db.dbs.as<uint64_t>(), db.dbl.as<uint16_t>(), (int)n1, (int)nr, s);
+      ctx->launches++;
+      db.dbl_valid = true;
+    }
+    CK(W.ql.alloc(tc_query_limb_bytes((int)n1)), "alloc query limbs");
+    launch_query_prep_batched(leaves, leaves_stride, W.qs.as<uint4>(), (int)n1, batch,
+                              ctx->Mq.tab, s);
+    record(ctx, 6);
+    ctx->launches += launch_tc_scan_batched(
+        db.dbl.as<uint16_t>(), W.qs.as<uint4>(), W.ql.as<uint16_t>(), W.res.as<uint64_t>(),
+        res_stride, (int)n1, (int)nr, batch, ctx->Mq.tab.q, ctx->Mq.tab.mu_lo, ctx->Mq.tab.mu_hi,
+        ctx->r64, ctx->r128, ctx->status.as<uint32_t>(), s) - 1;
+  } else if (batched) {
     launch_query_prep_batched(leaves, leaves_stride, W.qs.as<uint4>(), (int)n1, batch,
                               ctx->Mq.tab, s);
     record(ctx, 6);
@@ -417,6 +441,7 @@ int ensure_db_storage(opir_ctx *ctx, Db &db) {
 }
 
 int ingest_chunk_coeffs(opir_ctx *ctx, Db &db, size_t pt0, size_t count) {
+  db.dbl_valid = false;
   launch_db_ntt_scatter(ctx->ws.coeffs.as<uint64_t>(), pt0, count, db.dbs.as<uint64_t>(),
                         (int)db.shape.fst_dim_sz, (int)db.shape.other_dim_sz, ctx->Mq.tab, ctx->C,
                         ctx->stream);
@@ -461,7 +486,8 @@ int opir_ctx_create(const opir_params *P, int device, opir_ctx **out) {
   if (rc) return rc;
   rc = build_modtab(c, c->Mp, p);
   if (rc) return rc;
-  if (init_kernel_attributes() != cudaSuccess || init_scan_attributes() != cudaSuccess)
+  if (init_kernel_attributes() != cudaSuccess || init_scan_attributes() != cudaSuccess ||
+      init_tc_attributes() != cudaSuccess)
     return OPIR_ERR_CUDA;
   if (c->status.alloc(sizeof(uint32_t)) != cudaSuccess ||
       cudaMemset(c->status.p, 0, sizeof(uint32_t)) != cudaSuccess)
@@ -470,6 +496,10 @@ int opir_ctx_create(const opir_params *P, int device, opir_ctx **out) {
     return OPIR_ERR_CUDA;
   c->stream = c->own_stream;
   if (const char *v = getenv("OPIR_BATCH_SCAN")) c->batch_scan = atoi(v) != 0;
+  if (const char *v = getenv("OPIR_TC")) c->tc_mode = atoi(v) != 0;
+  if (const char *v = getenv("OPIR_TC_MIN_BATCH")) c->tc_min_batch = atoi(v);
+  c->r64 = (uint64_t)(((u128)1 << 64) % q);
+  c->r128 = mulmod(c->r64, c->r64, q);
   for (auto &e : c->ev)
     if (cudaEventCreate(&e) != cudaSuccess) return OPIR_ERR_CUDA;
   Consts &C = c->C;
@@ -626,6 +656,7 @@ int opir_db_upload_aligned(opir_ctx *ctx, uint32_t db_id, const uint64_t *aligne
   const size_t bytes = db->num_pt * (size_t)kN * 8;
   CK(tmp.alloc(bytes), "alloc upload");
   CK(cudaMemcpyAsync(tmp.p, aligned, bytes, cudaMemcpyHostToDevice, ctx->stream), "upload database");
+  db->dbl_valid = false;
   launch_db_from_aligned(tmp.as<uint64_t>(), db->dbs.as<uint64_t>(), (int)db->shape.fst_dim_sz,
                          (int)db->shape.other_dim_sz, ctx->stream);
   ctx->launches++;

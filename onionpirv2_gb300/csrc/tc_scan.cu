@@ -1,0 +1,453 @@
+// tc_scan.cu -- first dimension of a batch of queries on the tcgen05 tensor cores.
+//
+// Per NTT slot c the first dimension of B queries is the integer product
+// (n_rest x n1) . (n1 x 2B) of 60-bit residues, accumulated exactly
+// (matrix.cpp:79-97, 220-235 compute it with 64x64->128-bit multiply-adds,
+// server.cpp:178-293 reduce the 128-bit sums mod q).  Here every residue is
+// split into eight balanced 8-bit limbs, v = sum_i d_i 2^(8i) with d_i in
+// [-128, 127] (the top limb in [0, 16]); each limb is exact in bf16, a limb
+// product is at most 2^14 in magnitude and a sum of n1 <= 512 of them at most
+// 2^23, so the fp32 accumulation of tcgen05.mma kind::f16 is exact.
+//
+// MMA shape per tile: M = 16 database rows x 8 limbs = 128 (TMEM lanes),
+// N = 2B query polynomials x 8 limbs <= 512 (TMEM columns, two MMAs of <= 256),
+// K = n1.  Cell (row r, limb i ; query poly b', limb j) holds
+// x_ij = sum_k d_i(A[r,k]) d_j(Q[k,b']); the result is
+// sum_s Y_s 2^(8s), Y_s = sum_{i+j=s} x_ij.  The epilogue gathers the
+// anti-diagonal sums Y_s across the 8 lanes of a row with one skewed
+// shuffle pass, rebuilds the exact (<= 2^130) integer from them and reduces
+// it mod q -- the same value the 128-bit accumulation of the reference
+// reduces, without its wrap-around (the sum is exact here).
+//
+// Data layout in HBM (bf16 limbs, "core matrices" of 8 rows x 8 k):
+//   database  dbl[c][rb][k/8][r%16][i][k%8]      (rb = r / 16)
+//   queries   ql [c][k/8][b'][j][k%8]            (b' = 2 b + poly)
+// so the slice of a pipeline stage (32 k) of either operand is contiguous and
+// lands in shared memory in the K-major, no-swizzle canonical layout that the
+// tcgen05 shared-memory descriptors below describe (leading byte offset =
+// stride between core matrices along k, stride byte offset = 128 between
+// 8-row groups).
+#include <cuda_bf16.h>
+
+#include "async.cuh"
+#include "common.cuh"
+#include "kernels.h"
+
+namespace opir {
+namespace {
+
+constexpr int kTcRows = 16;                 // database rows per tile
+constexpr int kTcKC = 32;                   // k per pipeline stage
+constexpr int kTcKB = kTcKC / 8;            // core matrices along k per stage
+constexpr int kTcStages = 5;
+constexpr int kTcMaxNB = 64;                // query polynomials per pass (32 queries)
+constexpr uint32_t kTcABytes = kTcKB * kTcRows * 128;        // 8 KB
+constexpr uint32_t kTcBBytesMax = kTcKB * kTcMaxNB * 128;    // 32 KB
+constexpr uint32_t kTcStageBytes = kTcABytes + kTcBBytesMax;
+constexpr int kTcYStride = 168;             // int32 words per (warp, row) block of Y staging
+constexpr int kTcThreads = 192;             // 4 epilogue warps, producer, MMA
+constexpr uint32_t kTcTmemCols = 512;
+
+constexpr uint32_t kErrTcWaitFull = 8u;
+constexpr uint32_t kErrTcWaitEmpty = 16u;
+constexpr uint32_t kErrTcWaitAcc = 32u;
+constexpr uint32_t kErrTcDrain = 64u;
+constexpr uint32_t kErrTcRange = 128u;
+
+struct TcGeom {
+  int n1, n_rest, batch, nb;  // nb = query polynomials in the pass (2 x padded batch)
+  int n_rb, nkc;              // row tiles, k-chunks per tile
+  long long units;            // N * n_rb tiles
+  uint32_t b_bytes;           // query bytes per stage
+  uint32_t idesc[2];          // instruction descriptors of the two column halves
+  int halves;
+};
+
+// Shared-memory matrix descriptor (tcgen05): start address, leading byte
+// offset (k direction), stride byte offset (8-row groups), version 1, no
+// swizzle.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((uint64_t)1 << 46);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                       uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_ld32(uint32_t addr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
+      "%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(addr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// sum_s y_s 2^(8s) (exact, >= 0 and < 2^132) mod q
+__device__ __forceinline__ uint64_t tc_combine(const int (&y)[16], uint64_t q, uint64_t mu_lo,
+                                               uint64_t mu_hi, uint64_t r64, uint64_t r128,
+                                               bool &range_ok) {
+  uint32_t w[4];
+  long long carry = 0;
+#pragma unroll
+  for (int g = 0; g < 4; ++g) {
+    const long long s = carry + (long long)y[4 * g] + (long long)y[4 * g + 1] * 256 +
+                        (long long)y[4 * g + 2] * 65536 + (long long)y[4 * g + 3] * 16777216;
+    w[g] = (uint32_t)s;
+    carry = s >> 32;  // arithmetic: floor division
+  }
+  range_ok = carry >= 0 && carry < 16;
+  const uint64_t lo = ((uint64_t)w[1] << 32) | w[0];
+  const uint64_t hi = ((uint64_t)w[3] << 32) | w[2];
+  // hi 2^64 + lo + carry 2^128 == hi r64 + lo + carry r128 (mod q); < 2^125
+  U128 acc = mul_wide(hi, r64);
+  add_to(acc, U128{lo, 0});
+  add_to(acc, U128{(uint64_t)(carry & 15) * r128, 0});
+  return barrett128(acc, q, mu_lo, mu_hi);
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1)
+    tc_scan_kernel(const uint16_t *__restrict__ dbl, const uint16_t *__restrict__ ql, uint64_t *out,
+                   size_t out_stride, int b_base, TcGeom G, uint64_t q, uint64_t mu_lo,
+                   uint64_t mu_hi, uint64_t r64, uint64_t r128, uint32_t *status) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  int *ysm = reinterpret_cast<int *>(smem + kTcStages * kTcStageBytes);
+  uint64_t *bars = reinterpret_cast<uint64_t *>(ysm + 4 * 4 * kTcYStride);
+  uint64_t *full = bars, *empty = bars + kTcStages;
+  uint64_t *acc_full = bars + 2 * kTcStages, *acc_empty = acc_full + 1, *drained = acc_full + 2;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * kTcStages + 3);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kTcStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(acc_full, 1);
+    mbar_init(acc_empty, 4);
+    mbar_init(drained, 1);
+    mbar_fence_init();
+  }
+  if (warp == 5) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(kTcTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t smem_base = smem_u32(smem);
+  const int kblk = G.n1 / 8;
+
+  if (warp == 4) {
+    // ------------------------------ producer ------------------------------
+    if (lane == 0) {
+      long long it = 0;
+      bool ok = true;
+      for (long long u = blockIdx.x; u < G.units && ok; u += gridDim.x) {
+        const long long c = u / G.n_rb, rb = u % G.n_rb;
+        const uint16_t *a_src = dbl + (size_t)(c * G.n_rb + rb) * kblk * (kTcRows * 64);
+        const uint16_t *b_src = ql + (size_t)c * kblk * G.nb * 64;
+        for (int kc = 0; kc < G.nkc; ++kc, ++it) {
+          const int s = (int)(it % kTcStages);
+          const long long round = it / kTcStages;
+          if (round > 0 && !mbar_wait(&empty[s], (uint32_t)((round - 1) & 1))) {
+            report_error(status, kErrTcWaitEmpty);
+            ok = false;
+            break;
+          }
+          unsigned char *st = smem + (size_t)s * kTcStageBytes;
+          mbar_arrive_expect_tx(&full[s], kTcABytes + G.b_bytes);
+          bulk_g2s(st, a_src + (size_t)kc * kTcKB * (kTcRows * 64), kTcABytes, &full[s]);
+          bulk_g2s(st + kTcABytes, b_src + (size_t)kc * kTcKB * G.nb * 64, G.b_bytes, &full[s]);
+        }
+      }
+      // never leave the CTA with copies still landing in its shared memory
+      const long long first = it > kTcStages ? it - kTcStages : 0;
+      for (long long j = first; j < it; ++j)
+        if (!mbar_wait(&full[j % kTcStages], (uint32_t)((j / kTcStages) & 1))) {
+          report_error(status, kErrTcDrain);
+          break;
+        }
+    }
+  } else if (warp == 5) {
+    // ------------------------------ MMA issue ------------------------------
+    if (lane == 0) {
+      const uint32_t lbo_a = kTcRows * 128, lbo_b = (uint32_t)G.nb * 128;
+      long long it = 0, j = 0;
+      bool ok = true;
+      for (long long u = blockIdx.x; u < G.units && ok; u += gridDim.x, ++j) {
+        if (j > 0 && !mbar_wait(acc_empty, (uint32_t)((j - 1) & 1))) {
+          report_error(status, kErrTcWaitAcc);
+          break;
+        }
+        tc_fence_after();
+        for (int kc = 0; kc < G.nkc; ++kc, ++it) {
+          const int s = (int)(it % kTcStages);
+          if (!mbar_wait(&full[s], (uint32_t)((it / kTcStages) & 1))) {
+            report_error(status, kErrTcWaitFull);
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t sa = smem_base + (uint32_t)s * kTcStageBytes, sb = sa + kTcABytes;
+#pragma unroll
+          for (int ks = 0; ks < kTcKC / 16; ++ks) {
+            const uint64_t da = smem_desc(sa + ks * 2 * lbo_a, lbo_a, 128);
+            const uint32_t acc = (kc > 0 || ks > 0) ? 1u : 0u;
+            tc_mma(tmem, da, smem_desc(sb + ks * 2 * lbo_b, lbo_b, 128), G.idesc[0], acc);
+            if (G.halves > 1)
+              tc_mma(tmem + 256, da, smem_desc(sb + 32 * 128 + ks * 2 * lbo_b, lbo_b, 128),
+                     G.idesc[1], acc);
+          }
+          tc_commit(&empty[s]);  // the stage is free once these MMAs have read it
+        }
+        if (ok) tc_commit(acc_full);
+      }
+      // wait for every MMA issued so far before the columns are released
+      tc_commit(drained);
+      if (!mbar_wait(drained, 0)) report_error(status, kErrTcDrain);
+    }
+  } else {
+    // ------------------------------ epilogue ------------------------------
+    const int t8 = lane & 7, rsub = lane >> 3;
+    int *yw = ysm + (warp * 4 + rsub) * kTcYStride;
+    const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+    long long j = 0;
+    bool range_ok = true;
+    for (long long u = blockIdx.x; u < G.units; u += gridDim.x, ++j) {
+      bool got = true;
+      if (lane == 0) got = mbar_wait_sleep(acc_full, (uint32_t)(j & 1));
+      got = __shfl_sync(0xffffffffu, got, 0);
+      if (!got) {
+        if (lane == 0) report_error(status, kErrTcWaitAcc);
+        break;
+      }
+      tc_fence_after();
+      const long long c = u / G.n_rb, rb = u % G.n_rb;
+      const size_t row = (size_t)rb * kTcRows + warp * 4 + rsub;
+      for (int grp = 0; grp < G.nb / 8; ++grp) {
+#pragma unroll
+        for (int hc = 0; hc < 2; ++hc) {
+          uint32_t r[32];
+          tmem_ld32(lane_addr + (uint32_t)((grp * 2 + hc) * 32), r);
+#pragma unroll
+          for (int bl = 0; bl < 4; ++bl) {
+            int x[8];
+#pragma unroll
+            for (int d = 0; d < 8; ++d) x[d] = __float2int_rn(__uint_as_float(r[bl * 8 + d]));
+            // skewed exchange: lane t8 collects Y_t8 and Y_(t8+8) of its row
+            int ylo = x[0], yhi = 0;
+#pragma unroll
+            for (int d = 1; d < 8; ++d) {
+              const int v = __shfl_sync(0xffffffffu, x[d], (lane & ~7) | ((lane - d) & 7));
+              if (d <= t8)
+                ylo += v;
+              else
+                yhi += v;
+            }
+            int *yb = yw + (hc * 4 + bl) * 20;
+            yb[t8] = ylo;
+            yb[t8 + 8] = yhi;
+          }
+        }
+        __syncwarp();
+        int y[16];
+        const int4 *src = reinterpret_cast<const int4 *>(yw + t8 * 20);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          const int4 t = src[v];
+          y[4 * v] = t.x;
+          y[4 * v + 1] = t.y;
+          y[4 * v + 2] = t.z;
+          y[4 * v + 3] = t.w;
+        }
+        __syncwarp();
+        bool ok_one = true;
+        const uint64_t val = tc_combine(y, q, mu_lo, mu_hi, r64, r128, ok_one);
+        range_ok &= ok_one;
+        const int bq = grp * 8 + t8;  // query polynomial in the pass
+        const int b = bq >> 1;
+        if (b < G.batch)
+          out[(size_t)(b_base + b) * out_stride + (row * 2 + (bq & 1)) * kN + c] = val;
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(acc_empty);
+    }
+    if (!range_ok) report_error(status, kErrTcRange);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 5) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(kTcTmemCols)
+                 : "memory");
+  }
+}
+
+// balanced 8-bit limbs of a residue < 2^60, as bf16 bit patterns
+__device__ __forceinline__ void limbs8(uint64_t v, uint16_t (&d)[8]) {
+  int carry = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    int x = (int)(v & 255u) + carry;
+    v >>= 8;
+    carry = x >= 128;
+    x -= carry << 8;
+    d[i] = __bfloat16_as_ushort(__float2bfloat16_rn((float)x));
+  }
+}
+
+// one thread: 8 consecutive k of one (slot, row) -> one 128-byte core matrix
+__global__ void db_limb_kernel(const uint64_t *__restrict__ dbs, uint16_t *__restrict__ dbl,
+                               int n1, int n_rest) {
+  const int kblk = n1 / 8, n_rb = n_rest / kTcRows;
+  const long long total = (long long)kN * n_rb * kblk * kTcRows;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int r16 = (int)(t % kTcRows);
+    long long rest = t / kTcRows;
+    const int kb = (int)(rest % kblk);
+    rest /= kblk;
+    const int rb = (int)(rest % n_rb);
+    const long long c = rest / n_rb;
+    const uint64_t *src = dbs + (size_t)c * n1 * n_rest + (size_t)kb * 8 * n_rest +
+                          (size_t)rb * kTcRows + r16;
+    uint16_t d[8][8];  // [kk][limb]
+#pragma unroll
+    for (int kk = 0; kk < 8; ++kk) {
+      const uint64_t w = src[(size_t)kk * n_rest];
+      limbs8((w & 0x3FFFFFFFull) + ((w >> 32) << 30), d[kk]);
+    }
+    uint4 *dst = reinterpret_cast<uint4 *>(dbl + (size_t)t * 64);
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+      dst[i] = make_uint4(d[0][i] | (uint32_t)d[1][i] << 16, d[2][i] | (uint32_t)d[3][i] << 16,
+                          d[4][i] | (uint32_t)d[5][i] << 16, d[6][i] | (uint32_t)d[7][i] << 16);
+  }
+}
+
+// one thread: 8 consecutive k of one (slot, query polynomial) of the pass
+__global__ void query_limb_kernel(const uint4 *__restrict__ qsb, uint16_t *__restrict__ ql,
+                                  int n1, int batch, int b_base, int nb, int pass_batch) {
+  const int kblk = n1 / 8;
+  const long long total = (long long)kN * kblk * nb;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int bq = (int)(t % nb);
+    const long long rest = t / nb;
+    const int kb = (int)(rest % kblk);
+    const long long c = rest / kblk;
+    const int b = bq >> 1;
+    uint16_t d[8][8];
+#pragma unroll
+    for (int kk = 0; kk < 8; ++kk) {
+      uint64_t v = 0;
+      if (b < pass_batch) {
+        const uint4 w = qsb[((size_t)c * n1 + kb * 8 + kk) * batch + b_base + b];
+        v = (bq & 1) ? (uint64_t)w.z + ((uint64_t)w.w << 30) : (uint64_t)w.x + ((uint64_t)w.y << 30);
+      }
+      limbs8(v, d[kk]);
+    }
+    uint4 *dst = reinterpret_cast<uint4 *>(ql + (size_t)t * 64);
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+      dst[i] = make_uint4(d[0][i] | (uint32_t)d[1][i] << 16, d[2][i] | (uint32_t)d[3][i] << 16,
+                          d[4][i] | (uint32_t)d[5][i] << 16, d[6][i] | (uint32_t)d[7][i] << 16);
+  }
+}
+
+constexpr size_t kTcSmem =
+    kTcStages * kTcStageBytes + 4 * 4 * kTcYStride * sizeof(int) + (2 * kTcStages + 4) * 8;
+
+int g_tc_sms = 0;
+
+uint32_t make_idesc(int n) {
+  // D f32 (bits 4-5 = 1), A and B bf16 (bits 7-9, 10-12 = 1), both K-major,
+  // N >> 3 at bits 17-22, M >> 4 at bits 24-28 (M = 128)
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((128u >> 4) << 24);
+}
+
+}  // namespace
+
+bool tc_scan_supported(int n1, int n_rest) {
+  return n1 % kTcKC == 0 && n1 <= 512 && n_rest % kTcRows == 0 && n_rest >= kTcRows;
+}
+
+size_t tc_db_limb_bytes(int n1, int n_rest) { return (size_t)kN * n1 * n_rest * 16; }
+size_t tc_query_limb_bytes(int n1) { return (size_t)kN * n1 * kTcMaxNB * 16; }
+
+cudaError_t init_tc_attributes() {
+  int dev;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&g_tc_sms, cudaDevAttrMultiProcessorCount, dev);
+  return cudaFuncSetAttribute(tc_scan_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)kTcSmem);
+}
+
+void launch_db_limbs(const uint64_t *dbs, uint16_t *dbl, int n1, int n_rest, cudaStream_t s) {
+  const long long total = (long long)kN * (n_rest / kTcRows) * (n1 / 8) * kTcRows;
+  const long long blocks = (total + 255) / 256;
+  db_limb_kernel<<<(unsigned)(blocks < 65536 ? blocks : 65536), 256, 0, s>>>(dbs, dbl, n1, n_rest);
+}
+
+int launch_tc_scan_batched(const uint16_t *dbl, const uint4 *qsb, uint16_t *ql, uint64_t *out,
+                           size_t out_stride, int n1, int n_rest, int batch, uint64_t q,
+                           uint64_t mu_lo, uint64_t mu_hi, uint64_t r64, uint64_t r128,
+                           uint32_t *status, cudaStream_t s) {
+  int launches = 0;
+  for (int b0 = 0; b0 < batch; b0 += kTcMaxNB / 2) {
+    const int pb = batch - b0 < kTcMaxNB / 2 ? batch - b0 : kTcMaxNB / 2;
+    const int padded = (pb + 3) / 4 * 4;  // 8 query polynomials per epilogue group
+    TcGeom G;
+    G.n1 = n1;
+    G.n_rest = n_rest;
+    G.batch = pb;
+    G.nb = 2 * padded;
+    G.n_rb = n_rest / kTcRows;
+    G.nkc = n1 / kTcKC;
+    G.units = (long long)kN * G.n_rb;
+    G.b_bytes = (uint32_t)(kTcKB * G.nb * 128);
+    const int ncols = G.nb * 8;
+    G.halves = ncols > 256 ? 2 : 1;
+    G.idesc[0] = make_idesc(ncols > 256 ? 256 : ncols);
+    G.idesc[1] = make_idesc(ncols > 256 ? ncols - 256 : 16);
+    const long long qtotal = (long long)kN * (n1 / 8) * G.nb;
+    const long long qblocks = (qtotal + 255) / 256;
+    query_limb_kernel<<<(unsigned)(qblocks < 65536 ? qblocks : 65536), 256, 0, s>>>(
+        qsb, ql, n1, batch, b0, G.nb, pb);
+    const int sms = g_tc_sms > 0 ? g_tc_sms : 152;
+    const long long grid = G.units < sms ? G.units : sms;
+    tc_scan_kernel<<<(unsigned)grid, kTcThreads, kTcSmem, s>>>(dbl, ql, out, out_stride, b0, G, q,
+                                                              mu_lo, mu_hi, r64, r128, status);
+    launches += 2;
+  }
+  return launches;
+}
+
+}  // namespace opir

@@ -226,11 +226,14 @@ def test_one_cta_and_cluster_tree_forms(oracle_lib, gpu_lib, monkeypatch, thresh
     server.close()
 
 
+@pytest.mark.parametrize("engine", ["tensor", "imad"])
 @pytest.mark.parametrize("batch", [3, 33])
-def test_batched_scan_matches_single_and_oracle(oracle_lib, gpu_lib, monkeypatch, batch):
+def test_batched_scan_matches_single_and_oracle(oracle_lib, gpu_lib, monkeypatch, batch, engine):
     """Batched GEMM (one pass over the database for up to 32 queries) equals
-    the per-query scan and the oracle, also for a partial second group."""
+    the per-query scan and the oracle, also for a partial second group, on
+    both engines (bf16-limb tensor cores, integer multiply-adds)."""
     from onionpirv2_gb300 import PirParams, PirServer
+    monkeypatch.setenv("OPIR_TC", "1" if engine == "tensor" else "0")
     o = oracle_lib.Oracle(1 << 13, 64)  # 64 x 128
     P = o.P
     assert (P.n1, P.n_rest) == (64, 128)
@@ -270,3 +273,42 @@ def test_batched_scan_matches_single_and_oracle(oracle_lib, gpu_lib, monkeypatch
     assert np.array_equal(resp, resp2)
     server.close()
     server2.close()
+
+
+@pytest.mark.parametrize("shape,batch", [
+    ((4096, 256), 2),       # 256 x 16: one row tile per slot
+    ((4096, 256), 20),      # 40 query polynomials: a 256 + 64 column split
+    ((1 << 15, 512), 5),    # 512 x 64
+    ((1 << 15, 512), 32),   # a full pass: 512 tensor-memory columns
+])
+def test_tensor_core_first_dim_matches_single_queries(oracle_lib, gpu_lib, monkeypatch, shape,
+                                                      batch):
+    """The tensor-core batched product gives every query the response of the
+    per-query scan (which the oracle pins) for several shapes and batch
+    sizes, and the oracle's response for the first and last query."""
+    from onionpirv2_gb300 import PirParams, PirServer
+    monkeypatch.setenv("OPIR_TC", "1")
+    o = oracle_lib.Oracle(*shape)
+    P = o.P
+    server = PirServer(PirParams(num_entries=shape[0], max_fst_dim=shape[1]))
+    server.gen_data(123)
+    keys = [make_client(o, 900 + j) for j in range(3)]
+    for j, (sk, gk, gswk) in enumerate(keys):
+        server.set_client_galois_key(j, gk)
+        server.set_client_gsw_key(j, gswk)
+    ids = [j % 3 for j in range(batch)]
+    idxs = [(j * 7919 + 11) % P.num_entries for j in range(batch)]
+    queries = [o.make_query(keys[ids[j]][0], 40 + j, idxs[j]) for j in range(batch)]
+    resp, packed = server.make_query_batch(ids, np.stack(queries))
+    for j in range(batch):
+        single = server.make_query(ids[j], queries[j])
+        assert np.array_equal(resp[j], single), j
+        assert packed[j].tobytes() == single.packed
+    db = o.build_db(123)
+    for j in (0, batch - 1):
+        sk, gk, gswk = keys[ids[j]]
+        ref, _, _, _ = o.make_query_server(db, gk, o.gsw_key_to_ntt(gswk), queries[j])
+        assert np.array_equal(resp[j], ref), j
+        plain, _ = o.decrypt(sk, resp[j], 2)
+        assert np.array_equal(o.entry_from_plain(idxs[j], plain), server.direct_get_entry(idxs[j]))
+    server.close()
