@@ -21,8 +21,9 @@
 //
 // Data layout in HBM (bf16 limbs, "core matrices" of 8 rows x 8 k):
 //   database  dbl[c][rb][k/8][r%16][i][k%8]      (rb = r / 16)
-//   queries   ql [c][k/8][b'][j][k%8]            (b' = 2 b + poly)
-// so the slice of a pipeline stage (32 k) of either operand is contiguous and
+//   queries   ql [c][h][k/8][b'][j][k%8]         (b' = 2 b + poly - 32 h)
+// (h: column half of at most 32 query polynomials = 256 TMEM columns), so the
+// slice of a pipeline stage (32 k) of either operand is contiguous and
 // lands in shared memory in the K-major, no-swizzle canonical layout that the
 // tcgen05 shared-memory descriptors below describe (leading byte offset =
 // stride between core matrices along k, stride byte offset = 128 between
@@ -39,14 +40,17 @@ namespace {
 constexpr int kTcRows = 16;                 // database rows per tile
 constexpr int kTcKC = 32;                   // k per pipeline stage
 constexpr int kTcKB = kTcKC / 8;            // core matrices along k per stage
-constexpr int kTcStages = 5;
+constexpr int kTcStages = 8;
 constexpr int kTcMaxNB = 64;                // query polynomials per pass (32 queries)
+constexpr int kTcHalfNB = 32;               // query polynomials per tile (256 TMEM columns)
 constexpr uint32_t kTcABytes = kTcKB * kTcRows * 128;        // 8 KB
-constexpr uint32_t kTcBBytesMax = kTcKB * kTcMaxNB * 128;    // 32 KB
+constexpr uint32_t kTcBBytesMax = kTcKB * kTcHalfNB * 128;   // 16 KB
 constexpr uint32_t kTcStageBytes = kTcABytes + kTcBBytesMax;
 constexpr int kTcYStride = 168;             // int32 words per (warp, row) block of Y staging
-constexpr int kTcThreads = 192;             // 4 epilogue warps, producer, MMA
-constexpr uint32_t kTcTmemCols = 512;
+constexpr int kTcEpiWarps = 8;              // two per TMEM lane quadrant
+constexpr int kTcThreads = (kTcEpiWarps + 2) * 32;  // epilogue warps, producer, MMA
+constexpr int kTcProducer = kTcEpiWarps, kTcMma = kTcEpiWarps + 1;
+constexpr uint32_t kTcTmemCols = 512;       // two 256-column accumulators
 
 constexpr uint32_t kErrTcWaitFull = 8u;
 constexpr uint32_t kErrTcWaitEmpty = 16u;
@@ -55,12 +59,12 @@ constexpr uint32_t kErrTcDrain = 64u;
 constexpr uint32_t kErrTcRange = 128u;
 
 struct TcGeom {
-  int n1, n_rest, batch, nb;  // nb = query polynomials in the pass (2 x padded batch)
+  int n1, n_rest, batch;      // batch: queries of the pass
+  int nh, nbh;                // column halves, query polynomials per half (multiple of 8)
   int n_rb, nkc;              // row tiles, k-chunks per tile
-  long long units;            // N * n_rb tiles
+  long long units;            // N * n_rb * nh tiles
   uint32_t b_bytes;           // query bytes per stage
-  uint32_t idesc[2];          // instruction descriptors of the two column halves
-  int halves;
+  uint32_t idesc;             // instruction descriptor (M = 128, N = 8 nbh)
 };
 
 // Shared-memory matrix descriptor (tcgen05): start address, leading byte
@@ -132,10 +136,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                    uint64_t mu_hi, uint64_t r64, uint64_t r128, uint32_t *status) {
   extern __shared__ __align__(1024) unsigned char smem[];
   int *ysm = reinterpret_cast<int *>(smem + kTcStages * kTcStageBytes);
-  uint64_t *bars = reinterpret_cast<uint64_t *>(ysm + 4 * 4 * kTcYStride);
+  uint64_t *bars = reinterpret_cast<uint64_t *>(ysm + kTcEpiWarps * 4 * kTcYStride);
   uint64_t *full = bars, *empty = bars + kTcStages;
-  uint64_t *acc_full = bars + 2 * kTcStages, *acc_empty = acc_full + 1, *drained = acc_full + 2;
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * kTcStages + 3);
+  uint64_t *acc_full = bars + 2 * kTcStages;  // [2]
+  uint64_t *acc_empty = acc_full + 2;         // [2]
+  uint64_t *drained = acc_full + 4;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * kTcStages + 5);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   if (threadIdx.x == 0) {
@@ -143,12 +149,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    mbar_init(acc_full, 1);
-    mbar_init(acc_empty, 4);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&acc_full[b], 1);
+      mbar_init(&acc_empty[b], kTcEpiWarps);
+    }
     mbar_init(drained, 1);
     mbar_fence_init();
   }
-  if (warp == 5) {
+  if (warp == kTcMma) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(tmem_slot)),
                  "r"(kTcTmemCols)
@@ -161,16 +169,18 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const uint32_t tmem = *tmem_slot;
   const uint32_t smem_base = smem_u32(smem);
   const int kblk = G.n1 / 8;
+  const long long per_c = (long long)G.n_rb * G.nh;
 
-  if (warp == 4) {
+  if (warp == kTcProducer) {
     // ------------------------------ producer ------------------------------
     if (lane == 0) {
       long long it = 0;
       bool ok = true;
       for (long long u = blockIdx.x; u < G.units && ok; u += gridDim.x) {
-        const long long c = u / G.n_rb, rb = u % G.n_rb;
+        const long long c = u / per_c, rem = u % per_c;
+        const long long rb = rem / G.nh, hf = rem % G.nh;
         const uint16_t *a_src = dbl + (size_t)(c * G.n_rb + rb) * kblk * (kTcRows * 64);
-        const uint16_t *b_src = ql + (size_t)c * kblk * G.nb * 64;
+        const uint16_t *b_src = ql + (size_t)(c * G.nh + hf) * kblk * G.nbh * 64;
         for (int kc = 0; kc < G.nkc; ++kc, ++it) {
           const int s = (int)(it % kTcStages);
           const long long round = it / kTcStages;
@@ -182,7 +192,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           unsigned char *st = smem + (size_t)s * kTcStageBytes;
           mbar_arrive_expect_tx(&full[s], kTcABytes + G.b_bytes);
           bulk_g2s(st, a_src + (size_t)kc * kTcKB * (kTcRows * 64), kTcABytes, &full[s]);
-          bulk_g2s(st + kTcABytes, b_src + (size_t)kc * kTcKB * G.nb * 64, G.b_bytes, &full[s]);
+          bulk_g2s(st + kTcABytes, b_src + (size_t)kc * kTcKB * G.nbh * 64, G.b_bytes, &full[s]);
         }
       }
       // never leave the CTA with copies still landing in its shared memory
@@ -193,18 +203,21 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           break;
         }
     }
-  } else if (warp == 5) {
+  } else if (warp == kTcMma) {
     // ------------------------------ MMA issue ------------------------------
     if (lane == 0) {
-      const uint32_t lbo_a = kTcRows * 128, lbo_b = (uint32_t)G.nb * 128;
+      const uint32_t lbo_a = kTcRows * 128, lbo_b = (uint32_t)G.nbh * 128;
       long long it = 0, j = 0;
       bool ok = true;
       for (long long u = blockIdx.x; u < G.units && ok; u += gridDim.x, ++j) {
-        if (j > 0 && !mbar_wait(acc_empty, (uint32_t)((j - 1) & 1))) {
+        const int buf = (int)(j & 1);
+        // accumulator buf was last used by tile j - 2
+        if (j >= 2 && !mbar_wait(&acc_empty[buf], (uint32_t)(((j >> 1) - 1) & 1))) {
           report_error(status, kErrTcWaitAcc);
           break;
         }
         tc_fence_after();
+        const uint32_t d = tmem + (uint32_t)buf * 256;
         for (int kc = 0; kc < G.nkc; ++kc, ++it) {
           const int s = (int)(it % kTcStages);
           if (!mbar_wait(&full[s], (uint32_t)((it / kTcStages) & 1))) {
@@ -215,17 +228,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           tc_fence_after();
           const uint32_t sa = smem_base + (uint32_t)s * kTcStageBytes, sb = sa + kTcABytes;
 #pragma unroll
-          for (int ks = 0; ks < kTcKC / 16; ++ks) {
-            const uint64_t da = smem_desc(sa + ks * 2 * lbo_a, lbo_a, 128);
-            const uint32_t acc = (kc > 0 || ks > 0) ? 1u : 0u;
-            tc_mma(tmem, da, smem_desc(sb + ks * 2 * lbo_b, lbo_b, 128), G.idesc[0], acc);
-            if (G.halves > 1)
-              tc_mma(tmem + 256, da, smem_desc(sb + 32 * 128 + ks * 2 * lbo_b, lbo_b, 128),
-                     G.idesc[1], acc);
-          }
+          for (int ks = 0; ks < kTcKC / 16; ++ks)
+            tc_mma(d, smem_desc(sa + ks * 2 * lbo_a, lbo_a, 128),
+                   smem_desc(sb + ks * 2 * lbo_b, lbo_b, 128), G.idesc,
+                   (kc > 0 || ks > 0) ? 1u : 0u);
           tc_commit(&empty[s]);  // the stage is free once these MMAs have read it
         }
-        if (ok) tc_commit(acc_full);
+        if (ok) tc_commit(&acc_full[buf]);
       }
       // wait for every MMA issued so far before the columns are released
       tc_commit(drained);
@@ -233,27 +242,34 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
   } else {
     // ------------------------------ epilogue ------------------------------
+    // warp: TMEM lane quadrant qd (rows 4 qd .. 4 qd + 3 of the tile), and
+    // every other group of 8 query polynomials starting at part
+    const int qd = warp & 3, part = warp >> 2;
     const int t8 = lane & 7, rsub = lane >> 3;
     int *yw = ysm + (warp * 4 + rsub) * kTcYStride;
-    const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+    const uint32_t lane_bits = (uint32_t)(qd * 32) << 16;
+    const int groups = G.nbh / 8;
     long long j = 0;
     bool range_ok = true;
     for (long long u = blockIdx.x; u < G.units; u += gridDim.x, ++j) {
+      const int buf = (int)(j & 1);
       bool got = true;
-      if (lane == 0) got = mbar_wait_sleep(acc_full, (uint32_t)(j & 1));
+      if (lane == 0) got = mbar_wait_sleep(&acc_full[buf], (uint32_t)((j >> 1) & 1));
       got = __shfl_sync(0xffffffffu, got, 0);
       if (!got) {
         if (lane == 0) report_error(status, kErrTcWaitAcc);
         break;
       }
       tc_fence_after();
-      const long long c = u / G.n_rb, rb = u % G.n_rb;
-      const size_t row = (size_t)rb * kTcRows + warp * 4 + rsub;
-      for (int grp = 0; grp < G.nb / 8; ++grp) {
+      const long long c = u / per_c, rem = u % per_c;
+      const long long rb = rem / G.nh, hf = rem % G.nh;
+      const size_t row = (size_t)rb * kTcRows + qd * 4 + rsub;
+      const uint32_t acc_addr = tmem + lane_bits + (uint32_t)buf * 256;
+      for (int grp = part; grp < groups; grp += 2) {
 #pragma unroll
         for (int hc = 0; hc < 2; ++hc) {
           uint32_t r[32];
-          tmem_ld32(lane_addr + (uint32_t)((grp * 2 + hc) * 32), r);
+          tmem_ld32(acc_addr + (uint32_t)((grp * 2 + hc) * 32), r);
 #pragma unroll
           for (int bl = 0; bl < 4; ++bl) {
             int x[8];
@@ -289,20 +305,20 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         bool ok_one = true;
         const uint64_t val = tc_combine(y, q, mu_lo, mu_hi, r64, r128, ok_one);
         range_ok &= ok_one;
-        const int bq = grp * 8 + t8;  // query polynomial in the pass
+        const int bq = (int)hf * kTcHalfNB + grp * 8 + t8;  // query polynomial in the pass
         const int b = bq >> 1;
         if (b < G.batch)
           out[(size_t)(b_base + b) * out_stride + (row * 2 + (bq & 1)) * kN + c] = val;
       }
       tc_fence_before();
       __syncwarp();
-      if (lane == 0) mbar_arrive(acc_empty);
+      if (lane == 0) mbar_arrive(&acc_empty[buf]);
     }
     if (!range_ok) report_error(status, kErrTcRange);
   }
   tc_fence_before();
   __syncthreads();
-  if (warp == 5) {
+  if (warp == kTcMma) {
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                  "r"(kTcTmemCols)
@@ -352,17 +368,21 @@ __global__ void db_limb_kernel(const uint64_t *__restrict__ dbs, uint16_t *__res
   }
 }
 
-// one thread: 8 consecutive k of one (slot, query polynomial) of the pass
+// one thread: 8 consecutive k of one (slot, query polynomial) of the pass;
+// ql[c][h][k/8][b' - nbh h][j][k%8]
 __global__ void query_limb_kernel(const uint4 *__restrict__ qsb, uint16_t *__restrict__ ql,
-                                  int n1, int batch, int b_base, int nb, int pass_batch) {
+                                  int n1, int batch, int b_base, int nh, int nbh, int pass_batch) {
   const int kblk = n1 / 8;
-  const long long total = (long long)kN * kblk * nb;
+  const long long total = (long long)kN * nh * kblk * nbh;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
        t += (long long)gridDim.x * blockDim.x) {
-    const int bq = (int)(t % nb);
-    const long long rest = t / nb;
+    const int bl = (int)(t % nbh);
+    long long rest = t / nbh;
     const int kb = (int)(rest % kblk);
-    const long long c = rest / kblk;
+    rest /= kblk;
+    const int hf = (int)(rest % nh);
+    const long long c = rest / nh;
+    const int bq = hf * kTcHalfNB + bl;
     const int b = bq >> 1;
     uint16_t d[8][8];
 #pragma unroll
@@ -382,8 +402,9 @@ __global__ void query_limb_kernel(const uint4 *__restrict__ qsb, uint16_t *__res
   }
 }
 
-constexpr size_t kTcSmem =
-    kTcStages * kTcStageBytes + 4 * 4 * kTcYStride * sizeof(int) + (2 * kTcStages + 4) * 8;
+constexpr size_t kTcSmem = kTcStages * kTcStageBytes + kTcEpiWarps * 4 * kTcYStride * sizeof(int) +
+                           (2 * kTcStages + 6) * 8;
+static_assert(kTcSmem <= 227 * 1024, "shared memory per CTA");
 
 int g_tc_sms = 0;
 
@@ -423,24 +444,24 @@ int launch_tc_scan_batched(const uint16_t *dbl, const uint4 *qsb, uint16_t *ql, 
   int launches = 0;
   for (int b0 = 0; b0 < batch; b0 += kTcMaxNB / 2) {
     const int pb = batch - b0 < kTcMaxNB / 2 ? batch - b0 : kTcMaxNB / 2;
-    const int padded = (pb + 3) / 4 * 4;  // 8 query polynomials per epilogue group
+    // 8 query polynomials per epilogue group; two 32-polynomial halves
+    // above 16 queries
+    const int padded = pb > kTcHalfNB / 2 ? kTcMaxNB / 2 : (pb + 3) / 4 * 4;
     TcGeom G;
     G.n1 = n1;
     G.n_rest = n_rest;
     G.batch = pb;
-    G.nb = 2 * padded;
+    G.nh = padded > kTcHalfNB / 2 ? 2 : 1;
+    G.nbh = 2 * padded / G.nh;
     G.n_rb = n_rest / kTcRows;
     G.nkc = n1 / kTcKC;
-    G.units = (long long)kN * G.n_rb;
-    G.b_bytes = (uint32_t)(kTcKB * G.nb * 128);
-    const int ncols = G.nb * 8;
-    G.halves = ncols > 256 ? 2 : 1;
-    G.idesc[0] = make_idesc(ncols > 256 ? 256 : ncols);
-    G.idesc[1] = make_idesc(ncols > 256 ? ncols - 256 : 16);
-    const long long qtotal = (long long)kN * (n1 / 8) * G.nb;
+    G.units = (long long)kN * G.n_rb * G.nh;
+    G.b_bytes = (uint32_t)(kTcKB * G.nbh * 128);
+    G.idesc = make_idesc(G.nbh * 8);
+    const long long qtotal = (long long)kN * G.nh * (n1 / 8) * G.nbh;
     const long long qblocks = (qtotal + 255) / 256;
     query_limb_kernel<<<(unsigned)(qblocks < 65536 ? qblocks : 65536), 256, 0, s>>>(
-        qsb, ql, n1, batch, b0, G.nb, pb);
+        qsb, ql, n1, batch, b0, G.nh, G.nbh, pb);
     const int sms = g_tc_sms > 0 ? g_tc_sms : 152;
     const long long grid = G.units < sms ? G.units : sms;
     tc_scan_kernel<<<(unsigned)grid, kTcThreads, kTcSmem, s>>>(dbl, ql, out, out_stride, b0, G, q,
