@@ -349,11 +349,11 @@ int run_pipeline(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
       db.dbl_valid = true;
     }
     CK(W.ql.alloc(tc_query_limb_bytes((int)n1)), "alloc query limbs");
-    launch_query_prep_batched(leaves, leaves_stride, W.qs.as<uint4>(), (int)n1, batch,
-                              ctx->Mq.tab, s);
+    launch_query_prep_plane(leaves, leaves_stride, W.qs.as<uint64_t>(), (int)n1, batch,
+                            ctx->Mq.tab, s);
     record(ctx, 6);
     ctx->launches += launch_tc_scan_batched(
-        db.dbl.as<uint16_t>(), W.qs.as<uint4>(), W.ql.as<uint16_t>(), W.res.as<uint64_t>(),
+        db.dbl.as<uint16_t>(), W.qs.as<uint64_t>(), W.ql.as<uint16_t>(), W.res.as<uint64_t>(),
         res_stride, (int)n1, (int)nr, batch, ctx->Mq.tab.q, ctx->Mq.tab.mu_lo, ctx->Mq.tab.mu_hi,
         ctx->r64, ctx->r128, ctx->status.as<uint32_t>(), s) - 1;
   } else if (batched) {

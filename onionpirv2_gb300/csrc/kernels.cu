@@ -74,6 +74,29 @@ __global__ void __launch_bounds__(T) query_prep_kernel(const uint64_t *leaves,
   }
 }
 
+// The same transform into a plain plane[b][k][poly][c] (NTT form, fully
+// reduced): one coalesced 64-byte run per thread and polynomial.  Input of
+// the tensor-core product, which splits it into limbs.
+__global__ void __launch_bounds__(T) query_prep_plane_kernel(const uint64_t *leaves,
+                                                             size_t leaves_stride,
+                                                             uint64_t *plane, int n1, ModTab M) {
+  __shared__ uint64_t sa[kSmemPoly], sb[kSmemPoly];
+  const int tid = threadIdx.x;
+  const int k = blockIdx.x, b = blockIdx.y;
+  const uint64_t *ct = leaves + b * leaves_stride + (size_t)k * 2 * kN;
+  uint64_t r0[8], r1[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    r0[e] = ct[strided_idx(tid, e)];
+    r1[e] = ct[kN + strided_idx(tid, e)];
+  }
+  ntt_fwd(r0, sa, sb, M);
+  ntt_fwd(r1, sa, sb, M);
+  uint64_t *dst = plane + ((size_t)b * n1 + k) * 2 * kN;
+  stg_slot8(dst, r0);
+  stg_slot8(dst + kN, r1);
+}
+
 // ---------------------------------------------------------------------------
 // mod switch (server.cpp:779-801) + response packing (server.cpp:581-633)
 // ---------------------------------------------------------------------------
@@ -240,6 +263,11 @@ void launch_query_prep_batched(const uint64_t *leaves, size_t leaves_stride, uin
                                int batch, const ModTab &Mq, cudaStream_t s) {
   query_prep_kernel<<<dim3(n1, batch), T, 0, s>>>(leaves, leaves_stride, qsb, 1,
                                                    (size_t)n1 * batch, (size_t)batch, Mq);
+}
+
+void launch_query_prep_plane(const uint64_t *leaves, size_t leaves_stride, uint64_t *plane,
+                             int n1, int batch, const ModTab &Mq, cudaStream_t s) {
+  query_prep_plane_kernel<<<dim3(n1, batch), T, 0, s>>>(leaves, leaves_stride, plane, n1, Mq);
 }
 
 void launch_modswitch_pack(const uint64_t *res, size_t res_stride, uint64_t *resp,

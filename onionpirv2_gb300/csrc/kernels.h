@@ -79,17 +79,22 @@ bool launch_scan_batched(const uint64_t *dbs, const uint4 *qsb, uint64_t *out, s
                          int n1, int n_rest, int batch, const Consts &C, uint64_t mu_lo,
                          uint64_t mu_hi, uint32_t *status, cudaStream_t s);
 
+// NTT the first n1 leaves into a plain plane[b][k][poly][c] of residues
+// (query operand of the tensor-core path)
+void launch_query_prep_plane(const uint64_t *leaves, size_t leaves_stride, uint64_t *plane,
+                             int n1, int batch, const ModTab &Mq, cudaStream_t s);
 // Batched product on the tcgen05 tensor cores (tc_scan.cu): residues split
 // into 8-bit limbs held as bf16, exact fp32 accumulation in tensor memory.
 // The database needs its limb plane dbl (tc_db_limb_bytes, built by
-// launch_db_limbs from dbs); ql is scratch of tc_query_limb_bytes.  Output
-// as launch_scan.  Returns the number of kernels launched.
+// launch_db_limbs from dbs); plane is the query operand of
+// launch_query_prep_plane, ql scratch of tc_query_limb_bytes.  Output as
+// launch_scan.  Returns the number of kernels launched.
 bool tc_scan_supported(int n1, int n_rest);
 size_t tc_db_limb_bytes(int n1, int n_rest);
 size_t tc_query_limb_bytes(int n1);
 cudaError_t init_tc_attributes();
 void launch_db_limbs(const uint64_t *dbs, uint16_t *dbl, int n1, int n_rest, cudaStream_t s);
-int launch_tc_scan_batched(const uint16_t *dbl, const uint4 *qsb, uint16_t *ql, uint64_t *out,
+int launch_tc_scan_batched(const uint16_t *dbl, const uint64_t *plane, uint16_t *ql, uint64_t *out,
                            size_t out_stride, int n1, int n_rest, int batch, uint64_t q,
                            uint64_t mu_lo, uint64_t mu_hi, uint64_t r64, uint64_t r128,
                            uint32_t *status, cudaStream_t s);

@@ -368,33 +368,30 @@ __global__ void db_limb_kernel(const uint64_t *__restrict__ dbs, uint16_t *__res
   }
 }
 
-// one thread: 8 consecutive k of one (slot, query polynomial) of the pass;
-// ql[c][h][k/8][b' - nbh h][j][k%8]
-__global__ void query_limb_kernel(const uint4 *__restrict__ qsb, uint16_t *__restrict__ ql,
-                                  int n1, int batch, int b_base, int nh, int nbh, int pass_batch) {
+// one thread: 8 consecutive k of one (slot, query polynomial) of the pass,
+// from plane[b][k][poly][c] (consecutive threads read consecutive slots) to
+// ql[c][h][k/8][b' - nbh h][j][k%8] (one 128-byte core matrix per thread)
+__global__ void query_limb_kernel(const uint64_t *__restrict__ plane, uint16_t *__restrict__ ql,
+                                  int n1, int b_base, int nh, int nbh, int pass_batch) {
   const int kblk = n1 / 8;
   const long long total = (long long)kN * nh * kblk * nbh;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
        t += (long long)gridDim.x * blockDim.x) {
-    const int bl = (int)(t % nbh);
-    long long rest = t / nbh;
+    const int c = (int)(t % kN);
+    long long rest = t / kN;
+    const int bl = (int)(rest % nbh);
+    rest /= nbh;
     const int kb = (int)(rest % kblk);
-    rest /= kblk;
-    const int hf = (int)(rest % nh);
-    const long long c = rest / nh;
+    const int hf = (int)(rest / kblk);
     const int bq = hf * kTcHalfNB + bl;
     const int b = bq >> 1;
     uint16_t d[8][8];
+    const uint64_t *src =
+        plane + (((size_t)(b_base + b) * n1 + kb * 8) * 2 + (bq & 1)) * kN + c;
 #pragma unroll
-    for (int kk = 0; kk < 8; ++kk) {
-      uint64_t v = 0;
-      if (b < pass_batch) {
-        const uint4 w = qsb[((size_t)c * n1 + kb * 8 + kk) * batch + b_base + b];
-        v = (bq & 1) ? (uint64_t)w.z + ((uint64_t)w.w << 30) : (uint64_t)w.x + ((uint64_t)w.y << 30);
-      }
-      limbs8(v, d[kk]);
-    }
-    uint4 *dst = reinterpret_cast<uint4 *>(ql + (size_t)t * 64);
+    for (int kk = 0; kk < 8; ++kk) limbs8(b < pass_batch ? src[(size_t)kk * 2 * kN] : 0, d[kk]);
+    uint4 *dst = reinterpret_cast<uint4 *>(
+        ql + ((((size_t)c * nh + hf) * kblk + kb) * nbh + bl) * 64);
 #pragma unroll
     for (int i = 0; i < 8; ++i)
       dst[i] = make_uint4(d[0][i] | (uint32_t)d[1][i] << 16, d[2][i] | (uint32_t)d[3][i] << 16,
@@ -437,7 +434,7 @@ void launch_db_limbs(const uint64_t *dbs, uint16_t *dbl, int n1, int n_rest, cud
   db_limb_kernel<<<(unsigned)(blocks < 65536 ? blocks : 65536), 256, 0, s>>>(dbs, dbl, n1, n_rest);
 }
 
-int launch_tc_scan_batched(const uint16_t *dbl, const uint4 *qsb, uint16_t *ql, uint64_t *out,
+int launch_tc_scan_batched(const uint16_t *dbl, const uint64_t *plane, uint16_t *ql, uint64_t *out,
                            size_t out_stride, int n1, int n_rest, int batch, uint64_t q,
                            uint64_t mu_lo, uint64_t mu_hi, uint64_t r64, uint64_t r128,
                            uint32_t *status, cudaStream_t s) {
@@ -461,7 +458,7 @@ int launch_tc_scan_batched(const uint16_t *dbl, const uint4 *qsb, uint16_t *ql, 
     const long long qtotal = (long long)kN * G.nh * (n1 / 8) * G.nbh;
     const long long qblocks = (qtotal + 255) / 256;
     query_limb_kernel<<<(unsigned)(qblocks < 65536 ? qblocks : 65536), 256, 0, s>>>(
-        qsb, ql, n1, batch, b0, G.nh, G.nbh, pb);
+        plane, ql, n1, b0, G.nh, G.nbh, pb);
     const int sms = g_tc_sms > 0 ? g_tc_sms : 152;
     const long long grid = G.units < sms ? G.units : sms;
     tc_scan_kernel<<<(unsigned)grid, kTcThreads, kTcSmem, s>>>(dbl, ql, out, out_stride, b0, G, q,
