@@ -31,15 +31,21 @@ constexpr int T = kNttThreads;
 //   c' = apply_galois(c_i, N/k + 1)   (automorphism + key switch with p)
 //   c_2i = c_i + c';  c_2i+1 = (c_i - c') * x^-k
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(T) expand_level_kernel(const uint64_t *cur, uint64_t *nxt,
-                                                         size_t in_stride, size_t out_stride,
-                                                         const __grid_constant__ KeyBatch kb,
-                                                         int level, ModTab Mq, ModTab Mp,
-                                                         Consts C) {
+//
+// One CTA per node.  The key switch runs modulus by modulus so that only one
+// transform operand is live at a time (two CTAs fit on an SM): the q part
+// leaves INTT(NTT_q(sigma(c1)) * K_q[kk]) in shared memory, the p part then
+// rounds against it and writes polynomial kk of both children.
+__global__ void __launch_bounds__(T, 2) expand_level_kernel(const uint64_t *cur, uint64_t *nxt,
+                                                            size_t in_stride, size_t out_stride,
+                                                            const __grid_constant__ KeyBatch kb,
+                                                            int level, ModTab Mq, ModTab Mp,
+                                                            Consts C) {
   extern __shared__ uint64_t smem[];
   uint64_t *sa = smem, *sb = smem + kSmemPoly;
   uint64_t *s_sig0 = smem + 2 * kSmemPoly;  // sigma(c0), natural index
   uint64_t *s_sig1 = s_sig0 + kN;           // sigma(c1)
+  uint64_t *s_q = s_sig1 + kN;              // [2][N] q part of the key switch, natural index
   const int tid = threadIdx.x;
   const int node = blockIdx.x, b = blockIdx.y;
   const int k = 1 << level;
@@ -63,88 +69,87 @@ __global__ void __launch_bounds__(T) expand_level_kernel(const uint64_t *cur, ui
   }
   __syncthreads();
 
-  // T = sigma(c1) in NTT form mod q and mod p
-  uint64_t tq[8], tp[8];
+  const uint64_t *key = kb.q[b].galois + (size_t)level * 4 * kN;
+  // ---- modulus q: s_q[kk] = INTT_q(NTT_q(sigma(c1)) * K[kk] mod q)
+  {
+    uint64_t t[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) t[e] = s_sig1[strided_idx(tid, e)];
+    ntt_fwd(t, sa, sb, Mq);
+#pragma unroll 1
+    for (int kk = 0; kk < 2; ++kk) {
+      uint64_t a[8];
+      ldg_slot8(key + (2 * kk) * kN, a);
+#pragma unroll
+      for (int e = 0; e < 8; ++e) a[e] = mul_mod(t[e], a[e], Mq);
+      ntt_inv(a, sa, sb, Mq);
+#pragma unroll
+      for (int e = 0; e < 8; ++e) s_q[kk * kN + strided_idx(tid, e)] = a[e];  // own slots only
+    }
+  }
+  // ---- modulus p, rounding and the children
+  uint64_t *ce = nxt + b * out_stride + (size_t)(2 * node) * 2 * kN;
+  uint64_t *co = ce + 2 * kN;
+  uint64_t t[8];
 #pragma unroll
   for (int e = 0; e < 8; ++e) {
     const uint64_t v = s_sig1[strided_idx(tid, e)];
-    tq[e] = v;
-    tp[e] = v >= p ? v - p : v;  // q < 2p
+    t[e] = v >= p ? v - p : v;  // q < 2p
   }
-  ntt_fwd(tq, sa, sb, Mq);
-  ntt_fwd(tp, sa, sb, Mp);
-
-  const uint64_t *key = kb.q[b].galois + (size_t)level * 4 * kN;
-  uint64_t out[2][8];
-#pragma unroll
+  ntt_fwd(t, sa, sb, Mp);
+#pragma unroll 1
   for (int kk = 0; kk < 2; ++kk) {
-    const uint64_t *kq = key + (2 * kk + 0) * kN, *kp = key + (2 * kk + 1) * kN;
-    uint64_t aq[8], ap[8];
-    ldg_slot8(kq, aq);
-    ldg_slot8(kp, ap);
+    uint64_t a[8];
+    ldg_slot8(key + (2 * kk + 1) * kN, a);
+#pragma unroll
+    for (int e = 0; e < 8; ++e) a[e] = mul_mod(t[e], a[e], Mp);
+    ntt_inv(a, sa, sb, Mp);
 #pragma unroll
     for (int e = 0; e < 8; ++e) {
-      aq[e] = mul_mod(tq[e], aq[e], Mq);
-      ap[e] = mul_mod(tp[e], ap[e], Mp);
-    }
-    ntt_inv(aq, sa, sb, Mq);
-    ntt_inv(ap, sa, sb, Mp);
-    // round(X / p) mod q = (x_q + p/2 - ((x_p + p/2) mod p)) * p^-1 mod q
-#pragma unroll
-    for (int e = 0; e < 8; ++e) {
-      const uint64_t rr = add_mod(ap[e], C.p_half, p);
-      const uint64_t v = sub_mod(add_mod(aq[e], C.p_half_mod_q, q), rr, q);
-      out[kk][e] = mul_shoup(v, C.p_inv_q, C.p_inv_q_s, q);
-    }
-  }
-
-  uint64_t *ce = nxt + b * out_stride + (size_t)(2 * node) * 2 * kN;
-  uint64_t *co = ce + 2 * kN;
-#pragma unroll
-  for (int e = 0; e < 8; ++e) {
-    const int i = strided_idx(tid, e);
-    const uint64_t cp0 = add_mod(s_sig0[i], out[0][e], q);
-    const uint64_t cp1 = out[1][e];
-    const uint64_t x0 = ci[i], x1 = ci[kN + i];
-    ce[i] = add_mod(x0, cp0, q);
-    ce[kN + i] = add_mod(x1, cp1, q);
-    const uint64_t d0 = sub_mod(x0, cp0, q), d1 = sub_mod(x1, cp1, q);
-    // multiply by x^-k (utils.cpp:6-26): coefficient i moves to i - k, wrapping
-    // ones are negated (zero stays zero)
-    if (i >= k) {
-      co[i - k] = d0;
-      co[kN + i - k] = d1;
-    } else {
-      co[kN - k + i] = neg_mod(d0, q);
-      co[2 * kN - k + i] = neg_mod(d1, q);
+      const int i = strided_idx(tid, e);
+      // round(X / p) mod q = (x_q + p/2 - ((x_p + p/2) mod p)) * p^-1 mod q
+      const uint64_t rr = add_mod(a[e], C.p_half, p);
+      const uint64_t v = sub_mod(add_mod(s_q[kk * kN + i], C.p_half_mod_q, q), rr, q);
+      const uint64_t o = mul_shoup(v, C.p_inv_q, C.p_inv_q_s, q);
+      // polynomial kk of c' = apply_galois(c_i); children c_i +- c' (the odd one times x^-k)
+      const uint64_t cp = kk == 0 ? add_mod(s_sig0[i], o, q) : o;
+      const uint64_t x = ci[kk * kN + i];
+      ce[kk * kN + i] = add_mod(x, cp, q);
+      const uint64_t d = sub_mod(x, cp, q);
+      // multiply by x^-k (utils.cpp:6-26): coefficient i moves to i - k, wrapping
+      // ones are negated (zero stays zero)
+      if (i >= k)
+        co[kk * kN + i - k] = d;
+      else
+        co[kk * kN + kN - k + i] = neg_mod(d, q);
     }
   }
 }
 
 // ---------------------------------------------------------------------------
 // RGSW external product core (gsw_eval.cpp:33-106, 184-252):
-// decompose both polynomials of ct (coefficient form, given in the strided
-// distribution) into l digits of base_log2 bits each, NTT every digit, and
-// accumulate digit_j * gsw[j][k] in 128 bits; reduce mod q.  Output: NTT
-// form, slot distribution.
+// decompose both polynomials of ct (coefficient form, in shared memory at
+// natural index; each thread reads only its own strided slots) into l digits
+// of base_log2 bits each, NTT every digit, and accumulate digit_j * gsw[j][k]
+// in 128 bits; reduce mod q.  Output: NTT form, slot distribution.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void ext_product_core(const uint64_t x[2][8], const uint64_t *gsw,
-                                                 int l, int base_log2, uint64_t *sa,
-                                                 uint64_t *sb, const ModTab &M,
-                                                 uint64_t out[2][8]) {
+__device__ __forceinline__ void ext_product_core(const uint64_t *src, const uint64_t *gsw, int l,
+                                                 int base_log2, uint64_t *sa, uint64_t *sb,
+                                                 const ModTab &M, uint64_t out[2][8]) {
   const int tid = threadIdx.x;
   const uint64_t mask = (1ULL << base_log2) - 1;
   U128 acc0[8], acc1[8];
 #pragma unroll
   for (int e = 0; e < 8; ++e) acc0[e] = acc1[e] = U128{0, 0};
-#pragma unroll
+#pragma unroll 1
   for (int poly = 0; poly < 2; ++poly) {
+#pragma unroll 1
     for (int pp = l - 1; pp >= 0; --pp) {
       const int j = poly * l + (l - 1 - pp);
       const int sh = pp * base_log2;
       uint64_t d[8];
 #pragma unroll
-      for (int e = 0; e < 8; ++e) d[e] = (x[poly][e] >> sh) & mask;
+      for (int e = 0; e < 8; ++e) d[e] = (src[poly * kN + strided_idx(tid, e)] >> sh) & mask;
       ntt_fwd(d, sa, sb, M);
       const uint64_t *g0 = gsw + (size_t)j * 2 * kN, *g1 = g0 + kN;
       uint64_t w0[8], w1[8];
@@ -166,72 +171,74 @@ __device__ __forceinline__ void ext_product_core(const uint64_t x[2][8], const u
 
 // query_to_gsw (gsw_eval.cpp:254-286) for every leaf n1 + j, j < num_cts:
 // row (j % l) of RGSW (j / l) = NTT(ct); row l + (j % l) = RGSW(sk) x ct.
-__global__ void __launch_bounds__(T) query_to_gsw_kernel(const uint64_t *leaves,
-                                                         size_t leaves_stride, uint64_t *gsw_out,
-                                                         size_t gsw_stride,
-                                                         const __grid_constant__ KeyBatch kb,
-                                                         int n1, ModTab M, Consts C) {
-  __shared__ uint64_t sa[kSmemPoly], sb[kSmemPoly];
+__global__ void __launch_bounds__(T, 2) query_to_gsw_kernel(const uint64_t *leaves,
+                                                            size_t leaves_stride,
+                                                            uint64_t *gsw_out, size_t gsw_stride,
+                                                            const __grid_constant__ KeyBatch kb,
+                                                            int n1, ModTab M, Consts C) {
+  extern __shared__ uint64_t smem[];
+  uint64_t *sa = smem, *sb = smem + kSmemPoly, *sx = smem + 2 * kSmemPoly;  // sx: [2][N]
   const int tid = threadIdx.x;
   const int j = blockIdx.x, b = blockIdx.y;
   const int l = C.l;
   const int dim = j / l, kk = j % l;
   const uint64_t *ct = leaves + b * leaves_stride + (size_t)(n1 + j) * 2 * kN;
   uint64_t *rgsw = gsw_out + b * gsw_stride + (size_t)dim * 2 * l * 2 * kN;
-  uint64_t x[2][8];
-#pragma unroll
-  for (int poly = 0; poly < 2; ++poly)
-#pragma unroll
-    for (int e = 0; e < 8; ++e) x[poly][e] = ct[poly * kN + strided_idx(tid, e)];
   // first half: the ciphertext itself in NTT form
   uint64_t *row0 = rgsw + (size_t)kk * 2 * kN;
-#pragma unroll
+#pragma unroll 1
   for (int poly = 0; poly < 2; ++poly) {
     uint64_t r[8];
 #pragma unroll
-    for (int e = 0; e < 8; ++e) r[e] = x[poly][e];
+    for (int e = 0; e < 8; ++e) {
+      const int i = poly * kN + strided_idx(tid, e);
+      r[e] = ct[i];
+      sx[i] = r[e];  // own slots only
+    }
     ntt_fwd(r, sa, sb, M);
-#pragma unroll
     stg_slot8(row0 + poly * kN, r);
   }
   // second half: external product with RGSW(sk) under the key gadget
   uint64_t out[2][8];
-  ext_product_core(x, kb.q[b].gsw_key, C.l_key, C.base_log2_key, sa, sb, M, out);
+  ext_product_core(sx, kb.q[b].gsw_key, C.l_key, C.base_log2_key, sa, sb, M, out);
   uint64_t *row1 = rgsw + (size_t)(l + kk) * 2 * kN;
 #pragma unroll
-  for (int poly = 0; poly < 2; ++poly)
-#pragma unroll
-    stg_slot8(row1 + poly * kN, out[poly]);
+  for (int poly = 0; poly < 2; ++poly) stg_slot8(row1 + poly * kN, out[poly]);
 }
 
 // other_dim_mux (server.cpp:295-334) for pair j: y -= x; y = RGSW x y; y =
 // INTT(y); x += y.
-__global__ void __launch_bounds__(T) fold_kernel(uint64_t *res, size_t res_stride,
-                                                 const uint64_t *gsw, size_t gsw_stride, int half,
-                                                 ModTab M, Consts C) {
-  __shared__ uint64_t sa[kSmemPoly], sb[kSmemPoly];
+__global__ void __launch_bounds__(T, 2) fold_kernel(uint64_t *res, size_t res_stride,
+                                                    const uint64_t *gsw, size_t gsw_stride,
+                                                    int half, ModTab M, Consts C) {
+  extern __shared__ uint64_t smem[];
+  uint64_t *sa = smem, *sb = smem + kSmemPoly, *sd = smem + 2 * kSmemPoly;  // sd: [2][N]
   const int tid = threadIdx.x;
   const int j = blockIdx.x, b = blockIdx.y;
   const uint64_t q = C.q;
   uint64_t *xp = res + b * res_stride + (size_t)j * 2 * kN;
   const uint64_t *yp = res + b * res_stride + (size_t)(j + half) * 2 * kN;
-  uint64_t d[2][8];
 #pragma unroll
-  for (int poly = 0; poly < 2; ++poly)
-#pragma unroll
-    for (int e = 0; e < 8; ++e) {
-      const int i = poly * kN + strided_idx(tid, e);
-      d[poly][e] = sub_mod(yp[i], xp[i], q);
-    }
+  for (int i2 = 0; i2 < 16; ++i2) {
+    const int i = (i2 >> 3) * kN + strided_idx(tid, i2 & 7);
+    sd[i] = sub_mod(yp[i], xp[i], q);  // own slots only
+  }
   uint64_t out[2][8];
-  ext_product_core(d, gsw + b * gsw_stride, C.l, C.base_log2, sa, sb, M, out);
+  ext_product_core(sd, gsw + b * gsw_stride, C.l, C.base_log2, sa, sb, M, out);
+  // polynomial 1 waits in shared memory (sd is no longer read) while
+  // polynomial 0 is transformed back
 #pragma unroll
+  for (int e = 0; e < 8; ++e) sd[slot_idx(tid, e)] = out[1][e];
+#pragma unroll 1
   for (int poly = 0; poly < 2; ++poly) {
-    ntt_inv(out[poly], sa, sb, M);
+    uint64_t r[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) r[e] = poly ? sd[slot_idx(tid, e)] : out[0][e];
+    ntt_inv(r, sa, sb, M);
 #pragma unroll
     for (int e = 0; e < 8; ++e) {
       const int i = poly * kN + strided_idx(tid, e);
-      xp[i] = add_mod(xp[i], out[poly][e], q);
+      xp[i] = add_mod(xp[i], r[e], q);
     }
   }
 }
@@ -492,14 +499,22 @@ int g_qtg_threshold = 40;
 
 }  // namespace
 
-constexpr size_t kExpandSmem = (2 * kSmemPoly + 2 * kN) * sizeof(uint64_t);
+constexpr size_t kExpandSmem = (2 * kSmemPoly + 4 * kN) * sizeof(uint64_t);
 
 constexpr size_t kClusterSmem = (2 * kSmemPoly + 2 * kN) * sizeof(uint64_t);
+// one-CTA fold and RGSW reconstruction: transform buffers + the source ciphertext
+constexpr size_t kExtSmem = (2 * kSmemPoly + 2 * kN) * sizeof(uint64_t);
 
 cudaError_t init_kernel_attributes() {
   cudaError_t e;
   if ((e = cudaFuncSetAttribute(expand_level_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)kExpandSmem)) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(fold_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)kExtSmem)) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(query_to_gsw_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)kExtSmem)) != cudaSuccess)
     return e;
   if ((e = cudaFuncSetAttribute(expand_cluster_kernel,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -551,7 +566,7 @@ void launch_query_to_gsw(const uint64_t *leaves, size_t leaves_stride, uint64_t 
           leaves + b0 * leaves_stride, leaves_stride, gsw_out + b0 * gsw_stride, gsw_stride, kb,
           n1, Mq, C);
     else
-      query_to_gsw_kernel<<<dim3(num_cts, nb), T, 0, s>>>(
+      query_to_gsw_kernel<<<dim3(num_cts, nb), T, kExtSmem, s>>>(
           leaves + b0 * leaves_stride, leaves_stride, gsw_out + b0 * gsw_stride, gsw_stride, kb,
           n1, Mq, C);
   }
@@ -563,7 +578,8 @@ void launch_fold(uint64_t *res, size_t res_stride, const uint64_t *gsw, size_t g
     fold_cluster_kernel<<<dim3(kFoldCluster * half, batch), T, kClusterSmem, s>>>(
         res, res_stride, gsw, gsw_stride, half, Mq, C);
   else
-    fold_kernel<<<dim3(half, batch), T, 0, s>>>(res, res_stride, gsw, gsw_stride, half, Mq, C);
+    fold_kernel<<<dim3(half, batch), T, kExtSmem, s>>>(res, res_stride, gsw, gsw_stride, half, Mq,
+                                                       C);
 }
 
 }  // namespace opir
