@@ -99,6 +99,18 @@ int opir_set_galois_key(opir_ctx *ctx, uint64_t client_id, const uint64_t *keys,
 int opir_set_gsw_key(opir_ctx *ctx, uint64_t client_id, const uint64_t *rows);
 int opir_erase_client(opir_ctx *ctx, uint64_t client_id);
 
+/* Key budget (no reference counterpart; the reference keeps every client's
+ * keys in std::map members, server.h:58-59).  With bytes > 0 the context keeps
+ * host copies of client keys and holds at most bytes / opir_key_bytes_per_client
+ * clients' keys in device memory, evicting the least recently used client
+ * not needed by a query in flight; evicted keys are copied back when that
+ * client queries again.  0 (the default) keeps every client's keys resident.
+ * Call before the first key is registered. */
+int opir_set_key_budget(opir_ctx *ctx, uint64_t bytes);
+uint64_t opir_key_bytes_per_client(const opir_ctx *ctx);
+/* clients whose keys are in device memory, and the slots of the budget (0: no budget) */
+int opir_resident_clients(opir_ctx *ctx, uint32_t *resident, uint32_t *slots);
+
 /* ---- queries (server.cpp:520-633) ---- */
 /* PirServer::make_query + mod_switch_inplace + save_resp_to_stream:
  * query[2][N] (coefficient form, mod q) -> resp[2][N] (mod small_q, may be
@@ -134,6 +146,47 @@ int opir_make_query_trace(opir_ctx *ctx, uint32_t db_id, uint64_t client_id,
  * calls share the array, so calls that overlap on the GPU race. */
 int opir_first_dim_noalloc(opir_ctx *ctx, uint32_t db_id, const uint64_t *d_fst_cts,
                            uint64_t *d_out);
+
+/* ---- serving: continuous batching ----
+ * No reference counterpart (PirServer::make_query, server.cpp:520-579,
+ * answers one query per call).  opir_serve_start starts a worker thread that
+ * takes submitted queries from per-database queues and runs them in batches
+ * of up to max_batch queries against the resident database, with up to
+ * `lanes` batches on the device at once.  A free lane takes a batch at once
+ * when the device is otherwise idle; while another batch runs it waits for a
+ * full batch or until the oldest request has waited max_wait_us.  Every
+ * response is the one opir_make_query returns for the same query.  While
+ * serving is active, opir_make_query* and database changes return
+ * OPIR_ERR_STATE; keys can be registered (a client's keys cannot change while
+ * its queries are in flight). */
+typedef struct opir_serve_config {
+  uint32_t max_batch;    /* queries per batch (>= 1)                    */
+  uint32_t lanes;        /* batches on the device at once (1 .. 4)      */
+  uint32_t max_wait_us;  /* see above                                   */
+} opir_serve_config;
+
+typedef struct opir_serve_stats {
+  uint64_t submitted, completed, failed, batches, queued;
+  double mean_batch;                  /* queries per batch                      */
+  double p50_ms, p99_ms, mean_ms, max_ms;  /* submission -> response ready       */
+  double queries_per_s;               /* completed / (last completion - first submission) */
+} opir_serve_stats;
+
+int opir_serve_start(opir_ctx *ctx, const opir_serve_config *cfg);
+/* finishes every queued query, then stops the worker; results stay pollable */
+int opir_serve_stop(opir_ctx *ctx);
+/* queue one query ([2][N] ciphertext, copied); *ticket identifies it */
+int opir_submit(opir_ctx *ctx, uint32_t db_id, uint64_t client_id, const uint64_t *query,
+                uint64_t *ticket);
+/* *done = 0: still queued or running.  *done = 1: resp ([2][N]) and packed
+ * (opir_response_bytes) are filled when not NULL, the ticket is released and
+ * the return value is the query's status. */
+int opir_poll(opir_ctx *ctx, uint64_t ticket, uint64_t *resp, uint8_t *packed, int *done);
+/* as opir_poll, blocking up to timeout_ms (OPIR_ERR_TIMEOUT: still pending) */
+int opir_wait(opir_ctx *ctx, uint64_t ticket, uint32_t timeout_ms, uint64_t *resp,
+              uint8_t *packed);
+/* counters and latency percentiles since opir_serve_start */
+int opir_serve_stats_get(opir_ctx *ctx, opir_serve_stats *out);
 
 /* ---- timing and accounting ---- */
 /* Enable per-stage CUDA-event timing of subsequent queries. */

@@ -37,6 +37,9 @@ EXPORTS = (
     "opir_make_query_device", "opir_make_query_trace", "opir_first_dim_noalloc",
     "opir_set_timing", "opir_stage_times",
     "opir_launch_count", "opir_sync", "opir_ntt", "opir_ntt_device",
+    "opir_set_key_budget", "opir_key_bytes_per_client", "opir_resident_clients",
+    "opir_serve_start", "opir_serve_stop", "opir_submit", "opir_poll", "opir_wait",
+    "opir_serve_stats_get",
 )
 
 
@@ -61,6 +64,30 @@ class OpirDbShape(ctypes.Structure):
         ("entry_size", ctypes.c_uint32),
         ("entries_per_pt", ctypes.c_uint32),
         ("bits_per_coeff", ctypes.c_uint32),
+    ]
+
+
+class OpirServeConfig(ctypes.Structure):
+    _fields_ = [
+        ("max_batch", ctypes.c_uint32),
+        ("lanes", ctypes.c_uint32),
+        ("max_wait_us", ctypes.c_uint32),
+    ]
+
+
+class OpirServeStats(ctypes.Structure):
+    _fields_ = [
+        ("submitted", ctypes.c_uint64),
+        ("completed", ctypes.c_uint64),
+        ("failed", ctypes.c_uint64),
+        ("batches", ctypes.c_uint64),
+        ("queued", ctypes.c_uint64),
+        ("mean_batch", ctypes.c_double),
+        ("p50_ms", ctypes.c_double),
+        ("p99_ms", ctypes.c_double),
+        ("mean_ms", ctypes.c_double),
+        ("max_ms", ctypes.c_double),
+        ("queries_per_s", ctypes.c_double),
     ]
 
 
@@ -118,6 +145,18 @@ def load(path: str = LIB):
     L.opir_sync.argtypes = [_vp]
     L.opir_ntt_device.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _vp, ctypes.c_uint64]
     L.opir_ntt.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _u64p, ctypes.c_uint64]
+    L.opir_set_key_budget.argtypes = [_vp, ctypes.c_uint64]
+    L.opir_key_bytes_per_client.argtypes = [_vp]
+    L.opir_key_bytes_per_client.restype = ctypes.c_uint64
+    L.opir_resident_clients.argtypes = [_vp, ctypes.POINTER(ctypes.c_uint32),
+                                        ctypes.POINTER(ctypes.c_uint32)]
+    L.opir_serve_start.argtypes = [_vp, ctypes.POINTER(OpirServeConfig)]
+    L.opir_serve_stop.argtypes = [_vp]
+    L.opir_submit.argtypes = [_vp, ctypes.c_uint32, ctypes.c_uint64, _u64p,
+                              ctypes.POINTER(ctypes.c_uint64)]
+    L.opir_poll.argtypes = [_vp, ctypes.c_uint64, _u64p, _u8p, ctypes.POINTER(ctypes.c_int)]
+    L.opir_wait.argtypes = [_vp, ctypes.c_uint64, ctypes.c_uint32, _u64p, _u8p]
+    L.opir_serve_stats_get.argtypes = [_vp, ctypes.POINTER(OpirServeStats)]
     _lib = L
     return L
 

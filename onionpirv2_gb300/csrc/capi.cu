@@ -15,15 +15,21 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
 #include <cstring>
 #include <map>
 #include <memory>
 #include <mutex>
 #include <string>
+#include <thread>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/onionpir_gpu.h"
 #include "kernels.h"
+#include "serve_core.h"
 
 using namespace opir;
 
@@ -146,10 +152,14 @@ struct Db {
 };
 
 struct Client {
-  DevBuf galois;
+  DevBuf galois;  // device copies (no key budget)
   uint32_t levels = 0;
   DevBuf gsw;
-  bool has_gsw = false;
+  bool has_galois = false, has_gsw = false;
+  // key budget: host copies; the device copy lives in a key-pool slot while
+  // resident (serve::KeyLru decides which clients are)
+  std::vector<uint64_t> h_galois, h_gsw;  // gsw rows in coefficient form
+  int inflight = 0;                       // serving batches reading these keys
 };
 
 struct Workspace {
@@ -160,6 +170,79 @@ struct Workspace {
 
 struct Err {
   int code;
+};
+
+double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch())
+      .count();
+}
+
+// Where one pipeline run enqueues its work.
+struct PipeEnv {
+  Workspace *W;
+  cudaStream_t s;
+  uint32_t *status;  // device status word (bounded-wait timeouts)
+  bool timed;        // record the stage events
+  bool keep_pins;    // leave the batch's clients pinned (serving: until the batch completes)
+};
+
+// ---- serving (continuous batching)
+struct Ticket {
+  uint32_t db = 0;
+  uint64_t client = 0;
+  std::vector<uint64_t> query, resp;
+  std::vector<uint8_t> packed;
+  int state = 0;  // 0 queued, 1 on the device, 2 done
+  int rc = 0;
+  double t_submit = 0, t_done = 0;
+};
+struct Serving;
+struct Lane {
+  Serving *owner = nullptr;
+  cudaStream_t stream = nullptr;
+  Workspace ws;
+  DevBuf status;
+  PinnedBuf h_status;
+  cudaEvent_t done = nullptr;
+  bool busy = false;
+  std::atomic<bool> finished{false};  // set by the stream callback
+  uint32_t db = 0;
+  std::vector<serve::Pending> reqs;
+  std::vector<uint64_t> clients;
+};
+struct Serving {
+  bool active = false, stop = false;
+  opir_serve_config cfg{};
+  std::thread worker;
+  // Wake-ups of the worker (submission, finished batch, stop): a counter
+  // under its own mutex, which nobody holds across a CUDA call -- the stream
+  // callback takes it, and a callback that blocked would stall its stream and
+  // any device-wide synchronisation behind it.
+  std::mutex wake_mu;
+  std::condition_variable wake_cv;
+  uint64_t wake_seq = 0;
+  void wake() {
+    {
+      std::lock_guard<std::mutex> g(wake_mu);
+      wake_seq++;
+    }
+    wake_cv.notify_all();
+  }
+  std::mutex mu;  // everything below; taken after opir_ctx::mu when both are held
+  std::condition_variable done_cv;
+  serve::BatchQueue queue;
+  std::unordered_map<uint64_t, Ticket> tickets;
+  uint64_t next_ticket = 1;
+  std::vector<std::unique_ptr<Lane>> lanes;
+  std::vector<double> lat_ms;
+  uint64_t submitted = 0, completed = 0, failed = 0, batches = 0, batched_queries = 0;
+  double t_first = 0, t_last = 0;
+  ~Serving() {
+    for (auto &L : lanes) {
+      if (L->done) cudaEventDestroy(L->done);
+      if (L->stream) cudaStreamDestroy(L->stream);
+    }
+  }
 };
 
 }  // namespace
@@ -184,6 +267,12 @@ struct opir_ctx {
   int tc_mode = 1;
   int tc_min_batch = 2;
   uint64_t r64 = 0, r128 = 0;  // 2^64 and 2^128 mod q
+  // key budget: client keys in a pool of fixed slots, least recently used out
+  uint64_t key_budget = 0;
+  size_t slot_words = 0;  // galois [kLogN][2][2][N] + RGSW(sk) [2 l_key][2][N]
+  DevBuf key_pool;
+  serve::KeyLru lru;
+  std::unique_ptr<Serving> serving;
   bool timing = false;
   cudaEvent_t ev[8] = {};
   float stage_ms[6] = {};
@@ -251,8 +340,7 @@ int build_modtab(opir_ctx *ctx, ModTables &T, uint64_t q) {
 }
 
 // ---- per-query workspace
-int ensure_workspace(opir_ctx *ctx, const Db &db, int batch) {
-  Workspace &W = ctx->ws;
+int ensure_workspace(opir_ctx *ctx, const Db &db, int batch, Workspace &W) {
   const size_t CT = 2 * (size_t)kN * 8;
   const size_t w = (size_t)1 << db.h;
   const size_t n1 = db.shape.fst_dim_sz, nr = db.shape.other_dim_sz;
@@ -272,35 +360,89 @@ struct Trace {
   uint64_t *leaves = nullptr, *gsw = nullptr, *first_dim = nullptr;
 };
 
-void record(opir_ctx *ctx, int i) {
-  if (ctx->timing) cudaEventRecord(ctx->ev[i], ctx->stream);
+void record(opir_ctx *ctx, const PipeEnv &E, int i) {
+  if (E.timed) cudaEventRecord(ctx->ev[i], E.s);
+}
+
+bool serving_active(const opir_ctx *ctx) { return ctx->serving && ctx->serving->active; }
+
+// Device key pointers of a client for a query on stream s.  With a key
+// budget the client is made resident first (its keys copied into a pool
+// slot on stream s, evicting the least recently used unpinned client) and
+// pinned; the caller unpins.
+int resolve_keys(opir_ctx *ctx, uint64_t id, const Db &db, cudaStream_t s, QueryDesc *d) {
+  auto it = ctx->clients.find(id);
+  if (it == ctx->clients.end() || !it->second->has_galois)
+    return ctx->fail(OPIR_ERR_UNKNOWN_CLIENT, "no Galois keys for client %llu",
+                     (unsigned long long)id);
+  Client &cl = *it->second;
+  if (cl.levels < (uint32_t)db.h)
+    return ctx->fail(OPIR_ERR_ARG, "client %llu has %u Galois levels, database needs %d",
+                     (unsigned long long)id, cl.levels, db.h);
+  if (db.ndim > 1 && !cl.has_gsw)
+    return ctx->fail(OPIR_ERR_UNKNOWN_CLIENT, "no RGSW key for client %llu", (unsigned long long)id);
+  if (!ctx->key_budget) {
+    d->galois = cl.galois.as<uint64_t>();
+    d->gsw_key = cl.gsw.as<uint64_t>();
+    return OPIR_OK;
+  }
+  uint64_t evicted;
+  bool fresh;
+  const int slot = ctx->lru.admit(id, &evicted, &fresh);
+  if (slot < 0)
+    return ctx->fail(OPIR_ERR_OOM, "key budget: all %d key slots are held by queries in flight",
+                     ctx->lru.slots());
+  uint64_t *base = ctx->key_pool.as<uint64_t>() + (size_t)slot * ctx->slot_words;
+  uint64_t *gal = base, *gsw = base + (size_t)kLogN * 4 * kN;
+  if (fresh) {
+    // a slot is only reused once no queued work reads it: same-stream order
+    // on the synchronous path, pins on the serving lanes
+    CK(cudaMemcpyAsync(gal, cl.h_galois.data(), cl.h_galois.size() * 8, cudaMemcpyHostToDevice, s),
+       "upload Galois keys");
+    if (cl.has_gsw) {
+      CK(cudaMemcpyAsync(gsw, cl.h_gsw.data(), cl.h_gsw.size() * 8, cudaMemcpyHostToDevice, s),
+         "upload RGSW key");
+      launch_ntt(ctx->Mq.tab, gsw, cl.h_gsw.size() / kN, false, s);  // server.cpp:497
+      ctx->launches++;
+    }
+  }
+  ctx->lru.pin(id);
+  d->galois = gal;
+  d->gsw_key = gsw;
+  return OPIR_OK;
 }
 
 // Enqueue the whole query pipeline for `batch` queries already on the device.
 int run_pipeline(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
                  const uint64_t *d_queries, uint64_t *d_resp, uint8_t *d_packed,
-                 const Trace *trace) {
+                 const Trace *trace, const PipeEnv &E) {
   if (batch <= 0) return ctx->fail(OPIR_ERR_ARG, "batch must be positive");
   if (!db.dbs.p) return ctx->fail(OPIR_ERR_STATE, "database has no data");
   std::vector<QueryDesc> desc(batch);
   for (int b = 0; b < batch; b++) {
-    auto it = ctx->clients.find(client_ids[b]);
-    if (it == ctx->clients.end() || !it->second->galois.p)
-      return ctx->fail(OPIR_ERR_UNKNOWN_CLIENT, "no Galois keys for client %llu",
-                       (unsigned long long)client_ids[b]);
-    if (it->second->levels < (uint32_t)db.h)
-      return ctx->fail(OPIR_ERR_ARG, "client %llu has %u Galois levels, database needs %d",
-                       (unsigned long long)client_ids[b], it->second->levels, db.h);
-    if (db.ndim > 1 && !it->second->has_gsw)
-      return ctx->fail(OPIR_ERR_UNKNOWN_CLIENT, "no RGSW key for client %llu",
-                       (unsigned long long)client_ids[b]);
-    desc[b].galois = it->second->galois.as<uint64_t>();
-    desc[b].gsw_key = it->second->gsw.as<uint64_t>();
+    const int rc = resolve_keys(ctx, client_ids[b], db, E.s, &desc[b]);
+    if (rc) {
+      if (ctx->key_budget)
+        for (int j = 0; j < b; j++) ctx->lru.unpin(client_ids[j]);
+      return rc;
+    }
   }
-  int rc = ensure_workspace(ctx, db, batch);
+  // pins only guard a batch's own clients from each other while it is set
+  // up, unless the caller keeps them until the batch completes
+  struct Unpin {
+    opir_ctx *ctx;
+    const uint64_t *ids;
+    int n;
+    bool keep;
+    ~Unpin() {
+      if (ctx->key_budget && !keep)
+        for (int j = 0; j < n; j++) ctx->lru.unpin(ids[j]);
+    }
+  } unpin{ctx, client_ids, batch, false};
+  int rc = ensure_workspace(ctx, db, batch, *E.W);
   if (rc) return rc;
-  Workspace &W = ctx->ws;
-  cudaStream_t s = ctx->stream;
+  Workspace &W = *E.W;
+  cudaStream_t s = E.s;
   const QueryDesc *qd = desc.data();  // host array: launchers pass it by value
   const size_t CTW = 2 * (size_t)kN;  // words per ciphertext
   const int h = db.h, u = db.u;
@@ -308,7 +450,7 @@ int run_pipeline(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
   const size_t n1 = db.shape.fst_dim_sz, nr = db.shape.other_dim_sz;
   const int l = (int)ctx->prm.gsw_l;
 
-  record(ctx, 0);
+  record(ctx, E, 0);
   // ---- expansion
   const uint64_t *cur = d_queries;
   size_t cur_stride = CTW;
@@ -324,7 +466,7 @@ int run_pipeline(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
   }
   const uint64_t *leaves = cur;
   const size_t leaves_stride = cur_stride;
-  record(ctx, 1);
+  record(ctx, E, 1);
   // ---- convert
   const size_t gsw_stride = (size_t)(db.ndim > 1 ? db.ndim - 1 : 1) * 2 * l * CTW;
   if (db.ndim > 1) {
@@ -332,7 +474,7 @@ int run_pipeline(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
                         (db.ndim - 1) * l, batch, ctx->Mq.tab, ctx->C, s);
     ctx->launches++;
   }
-  record(ctx, 2);
+  record(ctx, E, 2);
   // ---- first dimension
   const size_t qs_stride = (size_t)kN * n1;
   const size_t res_stride = nr * CTW;
@@ -346,35 +488,37 @@ int run_pipeline(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
       CK(db.dbl.alloc(tc_db_limb_bytes((int)n1, (int)nr)), "alloc database limb plane");
       launch_db_limbs(db.dbs.as<uint64_t>(), db.dbl.as<uint16_t>(), (int)n1, (int)nr, s);
       ctx->launches++;
+      // built once; batches on other streams read it afterwards
+      CK(cudaStreamSynchronize(s), "database limb plane");
       db.dbl_valid = true;
     }
-    CK(W.ql.alloc(tc_query_limb_bytes((int)n1)), "alloc query limbs");
+    CK(W.ql.alloc(tc_query_limb_bytes((int)n1, batch)), "alloc query limbs");
     launch_query_prep_plane(leaves, leaves_stride, W.qs.as<uint64_t>(), (int)n1, batch,
                             ctx->Mq.tab, s);
-    record(ctx, 6);
+    record(ctx, E, 6);
     ctx->launches += launch_tc_scan_batched(
         db.dbl.as<uint16_t>(), W.qs.as<uint64_t>(), W.ql.as<uint16_t>(), W.res.as<uint64_t>(),
         res_stride, (int)n1, (int)nr, batch, ctx->Mq.tab.q, ctx->Mq.tab.mu_lo, ctx->Mq.tab.mu_hi,
-        ctx->r64, ctx->r128, ctx->status.as<uint32_t>(), s) - 1;
+        ctx->r64, ctx->r128, E.status, s) - 1;
   } else if (batched) {
     launch_query_prep_batched(leaves, leaves_stride, W.qs.as<uint4>(), (int)n1, batch,
                               ctx->Mq.tab, s);
-    record(ctx, 6);
+    record(ctx, E, 6);
     launch_scan_batched(db.dbs.as<uint64_t>(), W.qs.as<uint4>(), W.res.as<uint64_t>(), res_stride,
                         (int)n1, (int)nr, batch, ctx->C, ctx->Mq.tab.mu_lo, ctx->Mq.tab.mu_hi,
-                        ctx->status.as<uint32_t>(), s);
+                        E.status, s);
   } else {
     launch_query_prep(leaves, leaves_stride, W.qs.as<uint4>(), qs_stride, (int)n1, batch,
                       ctx->Mq.tab, s);
-    record(ctx, 6);
+    record(ctx, E, 6);
     launch_scan(db.dbs.as<uint64_t>(), W.qs.as<uint4>(), qs_stride, W.res.as<uint64_t>(),
                 res_stride, (int)n1, (int)nr, batch, ctx->C, ctx->Mq.tab.mu_lo,
-                ctx->Mq.tab.mu_hi, ctx->status.as<uint32_t>(), s);
+                ctx->Mq.tab.mu_hi, E.status, s);
   }
-  record(ctx, 7);
+  record(ctx, E, 7);
   launch_ntt(ctx->Mq.tab, W.res.as<uint64_t>(), (size_t)batch * nr * 2, true, s);
   ctx->launches += 3;
-  record(ctx, 3);
+  record(ctx, E, 3);
   if (trace && trace->first_dim)
     CK(cudaMemcpyAsync(trace->first_dim, W.res.p, nr * CTW * 8, cudaMemcpyDeviceToHost, s),
        "trace first dim");
@@ -387,12 +531,12 @@ int run_pipeline(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
     ctx->launches++;
     cnt = half;
   }
-  record(ctx, 4);
+  record(ctx, E, 4);
   // ---- mod switch + pack
   launch_modswitch_pack(W.res.as<uint64_t>(), res_stride, d_resp, d_packed, ctx->resp_bytes, batch,
                         ctx->C, s);
   ctx->launches++;
-  record(ctx, 5);
+  record(ctx, E, 5);
   CK(cudaGetLastError(), "kernel launch");
   if (trace) {
     if (trace->leaves)
@@ -403,8 +547,13 @@ int run_pipeline(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
                          cudaMemcpyDeviceToHost, s),
          "trace gsw");
   }
-  ctx->stage_valid = ctx->timing;
+  if (E.W == &ctx->ws) ctx->stage_valid = E.timed;  // synchronous path
+  unpin.keep = E.keep_pins;
   return OPIR_OK;
+}
+
+PipeEnv sync_env(opir_ctx *ctx) {
+  return PipeEnv{&ctx->ws, ctx->stream, ctx->status.as<uint32_t>(), ctx->timing, false};
 }
 
 // Read and clear the device status word (call with the stream idle).
@@ -498,6 +647,7 @@ int opir_ctx_create(const opir_params *P, int device, opir_ctx **out) {
   if (const char *v = getenv("OPIR_BATCH_SCAN")) c->batch_scan = atoi(v) != 0;
   if (const char *v = getenv("OPIR_TC")) c->tc_mode = atoi(v) != 0;
   if (const char *v = getenv("OPIR_TC_MIN_BATCH")) c->tc_min_batch = atoi(v);
+  c->slot_words = (size_t)kLogN * 4 * kN + 2 * (size_t)P->gsw_l_key * 2 * kN;
   c->r64 = (uint64_t)(((u128)1 << 64) % q);
   c->r128 = mulmod(c->r64, c->r64, q);
   for (auto &e : c->ev)
@@ -535,6 +685,7 @@ int opir_ctx_create(const opir_params *P, int device, opir_ctx **out) {
 
 void opir_ctx_destroy(opir_ctx *ctx) {
   if (!ctx) return;
+  opir_serve_stop(ctx);
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (auto &e : ctx->ev)
@@ -590,6 +741,7 @@ int opir_db_create(opir_ctx *ctx, const opir_db_shape *shape, uint32_t *db_id) {
 int opir_db_destroy(opir_ctx *ctx, uint32_t db_id) {
   if (!ctx) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
+  if (serving_active(ctx)) return ctx->fail(OPIR_ERR_STATE, "serving is active");
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   if (!ctx->dbs.erase(db_id)) return ctx->fail(OPIR_ERR_UNKNOWN_DB, "unknown database %u", db_id);
@@ -600,6 +752,7 @@ int opir_db_push_chunk(opir_ctx *ctx, uint32_t db_id, const uint8_t *entries, ui
                        uint64_t chunk_idx) {
   if (!ctx || !entries) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
+  if (serving_active(ctx)) return ctx->fail(OPIR_ERR_STATE, "serving is active");
   Db *db = find_db(ctx, db_id);
   if (!db) return ctx->fail(OPIR_ERR_UNKNOWN_DB, "unknown database %u", db_id);
   const opir_db_shape &S = db->shape;
@@ -628,6 +781,7 @@ int opir_db_push_chunk(opir_ctx *ctx, uint32_t db_id, const uint8_t *entries, ui
 int opir_db_fill_synthetic(opir_ctx *ctx, uint32_t db_id, uint64_t seed) {
   if (!ctx) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
+  if (serving_active(ctx)) return ctx->fail(OPIR_ERR_STATE, "serving is active");
   Db *db = find_db(ctx, db_id);
   if (!db) return ctx->fail(OPIR_ERR_UNKNOWN_DB, "unknown database %u", db_id);
   cudaSetDevice(ctx->device);
@@ -649,6 +803,7 @@ int opir_db_fill_synthetic(opir_ctx *ctx, uint32_t db_id, uint64_t seed) {
 int opir_db_upload_aligned(opir_ctx *ctx, uint32_t db_id, const uint64_t *aligned) {
   if (!ctx || !aligned) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
+  if (serving_active(ctx)) return ctx->fail(OPIR_ERR_STATE, "serving is active");
   Db *db = find_db(ctx, db_id);
   if (!db) return ctx->fail(OPIR_ERR_UNKNOWN_DB, "unknown database %u", db_id);
   cudaSetDevice(ctx->device);
@@ -671,11 +826,21 @@ int opir_set_galois_key(opir_ctx *ctx, uint64_t client_id, const uint64_t *keys,
   cudaSetDevice(ctx->device);
   auto &cl = ctx->clients[client_id];
   if (!cl) cl = std::make_unique<Client>();
-  const size_t bytes = (size_t)levels * 4 * kN * 8;
-  CK(cudaStreamSynchronize(ctx->stream), "sync");
-  CK(cl->galois.alloc(bytes), "alloc Galois keys");
-  CK(cudaMemcpy(cl->galois.p, keys, bytes, cudaMemcpyHostToDevice), "upload Galois keys");
+  if (cl->inflight)
+    return ctx->fail(OPIR_ERR_STATE, "client %llu has queries in flight",
+                     (unsigned long long)client_id);
+  const size_t words = (size_t)levels * 4 * kN;
+  if (ctx->key_budget) {
+    // host copy; copied to a key slot when a query needs it
+    cl->h_galois.assign(keys, keys + words);
+    ctx->lru.erase(client_id);
+  } else {
+    CK(cudaStreamSynchronize(ctx->stream), "sync");
+    CK(cl->galois.alloc(words * 8), "alloc Galois keys");
+    CK(cudaMemcpy(cl->galois.p, keys, words * 8, cudaMemcpyHostToDevice), "upload Galois keys");
+  }
   cl->levels = levels;
+  cl->has_galois = true;
   return OPIR_OK;
 }
 
@@ -685,14 +850,22 @@ int opir_set_gsw_key(opir_ctx *ctx, uint64_t client_id, const uint64_t *rows) {
   cudaSetDevice(ctx->device);
   auto &cl = ctx->clients[client_id];
   if (!cl) cl = std::make_unique<Client>();
+  if (cl->inflight)
+    return ctx->fail(OPIR_ERR_STATE, "client %llu has queries in flight",
+                     (unsigned long long)client_id);
   const size_t polys = 2 * (size_t)ctx->prm.gsw_l_key * 2;
-  CK(cudaStreamSynchronize(ctx->stream), "sync");
-  CK(cl->gsw.alloc(polys * kN * 8), "alloc RGSW key");
-  CK(cudaMemcpy(cl->gsw.p, rows, polys * kN * 8, cudaMemcpyHostToDevice), "upload RGSW key");
-  launch_ntt(ctx->Mq.tab, cl->gsw.as<uint64_t>(), polys, false, ctx->stream);  // server.cpp:497
-  ctx->launches++;
-  CK(cudaGetLastError(), "key NTT");
-  CK(cudaStreamSynchronize(ctx->stream), "key NTT");
+  if (ctx->key_budget) {
+    cl->h_gsw.assign(rows, rows + polys * kN);
+    ctx->lru.erase(client_id);
+  } else {
+    CK(cudaStreamSynchronize(ctx->stream), "sync");
+    CK(cl->gsw.alloc(polys * kN * 8), "alloc RGSW key");
+    CK(cudaMemcpy(cl->gsw.p, rows, polys * kN * 8, cudaMemcpyHostToDevice), "upload RGSW key");
+    launch_ntt(ctx->Mq.tab, cl->gsw.as<uint64_t>(), polys, false, ctx->stream);  // server.cpp:497
+    ctx->launches++;
+    CK(cudaGetLastError(), "key NTT");
+    CK(cudaStreamSynchronize(ctx->stream), "key NTT");
+  }
   cl->has_gsw = true;
   return OPIR_OK;
 }
@@ -701,9 +874,43 @@ int opir_erase_client(opir_ctx *ctx, uint64_t client_id) {
   if (!ctx) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
   cudaSetDevice(ctx->device);
-  cudaStreamSynchronize(ctx->stream);
-  if (!ctx->clients.erase(client_id))
+  auto it = ctx->clients.find(client_id);
+  if (it == ctx->clients.end())
     return ctx->fail(OPIR_ERR_UNKNOWN_CLIENT, "unknown client %llu", (unsigned long long)client_id);
+  if (it->second->inflight)
+    return ctx->fail(OPIR_ERR_STATE, "client %llu has queries in flight",
+                     (unsigned long long)client_id);
+  cudaStreamSynchronize(ctx->stream);
+  ctx->lru.erase(client_id);
+  ctx->clients.erase(it);
+  return OPIR_OK;
+}
+
+int opir_set_key_budget(opir_ctx *ctx, uint64_t bytes) {
+  if (!ctx) return OPIR_ERR_ARG;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  if (!ctx->clients.empty() || serving_active(ctx))
+    return ctx->fail(OPIR_ERR_STATE, "set the key budget before registering clients");
+  cudaSetDevice(ctx->device);
+  const size_t slot_bytes = ctx->slot_words * 8;
+  const uint64_t slots = bytes / slot_bytes;
+  if (bytes && !slots)
+    return ctx->fail(OPIR_ERR_ARG, "key budget below one client's keys (%zu bytes)", slot_bytes);
+  if (slots > (1u << 20)) return ctx->fail(OPIR_ERR_ARG, "key budget too large");
+  ctx->key_pool.release();
+  if (slots) CK(ctx->key_pool.alloc(slots * slot_bytes), "alloc key pool");
+  ctx->key_budget = bytes;
+  ctx->lru.reset((int)slots);
+  return OPIR_OK;
+}
+
+uint64_t opir_key_bytes_per_client(const opir_ctx *ctx) { return ctx ? ctx->slot_words * 8 : 0; }
+
+int opir_resident_clients(opir_ctx *ctx, uint32_t *resident, uint32_t *slots) {
+  if (!ctx || !resident || !slots) return OPIR_ERR_ARG;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  *resident = ctx->key_budget ? (uint32_t)ctx->lru.used() : (uint32_t)ctx->clients.size();
+  *slots = ctx->key_budget ? (uint32_t)ctx->lru.slots() : 0;
   return OPIR_OK;
 }
 
@@ -725,7 +932,7 @@ static int query_host(opir_ctx *ctx, uint32_t db_id, uint32_t batch, const uint6
   CK(cudaMemcpyAsync(W.queries.p, W.h_in.p, batch * CTB, cudaMemcpyHostToDevice, ctx->stream),
      "upload queries");
   int rc = run_pipeline(ctx, *db, (int)batch, client_ids, W.queries.as<uint64_t>(),
-                        W.resp.as<uint64_t>(), W.packed.as<uint8_t>(), trace);
+                        W.resp.as<uint64_t>(), W.packed.as<uint8_t>(), trace, sync_env(ctx));
   if (rc) return rc;
   uint8_t *h_resp = static_cast<uint8_t *>(W.h_out.p);
   uint8_t *h_packed = h_resp + batch * CTB;
@@ -750,6 +957,8 @@ int opir_make_query(opir_ctx *ctx, uint32_t db_id, uint64_t client_id, const uin
                     uint64_t *resp, uint8_t *packed) {
   if (!ctx || !query) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
+  if (serving_active(ctx))
+    return ctx->fail(OPIR_ERR_STATE, "serving is active: submit queries with opir_submit");
   return query_host(ctx, db_id, 1, &client_id, query, resp, packed, nullptr);
 }
 
@@ -757,6 +966,8 @@ int opir_make_query_batch(opir_ctx *ctx, uint32_t db_id, uint32_t batch, const u
                           const uint64_t *queries, uint64_t *resps, uint8_t *packed) {
   if (!ctx || !queries || !client_ids || !batch) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
+  if (serving_active(ctx))
+    return ctx->fail(OPIR_ERR_STATE, "serving is active: submit queries with opir_submit");
   return query_host(ctx, db_id, batch, client_ids, queries, resps, packed, nullptr);
 }
 
@@ -764,10 +975,13 @@ int opir_make_query_device(opir_ctx *ctx, uint32_t db_id, uint32_t batch, const 
                            const uint64_t *d_queries, uint64_t *d_resps, uint8_t *d_packed) {
   if (!ctx || !d_queries || !client_ids || !batch) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
+  if (serving_active(ctx))
+    return ctx->fail(OPIR_ERR_STATE, "serving is active: submit queries with opir_submit");
   Db *db = find_db(ctx, db_id);
   if (!db) return ctx->fail(OPIR_ERR_UNKNOWN_DB, "unknown database %u", db_id);
   cudaSetDevice(ctx->device);
-  return run_pipeline(ctx, *db, (int)batch, client_ids, d_queries, d_resps, d_packed, nullptr);
+  return run_pipeline(ctx, *db, (int)batch, client_ids, d_queries, d_resps, d_packed, nullptr,
+                      sync_env(ctx));
 }
 
 int opir_make_query_trace(opir_ctx *ctx, uint32_t db_id, uint64_t client_id, const uint64_t *query,
@@ -775,6 +989,8 @@ int opir_make_query_trace(opir_ctx *ctx, uint32_t db_id, uint64_t client_id, con
                           uint8_t *packed) {
   if (!ctx || !query) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
+  if (serving_active(ctx))
+    return ctx->fail(OPIR_ERR_STATE, "serving is active: submit queries with opir_submit");
   Trace t;
   t.leaves = leaves;
   t.gsw = gsw;
@@ -833,6 +1049,398 @@ int opir_ntt_device(opir_ctx *ctx, int mod, int inverse, uint64_t *d_polys, uint
   launch_ntt(mod ? ctx->Mp.tab : ctx->Mq.tab, d_polys, count, inverse != 0, ctx->stream);
   ctx->launches++;
   CK(cudaGetLastError(), "ntt launch");
+  return OPIR_OK;
+}
+
+}  // extern "C"
+
+
+// ===========================================================================
+// Serving: continuous batching (no counterpart in the reference, which
+// answers one make_query call at a time).  A worker thread takes submitted
+// queries from per-database FIFOs (serve_core.h), forms a batch whenever a
+// lane (stream + workspace) is free and the dispatch rule allows, and runs
+// the whole pipeline for it; up to cfg.lanes batches are on the device at
+// once, so a batch's transfers and kernels overlap the previous one's.
+// ===========================================================================
+namespace {
+
+void CUDART_CB lane_done_cb(void *arg) {
+  // runs on a CUDA runtime thread: no CUDA calls, no lock held by anyone
+  // across a CUDA call
+  Lane *L = static_cast<Lane *>(arg);
+  L->finished.store(true);
+  L->owner->wake();
+}
+
+// (ctx->mu and S.mu held)
+void fail_ticket(Serving &S, uint64_t ticket, int rc, double t) {
+  auto it = S.tickets.find(ticket);
+  if (it == S.tickets.end()) return;
+  it->second.state = 2;
+  it->second.rc = rc;
+  it->second.t_done = t;
+  it->second.query.clear();
+  S.failed++;
+}
+
+// (ctx->mu and S.mu held)
+int dispatch(opir_ctx *ctx, Serving &S, Lane &L) {
+  std::vector<serve::Pending> reqs = S.queue.pop_batch(S.cfg.max_batch);
+  if (reqs.empty()) return OPIR_OK;
+  const double t = now_s();
+  Db *db = find_db(ctx, reqs[0].db);
+  std::vector<serve::Pending> ok;
+  std::vector<uint64_t> ids;
+  for (const auto &r : reqs) {
+    auto it = ctx->clients.find(r.client);
+    const bool servable = db && it != ctx->clients.end() && it->second->has_galois &&
+                          it->second->levels >= (uint32_t)db->h &&
+                          (db->ndim == 1 || it->second->has_gsw);
+    if (!servable) {
+      fail_ticket(S, r.ticket, db ? OPIR_ERR_UNKNOWN_CLIENT : OPIR_ERR_UNKNOWN_DB, t);
+      continue;
+    }
+    ok.push_back(r);
+    ids.push_back(r.client);
+  }
+  S.done_cv.notify_all();
+  if (ok.empty()) return OPIR_OK;
+  const int n = (int)ok.size();
+  const size_t CTB = 2 * (size_t)kN * 8;
+  Workspace &W = L.ws;
+  int rc = OPIR_OK;
+  auto fail_all = [&](int code) {
+    for (const auto &r : ok) fail_ticket(S, r.ticket, code, now_s());
+    S.done_cv.notify_all();
+    return code;
+  };
+  if (W.queries.alloc(n * CTB) != cudaSuccess || W.resp.alloc(n * CTB) != cudaSuccess ||
+      W.packed.alloc(n * ctx->resp_bytes + 16) != cudaSuccess ||
+      W.h_in.alloc(n * CTB) != cudaSuccess ||
+      W.h_out.alloc(n * (CTB + ctx->resp_bytes)) != cudaSuccess) {
+    cudaGetLastError();
+    ctx->fail(OPIR_ERR_OOM, "serving lane buffers");
+    return fail_all(OPIR_ERR_OOM);
+  }
+  for (int j = 0; j < n; j++) {
+    Ticket &tk = S.tickets[ok[j].ticket];
+    std::memcpy(static_cast<uint8_t *>(W.h_in.p) + j * CTB, tk.query.data(), CTB);
+    tk.query.clear();
+    tk.query.shrink_to_fit();
+    tk.state = 1;
+  }
+  if (cudaMemcpyAsync(W.queries.p, W.h_in.p, n * CTB, cudaMemcpyHostToDevice, L.stream) !=
+      cudaSuccess)
+    return fail_all(ctx->cuda_fail(cudaGetLastError(), "upload queries"));
+  const PipeEnv E{&W, L.stream, L.status.as<uint32_t>(), false, true};
+  rc = run_pipeline(ctx, *db, n, ids.data(), W.queries.as<uint64_t>(), W.resp.as<uint64_t>(),
+                    W.packed.as<uint8_t>(), nullptr, E);
+  if (rc) return fail_all(rc);
+  uint8_t *h_resp = static_cast<uint8_t *>(W.h_out.p);
+  if (cudaMemcpyAsync(h_resp, W.resp.p, n * CTB, cudaMemcpyDeviceToHost, L.stream) != cudaSuccess ||
+      cudaMemcpyAsync(h_resp + n * CTB, W.packed.p, n * ctx->resp_bytes, cudaMemcpyDeviceToHost,
+                      L.stream) != cudaSuccess ||
+      cudaMemcpyAsync(L.h_status.p, L.status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                      L.stream) != cudaSuccess ||
+      cudaEventRecord(L.done, L.stream) != cudaSuccess ||
+      cudaLaunchHostFunc(L.stream, lane_done_cb, &L) != cudaSuccess) {
+    // the batch may still run: wait for it before the buffers are reused
+    cudaStreamSynchronize(L.stream);
+    if (ctx->key_budget)
+      for (uint64_t id : ids) ctx->lru.unpin(id);
+    return fail_all(ctx->cuda_fail(cudaGetLastError(), "serving batch"));
+  }
+  for (uint64_t id : ids) ctx->clients[id]->inflight++;
+  L.busy = true;
+  L.finished = false;
+  L.db = ok[0].db;
+  L.reqs = std::move(ok);
+  L.clients = std::move(ids);
+  S.batches++;
+  S.batched_queries += n;
+  return OPIR_OK;
+}
+
+// (ctx->mu and S.mu held; the lane's stream has passed its callback)
+void complete_lane(opir_ctx *ctx, Serving &S, Lane &L) {
+  const int n = (int)L.reqs.size();
+  const size_t CTB = 2 * (size_t)kN * 8;
+  const uint32_t st = *static_cast<const uint32_t *>(L.h_status.p);
+  int rc = OPIR_OK;
+  if (st) {
+    rc = OPIR_ERR_TIMEOUT;
+    cudaMemsetAsync(L.status.p, 0, sizeof(uint32_t), L.stream);
+  }
+  const double t = now_s();
+  const uint8_t *h_resp = static_cast<const uint8_t *>(L.ws.h_out.p);
+  const uint8_t *h_packed = h_resp + n * CTB;
+  for (int j = 0; j < n; j++) {
+    auto it = S.tickets.find(L.reqs[j].ticket);
+    if (it == S.tickets.end()) continue;
+    Ticket &tk = it->second;
+    tk.state = 2;
+    tk.rc = rc;
+    tk.t_done = t;
+    if (rc) {
+      S.failed++;
+      continue;
+    }
+    tk.resp.resize(2 * kN);
+    std::memcpy(tk.resp.data(), h_resp + j * CTB, CTB);
+    tk.packed.assign(h_packed + j * ctx->resp_bytes, h_packed + (j + 1) * ctx->resp_bytes);
+    S.completed++;
+    S.lat_ms.push_back((t - tk.t_submit) * 1e3);
+    S.t_last = t;
+  }
+  for (uint64_t id : L.clients) {
+    auto it = ctx->clients.find(id);
+    if (it != ctx->clients.end() && it->second->inflight > 0) it->second->inflight--;
+    if (ctx->key_budget) ctx->lru.unpin(id);
+  }
+  L.busy = false;
+  L.finished = false;
+  L.reqs.clear();
+  L.clients.clear();
+  S.done_cv.notify_all();
+}
+
+void serve_loop(opir_ctx *ctx) {
+  Serving &S = *ctx->serving;
+  cudaSetDevice(ctx->device);
+  const double max_wait = S.cfg.max_wait_us * 1e-6;
+  for (;;) {
+    uint64_t seen;
+    {
+      std::lock_guard<std::mutex> g(S.wake_mu);
+      seen = S.wake_seq;
+    }
+    bool act = false;
+    double timeout = 0.01;
+    {
+      std::lock_guard<std::mutex> g(S.mu);
+      int busy = 0, idle = 0;
+      bool finished = false;
+      for (auto &L : S.lanes) {
+        if (L->busy) {
+          busy++;
+          finished |= L->finished.load();
+        } else {
+          idle++;
+        }
+      }
+      const double wait = S.queue.size() ? now_s() - S.queue.oldest() : 0.0;
+      act = finished || serve::should_dispatch(S.queue.size(), S.cfg.max_batch, busy, idle,
+                                               S.stop ? 1e30 : wait, max_wait);
+      if (!act && S.stop && !S.queue.size() && !busy) return;
+      // until a submission, a finished batch, stop, or the oldest request's deadline
+      if (S.queue.size() && busy) timeout = std::max(0.0, max_wait - wait);
+    }
+    if (!act) {
+      std::unique_lock<std::mutex> lk(S.wake_mu);
+      S.wake_cv.wait_for(lk, std::chrono::duration<double>(timeout + 2e-5),
+                         [&] { return S.wake_seq != seen; });
+      continue;
+    }
+    std::lock_guard<std::mutex> g(ctx->mu);
+    std::lock_guard<std::mutex> g2(S.mu);
+    for (auto &L : S.lanes)
+      if (L->busy && L->finished.load()) complete_lane(ctx, S, *L);
+    for (;;) {
+      int busy = 0, idle = 0;
+      Lane *free_lane = nullptr;
+      for (auto &L : S.lanes) {
+        if (L->busy) {
+          busy++;
+        } else {
+          idle++;
+          if (!free_lane) free_lane = L.get();
+        }
+      }
+      const double wait = S.queue.size() ? now_s() - S.queue.oldest() : 0.0;
+      if (!serve::should_dispatch(S.queue.size(), S.cfg.max_batch, busy, idle,
+                                  S.stop ? 1e30 : wait, max_wait))
+        break;
+      dispatch(ctx, S, *free_lane);
+    }
+  }
+}
+
+// Size a lane's buffers for max_batch queries on every resident database
+// (and build the tensor-core limb planes), so that no batch allocates --
+// freeing device memory would synchronise the device under the worker's locks.
+int presize_lane(opir_ctx *ctx, Lane &L, int max_batch) {
+  const size_t CTB = 2 * (size_t)kN * 8;
+  Workspace &W = L.ws;
+  for (auto &kv : ctx->dbs) {
+    Db &db = *kv.second;
+    int rc = ensure_workspace(ctx, db, max_batch, W);
+    if (rc) return rc;
+    const int n1 = (int)db.shape.fst_dim_sz, nr = (int)db.shape.other_dim_sz;
+    if (max_batch >= 2 && ctx->batch_scan && ctx->tc_mode == 1 && tc_scan_supported(n1, nr)) {
+      CK(W.ql.alloc(tc_query_limb_bytes(n1, max_batch)), "alloc query limbs");
+      if (!db.dbl_valid) {
+        CK(db.dbl.alloc(tc_db_limb_bytes(n1, nr)), "alloc database limb plane");
+        launch_db_limbs(db.dbs.as<uint64_t>(), db.dbl.as<uint16_t>(), n1, nr, L.stream);
+        ctx->launches++;
+        CK(cudaStreamSynchronize(L.stream), "database limb plane");
+        db.dbl_valid = true;
+      }
+    }
+  }
+  CK(W.queries.alloc(max_batch * CTB), "alloc queries");
+  CK(W.resp.alloc(max_batch * CTB), "alloc response");
+  CK(W.packed.alloc(max_batch * ctx->resp_bytes + 16), "alloc packed");
+  CK(W.h_in.alloc(max_batch * CTB), "alloc pinned");
+  CK(W.h_out.alloc(max_batch * (CTB + ctx->resp_bytes)), "alloc pinned");
+  return OPIR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int opir_serve_start(opir_ctx *ctx, const opir_serve_config *cfg) {
+  if (!ctx || !cfg || !cfg->max_batch || cfg->lanes < 1 || cfg->lanes > 4) return OPIR_ERR_ARG;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  if (serving_active(ctx)) return ctx->fail(OPIR_ERR_STATE, "serving is already active");
+  cudaSetDevice(ctx->device);
+  // queued synchronous work may still read key slots that a lane would refill
+  CK(cudaStreamSynchronize(ctx->stream), "sync");
+  auto S = std::make_unique<Serving>();
+  S->cfg = *cfg;
+  for (uint32_t i = 0; i < cfg->lanes; i++) {
+    auto L = std::make_unique<Lane>();
+    L->owner = S.get();
+    CK(cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking), "lane stream");
+    CK(cudaEventCreateWithFlags(&L->done, cudaEventDisableTiming), "lane event");
+    CK(L->status.alloc(sizeof(uint32_t)), "lane status");
+    CK(cudaMemset(L->status.p, 0, sizeof(uint32_t)), "lane status");
+    CK(L->h_status.alloc(sizeof(uint32_t)), "lane status");
+    const int rc = presize_lane(ctx, *L, (int)cfg->max_batch);
+    if (rc) return rc;
+    S->lanes.push_back(std::move(L));
+  }
+  S->active = true;
+  ctx->serving = std::move(S);
+  ctx->serving->worker = std::thread(serve_loop, ctx);
+  return OPIR_OK;
+}
+
+int opir_serve_stop(opir_ctx *ctx) {
+  if (!ctx) return OPIR_ERR_ARG;
+  Serving *S;
+  {
+    std::lock_guard<std::mutex> g(ctx->mu);
+    if (!serving_active(ctx)) return OPIR_OK;
+    S = ctx->serving.get();
+  }
+  {
+    std::lock_guard<std::mutex> g(S->mu);
+    S->stop = true;
+  }
+  S->wake();
+  if (S->worker.joinable()) S->worker.join();
+  std::lock_guard<std::mutex> g(ctx->mu);
+  S->active = false;
+  return OPIR_OK;
+}
+
+int opir_submit(opir_ctx *ctx, uint32_t db_id, uint64_t client_id, const uint64_t *query,
+                uint64_t *ticket) {
+  if (!ctx || !query || !ticket) return OPIR_ERR_ARG;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  if (!serving_active(ctx)) return ctx->fail(OPIR_ERR_STATE, "serving is not active");
+  Db *db = find_db(ctx, db_id);
+  if (!db) return ctx->fail(OPIR_ERR_UNKNOWN_DB, "unknown database %u", db_id);
+  auto it = ctx->clients.find(client_id);
+  if (it == ctx->clients.end() || !it->second->has_galois ||
+      (db->ndim > 1 && !it->second->has_gsw))
+    return ctx->fail(OPIR_ERR_UNKNOWN_CLIENT, "no keys for client %llu",
+                     (unsigned long long)client_id);
+  if (it->second->levels < (uint32_t)db->h)
+    return ctx->fail(OPIR_ERR_ARG, "client %llu has %u Galois levels, database needs %d",
+                     (unsigned long long)client_id, it->second->levels, db->h);
+  Serving &S = *ctx->serving;
+  {
+    std::lock_guard<std::mutex> g2(S.mu);
+    if (S.stop) return ctx->fail(OPIR_ERR_STATE, "serving is stopping");
+    const uint64_t id = S.next_ticket++;
+    Ticket &tk = S.tickets[id];
+    tk.db = db_id;
+    tk.client = client_id;
+    tk.query.assign(query, query + 2 * (size_t)kN);
+    tk.t_submit = now_s();
+    if (!S.submitted) S.t_first = tk.t_submit;
+    S.submitted++;
+    S.queue.push(serve::Pending{id, db_id, client_id, tk.t_submit});
+    *ticket = id;
+  }
+  S.wake();
+  return OPIR_OK;
+}
+
+static int take_ticket(opir_ctx *ctx, Serving &S, uint64_t ticket, uint64_t *resp,
+                       uint8_t *packed) {
+  auto it = S.tickets.find(ticket);
+  Ticket &tk = it->second;
+  const int rc = tk.rc;
+  if (!rc) {
+    if (resp) std::memcpy(resp, tk.resp.data(), 2 * (size_t)kN * 8);
+    if (packed) std::memcpy(packed, tk.packed.data(), ctx->resp_bytes);
+  }
+  S.tickets.erase(it);
+  return rc;
+}
+
+int opir_poll(opir_ctx *ctx, uint64_t ticket, uint64_t *resp, uint8_t *packed, int *done) {
+  if (!ctx || !done) return OPIR_ERR_ARG;
+  *done = 0;
+  Serving *S = ctx->serving.get();
+  if (!S) return OPIR_ERR_STATE;
+  std::lock_guard<std::mutex> g(S->mu);
+  auto it = S->tickets.find(ticket);
+  if (it == S->tickets.end()) return OPIR_ERR_ARG;
+  if (it->second.state != 2) return OPIR_OK;
+  *done = 1;
+  return take_ticket(ctx, *S, ticket, resp, packed);
+}
+
+int opir_wait(opir_ctx *ctx, uint64_t ticket, uint32_t timeout_ms, uint64_t *resp,
+              uint8_t *packed) {
+  if (!ctx) return OPIR_ERR_ARG;
+  Serving *S = ctx->serving.get();
+  if (!S) return OPIR_ERR_STATE;
+  std::unique_lock<std::mutex> lk(S->mu);
+  const bool ready = S->done_cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] {
+    auto it = S->tickets.find(ticket);
+    return it == S->tickets.end() || it->second.state == 2;
+  });
+  if (S->tickets.find(ticket) == S->tickets.end()) return OPIR_ERR_ARG;
+  if (!ready) return OPIR_ERR_TIMEOUT;
+  return take_ticket(ctx, *S, ticket, resp, packed);
+}
+
+int opir_serve_stats_get(opir_ctx *ctx, opir_serve_stats *out) {
+  if (!ctx || !out) return OPIR_ERR_ARG;
+  Serving *S = ctx->serving.get();
+  if (!S) return OPIR_ERR_STATE;
+  std::lock_guard<std::mutex> g(S->mu);
+  std::memset(out, 0, sizeof *out);
+  out->submitted = S->submitted;
+  out->completed = S->completed;
+  out->failed = S->failed;
+  out->batches = S->batches;
+  out->queued = S->queue.size();
+  out->mean_batch = S->batches ? (double)S->batched_queries / (double)S->batches : 0.0;
+  out->p50_ms = serve::percentile(S->lat_ms, 50);
+  out->p99_ms = serve::percentile(S->lat_ms, 99);
+  out->max_ms = serve::percentile(S->lat_ms, 100);
+  double sum = 0;
+  for (double v : S->lat_ms) sum += v;
+  out->mean_ms = S->lat_ms.empty() ? 0.0 : sum / (double)S->lat_ms.size();
+  const double span = S->t_last - S->t_first;
+  out->queries_per_s = span > 0 ? (double)S->completed / span : 0.0;
   return OPIR_OK;
 }
 

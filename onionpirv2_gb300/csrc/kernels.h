@@ -87,11 +87,11 @@ void launch_query_prep_plane(const uint64_t *leaves, size_t leaves_stride, uint6
 // into 8-bit limbs held as bf16, exact fp32 accumulation in tensor memory.
 // The database needs its limb plane dbl (tc_db_limb_bytes, built by
 // launch_db_limbs from dbs); plane is the query operand of
-// launch_query_prep_plane, ql scratch of tc_query_limb_bytes.  Output as
+// launch_query_prep_plane, ql scratch of tc_query_limb_bytes(n1, batch).  Output as
 // launch_scan.  Returns the number of kernels launched.
 bool tc_scan_supported(int n1, int n_rest);
 size_t tc_db_limb_bytes(int n1, int n_rest);
-size_t tc_query_limb_bytes(int n1);
+size_t tc_query_limb_bytes(int n1, int batch);
 cudaError_t init_tc_attributes();
 void launch_db_limbs(const uint64_t *dbs, uint16_t *dbl, int n1, int n_rest, cudaStream_t s);
 int launch_tc_scan_batched(const uint16_t *dbl, const uint64_t *plane, uint16_t *ql, uint64_t *out,

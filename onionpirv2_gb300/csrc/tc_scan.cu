@@ -418,7 +418,11 @@ bool tc_scan_supported(int n1, int n_rest) {
 }
 
 size_t tc_db_limb_bytes(int n1, int n_rest) { return (size_t)kN * n1 * n_rest * 16; }
-size_t tc_query_limb_bytes(int n1) { return (size_t)kN * n1 * kTcMaxNB * 16; }
+size_t tc_query_limb_bytes(int n1, int batch) {
+  const int pb = batch < kTcMaxNB / 2 ? batch : kTcMaxNB / 2;  // queries of the largest pass
+  const int padded = pb > kTcHalfNB / 2 ? kTcMaxNB / 2 : (pb + 3) / 4 * 4;
+  return (size_t)kN * n1 * 2 * padded * 16;
+}
 
 cudaError_t init_tc_attributes() {
   int dev;

@@ -183,16 +183,18 @@ class PirServer:
         self._check(self._L.opir_erase_client(self._ctx, client_id))
 
     # ---- queries
-    def make_query(self, client_id: int, query) -> ResponseCiphertext:
+    def make_query(self, client_id: int, query, db_id: Optional[int] = None) -> ResponseCiphertext:
         """Answer one query (server.cpp:520-579); returns the response
-        ciphertext mod small_q with its packed bytes attached."""
+        ciphertext mod small_q with its packed bytes attached.  `db_id`
+        selects a database added with add_database (default: this server's)."""
         q = _read_u64(query)
         if q.size != 2 * N:
             raise ValueError("query must be one ciphertext [2][N]")
         resp = np.zeros(2 * N, np.uint64)
         packed = np.zeros(self.resp_bytes, np.uint8)
-        self._check(self._L.opir_make_query(self._ctx, self.db_id, client_id, _capi.p64(q),
-                                            _capi.p64(resp), _capi.p8(packed)))
+        self._check(self._L.opir_make_query(self._ctx, self.db_id if db_id is None else db_id,
+                                            client_id, _capi.p64(q), _capi.p64(resp),
+                                            _capi.p8(packed)))
         out = resp.reshape(2, N).view(ResponseCiphertext)
         out.packed = packed.tobytes()
         return out
@@ -245,6 +247,82 @@ class PirServer:
             raise ValueError("response was not produced by make_query")
         stream.write(packed)
         return len(packed)
+
+    # ---- further databases on this context (served side by side)
+    def add_database(self, pir_params: PirParams, seed: Optional[int] = None) -> int:
+        """Create another resident database with the same ciphertext
+        parameters; filled with seeded entries when `seed` is given.  Returns
+        its id (the constructor's database is ``self.db_id``)."""
+        P, Q = pir_params, self.pir_params
+        if (P.coeff_modulus, P.plain_mod, P.small_q, P.gsw_l, P.gsw_l_key) != (
+                Q.coeff_modulus, Q.plain_mod, Q.small_q, Q.gsw_l, Q.gsw_l_key):
+            raise ValueError("a database on this context must share its ciphertext parameters")
+        shape = _capi.OpirDbShape(
+            fst_dim_sz=P.get_fst_dim_sz(), other_dim_sz=P.get_other_dim_sz(),
+            entry_size=P.get_entry_size(), entries_per_pt=P.get_num_entries_per_plaintext(),
+            bits_per_coeff=P.get_num_bits_per_coeff())
+        db = ctypes.c_uint32()
+        self._check(self._L.opir_db_create(self._ctx, ctypes.byref(shape), ctypes.byref(db)))
+        if seed is not None:
+            self._check(self._L.opir_db_fill_synthetic(self._ctx, db.value, seed))
+        return db.value
+
+    # ---- key budget (client keys in a bounded pool, least recently used out)
+    def set_key_budget(self, nbytes: int):
+        self._check(self._L.opir_set_key_budget(self._ctx, int(nbytes)))
+
+    def key_bytes_per_client(self) -> int:
+        return int(self._L.opir_key_bytes_per_client(self._ctx))
+
+    def resident_clients(self):
+        """(clients with keys in device memory, slots of the budget or 0)"""
+        r, sl = ctypes.c_uint32(), ctypes.c_uint32()
+        self._check(self._L.opir_resident_clients(self._ctx, ctypes.byref(r), ctypes.byref(sl)))
+        return r.value, sl.value
+
+    # ---- serving: continuous batching
+    def serve_start(self, max_batch: int = 32, lanes: int = 2, max_wait_us: int = 2000):
+        cfg = _capi.OpirServeConfig(max_batch=max_batch, lanes=lanes, max_wait_us=max_wait_us)
+        self._check(self._L.opir_serve_start(self._ctx, ctypes.byref(cfg)))
+
+    def serve_stop(self):
+        self._check(self._L.opir_serve_stop(self._ctx))
+
+    def submit(self, client_id: int, query, db_id: Optional[int] = None) -> int:
+        """Queue one query; returns its ticket."""
+        q = _read_u64(query)
+        if q.size != 2 * N:
+            raise ValueError("query must be one ciphertext [2][N]")
+        t = ctypes.c_uint64()
+        self._check(self._L.opir_submit(self._ctx, self.db_id if db_id is None else db_id,
+                                        client_id, _capi.p64(q), ctypes.byref(t)))
+        return t.value
+
+    def _response(self, resp, packed) -> ResponseCiphertext:
+        out = resp.reshape(2, N).view(ResponseCiphertext)
+        out.packed = packed.tobytes()
+        return out
+
+    def poll(self, ticket: int) -> Optional[ResponseCiphertext]:
+        """The response of a ticket, or None while it is queued or running."""
+        resp = np.zeros(2 * N, np.uint64)
+        packed = np.zeros(self.resp_bytes, np.uint8)
+        done = ctypes.c_int()
+        self._check(self._L.opir_poll(self._ctx, ticket, _capi.p64(resp), _capi.p8(packed),
+                                      ctypes.byref(done)))
+        return self._response(resp, packed) if done.value else None
+
+    def wait(self, ticket: int, timeout_ms: int = 60000) -> ResponseCiphertext:
+        resp = np.zeros(2 * N, np.uint64)
+        packed = np.zeros(self.resp_bytes, np.uint8)
+        self._check(self._L.opir_wait(self._ctx, ticket, timeout_ms, _capi.p64(resp),
+                                      _capi.p8(packed)))
+        return self._response(resp, packed)
+
+    def serve_stats(self) -> dict:
+        st = _capi.OpirServeStats()
+        self._check(self._L.opir_serve_stats_get(self._ctx, ctypes.byref(st)))
+        return {name: getattr(st, name) for name, _ in st._fields_}
 
     # ---- timing / accounting
     def set_timing(self, enable: bool = True):
