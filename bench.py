@@ -373,7 +373,8 @@ def main():
         e1.synchronize()
     e2e_ms = e0.elapsed_time(e1)
 
-    # ---- batched: B queries per step share one pass over the database
+    # ---- batched: B queries per step share one pass over the database,
+    # on both first-dimension engines (bf16-limb tensor cores, integer IMAD)
     batched = None
     if args.batch > 1:
         B = args.batch
@@ -383,28 +384,46 @@ def main():
             server.make_query_device(ids, dq.data_ptr() + i * B * qbytes,
                                      dresp.data_ptr() + i * B * qbytes, dpack.data_ptr() + i * B * rb)
 
-        with torch.cuda.stream(stream):
-            for i in range(3):
-                bstep(i)
-            stream.synchronize()
-            b0, b1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            b0.record(stream)
-            for i in range(args.batch_steps):
-                bstep(i % (args.batch_steps + 3))
-            b1.record(stream)
-            b1.synchronize()
-            bms = b0.elapsed_time(b1) / args.batch_steps
-            server.set_timing(True)
-            bst = []
-            for i in range(min(args.batch_steps, 5)):
-                bstep(i)
+        def run_batched(engine):
+            server.set_batch_engine(engine)
+            with torch.cuda.stream(stream):
+                for i in range(3):
+                    bstep(i)
                 stream.synchronize()
-                bst.append(server.stage_times())
-            server.set_timing(False)
-        bqps = B * world / (bms / 1e3)
-        batched = {"batch": B, "value": bqps, "unit": "queries/s", "ms_per_batch": bms,
-                   "speedup_vs_single": bqps / qps, "path": "imad batched GEMM",
-                   "stages_ms": {k: statistics.mean(x[k] for x in bst) for k in bst[0]}}
+                b0, b1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                b0.record(stream)
+                for i in range(args.batch_steps):
+                    bstep(i % (args.batch_steps + 3))
+                b1.record(stream)
+                b1.synchronize()
+                bms = b0.elapsed_time(b1) / args.batch_steps
+                server.set_timing(True)
+                bst = []
+                for i in range(min(args.batch_steps, 5)):
+                    bstep(i)
+                    stream.synchronize()
+                    bst.append(server.stage_times())
+                server.set_timing(False)
+            # bit-exact against the single-query responses of the same queries
+            same = bool(np.array_equal(dresp[:B].cpu().numpy().view(np.uint64).reshape(B, -1),
+                                       single_resps[:B]))
+            server.set_batch_engine("auto")
+            return {"value": B * world / (bms / 1e3), "unit": "queries/s", "ms_per_batch": bms,
+                    "stages_ms": {k: statistics.mean(x[k] for x in bst) for k in bst[0]},
+                    "matches_single_query_responses": same}
+
+        # responses of the first B queries through the single-query path
+        with torch.cuda.stream(stream):
+            for i in range(B):
+                server.make_query_device([i % NUM_CLIENTS], dq.data_ptr() + i * qbytes,
+                                         dresp.data_ptr() + i * qbytes, dpack.data_ptr() + i * rb)
+            stream.synchronize()
+        single_resps = dresp[:B].cpu().numpy().view(np.uint64).reshape(B, -1).copy()
+        tensor = run_batched("tensor")
+        imad = run_batched("imad")
+        batched = dict(tensor, batch=B, engine="tensor (tcgen05, 8-bit limbs in bf16, exact)",
+                       speedup_vs_single=tensor["value"] / qps,
+                       imad=dict(imad, engine="integer multiply-add GEMM"))
     clocks.stop()
     e2e_qps = e2e_steps * world / (e2e_ms / 1e3)
 

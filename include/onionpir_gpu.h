@@ -147,6 +147,21 @@ int opir_make_query_trace(opir_ctx *ctx, uint32_t db_id, uint64_t client_id,
 int opir_first_dim_noalloc(opir_ctx *ctx, uint32_t db_id, const uint64_t *d_fst_cts,
                            uint64_t *d_out);
 
+/* ---- first-dimension engine for batches (no reference counterpart) ----
+ * A batch of queries on one database shares one pass over it: the product
+ * becomes a per-slot (n_rest x n1) . (n1 x 2B) GEMM.  AUTO: the tcgen05
+ * tensor-core engine (residues split into 8-bit limbs, exact) from
+ * tensor_min_batch queries on when the shape allows it, the integer
+ * multiply-add GEMM otherwise; SCAN: one streaming pass per query; IMAD /
+ * TENSOR: that engine whenever the shape allows it.  All give the same bits. */
+enum {
+  OPIR_ENGINE_AUTO = 0,
+  OPIR_ENGINE_SCAN = 1,
+  OPIR_ENGINE_IMAD = 2,
+  OPIR_ENGINE_TENSOR = 3
+};
+int opir_set_batch_engine(opir_ctx *ctx, int engine, uint32_t tensor_min_batch);
+
 /* ---- serving: continuous batching ----
  * No reference counterpart (PirServer::make_query, server.cpp:520-579,
  * answers one query per call).  opir_serve_start starts a worker thread that

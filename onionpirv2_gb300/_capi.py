@@ -39,8 +39,10 @@ EXPORTS = (
     "opir_launch_count", "opir_sync", "opir_ntt", "opir_ntt_device",
     "opir_set_key_budget", "opir_key_bytes_per_client", "opir_resident_clients",
     "opir_serve_start", "opir_serve_stop", "opir_submit", "opir_poll", "opir_wait",
-    "opir_serve_stats_get",
+    "opir_serve_stats_get", "opir_set_batch_engine",
 )
+
+ENGINES = {"auto": 0, "scan": 1, "imad": 2, "tensor": 3}
 
 
 class OpirParams(ctypes.Structure):
@@ -157,6 +159,7 @@ def load(path: str = LIB):
     L.opir_poll.argtypes = [_vp, ctypes.c_uint64, _u64p, _u8p, ctypes.POINTER(ctypes.c_int)]
     L.opir_wait.argtypes = [_vp, ctypes.c_uint64, ctypes.c_uint32, _u64p, _u8p]
     L.opir_serve_stats_get.argtypes = [_vp, ctypes.POINTER(OpirServeStats)]
+    L.opir_set_batch_engine.argtypes = [_vp, ctypes.c_int, ctypes.c_uint32]
     _lib = L
     return L
 

@@ -998,6 +998,16 @@ int opir_make_query_trace(opir_ctx *ctx, uint32_t db_id, uint64_t client_id, con
   return query_host(ctx, db_id, 1, &client_id, query, resp, packed, &t);
 }
 
+int opir_set_batch_engine(opir_ctx *ctx, int engine, uint32_t tensor_min_batch) {
+  if (!ctx || engine < OPIR_ENGINE_AUTO || engine > OPIR_ENGINE_TENSOR) return OPIR_ERR_ARG;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  if (serving_active(ctx)) return ctx->fail(OPIR_ERR_STATE, "serving is active");
+  ctx->batch_scan = engine != OPIR_ENGINE_SCAN;
+  ctx->tc_mode = (engine == OPIR_ENGINE_AUTO || engine == OPIR_ENGINE_TENSOR) ? 1 : 0;
+  ctx->tc_min_batch = engine == OPIR_ENGINE_TENSOR ? 2 : (tensor_min_batch ? (int)tensor_min_batch : 2);
+  return OPIR_OK;
+}
+
 int opir_set_timing(opir_ctx *ctx, int enable) {
   if (!ctx) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);

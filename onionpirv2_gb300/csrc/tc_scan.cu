@@ -6,8 +6,10 @@
 // server.cpp:178-293 reduce the 128-bit sums mod q).  Here every residue is
 // split into eight balanced 8-bit limbs, v = sum_i d_i 2^(8i) with d_i in
 // [-128, 127] (the top limb in [0, 16]); each limb is exact in bf16, a limb
-// product is at most 2^14 in magnitude and a sum of n1 <= 512 of them at most
-// 2^23, so the fp32 accumulation of tcgen05.mma kind::f16 is exact.
+// product is at most 2^14 in magnitude and a sum of 512 of them at most 2^23,
+// so the fp32 accumulation of tcgen05.mma kind::f16 is exact.  Longer first
+// dimensions run as segments of at most 512 k, each reduced mod q and added
+// to the previous segments' result.
 //
 // MMA shape per tile: M = 16 database rows x 8 limbs = 128 (TMEM lanes),
 // N = 2B query polynomials x 8 limbs <= 512 (TMEM columns, two MMAs of <= 256),
@@ -60,8 +62,10 @@ constexpr uint32_t kErrTcRange = 128u;
 
 struct TcGeom {
   int n1, n_rest, batch;      // batch: queries of the pass
+  int k0;                     // first k of this segment (multiple of 32)
+  int accumulate;             // add to the result of the previous segments
   int nh, nbh;                // column halves, query polynomials per half (multiple of 8)
-  int n_rb, nkc;              // row tiles, k-chunks per tile
+  int n_rb, nkc;              // row tiles, 32-k chunks of the segment
   long long units;            // N * n_rb * nh tiles
   uint32_t b_bytes;           // query bytes per stage
   uint32_t idesc;             // instruction descriptor (M = 128, N = 8 nbh)
@@ -179,8 +183,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       for (long long u = blockIdx.x; u < G.units && ok; u += gridDim.x) {
         const long long c = u / per_c, rem = u % per_c;
         const long long rb = rem / G.nh, hf = rem % G.nh;
-        const uint16_t *a_src = dbl + (size_t)(c * G.n_rb + rb) * kblk * (kTcRows * 64);
-        const uint16_t *b_src = ql + (size_t)(c * G.nh + hf) * kblk * G.nbh * 64;
+        const uint16_t *a_src =
+            dbl + ((size_t)(c * G.n_rb + rb) * kblk + G.k0 / 8) * (kTcRows * 64);
+        const uint16_t *b_src = ql + ((size_t)(c * G.nh + hf) * kblk + G.k0 / 8) * G.nbh * 64;
         for (int kc = 0; kc < G.nkc; ++kc, ++it) {
           const int s = (int)(it % kTcStages);
           const long long round = it / kTcStages;
@@ -303,12 +308,15 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         }
         __syncwarp();
         bool ok_one = true;
-        const uint64_t val = tc_combine(y, q, mu_lo, mu_hi, r64, r128, ok_one);
+        uint64_t val = tc_combine(y, q, mu_lo, mu_hi, r64, r128, ok_one);
         range_ok &= ok_one;
         const int bq = (int)hf * kTcHalfNB + grp * 8 + t8;  // query polynomial in the pass
         const int b = bq >> 1;
-        if (b < G.batch)
-          out[(size_t)(b_base + b) * out_stride + (row * 2 + (bq & 1)) * kN + c] = val;
+        if (b < G.batch) {
+          uint64_t *o = out + (size_t)(b_base + b) * out_stride + (row * 2 + (bq & 1)) * kN + c;
+          if (G.accumulate) val = add_mod(val, *o, q);
+          *o = val;
+        }
       }
       tc_fence_before();
       __syncwarp();
@@ -413,8 +421,10 @@ uint32_t make_idesc(int n) {
 
 }  // namespace
 
+constexpr int kTcMaxSegment = 512;  // k per exact fp32 accumulation
+
 bool tc_scan_supported(int n1, int n_rest) {
-  return n1 % kTcKC == 0 && n1 <= 512 && n_rest % kTcRows == 0 && n_rest >= kTcRows;
+  return n1 % kTcKC == 0 && n1 > 0 && n_rest % kTcRows == 0 && n_rest >= kTcRows;
 }
 
 size_t tc_db_limb_bytes(int n1, int n_rest) { return (size_t)kN * n1 * n_rest * 16; }
@@ -455,7 +465,6 @@ int launch_tc_scan_batched(const uint16_t *dbl, const uint64_t *plane, uint16_t 
     G.nh = padded > kTcHalfNB / 2 ? 2 : 1;
     G.nbh = 2 * padded / G.nh;
     G.n_rb = n_rest / kTcRows;
-    G.nkc = n1 / kTcKC;
     G.units = (long long)kN * G.n_rb * G.nh;
     G.b_bytes = (uint32_t)(kTcKB * G.nbh * 128);
     G.idesc = make_idesc(G.nbh * 8);
@@ -465,9 +474,16 @@ int launch_tc_scan_batched(const uint16_t *dbl, const uint64_t *plane, uint16_t 
         plane, ql, n1, b0, G.nh, G.nbh, pb);
     const int sms = g_tc_sms > 0 ? g_tc_sms : 152;
     const long long grid = G.units < sms ? G.units : sms;
-    tc_scan_kernel<<<(unsigned)grid, kTcThreads, kTcSmem, s>>>(dbl, ql, out, out_stride, b0, G, q,
-                                                              mu_lo, mu_hi, r64, r128, status);
-    launches += 2;
+    launches++;
+    for (int k0 = 0; k0 < n1; k0 += kTcMaxSegment) {
+      const int klen = n1 - k0 < kTcMaxSegment ? n1 - k0 : kTcMaxSegment;
+      G.k0 = k0;
+      G.nkc = klen / kTcKC;
+      G.accumulate = k0 > 0;
+      tc_scan_kernel<<<(unsigned)grid, kTcThreads, kTcSmem, s>>>(dbl, ql, out, out_stride, b0, G,
+                                                                q, mu_lo, mu_hi, r64, r128, status);
+      launches++;
+    }
   }
   return launches;
 }

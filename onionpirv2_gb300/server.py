@@ -280,6 +280,13 @@ class PirServer:
         self._check(self._L.opir_resident_clients(self._ctx, ctypes.byref(r), ctypes.byref(sl)))
         return r.value, sl.value
 
+    # ---- first-dimension engine of batches
+    def set_batch_engine(self, engine: str = "auto", tensor_min_batch: int = 0):
+        """'auto' (tensor cores when the shape allows, from tensor_min_batch
+        queries on), 'scan' (one pass per query), 'imad' or 'tensor'."""
+        self._check(self._L.opir_set_batch_engine(self._ctx, _capi.ENGINES[engine],
+                                                  tensor_min_batch))
+
     # ---- serving: continuous batching
     def serve_start(self, max_batch: int = 32, lanes: int = 2, max_wait_us: int = 2000):
         cfg = _capi.OpirServeConfig(max_batch=max_batch, lanes=lanes, max_wait_us=max_wait_us)

@@ -280,6 +280,7 @@ def test_batched_scan_matches_single_and_oracle(oracle_lib, gpu_lib, monkeypatch
     ((4096, 256), 20),      # 40 query polynomials: a 256 + 64 column split
     ((1 << 15, 512), 5),    # 512 x 64
     ((1 << 15, 512), 32),   # a full pass: 512 tensor-memory columns
+    ((1 << 14, 1024), 6),   # 1024 x 16: two k segments of 512, the second accumulating
 ])
 def test_tensor_core_first_dim_matches_single_queries(oracle_lib, gpu_lib, monkeypatch, shape,
                                                       batch):
