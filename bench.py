@@ -66,6 +66,13 @@ def parse():
     ap.add_argument("--micro", choices=["ntt"], default=None,
                     help="kernel micro-benchmark instead of the query benchmark")
     ap.add_argument("--count", type=int, default=152 * 64, help="polynomials for --micro ntt")
+    ap.add_argument("--serve-rate", type=float, default=1500.0,
+                    help="offered queries/s of the serving measurement (0 = skip)")
+    ap.add_argument("--serve-seconds", type=float, default=1.5)
+    ap.add_argument("--serve", action="store_true",
+                    help="serving benchmark alone: three resident databases (4096, 262,144 and "
+                         "2,097,152 plaintexts), 512 clients under a key budget, Poisson arrivals")
+    ap.add_argument("--serve-clients", type=int, default=512)
     return ap.parse_args()
 
 
@@ -90,6 +97,112 @@ def make_inputs(params, count, seed=1):
         clients.append((gk, gsw))
     queries = rng.integers(0, q, size=(count, 2, N), dtype=np.uint64)
     return clients, queries
+
+
+def make_clients(params, count, height, rng):
+    """`count` clients' seeded uniform Galois keys of `height` levels and RGSW keys."""
+    q, p = params.coeff_modulus[0], params.coeff_modulus[-1]
+    out = []
+    for _ in range(count):
+        gk = np.empty((height, 2, 2, N), np.uint64)
+        gk[:, :, 0, :] = rng.integers(0, q, size=(height, 2, N), dtype=np.uint64)
+        gk[:, :, 1, :] = rng.integers(0, p, size=(height, 2, N), dtype=np.uint64)
+        gsw = rng.integers(0, q, size=(2 * params.get_l_key(), 2, N), dtype=np.uint64)
+        out.append((gk, gsw))
+    return out
+
+
+def serve_leg(server, dbs, queries, nclients, rate, seconds, seed=7, max_batch=32, lanes=2,
+              max_wait_us=2000, check=8):
+    """Continuous batching under seeded Poisson arrivals: `rate` queries/s for
+    `seconds`, uniform choice of database, client and query.  Returns the
+    server's counters and latency percentiles, the arrival count, and whether
+    the first `check` responses equal the synchronous path's bit for bit."""
+    rng = np.random.default_rng(seed)
+    n = max(1, int(rate * seconds))
+    gaps = rng.exponential(1.0 / rate, size=n)
+    pick_db = rng.integers(0, len(dbs), size=n)
+    pick_q = rng.integers(0, queries.shape[0], size=n)
+    pick_c = rng.integers(0, nclients, size=n)
+    server.serve_start(max_batch=max_batch, lanes=lanes, max_wait_us=max_wait_us)
+    tickets = []
+    t = time.perf_counter()
+    for j in range(n):
+        t += gaps[j]
+        while True:
+            d = t - time.perf_counter()
+            if d <= 0:
+                break
+            if d > 6e-4:
+                time.sleep(d - 4e-4)
+        tickets.append(server.submit(int(pick_c[j]), queries[pick_q[j]], db_id=dbs[pick_db[j]]))
+    kept = {}
+    for j, tk in enumerate(tickets):
+        r = server.wait(tk, 600000)
+        if j < check:
+            kept[j] = r
+    stats = server.serve_stats()
+    server.serve_stop()
+    same = all(np.array_equal(kept[j], server.make_query(int(pick_c[j]), queries[pick_q[j]],
+                                                         db_id=dbs[pick_db[j]]))
+               for j in kept)
+    return stats, n, same
+
+
+def serve_main(args):
+    """Serving benchmark: three resident databases, 512 clients, Poisson arrivals."""
+    import torch
+    from onionpirv2_gb300 import PirParams, PirServer
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    names = ["db4096", "db262144", "db2097152"]
+    params = [PirParams.preset(w) for w in names]
+    server = PirServer(params[1], device=local)
+    t0 = time.perf_counter()
+    server.gen_data(DB_SEED)
+    dbs = [server.add_database(params[0], seed=DB_SEED + 1), server.db_id,
+           server.add_database(params[2], seed=DB_SEED + 2)]
+    ingest_s = time.perf_counter() - t0
+    height = max(p.get_expan_height() for p in params)
+    per = server.key_bytes_per_client()
+    slots = max(2, args.serve_clients // 2)
+    server.set_key_budget(slots * per)  # half the clients' keys fit: LRU admission
+    rng = np.random.default_rng(3)
+    for cid, (gk, gsw) in enumerate(make_clients(params[1], args.serve_clients, height, rng)):
+        server.set_client_galois_key(cid, gk)
+        server.set_client_gsw_key(cid, gsw)
+    queries = rng.integers(0, params[1].coeff_modulus[0], size=(256, 2, N), dtype=np.uint64)
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.5)
+    # warm-up: limb planes, workspaces and first-touch costs
+    serve_leg(server, dbs, queries, args.serve_clients, 200.0, 0.2, seed=1, check=0)
+    t1 = time.time()
+    stats, n, same = serve_leg(server, dbs, queries, args.serve_clients, args.serve_rate,
+                               args.serve_seconds, seed=11)
+    t2 = time.time()
+    clocks.stop()
+    resident, nslots = server.resident_clients()
+    line = {
+        "metric": "server queries/s under Poisson arrivals (continuous batching, 3 resident DBs)",
+        "value": stats["queries_per_s"], "unit": "queries/s", "n_gpus": 1,
+        "steps": n, "warmup": 40, "ms_per_step": 1e3 / max(stats["queries_per_s"], 1e-9),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+        "data": "synthetic",
+        "config": {"workload": "serving: db4096 + db262144 + db2097152 resident",
+                   "clients": args.serve_clients, "key_slots": nslots,
+                   "offered_qps": args.serve_rate, "seconds": args.serve_seconds,
+                   "arrivals": "seeded Poisson, uniform database, client and query",
+                   "max_batch": 32, "lanes": 2, "max_wait_us": 2000},
+        "p50_ms": stats["p50_ms"], "p99_ms": stats["p99_ms"], "mean_ms": stats["mean_ms"],
+        "max_ms": stats["max_ms"], "completed": stats["completed"], "failed": stats["failed"],
+        "batches": stats["batches"], "mean_batch": stats["mean_batch"],
+        "resident_clients": resident, "bit_exact_sample": same, "ingest_s": ingest_s,
+        "clocks": clocks.summary(t1, t2),
+    }
+    print(json.dumps(line), flush=True)
+    server.close()
+    return 0
 
 
 class ClockSampler:
@@ -279,6 +392,8 @@ def main():
         return run_reference(args)
     if args.micro == "ntt":
         return run_micro_ntt(args)
+    if args.serve:
+        return serve_main(args)
     rank, world, local = dist_env()
     import torch
     if not torch.cuda.is_available():
@@ -424,6 +539,20 @@ def main():
         batched = dict(tensor, batch=B, engine="tensor (tcgen05, 8-bit limbs in bf16, exact)",
                        speedup_vs_single=tensor["value"] / qps,
                        imad=dict(imad, engine="integer multiply-add GEMM"))
+    # ---- serving: continuous batching under Poisson arrivals over this
+    # database and a small second one (the full three-database run: --serve)
+    serving = None
+    if args.serve_rate > 0 and world == 1:
+        from onionpirv2_gb300 import PirParams as _PP
+        small = server.add_database(_PP.preset("db4096"), seed=DB_SEED + 1)
+        sstats, sn, ssame = serve_leg(server, [server.db_id, small], queries, NUM_CLIENTS,
+                                      args.serve_rate, args.serve_seconds)
+        serving = {"databases": [args.workload, "db4096"], "offered_qps": args.serve_rate,
+                   "arrivals": sn, "queries_per_s": sstats["queries_per_s"],
+                   "p50_ms": sstats["p50_ms"], "p99_ms": sstats["p99_ms"],
+                   "mean_batch": sstats["mean_batch"], "batches": sstats["batches"],
+                   "failed": sstats["failed"], "bit_exact_sample": ssame,
+                   "policy": "max_batch 32, 2 lanes, max_wait 2 ms"}
     clocks.stop()
     e2e_qps = e2e_steps * world / (e2e_ms / 1e3)
 
@@ -454,6 +583,7 @@ def main():
         "clocks": clocks.summary(t0, t1),
         "ingest_s": ingest_s,
         "batched": batched,
+        "serving": serving,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cb, match = cpu_baseline(params, args.workload, clients, queries, gpu_resps,
