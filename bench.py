@@ -262,9 +262,9 @@ class ClockSampler:
                 "sm_max_mhz": num(sel[0][1]), "reasons": reasons, "samples": len(sel)}
 
 
-def read_traffic(workload):
-    """DRAM bytes per scan launch from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", f"scan_kernel_{workload}.md")
+def read_traffic(workload, kernel="scan_kernel"):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
     try:
         with open(path) as f:
             for line in f:
@@ -275,13 +275,15 @@ def read_traffic(workload):
     return None
 
 
-def measured_peak():
+def measured_peak(key="hbm_gbs"):
+    """Measured peak (HBM GB/s, or bf16 TFLOP/s) of this GPU pool."""
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    fallback = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}
     try:
         with open(path) as f:
-            return float(json.load(f)["hbm_gbs"]), "measured"
+            return float(json.load(f)[key]), "measured"
     except (OSError, KeyError, ValueError):
-        return 6800.0, "fallback"
+        return fallback[key], "fallback"
 
 
 def cpu_baseline(params, workload, clients, queries, gpu_resps, nq):
@@ -536,8 +538,21 @@ def main():
         single_resps = dresp[:B].cpu().numpy().view(np.uint64).reshape(B, -1).copy()
         tensor = run_batched("tensor")
         imad = run_batched("imad")
+        # tensor-core kernel roofline: algorithmic bf16 flops of the limb GEMM
+        # (64 limb products per 60x60-bit MAC) / its launch time (stage events)
+        n1, nrest = params.get_fst_dim_sz(), params.get_other_dim_sz()
+        flops = 2.0 * 64 * nrest * 2 * B * n1 * N
+        tms = tensor["stages_ms"]["scan_kernel"]
+        tpeak, tkind = measured_peak("bf16_tflops_sustained")
+        tach = flops / (tms / 1e3) / 1e12
         batched = dict(tensor, batch=B, engine="tensor (tcgen05, 8-bit limbs in bf16, exact)",
                        speedup_vs_single=tensor["value"] / qps,
+                       roofline={"bound": "tensor", "achieved": tach, "peak": tpeak,
+                                 "unit": "TFLOP/s", "frac": tach / tpeak,
+                                 "traffic": read_traffic(f"{args.workload}_b{B}", "tc_scan_kernel"),
+                                 "kernel": "tc_scan_kernel (first dimension of the batch)",
+                                 "flops_per_step": flops,
+                                 "peak_source": f"{tkind} bf16_tflops_sustained"},
                        imad=dict(imad, engine="integer multiply-add GEMM"))
     # ---- serving: continuous batching under Poisson arrivals over this
     # database and a small second one (the full three-database run: --serve)

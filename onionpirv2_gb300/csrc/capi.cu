@@ -495,11 +495,13 @@ int run_pipeline(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
     CK(W.ql.alloc(tc_query_limb_bytes((int)n1, batch)), "alloc query limbs");
     launch_query_prep_plane(leaves, leaves_stride, W.qs.as<uint64_t>(), (int)n1, batch,
                             ctx->Mq.tab, s);
+    launch_tc_query_limbs(W.qs.as<uint64_t>(), W.ql.as<uint16_t>(), (int)n1, batch, s);
+    ctx->launches += (batch + 31) / 32;
     record(ctx, E, 6);
-    ctx->launches += launch_tc_scan_batched(
-        db.dbl.as<uint16_t>(), W.qs.as<uint64_t>(), W.ql.as<uint16_t>(), W.res.as<uint64_t>(),
-        res_stride, (int)n1, (int)nr, batch, ctx->Mq.tab.q, ctx->Mq.tab.mu_lo, ctx->Mq.tab.mu_hi,
-        ctx->r64, ctx->r128, E.status, s) - 1;
+    ctx->launches += launch_tc_scan(db.dbl.as<uint16_t>(), W.ql.as<uint16_t>(), W.res.as<uint64_t>(),
+                                    res_stride, (int)n1, (int)nr, batch, ctx->Mq.tab.q,
+                                    ctx->Mq.tab.mu_lo, ctx->Mq.tab.mu_hi, ctx->r64, ctx->r128,
+                                    E.status, s) - 1;
   } else if (batched) {
     launch_query_prep_batched(leaves, leaves_stride, W.qs.as<uint4>(), (int)n1, batch,
                               ctx->Mq.tab, s);

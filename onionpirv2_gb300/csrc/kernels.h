@@ -86,18 +86,20 @@ void launch_query_prep_plane(const uint64_t *leaves, size_t leaves_stride, uint6
 // Batched product on the tcgen05 tensor cores (tc_scan.cu): residues split
 // into 8-bit limbs held as bf16, exact fp32 accumulation in tensor memory.
 // The database needs its limb plane dbl (tc_db_limb_bytes, built by
-// launch_db_limbs from dbs); plane is the query operand of
-// launch_query_prep_plane, ql scratch of tc_query_limb_bytes(n1, batch).  Output as
-// launch_scan.  Returns the number of kernels launched.
+// launch_db_limbs from dbs).  launch_tc_query_limbs splits the query plane
+// of launch_query_prep_plane into ql (tc_query_limb_bytes(n1, batch) bytes);
+// launch_tc_scan then writes the output of launch_scan and returns the number
+// of kernels it launched.
 bool tc_scan_supported(int n1, int n_rest);
 size_t tc_db_limb_bytes(int n1, int n_rest);
 size_t tc_query_limb_bytes(int n1, int batch);
 cudaError_t init_tc_attributes();
 void launch_db_limbs(const uint64_t *dbs, uint16_t *dbl, int n1, int n_rest, cudaStream_t s);
-int launch_tc_scan_batched(const uint16_t *dbl, const uint64_t *plane, uint16_t *ql, uint64_t *out,
-                           size_t out_stride, int n1, int n_rest, int batch, uint64_t q,
-                           uint64_t mu_lo, uint64_t mu_hi, uint64_t r64, uint64_t r128,
-                           uint32_t *status, cudaStream_t s);
+void launch_tc_query_limbs(const uint64_t *plane, uint16_t *ql, int n1, int batch,
+                           cudaStream_t s);
+int launch_tc_scan(const uint16_t *dbl, const uint16_t *ql, uint64_t *out, size_t out_stride,
+                   int n1, int n_rest, int batch, uint64_t q, uint64_t mu_lo, uint64_t mu_hi,
+                   uint64_t r64, uint64_t r128, uint32_t *status, cudaStream_t s);
 
 // ---- one folding level (other_dim_mux): res[b][j] += INTT(RGSW x (res[j+half]-res[j]))
 void launch_fold(uint64_t *res, size_t res_stride, const uint64_t *gsw, size_t gsw_stride,

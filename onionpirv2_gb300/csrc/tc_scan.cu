@@ -428,10 +428,38 @@ bool tc_scan_supported(int n1, int n_rest) {
 }
 
 size_t tc_db_limb_bytes(int n1, int n_rest) { return (size_t)kN * n1 * n_rest * 16; }
-size_t tc_query_limb_bytes(int n1, int batch) {
-  const int pb = batch < kTcMaxNB / 2 ? batch : kTcMaxNB / 2;  // queries of the largest pass
+namespace {
+// Geometry of the pass of `pb` queries starting at query b0.
+TcGeom pass_geom(int n1, int n_rest, int pb) {
+  // 8 query polynomials per epilogue group; two 32-polynomial halves above 16 queries
   const int padded = pb > kTcHalfNB / 2 ? kTcMaxNB / 2 : (pb + 3) / 4 * 4;
-  return (size_t)kN * n1 * 2 * padded * 16;
+  TcGeom G;
+  G.n1 = n1;
+  G.n_rest = n_rest;
+  G.batch = pb;
+  G.nh = padded > kTcHalfNB / 2 ? 2 : 1;
+  G.nbh = 2 * padded / G.nh;
+  G.n_rb = n_rest / kTcRows;
+  G.units = (long long)kN * G.n_rb * G.nh;
+  G.b_bytes = (uint32_t)(kTcKB * G.nbh * 128);
+  G.idesc = make_idesc(G.nbh * 8);
+  G.k0 = 0;
+  G.nkc = 0;
+  G.accumulate = 0;
+  return G;
+}
+// query limbs of one pass (elements); passes follow each other in ql
+size_t pass_limb_elems(int n1, int pb) {
+  const TcGeom G = pass_geom(n1, kTcRows, pb);
+  return (size_t)kN * G.nh * (n1 / 8) * G.nbh * 64;
+}
+}  // namespace
+
+size_t tc_query_limb_bytes(int n1, int batch) {
+  size_t e = 0;
+  for (int b0 = 0; b0 < batch; b0 += kTcMaxNB / 2)
+    e += pass_limb_elems(n1, batch - b0 < kTcMaxNB / 2 ? batch - b0 : kTcMaxNB / 2);
+  return e * sizeof(uint16_t);
 }
 
 cudaError_t init_tc_attributes() {
@@ -448,42 +476,40 @@ void launch_db_limbs(const uint64_t *dbs, uint16_t *dbl, int n1, int n_rest, cud
   db_limb_kernel<<<(unsigned)(blocks < 65536 ? blocks : 65536), 256, 0, s>>>(dbs, dbl, n1, n_rest);
 }
 
-int launch_tc_scan_batched(const uint16_t *dbl, const uint64_t *plane, uint16_t *ql, uint64_t *out,
-                           size_t out_stride, int n1, int n_rest, int batch, uint64_t q,
-                           uint64_t mu_lo, uint64_t mu_hi, uint64_t r64, uint64_t r128,
-                           uint32_t *status, cudaStream_t s) {
-  int launches = 0;
+void launch_tc_query_limbs(const uint64_t *plane, uint16_t *ql, int n1, int batch,
+                           cudaStream_t s) {
+  size_t off = 0;
   for (int b0 = 0; b0 < batch; b0 += kTcMaxNB / 2) {
     const int pb = batch - b0 < kTcMaxNB / 2 ? batch - b0 : kTcMaxNB / 2;
-    // 8 query polynomials per epilogue group; two 32-polynomial halves
-    // above 16 queries
-    const int padded = pb > kTcHalfNB / 2 ? kTcMaxNB / 2 : (pb + 3) / 4 * 4;
-    TcGeom G;
-    G.n1 = n1;
-    G.n_rest = n_rest;
-    G.batch = pb;
-    G.nh = padded > kTcHalfNB / 2 ? 2 : 1;
-    G.nbh = 2 * padded / G.nh;
-    G.n_rb = n_rest / kTcRows;
-    G.units = (long long)kN * G.n_rb * G.nh;
-    G.b_bytes = (uint32_t)(kTcKB * G.nbh * 128);
-    G.idesc = make_idesc(G.nbh * 8);
+    const TcGeom G = pass_geom(n1, kTcRows, pb);
     const long long qtotal = (long long)kN * G.nh * (n1 / 8) * G.nbh;
     const long long qblocks = (qtotal + 255) / 256;
     query_limb_kernel<<<(unsigned)(qblocks < 65536 ? qblocks : 65536), 256, 0, s>>>(
-        plane, ql, n1, b0, G.nh, G.nbh, pb);
+        plane, ql + off, n1, b0, G.nh, G.nbh, pb);
+    off += pass_limb_elems(n1, pb);
+  }
+}
+
+int launch_tc_scan(const uint16_t *dbl, const uint16_t *ql, uint64_t *out, size_t out_stride,
+                   int n1, int n_rest, int batch, uint64_t q, uint64_t mu_lo, uint64_t mu_hi,
+                   uint64_t r64, uint64_t r128, uint32_t *status, cudaStream_t s) {
+  int launches = 0;
+  size_t off = 0;
+  for (int b0 = 0; b0 < batch; b0 += kTcMaxNB / 2) {
+    const int pb = batch - b0 < kTcMaxNB / 2 ? batch - b0 : kTcMaxNB / 2;
+    TcGeom G = pass_geom(n1, n_rest, pb);
     const int sms = g_tc_sms > 0 ? g_tc_sms : 152;
     const long long grid = G.units < sms ? G.units : sms;
-    launches++;
     for (int k0 = 0; k0 < n1; k0 += kTcMaxSegment) {
       const int klen = n1 - k0 < kTcMaxSegment ? n1 - k0 : kTcMaxSegment;
       G.k0 = k0;
       G.nkc = klen / kTcKC;
       G.accumulate = k0 > 0;
-      tc_scan_kernel<<<(unsigned)grid, kTcThreads, kTcSmem, s>>>(dbl, ql, out, out_stride, b0, G,
-                                                                q, mu_lo, mu_hi, r64, r128, status);
+      tc_scan_kernel<<<(unsigned)grid, kTcThreads, kTcSmem, s>>>(
+          dbl, ql + off, out, out_stride, b0, G, q, mu_lo, mu_hi, r64, r128, status);
       launches++;
     }
+    off += pass_limb_elems(n1, pb);
   }
   return launches;
 }

@@ -490,10 +490,11 @@ __global__ void __cluster_dims__(kQtgCluster, 1, 1) __launch_bounds__(T)
 }
 
 // Cluster form below these many ciphertexts per launch (batch included);
-// one-CTA form at or above.  From per-launch timings on GB300: the cluster
-// expansion wins at every level of a single query, the cluster fold only on
-// the narrow levels (<= 32 pairs), RGSW reconstruction is even.
-int g_expand_threshold = 1024;
+// one-CTA form at or above.  From per-launch timings on GB300 (the one-CTA
+// forms at two CTAs per SM): the cluster expansion wins below ~128 nodes
+// (128 and 256 measured alike, 1024 and 64 slower), the cluster fold on the
+// narrow levels (< 48 pairs), RGSW reconstruction is even.
+int g_expand_threshold = 128;
 int g_fold_threshold = 48;
 int g_qtg_threshold = 40;
 
@@ -527,11 +528,14 @@ cudaError_t init_kernel_attributes() {
                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)kClusterSmem)) != cudaSuccess)
     return e;
-  g_expand_threshold = 1024;
+  g_expand_threshold = 128;
   g_fold_threshold = 48;
   g_qtg_threshold = 40;
   if (const char *v = getenv("OPIR_CLUSTER_THRESHOLD"))  // one threshold for all (tests, sweeps)
     g_expand_threshold = g_fold_threshold = g_qtg_threshold = atoi(v);
+  if (const char *v = getenv("OPIR_EXPAND_THRESHOLD")) g_expand_threshold = atoi(v);
+  if (const char *v = getenv("OPIR_FOLD_THRESHOLD")) g_fold_threshold = atoi(v);
+  if (const char *v = getenv("OPIR_QTG_THRESHOLD")) g_qtg_threshold = atoi(v);
   return cudaSuccess;
 }
 
