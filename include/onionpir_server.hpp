@@ -106,6 +106,52 @@ class PirServer {
     return last_packed_.size();
   }
 
+  // Many queries at once, one pass over the database; each response equals
+  // make_query's for the same query.
+  std::vector<Ciphertext> make_query_batch(const std::vector<size_t> &client_ids,
+                                           const std::vector<Ciphertext> &queries) {
+    if (client_ids.size() != queries.size() || queries.empty())
+      throw std::invalid_argument("one client id per query");
+    const size_t ct = 2 * (size_t)params_.poly_degree;
+    std::vector<uint64_t> ids(client_ids.begin(), client_ids.end()), in(queries.size() * ct),
+        out(queries.size() * ct);
+    for (size_t i = 0; i < queries.size(); ++i) {
+      if (queries[i].size() != ct) throw std::invalid_argument("query must be one ciphertext");
+      std::copy(queries[i].begin(), queries[i].end(), in.begin() + i * ct);
+    }
+    check(opir_make_query_batch(ctx_, db_, (uint32_t)ids.size(), ids.data(), in.data(), out.data(),
+                                nullptr));
+    std::vector<Ciphertext> resps(queries.size());
+    for (size_t i = 0; i < queries.size(); ++i)
+      resps[i].assign(out.begin() + i * ct, out.begin() + (i + 1) * ct);
+    return resps;
+  }
+
+  // Serving: continuous batching on a worker thread (opir_serve_* in
+  // onionpir_gpu.h).  submit() may be called from any thread.
+  void serve_start(uint32_t max_batch = 32, uint32_t lanes = 2, uint32_t max_wait_us = 2000) {
+    opir_serve_config cfg{max_batch, lanes, max_wait_us};
+    check(opir_serve_start(ctx_, &cfg));
+  }
+  void serve_stop() { check(opir_serve_stop(ctx_)); }
+  uint64_t submit(size_t client_id, const Ciphertext &query) {
+    if (query.size() != 2 * (size_t)params_.poly_degree)
+      throw std::invalid_argument("query must be one ciphertext");
+    uint64_t ticket = 0;
+    check(opir_submit(ctx_, db_, client_id, query.data(), &ticket));
+    return ticket;
+  }
+  Ciphertext wait(uint64_t ticket, uint32_t timeout_ms = 60000) {
+    Ciphertext resp(2 * (size_t)params_.poly_degree);
+    check(opir_wait(ctx_, ticket, timeout_ms, resp.data(), nullptr));
+    return resp;
+  }
+  opir_serve_stats serve_stats() {
+    opir_serve_stats st{};
+    check(opir_serve_stats_get(ctx_, &st));
+    return st;
+  }
+
   opir_ctx *ctx() const { return ctx_; }
   uint32_t db_id() const { return db_; }
 

@@ -45,6 +45,8 @@ int main() {
   std::vector<uint64_t> query(2 * N), ref(2 * N), ct(2 * N), plain(N);
   std::vector<uint8_t> ref_packed(orc_response_bytes(o)), entry(P.entry_size),
       expect(P.entry_size);
+  std::vector<size_t> all_clients;
+  std::vector<onionpir::Ciphertext> all_queries, all_resps;
   for (size_t i = 0; i < iters; ++i) {
     const uint64_t client = 1000 + i, idx = (i * 2654435761ULL + 17) % P.num_entries;
     orc_keygen(o, 77 + i, sk.data());
@@ -54,6 +56,9 @@ int main() {
     server.set_client_gsw_key(client, gsw);
     orc_make_query(o, sk.data(), 377 + i, idx, query.data());
     const onionpir::Ciphertext resp = server.make_query(client, query);
+    all_clients.push_back(client);
+    all_queries.push_back(query);
+    all_resps.push_back(resp);
     std::stringstream stream;
     const size_t n = server.save_resp_to_stream(resp, stream);
     const std::string bytes = stream.str();
@@ -79,8 +84,23 @@ int main() {
   } catch (const std::out_of_range &) {
     threw = true;
   }
+  // the same queries as one batch, and through the serving loop
+  const std::vector<onionpir::Ciphertext> batch = server.make_query_batch(all_clients, all_queries);
+  int batch_same = 0, served_same = 0;
+  for (size_t i = 0; i < iters; ++i) batch_same += batch[i] == all_resps[i];
+  server.serve_start(4, 2, 500);
+  std::vector<uint64_t> tickets;
+  for (size_t i = 0; i < iters; ++i) tickets.push_back(server.submit(all_clients[i], all_queries[i]));
+  for (size_t i = 0; i < iters; ++i) served_same += server.wait(tickets[i]) == all_resps[i];
+  const opir_serve_stats st = server.serve_stats();
+  server.serve_stop();
   std::printf("Success rate: %d/%zu, bit-identical: %d/%zu, unknown client -> out_of_range: %s\n",
               success, iters, identical, iters, threw ? "yes" : "no");
+  std::printf("batch == single: %d/%zu, served == single: %d/%zu (%llu batches, p50 %.2f ms)\n",
+              batch_same, iters, served_same, iters, (unsigned long long)st.batches, st.p50_ms);
   orc_destroy(o);
-  return (success == (int)iters && identical == (int)iters && threw) ? 0 : 1;
+  return (success == (int)iters && identical == (int)iters && threw &&
+          batch_same == (int)iters && served_same == (int)iters)
+             ? 0
+             : 1;
 }

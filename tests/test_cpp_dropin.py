@@ -26,3 +26,4 @@ def test_cpp_pir_server_round_trip(oracle_lib, gpu_lib):
     print(r.stdout)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "Success rate: 13/13, bit-identical: 13/13" in r.stdout
+    assert "batch == single: 13/13, served == single: 13/13" in r.stdout
