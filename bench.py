@@ -76,6 +76,18 @@ def parse():
     return ap.parse_args()
 
 
+def aggregate_replicas(ms, steps, world, dist=None, device="cpu"):
+    """Whole-job throughput of `world` replicas (one per GPU, no data-path
+    collective): every rank's timed region is reduced to the slowest rank's,
+    and the queries of all ranks count.  Returns (max ms, queries/s)."""
+    if dist is not None and world > 1:
+        import torch
+        t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, steps * world / (ms / 1e3)
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -455,13 +467,7 @@ def main():
         t1 = time.time()
         torch.cuda.synchronize()
     launches = server.launch_count() - l0
-    ms = ev0.elapsed_time(ev1)
-    if pg:
-        import torch.distributed as dist
-        tt = torch.tensor([ms], device=f"cuda:{local}")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
-    qps = args.steps * world / (ms / 1e3)
+    ms, qps = aggregate_replicas(ev0.elapsed_time(ev1), args.steps, world, pg, f"cuda:{local}")
     gpu_resps = dresp[: args.cpu_queries].cpu().numpy().view(np.uint64)
 
     # ---- roofline pass: per-stage CUDA events inside the library
