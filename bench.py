@@ -73,6 +73,9 @@ def parse():
                     help="serving benchmark alone: three resident databases (4096, 262,144 and "
                          "2,097,152 plaintexts), 512 clients under a key budget, Poisson arrivals")
     ap.add_argument("--serve-clients", type=int, default=512)
+    ap.add_argument("--batch-sweep", default=None,
+                    help="comma-separated batch sizes: queries/s of every first-dimension "
+                         "engine at each size (one JSON line per size)")
     return ap.parse_args()
 
 
@@ -159,6 +162,56 @@ def serve_leg(server, dbs, queries, nclients, rate, seconds, seed=7, max_batch=3
                                                          db_id=dbs[pick_db[j]]))
                for j in kept)
     return stats, n, same
+
+
+def sweep_main(args):
+    """Queries/s of the scan, integer-GEMM and tensor-core engines per batch size."""
+    import torch
+    from onionpirv2_gb300 import PirParams, PirServer
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    params = PirParams.preset(args.workload)
+    server = PirServer(params, device=local)
+    stream = torch.cuda.Stream(device=local)
+    server.set_stream(stream.cuda_stream)
+    server.gen_data(DB_SEED)
+    sizes = [int(x) for x in args.batch_sweep.split(",")]
+    clients, queries = make_inputs(params, max(sizes) * 4)
+    for cid, (gk, gsw) in enumerate(clients):
+        server.set_client_galois_key(cid, gk)
+        server.set_client_gsw_key(cid, gsw)
+    dq = torch.from_numpy(queries.view(np.int64)).to(f"cuda:{local}")
+    nq = queries.shape[0]
+    dresp = torch.empty((nq, 2, N), dtype=torch.int64, device=f"cuda:{local}")
+    dpack = torch.empty((nq, server.resp_bytes), dtype=torch.uint8, device=f"cuda:{local}")
+    qbytes = 2 * N * 8
+    for B in sizes:
+        line = {"workload": args.workload, "batch": B, "unit": "queries/s"}
+        for engine in ("scan", "imad", "tensor"):
+            server.set_batch_engine(engine)
+
+            def bstep(i):
+                off = (i % 4) * B
+                ids = [(off + j) % NUM_CLIENTS for j in range(B)]
+                server.make_query_device(ids, dq.data_ptr() + off * qbytes,
+                                         dresp.data_ptr() + off * qbytes,
+                                         dpack.data_ptr() + off * server.resp_bytes)
+
+            with torch.cuda.stream(stream):
+                for i in range(3):
+                    bstep(i)
+                stream.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                steps = max(3, min(20, 256 // B))
+                e0.record(stream)
+                for i in range(steps):
+                    bstep(i)
+                e1.record(stream)
+                e1.synchronize()
+            line[engine] = B * steps / (e0.elapsed_time(e1) / 1e3)
+        print(json.dumps(line), flush=True)
+    server.close()
+    return 0
 
 
 def serve_main(args):
@@ -408,6 +461,8 @@ def main():
         return run_micro_ntt(args)
     if args.serve:
         return serve_main(args)
+    if args.batch_sweep:
+        return sweep_main(args)
     rank, world, local = dist_env()
     import torch
     if not torch.cuda.is_available():

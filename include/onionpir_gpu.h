@@ -148,12 +148,15 @@ int opir_first_dim_noalloc(opir_ctx *ctx, uint32_t db_id, const uint64_t *d_fst_
                            uint64_t *d_out);
 
 /* ---- first-dimension engine for batches (no reference counterpart) ----
- * A batch of queries on one database shares one pass over it: the product
- * becomes a per-slot (n_rest x n1) . (n1 x 2B) GEMM.  AUTO: the tcgen05
- * tensor-core engine (residues split into 8-bit limbs, exact) from
- * tensor_min_batch queries on when the shape allows it, the integer
- * multiply-add GEMM otherwise; SCAN: one streaming pass per query; IMAD /
- * TENSOR: that engine whenever the shape allows it.  All give the same bits. */
+ * A batch of queries on one database can share one pass over it: the
+ * product becomes a per-slot (n_rest x n1) . (n1 x 2B) GEMM.  AUTO (default):
+ * the tcgen05 tensor-core engine (residues split into 8-bit limbs, exact)
+ * from tensor_min_batch queries on (default 4; 0 keeps the current value)
+ * when the shape allows it (n1 a multiple of 32, n_rest of 16), else the
+ * integer multiply-add GEMM from 32 queries on, else one streaming pass per
+ * query -- the crossovers measured on GB300.  SCAN: one pass per query; IMAD /
+ * TENSOR: that engine for every batch of 2 or more the shape allows.  All
+ * give the same bits. */
 enum {
   OPIR_ENGINE_AUTO = 0,
   OPIR_ENGINE_SCAN = 1,

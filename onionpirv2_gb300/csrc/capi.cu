@@ -261,11 +261,13 @@ struct opir_ctx {
   std::map<uint64_t, std::unique_ptr<Client>> clients;
   Workspace ws;
   DevBuf status;  // device status word: bounded-wait timeouts (async.cuh)
-  bool batch_scan = true;  // batched GEMM for batches >= 2 (OPIR_BATCH_SCAN=0 turns it off)
-  // batched GEMM engine: 0 = integer multiply-add kernel, 1 = tensor cores
-  // from tc_min_batch queries on (OPIR_TC, OPIR_TC_MIN_BATCH)
-  int tc_mode = 1;
-  int tc_min_batch = 2;
+  // first-dimension engine of batches (opir_set_batch_engine): AUTO takes the
+  // tensor cores from tc_min_batch queries on, else the integer GEMM from
+  // imad_min_batch (shapes the tensor engine does not take), else one scan
+  // per query -- the crossovers measured on GB300 (bench.py --batch-sweep)
+  int engine = OPIR_ENGINE_AUTO;
+  int tc_min_batch = 4;
+  int imad_min_batch = 32;
   uint64_t r64 = 0, r128 = 0;  // 2^64 and 2^128 mod q
   // key budget: client keys in a pool of fixed slots, least recently used out
   uint64_t key_budget = 0;
@@ -365,6 +367,24 @@ void record(opir_ctx *ctx, const PipeEnv &E, int i) {
 }
 
 bool serving_active(const opir_ctx *ctx) { return ctx->serving && ctx->serving->active; }
+
+// The first-dimension engine of a batch (OPIR_ENGINE_SCAN/IMAD/TENSOR).
+int engine_for(const opir_ctx *ctx, int batch, int n1, int nr) {
+  const bool tc_ok = tc_scan_supported(n1, nr), imad_ok = nr % 32 == 0 && n1 % 16 == 0;
+  if (batch < 2) return OPIR_ENGINE_SCAN;
+  switch (ctx->engine) {
+    case OPIR_ENGINE_TENSOR:
+      return tc_ok ? OPIR_ENGINE_TENSOR : imad_ok ? OPIR_ENGINE_IMAD : OPIR_ENGINE_SCAN;
+    case OPIR_ENGINE_IMAD:
+      return imad_ok ? OPIR_ENGINE_IMAD : OPIR_ENGINE_SCAN;
+    case OPIR_ENGINE_SCAN:
+      return OPIR_ENGINE_SCAN;
+    default:
+      if (tc_ok && batch >= ctx->tc_min_batch) return OPIR_ENGINE_TENSOR;
+      if (imad_ok && batch >= ctx->imad_min_batch) return OPIR_ENGINE_IMAD;
+      return OPIR_ENGINE_SCAN;
+  }
+}
 
 // Device key pointers of a client for a query on stream s.  With a key
 // budget the client is made resident first (its keys copied into a pool
@@ -480,9 +500,8 @@ int run_pipeline(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
   const size_t res_stride = nr * CTW;
   // a batch of queries shares one pass over the database (batched GEMM);
   // a single query (or an unsupported shape) streams it once per query
-  const bool batched = batch >= 2 && ctx->batch_scan && nr % 32 == 0 && n1 % 16 == 0;
-  const bool tensor = batch >= 2 && ctx->batch_scan && ctx->tc_mode == 1 &&
-                      batch >= ctx->tc_min_batch && tc_scan_supported((int)n1, (int)nr);
+  const int use = engine_for(ctx, batch, (int)n1, (int)nr);
+  const bool tensor = use == OPIR_ENGINE_TENSOR, batched = use == OPIR_ENGINE_IMAD;
   if (tensor) {
     if (!db.dbl_valid) {
       CK(db.dbl.alloc(tc_db_limb_bytes((int)n1, (int)nr)), "alloc database limb plane");
@@ -646,8 +665,10 @@ int opir_ctx_create(const opir_params *P, int device, opir_ctx **out) {
   if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess)
     return OPIR_ERR_CUDA;
   c->stream = c->own_stream;
-  if (const char *v = getenv("OPIR_BATCH_SCAN")) c->batch_scan = atoi(v) != 0;
-  if (const char *v = getenv("OPIR_TC")) c->tc_mode = atoi(v) != 0;
+  // test and sweep overrides of the engine choice
+  if (const char *v = getenv("OPIR_TC")) c->engine = atoi(v) ? OPIR_ENGINE_TENSOR : OPIR_ENGINE_IMAD;
+  if (const char *v = getenv("OPIR_BATCH_SCAN"))
+    if (!atoi(v)) c->engine = OPIR_ENGINE_SCAN;
   if (const char *v = getenv("OPIR_TC_MIN_BATCH")) c->tc_min_batch = atoi(v);
   c->slot_words = (size_t)kLogN * 4 * kN + 2 * (size_t)P->gsw_l_key * 2 * kN;
   c->r64 = (uint64_t)(((u128)1 << 64) % q);
@@ -1004,9 +1025,8 @@ int opir_set_batch_engine(opir_ctx *ctx, int engine, uint32_t tensor_min_batch) 
   if (!ctx || engine < OPIR_ENGINE_AUTO || engine > OPIR_ENGINE_TENSOR) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
   if (serving_active(ctx)) return ctx->fail(OPIR_ERR_STATE, "serving is active");
-  ctx->batch_scan = engine != OPIR_ENGINE_SCAN;
-  ctx->tc_mode = (engine == OPIR_ENGINE_AUTO || engine == OPIR_ENGINE_TENSOR) ? 1 : 0;
-  ctx->tc_min_batch = engine == OPIR_ENGINE_TENSOR ? 2 : (tensor_min_batch ? (int)tensor_min_batch : 2);
+  ctx->engine = engine;
+  if (tensor_min_batch) ctx->tc_min_batch = (int)tensor_min_batch;
   return OPIR_OK;
 }
 
@@ -1289,7 +1309,7 @@ int presize_lane(opir_ctx *ctx, Lane &L, int max_batch) {
     int rc = ensure_workspace(ctx, db, max_batch, W);
     if (rc) return rc;
     const int n1 = (int)db.shape.fst_dim_sz, nr = (int)db.shape.other_dim_sz;
-    if (max_batch >= 2 && ctx->batch_scan && ctx->tc_mode == 1 && tc_scan_supported(n1, nr)) {
+    if (engine_for(ctx, max_batch, n1, nr) == OPIR_ENGINE_TENSOR) {
       CK(W.ql.alloc(tc_query_limb_bytes(n1, max_batch)), "alloc query limbs");
       if (!db.dbl_valid) {
         CK(db.dbl.alloc(tc_db_limb_bytes(n1, nr)), "alloc database limb plane");
