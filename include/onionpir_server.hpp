@@ -127,6 +127,15 @@ class PirServer {
     return resps;
   }
 
+  // First-dimension engine of batches (OPIR_ENGINE_*; tensor_min_batch 0 keeps
+  // the current crossover) and the device-memory budget for client keys
+  // (before the first key is set; 0 = every client resident).
+  void set_batch_engine(int engine, uint32_t tensor_min_batch = 0) {
+    check(opir_set_batch_engine(ctx_, engine, tensor_min_batch));
+  }
+  void set_key_budget(uint64_t bytes) { check(opir_set_key_budget(ctx_, bytes)); }
+  uint64_t key_bytes_per_client() const { return opir_key_bytes_per_client(ctx_); }
+
   // Serving: continuous batching on a worker thread (opir_serve_* in
   // onionpir_gpu.h).  submit() may be called from any thread.
   void serve_start(uint32_t max_batch = 32, uint32_t lanes = 2, uint32_t max_wait_us = 2000) {
