@@ -152,13 +152,13 @@ struct Db {
 };
 
 struct Client {
-  DevBuf galois;  // device copies (no key budget)
+  DevBuf galois;  // device copies (no key budget): keys, then their Shoup companions
   uint32_t levels = 0;
   DevBuf gsw;
   bool has_galois = false, has_gsw = false;
   // key budget: host copies; the device copy lives in a key-pool slot while
   // resident (serve::KeyLru decides which clients are)
-  std::vector<uint64_t> h_galois, h_gsw;  // gsw rows in coefficient form
+  std::vector<uint64_t> h_galois, h_gsw;  // keys + companions; gsw rows in coefficient form
   int inflight = 0;                       // serving batches reading these keys
 };
 
@@ -271,7 +271,7 @@ struct opir_ctx {
   uint64_t r64 = 0, r128 = 0;  // 2^64 and 2^128 mod q
   // key budget: client keys in a pool of fixed slots, least recently used out
   uint64_t key_budget = 0;
-  size_t slot_words = 0;  // galois [kLogN][2][2][N] + RGSW(sk) [2 l_key][2][N]
+  size_t slot_words = 0;  // galois [kLogN][2][2][N] x 2 (keys, companions) + RGSW(sk) [2 l_key][2][N]
   DevBuf key_pool;
   serve::KeyLru lru;
   std::unique_ptr<Serving> serving;
@@ -401,8 +401,10 @@ int resolve_keys(opir_ctx *ctx, uint64_t id, const Db &db, cudaStream_t s, Query
                      (unsigned long long)id, cl.levels, db.h);
   if (db.ndim > 1 && !cl.has_gsw)
     return ctx->fail(OPIR_ERR_UNKNOWN_CLIENT, "no RGSW key for client %llu", (unsigned long long)id);
+  const size_t gwords = (size_t)cl.levels * 4 * kN;
   if (!ctx->key_budget) {
     d->galois = cl.galois.as<uint64_t>();
+    d->galois_s = d->galois + gwords;
     d->gsw_key = cl.gsw.as<uint64_t>();
     return OPIR_OK;
   }
@@ -413,7 +415,7 @@ int resolve_keys(opir_ctx *ctx, uint64_t id, const Db &db, cudaStream_t s, Query
     return ctx->fail(OPIR_ERR_OOM, "key budget: all %d key slots are held by queries in flight",
                      ctx->lru.slots());
   uint64_t *base = ctx->key_pool.as<uint64_t>() + (size_t)slot * ctx->slot_words;
-  uint64_t *gal = base, *gsw = base + (size_t)kLogN * 4 * kN;
+  uint64_t *gal = base, *gsw = base + (size_t)kLogN * 8 * kN;
   if (fresh) {
     // a slot is only reused once no queued work reads it: same-stream order
     // on the synchronous path, pins on the serving lanes
@@ -428,6 +430,7 @@ int resolve_keys(opir_ctx *ctx, uint64_t id, const Db &db, cudaStream_t s, Query
   }
   ctx->lru.pin(id);
   d->galois = gal;
+  d->galois_s = gal + gwords;
   d->gsw_key = gsw;
   return OPIR_OK;
 }
@@ -670,7 +673,7 @@ int opir_ctx_create(const opir_params *P, int device, opir_ctx **out) {
   if (const char *v = getenv("OPIR_BATCH_SCAN"))
     if (!atoi(v)) c->engine = OPIR_ENGINE_SCAN;
   if (const char *v = getenv("OPIR_TC_MIN_BATCH")) c->tc_min_batch = atoi(v);
-  c->slot_words = (size_t)kLogN * 4 * kN + 2 * (size_t)P->gsw_l_key * 2 * kN;
+  c->slot_words = (size_t)kLogN * 8 * kN + 2 * (size_t)P->gsw_l_key * 2 * kN;
   c->r64 = (uint64_t)(((u128)1 << 64) % q);
   c->r128 = mulmod(c->r64, c->r64, q);
   for (auto &e : c->ev)
@@ -853,14 +856,24 @@ int opir_set_galois_key(opir_ctx *ctx, uint64_t client_id, const uint64_t *keys,
     return ctx->fail(OPIR_ERR_STATE, "client %llu has queries in flight",
                      (unsigned long long)client_id);
   const size_t words = (size_t)levels * 4 * kN;
+  // keys (reduced mod their modulus) followed by their Shoup companions
+  // floor(k 2^64 / modulus): the expansion multiplies by them with two
+  // multiplications instead of a 128-bit product and a Barrett reduction
+  std::vector<uint64_t> kc(2 * words);
+  for (size_t w = 0; w < words; w++) {
+    const uint64_t mod = ((w / kN) & 1) ? ctx->Mp.tab.q : ctx->Mq.tab.q;  // [level][kk][q, p][N]
+    kc[w] = keys[w] % mod;
+    kc[words + w] = shoup(kc[w], mod);
+  }
   if (ctx->key_budget) {
     // host copy; copied to a key slot when a query needs it
-    cl->h_galois.assign(keys, keys + words);
+    cl->h_galois.swap(kc);
     ctx->lru.erase(client_id);
   } else {
     CK(cudaStreamSynchronize(ctx->stream), "sync");
-    CK(cl->galois.alloc(words * 8), "alloc Galois keys");
-    CK(cudaMemcpy(cl->galois.p, keys, words * 8, cudaMemcpyHostToDevice), "upload Galois keys");
+    CK(cl->galois.alloc(2 * words * 8), "alloc Galois keys");
+    CK(cudaMemcpy(cl->galois.p, kc.data(), 2 * words * 8, cudaMemcpyHostToDevice),
+       "upload Galois keys");
   }
   cl->levels = levels;
   cl->has_galois = true;

@@ -13,8 +13,9 @@ namespace opir {
 
 // Per-query key pointers.
 struct QueryDesc {
-  const uint64_t *galois;   // [h][2][2][N]   key k, modulus (q, p), NTT form
-  const uint64_t *gsw_key;  // [2 l_key][2][N] RGSW(sk), NTT form
+  const uint64_t *galois;    // [h][2][2][N]   key k, modulus (q, p), NTT form
+  const uint64_t *galois_s;  // the same layout: Shoup companions floor(k 2^64 / modulus)
+  const uint64_t *gsw_key;   // [2 l_key][2][N] RGSW(sk), NTT form
 };
 
 // Key pointers of up to kMaxKeyBatch queries, passed to kernels by value

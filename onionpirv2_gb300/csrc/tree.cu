@@ -70,7 +70,10 @@ __global__ void __launch_bounds__(T, 2) expand_level_kernel(const uint64_t *cur,
   __syncthreads();
 
   const uint64_t *key = kb.q[b].galois + (size_t)level * 4 * kN;
+  const uint64_t *key_s = kb.q[b].galois_s + (size_t)level * 4 * kN;
   // ---- modulus q: s_q[kk] = INTT_q(NTT_q(sigma(c1)) * K[kk] mod q)
+  // (Shoup products with the keys' precomputed companions, in [0, 4q): the
+  // inverse transform takes inputs below 4q)
   {
     uint64_t t[8];
 #pragma unroll
@@ -78,10 +81,11 @@ __global__ void __launch_bounds__(T, 2) expand_level_kernel(const uint64_t *cur,
     ntt_fwd(t, sa, sb, Mq);
 #pragma unroll 1
     for (int kk = 0; kk < 2; ++kk) {
-      uint64_t a[8];
+      uint64_t a[8], as[8];
       ldg_slot8(key + (2 * kk) * kN, a);
+      ldg_slot8(key_s + (2 * kk) * kN, as);
 #pragma unroll
-      for (int e = 0; e < 8; ++e) a[e] = mul_mod(t[e], a[e], Mq);
+      for (int e = 0; e < 8; ++e) a[e] = mul_shoup_lazy4(t[e], a[e], as[e], Mq.q);
       ntt_inv(a, sa, sb, Mq);
 #pragma unroll
       for (int e = 0; e < 8; ++e) s_q[kk * kN + strided_idx(tid, e)] = a[e];  // own slots only
@@ -99,10 +103,11 @@ __global__ void __launch_bounds__(T, 2) expand_level_kernel(const uint64_t *cur,
   ntt_fwd(t, sa, sb, Mp);
 #pragma unroll 1
   for (int kk = 0; kk < 2; ++kk) {
-    uint64_t a[8];
+    uint64_t a[8], as[8];
     ldg_slot8(key + (2 * kk + 1) * kN, a);
+    ldg_slot8(key_s + (2 * kk + 1) * kN, as);
 #pragma unroll
-    for (int e = 0; e < 8; ++e) a[e] = mul_mod(t[e], a[e], Mp);
+    for (int e = 0; e < 8; ++e) a[e] = mul_shoup_lazy4(t[e], a[e], as[e], Mp.q);
     ntt_inv(a, sa, sb, Mp);
 #pragma unroll
     for (int e = 0; e < 8; ++e) {
@@ -289,13 +294,15 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(T)
     t[e] = (m && v >= p) ? v - p : v;  // q < 2p
   }
   ntt_fwd(t, sa, sb, M);
-  const uint64_t *key = kb.q[b].galois + (size_t)level * 4 * kN + (size_t)(2 * kk + m) * kN;
-#pragma unroll
+  const size_t key_off = (size_t)level * 4 * kN + (size_t)(2 * kk + m) * kN;
   {
-    uint64_t kv[8];
-    ldg_slot8(key, kv);
+    // Shoup product with the key's companion: [0, 4 mod), which the inverse
+    // transform takes
+    uint64_t kv[8], ks[8];
+    ldg_slot8(kb.q[b].galois + key_off, kv);
+    ldg_slot8(kb.q[b].galois_s + key_off, ks);
 #pragma unroll
-    for (int e = 0; e < 8; ++e) t[e] = mul_mod(t[e], kv[e], M);
+    for (int e = 0; e < 8; ++e) t[e] = mul_shoup_lazy4(t[e], kv[e], ks[e], M.q);
   }
   ntt_inv(t, sa, sb, M);
   if (m == 1) {
