@@ -383,12 +383,16 @@ __global__ void query_limb_kernel(const uint64_t *__restrict__ plane, uint16_t *
                                   int n1, int b_base, int nh, int nbh, int pass_batch) {
   const int kblk = n1 / 8;
   const long long total = (long long)kN * nh * kblk * nbh;
+  // a warp covers 8 consecutive slots x 4 consecutive query polynomials:
+  // 64-byte runs of the plane per read, 512-byte runs of ql per write
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
        t += (long long)gridDim.x * blockDim.x) {
-    const int c = (int)(t % kN);
-    long long rest = t / kN;
-    const int bl = (int)(rest % nbh);
-    rest /= nbh;
+    const int lane = (int)(t & 31);
+    long long rest = t >> 5;
+    const int c = (int)(rest % (kN / 8)) * 8 + (lane & 7);
+    rest /= kN / 8;
+    const int bl = (int)(rest % (nbh / 4)) * 4 + (lane >> 3);
+    rest /= nbh / 4;
     const int kb = (int)(rest % kblk);
     const int hf = (int)(rest / kblk);
     const int bq = hf * kTcHalfNB + bl;
