@@ -962,7 +962,9 @@ static int query_host(opir_ctx *ctx, uint32_t db_id, uint32_t batch, const uint6
   CK(W.resp.alloc(batch * CTB), "alloc response");
   CK(W.packed.alloc(batch * ctx->resp_bytes + 16), "alloc packed");
   CK(W.h_in.alloc(batch * CTB), "alloc pinned");
-  CK(W.h_out.alloc(batch * (CTB + ctx->resp_bytes)), "alloc pinned");
+  // responses, packed bytes, then (16-byte aligned) the device status word
+  const size_t status_off = (batch * (CTB + ctx->resp_bytes) + 15) / 16 * 16;
+  CK(W.h_out.alloc(status_off + 16), "alloc pinned");
   CK(cudaStreamSynchronize(ctx->stream), "sync");
   std::memcpy(W.h_in.p, queries, batch * CTB);
   CK(cudaMemcpyAsync(W.queries.p, W.h_in.p, batch * CTB, cudaMemcpyHostToDevice, ctx->stream),
@@ -979,10 +981,16 @@ static int query_host(opir_ctx *ctx, uint32_t db_id, uint32_t batch, const uint6
     CK(cudaMemcpyAsync(h_packed, W.packed.p, batch * ctx->resp_bytes, cudaMemcpyDeviceToHost,
                        ctx->stream),
        "download responses");
+  // the status word travels with the responses: one synchronisation per call
+  uint32_t *h_status = reinterpret_cast<uint32_t *>(h_resp + status_off);
+  CK(cudaMemcpyAsync(h_status, ctx->status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                     ctx->stream),
+     "read status");
   CK(cudaStreamSynchronize(ctx->stream), "query");
-  {
-    int rc2 = check_status(ctx);
-    if (rc2) return rc2;
+  if (*h_status) {
+    const uint32_t st = *h_status;
+    CK(cudaMemset(ctx->status.p, 0, sizeof(uint32_t)), "clear status");
+    return ctx->fail(OPIR_ERR_TIMEOUT, "device pipeline wait timed out (status 0x%x)", st);
   }
   if (resps) std::memcpy(resps, h_resp, batch * CTB);
   if (packed) std::memcpy(packed, h_packed, batch * ctx->resp_bytes);
