@@ -176,7 +176,6 @@ __global__ void __launch_bounds__(256) scan_kernel(const uint64_t *__restrict__ 
 // ---------------------------------------------------------------------------
 // bulk-copy pipelined kernel
 // ---------------------------------------------------------------------------
-constexpr int kTileRows = 512;  // rows (of one or more planes) per tile
 
 struct ScanGeom {
   int n1, n_rest;
@@ -195,7 +194,7 @@ __global__ void __launch_bounds__(kWarps * 32 + 32, kMinBlocks)
     scan_bulk_kernel(const uint64_t *__restrict__ dbs, const uint4 *__restrict__ qs,
                      size_t qs_stride, uint64_t *out, size_t out_stride, ScanGeom G, Consts C,
                      uint64_t mu_lo, uint64_t mu_hi, uint32_t *status) {
-  static_assert(kRows * kWarps * 32 == kTileRows, "a tile is 512 rows");
+  constexpr int kTileRows = kRows * kWarps * 32;  // rows (of one or more planes) per tile
   static_assert(kStepK == 1 || kStepK == 2 || kStepK == 4 || kStepK == 8 || kStepK % 16 == 0,
                 "flush cadence: middle partial every 8 k-steps, outer ones every 16");
   constexpr int kStageDbBytes = kStepK * kTileRows * 8;
@@ -633,6 +632,7 @@ int g_batch_form = 3;  // accumulate spelling of scan_batch_kernel (OPIR_BATCH_M
 
 template <int R, int W, int K, int S, int B>
 cudaError_t set_attr() {
+  constexpr int kTileRows = R * W * 32;
   const int max_smem = S * (K * kTileRows * 8 + (kTileRows / 2) * K * 16) + 2 * S * 8;
   return cudaFuncSetAttribute(scan_bulk_kernel<R, W, K, S, B>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -644,6 +644,7 @@ bool launch_bulk(const uint64_t *dbs, const uint4 *qs, size_t qs_stride, uint64_
                  size_t out_stride, int n1, int n_rest, int batch, const Consts &C,
                  uint64_t mu_lo, uint64_t mu_hi, uint32_t *status, cudaStream_t s) {
   if (n1 % K != 0) return false;
+  constexpr int kTileRows = R * W * 32;
   ScanGeom G;
   G.n1 = n1;
   G.n_rest = n_rest;
@@ -676,8 +677,9 @@ bool launch_bulk(const uint64_t *dbs, const uint4 *qs, size_t qs_stride, uint64_
   X(2, 1, 16, 16, 2, 1)      \
   X(3, 1, 16, 8, 5, 1)       \
   X(4, 1, 16, 4, 12, 1)      \
-  X(5, 2, 8, 16, 3, 1)
-constexpr int kNumCfgs = 6;
+  X(5, 2, 8, 16, 3, 1)       \
+  X(6, 1, 8, 16, 3, 2)
+constexpr int kNumCfgs = 7;
 
 }  // namespace
 
