@@ -18,11 +18,12 @@ switch, packing).
          host threads, full queries on the same database and inputs; its
          responses are also compared bit for bit with the GPU's.
 
-Inputs: the database is seeded entries ingested on the GPU; Galois keys, the
-RGSW key and the query ciphertexts are seeded uniform residues (an RLWE
-ciphertext or key is uniform mod q, so they have the distribution of real
-ones).  The NTT-form database (4.29 GB) is larger than L2 (129 MB), so no
-L2 flush is needed between steps.
+Inputs: the database is seeded entries ingested on the GPU; four seeded
+PirClients (the CPU client library) make the Galois keys, RGSW keys and the
+queries for seeded entries, and after the timed regions every response is
+decoded by its client and compared with the database entry
+(`entries_decoded`).  The NTT-form database (4.29 GB) is larger than L2
+(129 MB), so no L2 flush is needed between steps.
 
 --impl reference times the reference algorithm on the host cores (the
 oracle port: the reference itself needs the absent SEAL fork) on the same
@@ -98,47 +99,97 @@ def dist_env():
     return rank, world, local
 
 
-def make_inputs(params, count, seed=1):
-    """Seeded uniform Galois keys, RGSW keys and query ciphertexts."""
-    rng = np.random.default_rng(seed)
-    q, p = params.coeff_modulus[0], params.coeff_modulus[-1]
-    h = params.get_expan_height()
-    clients = []
-    for _ in range(NUM_CLIENTS):
-        gk = np.empty((h, 2, 2, N), np.uint64)
-        gk[:, :, 0, :] = rng.integers(0, q, size=(h, 2, N), dtype=np.uint64)
-        gk[:, :, 1, :] = rng.integers(0, p, size=(h, 2, N), dtype=np.uint64)
-        gsw = rng.integers(0, q, size=(2 * params.get_l_key(), 2, N), dtype=np.uint64)
-        clients.append((gk, gsw))
-    queries = rng.integers(0, q, size=(count, 2, N), dtype=np.uint64)
-    return clients, queries
+def make_clients(params, count, seed=1, first=0):
+    """Seeded PirClients `first` .. `first + count - 1` of one database shape
+    (client c's secret seed is seed * 7919 + c, so the same client id has the
+    same secret key on every database)."""
+    from onionpirv2_gb300 import PirClient
+    return [PirClient(params, c, secret_seed=seed * 7919 + c) for c in range(first, first + count)]
 
 
-def make_clients(params, count, height, rng):
-    """`count` clients' seeded uniform Galois keys of `height` levels and RGSW keys."""
-    q, p = params.coeff_modulus[0], params.coeff_modulus[-1]
-    out = []
-    for _ in range(count):
-        gk = np.empty((height, 2, 2, N), np.uint64)
-        gk[:, :, 0, :] = rng.integers(0, q, size=(height, 2, N), dtype=np.uint64)
-        gk[:, :, 1, :] = rng.integers(0, p, size=(height, 2, N), dtype=np.uint64)
-        gsw = rng.integers(0, q, size=(2 * params.get_l_key(), 2, N), dtype=np.uint64)
-        out.append((gk, gsw))
-    return out
+def client_keys(clients, seed=1, threads=1):
+    """Every client's (Galois keys, RGSW key) on `threads` host threads."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    def one(c):
+        cid = c.get_client_id()
+        return (c.create_galois_keys(seed=seed * 104729 + cid),
+                c.generate_gsw_from_key(seed=seed * 130363 + cid))
+    if threads <= 1:
+        return [one(c) for c in clients]
+    with ThreadPoolExecutor(threads) as ex:
+        return list(ex.map(one, clients))
 
 
-def serve_leg(server, dbs, queries, nclients, rate, seconds, seed=7, max_batch=32, lanes=2,
-              max_wait_us=2000, check=8):
+def make_queries(clients, owners, entries, seed=1):
+    """Query j asks for entries[j] on behalf of clients[owners[j]]."""
+    return np.stack([clients[int(o)].fast_generate_query(int(e), seed=seed * 1000003 + j)
+                     for j, (o, e) in enumerate(zip(owners, entries))])
+
+
+class Inputs:
+    """NUM_CLIENTS seeded clients of one database, their keys, and `count`
+    queries for seeded entries; query i belongs to client i % NUM_CLIENTS."""
+
+    def __init__(self, params, count, seed=1):
+        self.params = params
+        self.clients = make_clients(params, NUM_CLIENTS, seed)
+        t = time.perf_counter()
+        self.keys = client_keys(self.clients, seed)
+        self.keygen_s = (time.perf_counter() - t) / NUM_CLIENTS
+        rng = np.random.default_rng(seed)
+        self.entries = rng.integers(0, params.get_num_entries(), size=count)
+        self.owners = np.arange(count) % NUM_CLIENTS
+        t = time.perf_counter()
+        self.queries = make_queries(self.clients, self.owners, self.entries, seed)
+        self.query_s = (time.perf_counter() - t) / count
+
+
+def decode_check(clients, owners, entries, packed, db_seed, entry_size, threads=1):
+    """Decode every packed response with its client: (entries equal to the
+    database's, lowest noise budget, seconds per decode)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from onionpirv2_gb300 import synthetic_entries
+
+    def one(j):
+        e, budget = clients[int(owners[j])].decode_response(int(entries[j]), packed[j])
+        ref = synthetic_entries(db_seed, int(entries[j]), 1, entry_size)[0]
+        return bool(np.array_equal(e, ref)), budget
+    t = time.perf_counter()
+    if threads <= 1:
+        res = [one(j) for j in range(len(packed))]
+    else:
+        with ThreadPoolExecutor(threads) as ex:
+            res = list(ex.map(one, range(len(packed))))
+    el = time.perf_counter() - t
+    return (sum(ok for ok, _ in res), min((b for _, b in res), default=0),
+            el / max(1, len(packed)))
+
+
+class QuerySet:
+    """Queries of one resident database: the clients that own them (same
+    ids and secret keys as the registered ones), their entries and seed."""
+
+    def __init__(self, params, db_id, db_seed, clients, owners, entries, seed, queries=None):
+        self.params, self.db_id, self.db_seed = params, db_id, db_seed
+        self.clients, self.owners, self.entries = clients, owners, entries
+        self.queries = (make_queries(clients, owners, entries, seed) if queries is None
+                        else queries)
+
+
+def serve_leg(server, qsets, rate, seconds, seed=7, max_batch=32, lanes=2, max_wait_us=2000,
+              check=8, threads=1):
     """Continuous batching under seeded Poisson arrivals: `rate` queries/s for
-    `seconds`, uniform choice of database, client and query.  Returns the
-    server's counters and latency percentiles, the arrival count, and whether
-    the first `check` responses equal the synchronous path's bit for bit."""
+    `seconds`, uniform choice of database and of query within it.  Returns the
+    server's counters and latency percentiles, the arrival count, whether the
+    first `check` responses equal the synchronous path's bit for bit, and how
+    many responses the clients decoded to the database entry."""
     rng = np.random.default_rng(seed)
     n = max(1, int(rate * seconds))
     gaps = rng.exponential(1.0 / rate, size=n)
-    pick_db = rng.integers(0, len(dbs), size=n)
-    pick_q = rng.integers(0, queries.shape[0], size=n)
-    pick_c = rng.integers(0, nclients, size=n)
+    pick_db = rng.integers(0, len(qsets), size=n)
+    pick_q = np.array([rng.integers(0, qsets[d].queries.shape[0]) for d in pick_db])
     server.serve_start(max_batch=max_batch, lanes=lanes, max_wait_us=max_wait_us)
     tickets = []
     t = time.perf_counter()
@@ -150,18 +201,22 @@ def serve_leg(server, dbs, queries, nclients, rate, seconds, seed=7, max_batch=3
                 break
             if d > 6e-4:
                 time.sleep(d - 4e-4)
-        tickets.append(server.submit(int(pick_c[j]), queries[pick_q[j]], db_id=dbs[pick_db[j]]))
-    kept = {}
-    for j, tk in enumerate(tickets):
-        r = server.wait(tk, 600000)
-        if j < check:
-            kept[j] = r
+        qs, k = qsets[pick_db[j]], pick_q[j]
+        tickets.append(server.submit(int(qs.owners[k]), qs.queries[k], db_id=qs.db_id))
+    resps = [server.wait(tk, 600000) for tk in tickets]
     stats = server.serve_stats()
     server.serve_stop()
-    same = all(np.array_equal(kept[j], server.make_query(int(pick_c[j]), queries[pick_q[j]],
-                                                         db_id=dbs[pick_db[j]]))
-               for j in kept)
-    return stats, n, same
+    same = all(np.array_equal(resps[j], server.make_query(
+        int(qsets[pick_db[j]].owners[pick_q[j]]), qsets[pick_db[j]].queries[pick_q[j]],
+        db_id=qsets[pick_db[j]].db_id)) for j in range(min(check, n)))
+    ok = 0
+    for d, qs in enumerate(qsets):
+        sel = [j for j in range(n) if pick_db[j] == d]
+        if sel:
+            ok += decode_check(qs.clients, qs.owners[pick_q[sel]], qs.entries[pick_q[sel]],
+                               [resps[j].packed for j in sel], qs.db_seed,
+                               qs.params.get_entry_size(), threads)[0]
+    return stats, n, same, ok
 
 
 def sweep_main(args):
@@ -176,7 +231,8 @@ def sweep_main(args):
     server.set_stream(stream.cuda_stream)
     server.gen_data(DB_SEED)
     sizes = [int(x) for x in args.batch_sweep.split(",")]
-    clients, queries = make_inputs(params, max(sizes) * 4)
+    inp = Inputs(params, max(sizes) * 4)
+    clients, queries = inp.keys, inp.queries
     for cid, (gk, gsw) in enumerate(clients):
         server.set_client_galois_key(cid, gk)
         server.set_client_gsw_key(cid, gsw)
@@ -228,23 +284,38 @@ def serve_main(args):
     dbs = [server.add_database(params[0], seed=DB_SEED + 1), server.db_id,
            server.add_database(params[2], seed=DB_SEED + 2)]
     ingest_s = time.perf_counter() - t0
-    height = max(p.get_expan_height() for p in params)
     per = server.key_bytes_per_client()
     slots = max(2, args.serve_clients // 2)
     server.set_key_budget(slots * per)  # half the clients' keys fit: LRU admission
+    # the clients: keys made on the host cores with the product PirClient
+    # (Galois keys for the deepest database serve the shallower ones too)
+    threads = os.cpu_count() or 1
+    deepest = max(range(3), key=lambda d: params[d].get_expan_height())
+    t = time.perf_counter()
+    keyed = make_clients(params[deepest], args.serve_clients)
+    keys = client_keys(keyed, threads=threads)
+    keygen_s = time.perf_counter() - t
+    for c, (gk, gsw) in zip(keyed, keys):
+        server.set_client_galois_key(c.get_client_id(), gk)
+        server.set_client_gsw_key(c.get_client_id(), gsw)
     rng = np.random.default_rng(3)
-    for cid, (gk, gsw) in enumerate(make_clients(params[1], args.serve_clients, height, rng)):
-        server.set_client_galois_key(cid, gk)
-        server.set_client_gsw_key(cid, gsw)
-    queries = rng.integers(0, params[1].coeff_modulus[0], size=(256, 2, N), dtype=np.uint64)
+    qsets = []
+    t = time.perf_counter()
+    for d in range(3):
+        cl = keyed if d == deepest else make_clients(params[d], args.serve_clients)
+        owners = rng.integers(0, args.serve_clients, size=256)
+        entries = rng.integers(0, params[d].get_num_entries(), size=256)
+        qsets.append(QuerySet(params[d], dbs[d], DB_SEED + (1, 0, 2)[d], cl, owners, entries,
+                              seed=20 + d))
+    query_s = (time.perf_counter() - t) / (3 * 256)
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.5)
     # warm-up: limb planes, workspaces and first-touch costs
-    serve_leg(server, dbs, queries, args.serve_clients, 200.0, 0.2, seed=1, check=0)
+    serve_leg(server, qsets, 200.0, 0.2, seed=1, check=0, threads=threads)
     t1 = time.time()
-    stats, n, same = serve_leg(server, dbs, queries, args.serve_clients, args.serve_rate,
-                               args.serve_seconds, seed=11)
+    stats, n, same, decoded = serve_leg(server, qsets, args.serve_rate, args.serve_seconds,
+                                        seed=11, threads=threads)
     t2 = time.time()
     clocks.stop()
     resident, nslots = server.resident_clients()
@@ -257,12 +328,21 @@ def serve_main(args):
         "config": {"workload": "serving: db4096 + db262144 + db2097152 resident",
                    "clients": args.serve_clients, "key_slots": nslots,
                    "offered_qps": args.serve_rate, "seconds": args.serve_seconds,
-                   "arrivals": "seeded Poisson, uniform database, client and query",
+                   "arrivals": "seeded Poisson, uniform database and query (256 client "
+                               "queries per database, owners uniform over the clients)",
                    "max_batch": 32, "lanes": 2, "max_wait_us": 2000},
         "p50_ms": stats["p50_ms"], "p99_ms": stats["p99_ms"], "mean_ms": stats["mean_ms"],
         "max_ms": stats["max_ms"], "completed": stats["completed"], "failed": stats["failed"],
         "batches": stats["batches"], "mean_batch": stats["mean_batch"],
         "resident_clients": resident, "bit_exact_sample": same, "ingest_s": ingest_s,
+        "entries_decoded": f"{decoded}/{n}",
+        "client": {"threads": threads, "clients": args.serve_clients,
+                   "keygen_s": keygen_s,
+                   "keys_per_s": args.serve_clients / keygen_s,
+                   "key_bytes_per_client": int(sum(a.nbytes for a in keys[0])),
+                   "query_ms": query_s * 1e3,
+                   "what": "PirClient (CPU): Galois keys + RGSW(sk) per client, one "
+                           "query per ms figure; every served response decoded"},
         "clocks": clocks.summary(t1, t2),
     }
     print(json.dumps(line), flush=True)
@@ -396,7 +476,12 @@ def run_reference(args):
     # a bounded sample: at most 200 timed queries (about 20 s on 16 cores) and
     # 3 warm-up queries, so the arm ends within minutes whatever K and W are
     steps, warm = min(args.steps, 200), min(args.warmup, 3)
-    clients, queries = make_inputs(params, warm + steps)
+    # the inputs of the GPU arm (same seeds), made by the oracle's own client
+    sks = [o.keygen(7919 + c) for c in range(NUM_CLIENTS)]
+    clients = [(o.galois_keys(sks[c], 104729 + c), o.gsw_key(sks[c], 130363 + c))
+               for c in range(NUM_CLIENTS)]
+    entries = np.random.default_rng(1).integers(0, params.get_num_entries(), size=warm + steps)
+    queries = [o.make_query(sks[j % NUM_CLIENTS], 1000003 + j, int(e)) for j, e in enumerate(entries)]
     gsw_ntt = [o.gsw_key_to_ntt(c[1]) for c in clients]
     for i in range(warm):
         o.make_query_server(db, clients[i % NUM_CLIENTS][0], gsw_ntt[i % NUM_CLIENTS], queries[i])
@@ -487,7 +572,8 @@ def main():
     ingest_s = time.perf_counter() - t_ingest
     total = args.warmup + args.steps
     nbatchq = args.batch * (args.batch_steps + 3) if args.batch > 1 else 0
-    clients, queries = make_inputs(params, max(total, nbatchq))
+    inp = Inputs(params, max(total, nbatchq))
+    clients, queries = inp.keys, inp.queries
     for cid, (gk, gsw) in enumerate(clients):
         server.set_client_galois_key(cid, gk)
         server.set_client_gsw_key(cid, gsw)
@@ -618,19 +704,31 @@ def main():
                                  "flops_per_step": flops,
                                  "peak_source": f"{tkind} bf16_tflops_sustained"},
                        imad=dict(imad, engine="integer multiply-add GEMM"))
+    # ---- client side: every response of the timed queries (rewritten by
+    # the batched passes, which equal them) decodes to its database entry
+    decoded, min_budget, decode_s = decode_check(
+        inp.clients, inp.owners[:total], inp.entries[:total], dpack[:total].cpu().numpy(),
+        DB_SEED, params.get_entry_size())
     # ---- serving: continuous batching under Poisson arrivals over this
     # database and a small second one (the full three-database run: --serve)
     serving = None
     if args.serve_rate > 0 and world == 1:
         from onionpirv2_gb300 import PirParams as _PP
-        small = server.add_database(_PP.preset("db4096"), seed=DB_SEED + 1)
-        sstats, sn, ssame = serve_leg(server, [server.db_id, small], queries, NUM_CLIENTS,
-                                      args.serve_rate, args.serve_seconds)
+        sp = _PP.preset("db4096")
+        small = server.add_database(sp, seed=DB_SEED + 1)
+        qsets = [QuerySet(params, server.db_id, DB_SEED, inp.clients, inp.owners, inp.entries,
+                          0, queries=inp.queries),
+                 QuerySet(sp, small, DB_SEED + 1, make_clients(sp, NUM_CLIENTS),
+                          np.arange(256) % NUM_CLIENTS,
+                          np.random.default_rng(5).integers(0, sp.get_num_entries(), size=256), 6)]
+        sstats, sn, ssame, sok = serve_leg(server, qsets, args.serve_rate, args.serve_seconds,
+                                           threads=os.cpu_count() or 1)
         serving = {"databases": [args.workload, "db4096"], "offered_qps": args.serve_rate,
                    "arrivals": sn, "queries_per_s": sstats["queries_per_s"],
                    "p50_ms": sstats["p50_ms"], "p99_ms": sstats["p99_ms"],
                    "mean_batch": sstats["mean_batch"], "batches": sstats["batches"],
                    "failed": sstats["failed"], "bit_exact_sample": ssame,
+                   "entries_decoded": f"{sok}/{sn}",
                    "policy": "max_batch 32, 2 lanes, max_wait 2 ms"}
     clocks.stop()
     e2e_qps = e2e_steps * world / (e2e_ms / 1e3)
@@ -661,6 +759,12 @@ def main():
         "gpu_launches": launches,
         "clocks": clocks.summary(t0, t1),
         "ingest_s": ingest_s,
+        "entries_decoded": f"{decoded}/{total}",
+        "min_noise_budget": min_budget,
+        "client": {"threads": 1, "keygen_ms": inp.keygen_s * 1e3, "query_ms": inp.query_s * 1e3,
+                   "decode_ms": decode_s * 1e3,
+                   "what": "PirClient (CPU) per client: Galois keys + RGSW(sk); per query: "
+                           "generation; per response: unpack, decrypt, entry"},
         "batched": batched,
         "serving": serving,
     }

@@ -19,19 +19,9 @@
 #include <vector>
 
 #include "onionpir_gpu.h"
+#include "onionpir_params.hpp"
 
 namespace onionpir {
-
-struct PirParams {
-  uint64_t q = 0, p = 0, t = 0, small_q = 0;  // CoeffModulus::Create / generate_prime results
-  uint32_t poly_degree = 2048;
-  uint32_t l = 5, base_log2 = 12, l_key = 10, base_log2_key = 6;
-  uint32_t fst_dim_sz = 0, other_dim_sz = 0;  // PirParams::get_dims()
-  uint32_t entry_size = 0, entries_per_pt = 1, bits_per_coeff = 15;
-};
-
-using Ciphertext = std::vector<uint64_t>;  // [2][N]
-using Entry = std::vector<uint8_t>;
 
 class PirServer {
  public:

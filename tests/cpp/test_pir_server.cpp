@@ -1,15 +1,17 @@
 // test_pir_server.cpp -- the reference's PirTest::test_pir loop
-// (src/tests.cpp:40-153) against the C++ PirServer drop-in
-// (include/onionpir_server.hpp), with the CPU oracle as the client.
-// Success criterion as in the reference (tests.cpp:110-134): the decrypted
-// entry equals the database entry; additionally the response must be
-// bit-identical to the oracle server's.
+// (src/tests.cpp:40-153) with the C++ drop-ins on both sides: the GPU
+// PirServer (include/onionpir_server.hpp) answers, the CPU PirClient
+// (include/onionpir_client.hpp) makes keys and queries and decodes the
+// response stream.  Success criterion as in the reference (tests.cpp:110-134):
+// the decrypted entry equals the database entry; additionally the response
+// must be bit-identical to the oracle server's.
 #include <cstdio>
 #include <cstring>
 #include <sstream>
 #include <stdexcept>
 #include <vector>
 
+#include "onionpir_client.hpp"
 #include "onionpir_server.hpp"
 #include "opir_oracle.h"
 
@@ -18,20 +20,7 @@ int main() {
   orc_ctx *o = orc_create(num_entries, max_fst_dim, 0, 5, 10, 16, 27, 60, 60);
   orc_params P;
   orc_get_params(o, &P);
-  onionpir::PirParams pp;
-  pp.q = P.q;
-  pp.p = P.p;
-  pp.t = P.t;
-  pp.small_q = P.small_q;
-  pp.l = (uint32_t)P.l;
-  pp.base_log2 = (uint32_t)P.base_log2;
-  pp.l_key = (uint32_t)P.l_key;
-  pp.base_log2_key = (uint32_t)P.base_log2_key;
-  pp.fst_dim_sz = (uint32_t)P.n1;
-  pp.other_dim_sz = (uint32_t)P.n_rest;
-  pp.entry_size = (uint32_t)P.entry_size;
-  pp.entries_per_pt = (uint32_t)P.entries_per_pt;
-  pp.bits_per_coeff = (uint32_t)P.bits_per_coeff;
+  const onionpir::PirParams pp = onionpir::PirParams::derive(num_entries, max_fst_dim);
 
   onionpir::PirServer server(pp);
   server.gen_data(seed);
@@ -40,32 +29,33 @@ int main() {
 
   const size_t N = 2048, iters = 13;  // EXPERIMENT_ITERATIONS = 10 + 3 warm-up
   int success = 0, identical = 0;
-  std::vector<int8_t> sk(N);
-  std::vector<uint64_t> gk(P.h * 4 * N), gsw(2 * P.l_key * 2 * N), gsw_ntt(gsw.size());
-  std::vector<uint64_t> query(2 * N), ref(2 * N), ct(2 * N), plain(N);
-  std::vector<uint8_t> ref_packed(orc_response_bytes(o)), entry(P.entry_size),
-      expect(P.entry_size);
+  std::vector<uint64_t> gsw_ntt(2 * P.l_key * 2 * N), ref(2 * N);
+  std::vector<uint8_t> ref_packed(orc_response_bytes(o)), expect(P.entry_size);
   std::vector<size_t> all_clients;
   std::vector<onionpir::Ciphertext> all_queries, all_resps;
   for (size_t i = 0; i < iters; ++i) {
-    const uint64_t client = 1000 + i, idx = (i * 2654435761ULL + 17) % P.num_entries;
-    orc_keygen(o, 77 + i, sk.data());
-    orc_make_galois_keys(o, sk.data(), 177 + i, gk.data());
-    orc_make_gsw_key(o, sk.data(), 277 + i, gsw.data());
-    server.set_client_galois_key(client, gk);
-    server.set_client_gsw_key(client, gsw);
-    orc_make_query(o, sk.data(), 377 + i, idx, query.data());
-    const onionpir::Ciphertext resp = server.make_query(client, query);
-    all_clients.push_back(client);
+    const uint64_t client_id = 1000 + i, idx = (i * 2654435761ULL + 17) % P.num_entries;
+    // odd iterations: keys and queries from OS entropy; even: seeded
+    const onionpir::PirClient client =
+        i % 2 ? onionpir::PirClient(pp, client_id) : onionpir::PirClient(pp, client_id, 77 + i);
+    const std::vector<uint64_t> gk = i % 2 ? client.create_galois_keys() : client.create_galois_keys(177 + i);
+    const std::vector<uint64_t> gsw =
+        i % 2 ? client.generate_gsw_from_key() : client.generate_gsw_from_key(277 + i);
+    server.set_client_galois_key(client_id, gk);
+    server.set_client_gsw_key(client_id, gsw);
+    const onionpir::Ciphertext query =
+        i % 2 ? client.fast_generate_query(idx) : client.fast_generate_query(idx, 377 + i);
+    const onionpir::Ciphertext resp = server.make_query(client_id, query);
+    all_clients.push_back(client_id);
     all_queries.push_back(query);
     all_resps.push_back(resp);
     std::stringstream stream;
     const size_t n = server.save_resp_to_stream(resp, stream);
     const std::string bytes = stream.str();
-    orc_unpack_response(o, reinterpret_cast<const uint8_t *>(bytes.data()), ct.data());
     int budget = 0;
-    orc_decrypt(o, sk.data(), ct.data(), 2, plain.data(), &budget);
-    orc_entry_from_plain(o, idx, plain.data(), entry.data());
+    const onionpir::Plaintext plain =
+        client.decrypt_mod_q(client.load_resp_from_stream(stream), &budget);
+    const onionpir::Entry entry = client.get_entry_from_plaintext(idx, plain);
     orc_gen_entries(o, seed, idx, 1, expect.data());
     const bool ok = n == ref_packed.size() && entry == expect;
     orc_gsw_key_to_ntt(o, gsw.data(), 2 * P.l_key, gsw_ntt.data());
@@ -80,7 +70,7 @@ int main() {
   }
   bool threw = false;
   try {
-    server.make_query(999999, query);
+    server.make_query(999999, all_queries[0]);
   } catch (const std::out_of_range &) {
     threw = true;
   }
