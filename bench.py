@@ -577,6 +577,11 @@ def main():
     for cid, (gk, gsw) in enumerate(clients):
         server.set_client_galois_key(cid, gk)
         server.set_client_gsw_key(cid, gsw)
+    # the autotuner picks the scan tile configuration and the engine per batch
+    # size for this database on this GPU (untimed; all choices are bit-exact)
+    t_tune = time.perf_counter()
+    tune = server.autotune(max_batch=max(2, args.batch))
+    tune_s = time.perf_counter() - t_tune
     rb = server.resp_bytes
     nq = queries.shape[0]
     dq = torch.from_numpy(queries.view(np.int64)).to(f"cuda:{local}")
@@ -759,6 +764,12 @@ def main():
         "gpu_launches": launches,
         "clocks": clocks.summary(t0, t1),
         "ingest_s": ingest_s,
+        "autotune": {"seconds": tune_s, "scan_choice": tune["scan_choice"],
+                     "scan_ms": [round(c["ms"], 4) for c in tune["scan_configs"]],
+                     "engine_by_batch": {str(b["batch"]): b["engine"] for b in tune["batches"]},
+                     "first_dim_ms_by_batch": {str(b["batch"]): {k: round(v, 3) for k, v in
+                                                                 b["ms"].items()}
+                                               for b in tune["batches"]}},
         "entries_decoded": f"{decoded}/{total}",
         "min_noise_budget": min_budget,
         "client": {"threads": 1, "keygen_ms": inp.keygen_s * 1e3, "query_ms": inp.query_s * 1e3,

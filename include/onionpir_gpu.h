@@ -165,6 +165,31 @@ enum {
 };
 int opir_set_batch_engine(opir_ctx *ctx, int engine, uint32_t tensor_min_batch);
 
+/* ---- autotuner (no reference counterpart) ----
+ * Times, on this GPU and for database db_id, every compiled tile
+ * configuration of the single-query scan, and the first-dimension product
+ * of every engine (one scan per query, integer GEMM, tensor-core limb GEMM)
+ * at the batch sizes 2, 4, ..., max_batch (at most 256), each after a
+ * warm-up, over `reps` repetitions (0: 3), on operands of valid residues.
+ * The database then scans with the fastest configuration, and under
+ * OPIR_ENGINE_AUTO a batch of B queries takes the engine that was fastest at
+ * the largest measured size <= B.  Builds the database's limb plane if the
+ * tensor engine can run on it.  Results are unchanged (every configuration
+ * and engine gives the same bits).  Not while serving (OPIR_ERR_STATE).
+ * times in ms of one first-dimension product; < 0: cannot run this shape. */
+typedef struct opir_tune_report {
+  uint32_t scan_configs;   /* compiled scan configurations (<= 16) */
+  uint32_t scan_desc[16][5]; /* rows per thread, warps, k-steps, stages, CTAs per SM */
+  float scan_ms[16];
+  int32_t scan_choice;     /* chosen configuration, -1: the plain kernel */
+  uint32_t batch_points;   /* number of batch sizes measured (<= 8) */
+  uint32_t batch[8];
+  float engine_ms[8][3];   /* [point][OPIR_ENGINE_SCAN - 1 .. OPIR_ENGINE_TENSOR - 1] */
+  int32_t engine[8];       /* chosen OPIR_ENGINE_* per point */
+} opir_tune_report;
+int opir_autotune(opir_ctx *ctx, uint32_t db_id, uint32_t max_batch, uint32_t reps,
+                  opir_tune_report *report);
+
 /* ---- serving: continuous batching ----
  * No reference counterpart (PirServer::make_query, server.cpp:520-579,
  * answers one query per call).  opir_serve_start starts a worker thread that

@@ -124,6 +124,13 @@ class PirServer {
     check(opir_set_batch_engine(ctx_, engine, tensor_min_batch));
   }
   void set_key_budget(uint64_t bytes) { check(opir_set_key_budget(ctx_, bytes)); }
+  // Measure the scan tile configurations and the engines at batch sizes
+  // 2 .. max_batch on this GPU and adopt the fastest (opir_autotune).
+  opir_tune_report autotune(uint32_t max_batch = 64, uint32_t reps = 3) {
+    opir_tune_report r{};
+    check(opir_autotune(ctx_, db_, max_batch, reps, &r));
+    return r;
+  }
   uint64_t key_bytes_per_client() const { return opir_key_bytes_per_client(ctx_); }
 
   // Serving: continuous batching on a worker thread (opir_serve_* in

@@ -39,7 +39,7 @@ EXPORTS = (
     "opir_launch_count", "opir_sync", "opir_ntt", "opir_ntt_device",
     "opir_set_key_budget", "opir_key_bytes_per_client", "opir_resident_clients",
     "opir_serve_start", "opir_serve_stop", "opir_submit", "opir_poll", "opir_wait",
-    "opir_serve_stats_get", "opir_set_batch_engine",
+    "opir_serve_stats_get", "opir_set_batch_engine", "opir_autotune",
 )
 
 ENGINES = {"auto": 0, "scan": 1, "imad": 2, "tensor": 3}
@@ -90,6 +90,19 @@ class OpirServeStats(ctypes.Structure):
         ("mean_ms", ctypes.c_double),
         ("max_ms", ctypes.c_double),
         ("queries_per_s", ctypes.c_double),
+    ]
+
+
+class OpirTuneReport(ctypes.Structure):
+    _fields_ = [
+        ("scan_configs", ctypes.c_uint32),
+        ("scan_desc", (ctypes.c_uint32 * 5) * 16),
+        ("scan_ms", ctypes.c_float * 16),
+        ("scan_choice", ctypes.c_int32),
+        ("batch_points", ctypes.c_uint32),
+        ("batch", ctypes.c_uint32 * 8),
+        ("engine_ms", (ctypes.c_float * 3) * 8),
+        ("engine", ctypes.c_int32 * 8),
     ]
 
 
@@ -160,6 +173,8 @@ def load(path: str = LIB):
     L.opir_wait.argtypes = [_vp, ctypes.c_uint64, ctypes.c_uint32, _u64p, _u8p]
     L.opir_serve_stats_get.argtypes = [_vp, ctypes.POINTER(OpirServeStats)]
     L.opir_set_batch_engine.argtypes = [_vp, ctypes.c_int, ctypes.c_uint32]
+    L.opir_autotune.argtypes = [_vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                ctypes.POINTER(OpirTuneReport)]
     _lib = L
     return L
 

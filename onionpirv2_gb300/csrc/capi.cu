@@ -11,6 +11,7 @@
 //                                                      server.cpp:581-633,779-801
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -30,6 +31,7 @@
 #include "../../include/onionpir_gpu.h"
 #include "kernels.h"
 #include "serve_core.h"
+#include "tune_core.h"
 
 using namespace opir;
 
@@ -149,6 +151,10 @@ struct Db {
   DevBuf dbs;
   DevBuf dbl;              // bf16 limb plane of dbs for the tensor-core product (built on demand)
   bool dbl_valid = false;  // cleared whenever dbs changes
+  // opir_autotune's choices: scan tile configuration (-1: the default) and
+  // the engine per batch size (empty: the fixed crossovers)
+  int scan_cfg = -1;
+  tune::EngineTable engines;
 };
 
 struct Client {
@@ -368,10 +374,21 @@ void record(opir_ctx *ctx, const PipeEnv &E, int i) {
 
 bool serving_active(const opir_ctx *ctx) { return ctx->serving && ctx->serving->active; }
 
-// The first-dimension engine of a batch (OPIR_ENGINE_SCAN/IMAD/TENSOR).
-int engine_for(const opir_ctx *ctx, int batch, int n1, int nr) {
-  const bool tc_ok = tc_scan_supported(n1, nr), imad_ok = nr % 32 == 0 && n1 % 16 == 0;
+bool imad_supported(int n1, int nr) { return nr % 32 == 0 && n1 % 16 == 0; }
+
+// The first-dimension engine of a batch (OPIR_ENGINE_SCAN/IMAD/TENSOR): the
+// explicit choice of opir_set_batch_engine, else the database's tuned table,
+// else the fixed crossovers.
+int engine_for(const opir_ctx *ctx, const Db &db, int batch) {
+  const int n1 = (int)db.shape.fst_dim_sz, nr = (int)db.shape.other_dim_sz;
+  const bool tc_ok = tc_scan_supported(n1, nr), imad_ok = imad_supported(n1, nr);
   if (batch < 2) return OPIR_ENGINE_SCAN;
+  if (ctx->engine == OPIR_ENGINE_AUTO && db.engines.points) {
+    const int e = tune::engine_at(db.engines, batch);
+    if (e == OPIR_ENGINE_TENSOR && tc_ok) return e;
+    if (e == OPIR_ENGINE_IMAD && imad_ok) return e;
+    return OPIR_ENGINE_SCAN;
+  }
   switch (ctx->engine) {
     case OPIR_ENGINE_TENSOR:
       return tc_ok ? OPIR_ENGINE_TENSOR : imad_ok ? OPIR_ENGINE_IMAD : OPIR_ENGINE_SCAN;
@@ -503,7 +520,7 @@ int run_pipeline(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
   const size_t res_stride = nr * CTW;
   // a batch of queries shares one pass over the database (batched GEMM);
   // a single query (or an unsupported shape) streams it once per query
-  const int use = engine_for(ctx, batch, (int)n1, (int)nr);
+  const int use = engine_for(ctx, db, batch);
   const bool tensor = use == OPIR_ENGINE_TENSOR, batched = use == OPIR_ENGINE_IMAD;
   if (tensor) {
     if (!db.dbl_valid) {
@@ -537,7 +554,7 @@ int run_pipeline(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
     record(ctx, E, 6);
     launch_scan(db.dbs.as<uint64_t>(), W.qs.as<uint4>(), qs_stride, W.res.as<uint64_t>(),
                 res_stride, (int)n1, (int)nr, batch, ctx->C, ctx->Mq.tab.mu_lo,
-                ctx->Mq.tab.mu_hi, E.status, s);
+                ctx->Mq.tab.mu_hi, E.status, s, db.scan_cfg);
   }
   record(ctx, E, 7);
   launch_ntt(ctx->Mq.tab, W.res.as<uint64_t>(), (size_t)batch * nr * 2, true, s);
@@ -1051,6 +1068,126 @@ int opir_set_batch_engine(opir_ctx *ctx, int engine, uint32_t tensor_min_batch) 
   return OPIR_OK;
 }
 
+int opir_autotune(opir_ctx *ctx, uint32_t db_id, uint32_t max_batch, uint32_t reps,
+                  opir_tune_report *report) {
+  if (!ctx) return OPIR_ERR_ARG;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  if (serving_active(ctx)) return ctx->fail(OPIR_ERR_STATE, "serving is active");
+  Db *db = find_db(ctx, db_id);
+  if (!db) return ctx->fail(OPIR_ERR_UNKNOWN_DB, "unknown database %u", db_id);
+  if (!db->dbs.p) return ctx->fail(OPIR_ERR_STATE, "database %u holds no data", db_id);
+  CK(cudaSetDevice(ctx->device), "set device");
+  if (reps == 0) reps = 3;
+  if (max_batch > 256) max_batch = 256;
+  opir_tune_report R{};
+  const int n1 = (int)db->shape.fst_dim_sz, nr = (int)db->shape.other_dim_sz;
+  const size_t CTW = 2 * (size_t)kN, res_stride = (size_t)nr * CTW, qs_stride = (size_t)kN * n1;
+  const int np = tune::batch_points(max_batch, R.batch);
+  const int bmax = np ? (int)R.batch[np - 1] : 1;
+  cudaStream_t s = ctx->stream;
+  uint32_t *status = ctx->status.as<uint32_t>();
+  // operands: bmax queries' n1 first-dimension leaves, copied from the
+  // database itself (valid residues mod q whatever q is) -- the work and the
+  // memory traffic of every kernel are independent of the values
+  DevBuf leaves, qs, ql, res;
+  const size_t leaf_words = (size_t)bmax * n1 * CTW, db_words = db->num_pt * (size_t)kN;
+  CK(leaves.alloc(leaf_words * 8), "autotune operands");
+  for (size_t off = 0; off < leaf_words; off += db_words) {
+    const size_t n = std::min(db_words, leaf_words - off);
+    CK(cudaMemcpyAsync(leaves.as<uint64_t>() + off, db->dbs.p, n * 8, cudaMemcpyDeviceToDevice, s),
+       "autotune operands");
+  }
+  CK(qs.alloc((size_t)bmax * kN * n1 * sizeof(uint4)), "autotune operands");
+  CK(res.alloc((size_t)bmax * res_stride * 8), "autotune output");
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0), "autotune events");
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return ctx->fail(OPIR_ERR_CUDA, "autotune events");
+  }
+  // ms of one call of fn after one warm-up call; -1 if fn cannot run the shape
+  auto time_it = [&](auto &&fn) -> float {
+    if (!fn()) return -1.0f;
+    cudaEventRecord(e0, s);
+    for (uint32_t r = 0; r < reps; r++) fn();
+    cudaEventRecord(e1, s);
+    if (cudaEventSynchronize(e1) != cudaSuccess) return -1.0f;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    return ms / (float)reps;
+  };
+  // ---- single-query scan: every compiled tile configuration
+  R.scan_configs = (uint32_t)std::min(scan_config_count(), 16);
+  for (uint32_t c = 0; c < R.scan_configs; c++) {
+    scan_config_desc((int)c, R.scan_desc[c]);
+    R.scan_ms[c] = time_it([&] {
+      launch_query_prep(leaves.as<uint64_t>(), n1 * CTW, qs.as<uint4>(), qs_stride, n1, 1,
+                        ctx->Mq.tab, s);
+      return launch_scan(db->dbs.as<uint64_t>(), qs.as<uint4>(), qs_stride, res.as<uint64_t>(),
+                         res_stride, n1, nr, 1, ctx->C, ctx->Mq.tab.mu_lo, ctx->Mq.tab.mu_hi,
+                         status, s, (int)c) == (int)c;
+    });
+  }
+  R.scan_choice = tune::pick(R.scan_ms, (int)R.scan_configs);
+  // ---- batches: one scan per query, integer GEMM, tensor-core limb GEMM
+  const bool tc_ok = tc_scan_supported(n1, nr), imad_ok = imad_supported(n1, nr);
+  bool limbs = db->dbl_valid;
+  if (tc_ok && np && !limbs) {
+    // an allocation failure (the plane takes 16 bytes per residue) leaves
+    // the tensor engine out of the table
+    if (db->dbl.alloc(tc_db_limb_bytes(n1, nr)) == cudaSuccess) {
+      launch_db_limbs(db->dbs.as<uint64_t>(), db->dbl.as<uint16_t>(), n1, nr, s);
+      ctx->launches++;
+      limbs = db->dbl_valid = cudaStreamSynchronize(s) == cudaSuccess;
+    } else {
+      cudaGetLastError();
+    }
+  }
+  if (tc_ok && limbs && np && ql.alloc(tc_query_limb_bytes(n1, bmax)) != cudaSuccess) {
+    cudaGetLastError();
+    limbs = false;
+  }
+  R.batch_points = (uint32_t)np;
+  for (int i = 0; i < np; i++) {
+    const int B = (int)R.batch[i];
+    R.engine_ms[i][OPIR_ENGINE_SCAN - 1] = time_it([&] {
+      launch_query_prep(leaves.as<uint64_t>(), n1 * CTW, qs.as<uint4>(), qs_stride, n1, B,
+                        ctx->Mq.tab, s);
+      launch_scan(db->dbs.as<uint64_t>(), qs.as<uint4>(), qs_stride, res.as<uint64_t>(),
+                  res_stride, n1, nr, B, ctx->C, ctx->Mq.tab.mu_lo, ctx->Mq.tab.mu_hi, status, s,
+                  R.scan_choice);
+      return true;
+    });
+    R.engine_ms[i][OPIR_ENGINE_IMAD - 1] = !imad_ok ? -1.0f : time_it([&] {
+      launch_query_prep_batched(leaves.as<uint64_t>(), n1 * CTW, qs.as<uint4>(), n1, B,
+                                ctx->Mq.tab, s);
+      return launch_scan_batched(db->dbs.as<uint64_t>(), qs.as<uint4>(), res.as<uint64_t>(),
+                                 res_stride, n1, nr, B, ctx->C, ctx->Mq.tab.mu_lo,
+                                 ctx->Mq.tab.mu_hi, status, s);
+    });
+    R.engine_ms[i][OPIR_ENGINE_TENSOR - 1] = !(tc_ok && limbs) ? -1.0f : time_it([&] {
+      launch_query_prep_plane(leaves.as<uint64_t>(), n1 * CTW, qs.as<uint64_t>(), n1, B,
+                              ctx->Mq.tab, s);
+      launch_tc_query_limbs(qs.as<uint64_t>(), ql.as<uint16_t>(), n1, B, s);
+      launch_tc_scan(db->dbl.as<uint16_t>(), ql.as<uint16_t>(), res.as<uint64_t>(), res_stride, n1,
+                     nr, B, ctx->Mq.tab.q, ctx->Mq.tab.mu_lo, ctx->Mq.tab.mu_hi, ctx->r64,
+                     ctx->r128, status, s);
+      return true;
+    });
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  CK(cudaGetLastError(), "autotune launches");
+  CK(cudaStreamSynchronize(s), "autotune");
+  int rc = check_status(ctx);
+  if (rc) return rc;
+  db->scan_cfg = R.scan_choice;
+  tune::build_table(db->engines, R.batch, np, R.engine_ms);
+  for (int i = 0; i < np; i++) R.engine[i] = db->engines.engine[i];
+  if (report) *report = R;
+  return OPIR_OK;
+}
+
 int opir_set_timing(opir_ctx *ctx, int enable) {
   if (!ctx) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
@@ -1330,7 +1467,10 @@ int presize_lane(opir_ctx *ctx, Lane &L, int max_batch) {
     int rc = ensure_workspace(ctx, db, max_batch, W);
     if (rc) return rc;
     const int n1 = (int)db.shape.fst_dim_sz, nr = (int)db.shape.other_dim_sz;
-    if (engine_for(ctx, max_batch, n1, nr) == OPIR_ENGINE_TENSOR) {
+    bool tensor = false;  // any batch size up to max_batch on the tensor engine
+    for (int b = 2; b <= max_batch && !tensor; b++)
+      tensor = engine_for(ctx, db, b) == OPIR_ENGINE_TENSOR;
+    if (tensor) {
       CK(W.ql.alloc(tc_query_limb_bytes(n1, max_batch)), "alloc query limbs");
       if (!db.dbl_valid) {
         CK(db.dbl.alloc(tc_db_limb_bytes(n1, nr)), "alloc database limb plane");
@@ -1558,7 +1698,8 @@ extern "C" int opir_first_dim_noalloc(opir_ctx *ctx, uint32_t db_id, const uint6
   // the operand is fully rewritten before the scan reads it: nothing to clear
   launch_query_prep(d_fst_cts, n1 * CTW, qs, (size_t)kN * n1, (int)n1, 1, ctx->Mq.tab, s);
   launch_scan(db->dbs.as<uint64_t>(), qs, (size_t)kN * n1, d_out, nr * CTW, (int)n1, (int)nr, 1,
-              ctx->C, ctx->Mq.tab.mu_lo, ctx->Mq.tab.mu_hi, ctx->status.as<uint32_t>(), s);
+              ctx->C, ctx->Mq.tab.mu_lo, ctx->Mq.tab.mu_hi, ctx->status.as<uint32_t>(), s,
+              db->scan_cfg);
   launch_ntt(ctx->Mq.tab, d_out, nr * 2, true, s);
   ctx->launches += 3;
   CK(cudaGetLastError(), "first dimension launch");

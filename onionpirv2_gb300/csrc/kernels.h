@@ -67,11 +67,17 @@ void launch_query_prep(const uint64_t *leaves, size_t leaves_stride, uint4 *qs, 
 void launch_query_prep_batched(const uint64_t *leaves, size_t leaves_stride, uint4 *qsb, int n1,
                                int batch, const ModTab &Mq, cudaStream_t s);
 // out[b][row][poly][c] = sum_k DB[c][k][row] * Q[b][c][k][poly] mod q  (NTT form)
-// (bulk-copy pipelined kernel when n_rest >= 2 and 4 | n1; status collects
-// bounded-wait timeouts, see async.cuh)
-void launch_scan(const uint64_t *dbs, const uint4 *qs, size_t qs_stride, uint64_t *out,
-                 size_t out_stride, int n1, int n_rest, int batch, const Consts &C,
-                 uint64_t mu_lo, uint64_t mu_hi, uint32_t *status, cudaStream_t s);
+// (bulk-copy pipelined kernel in tile configuration `cfg` -- < 0: the
+// default -- when the shape fits it, else a plain kernel; status collects
+// bounded-wait timeouts, see async.cuh).  Returns the configuration that
+// ran, -1 for the plain kernel.
+int launch_scan(const uint64_t *dbs, const uint4 *qs, size_t qs_stride, uint64_t *out,
+                size_t out_stride, int n1, int n_rest, int batch, const Consts &C,
+                uint64_t mu_lo, uint64_t mu_hi, uint32_t *status, cudaStream_t s, int cfg = -1);
+// compiled tile configurations of the bulk scan: {rows per thread, warps,
+// k-steps per stage, stages, CTAs per SM}
+int scan_config_count();
+void scan_config_desc(int i, uint32_t out[5]);
 cudaError_t init_scan_attributes();
 // Batched product: one pass over the database for up to 32 queries at a time
 // (qsb[c][k][b], out as launch_scan).  Returns false if the shape is not

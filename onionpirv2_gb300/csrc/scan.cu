@@ -743,12 +743,24 @@ bool launch_scan_batched(const uint64_t *dbs, const uint4 *qsb, uint64_t *out, s
   return true;
 }
 
-void launch_scan(const uint64_t *dbs, const uint4 *qs, size_t qs_stride, uint64_t *out,
-                 size_t out_stride, int n1, int n_rest, int batch, const Consts &C,
-                 uint64_t mu_lo, uint64_t mu_hi, uint32_t *status, cudaStream_t s) {
+int scan_config_count() { return kNumCfgs; }
+
+void scan_config_desc(int i, uint32_t out[5]) {
+  uint32_t d[kNumCfgs][5] = {
+#define OPIR_DESC(i, R, W, K, S, B) {R, W, K, S, B},
+      OPIR_SCAN_CONFIGS(OPIR_DESC)
+#undef OPIR_DESC
+  };
+  for (int k = 0; k < 5; k++) out[k] = (i >= 0 && i < kNumCfgs) ? d[i][k] : 0;
+}
+
+int launch_scan(const uint64_t *dbs, const uint4 *qs, size_t qs_stride, uint64_t *out,
+                size_t out_stride, int n1, int n_rest, int batch, const Consts &C,
+                uint64_t mu_lo, uint64_t mu_hi, uint32_t *status, cudaStream_t s, int cfg) {
+  if (cfg < 0 || cfg >= kNumCfgs) cfg = g_cfg;
   if (n_rest >= 2 && n1 % 8 == 0) {
     bool done = false;
-    switch (g_cfg) {
+    switch (cfg) {
 #define OPIR_CASE(i, R, W, K, S, B)                                                            \
   case i:                                                                                      \
     done = launch_bulk<R, W, K, S, B>(dbs, qs, qs_stride, out, out_stride, n1, n_rest, batch, \
@@ -757,7 +769,7 @@ void launch_scan(const uint64_t *dbs, const uint4 *qs, size_t qs_stride, uint64_
       OPIR_SCAN_CONFIGS(OPIR_CASE)
 #undef OPIR_CASE
     }
-    if (done) return;
+    if (done) return cfg;
   }
   if (n_rest % 2 == 0) {
     const size_t threads = (size_t)kN * (n_rest / 2);
@@ -770,6 +782,7 @@ void launch_scan(const uint64_t *dbs, const uint4 *qs, size_t qs_stride, uint64_
     scan_kernel<1><<<dim3(blocks, batch), 256, 0, s>>>(dbs, qs, qs_stride, out, out_stride, n1,
                                                       n_rest, C, mu_lo, mu_hi);
   }
+  return -1;
 }
 
 }  // namespace opir

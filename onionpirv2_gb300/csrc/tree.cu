@@ -350,7 +350,6 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(T)
 __device__ __forceinline__ void digit_mac(uint64_t d[8], const uint64_t *row, uint64_t *sa,
                                           uint64_t *sb, const ModTab &M, U128 acc0[8],
                                           U128 acc1[8]) {
-  const int tid = threadIdx.x;
   ntt_fwd(d, sa, sb, M);
   uint64_t w0[8], w1[8];
   ldg_slot8(row, w0);

@@ -288,6 +288,25 @@ class PirServer:
                                                   tensor_min_batch))
 
     # ---- serving: continuous batching
+    def autotune(self, max_batch: int = 64, reps: int = 3, db_id: Optional[int] = None) -> dict:
+        """Measure every scan tile configuration and every first-dimension
+        engine at batch sizes 2 .. max_batch on this GPU for one database,
+        and adopt the fastest (opir_autotune).  Returns the measurements."""
+        r = _capi.OpirTuneReport()
+        self._check(self._L.opir_autotune(self._ctx, self.db_id if db_id is None else db_id,
+                                          max_batch, reps, ctypes.byref(r)))
+        names = {1: "scan", 2: "imad", 3: "tensor"}
+        keys = ("rows", "warps", "ksteps", "stages", "ctas_per_sm")
+        return {
+            "scan_configs": [dict(zip(keys, list(r.scan_desc[i])), ms=float(r.scan_ms[i]))
+                             for i in range(r.scan_configs)],
+            "scan_choice": int(r.scan_choice),
+            "batches": [{"batch": int(r.batch[i]),
+                         "ms": {names[e + 1]: float(r.engine_ms[i][e]) for e in range(3)},
+                         "engine": names.get(int(r.engine[i]), "scan")}
+                        for i in range(r.batch_points)],
+        }
+
     def serve_start(self, max_batch: int = 32, lanes: int = 2, max_wait_us: int = 2000):
         cfg = _capi.OpirServeConfig(max_batch=max_batch, lanes=lanes, max_wait_us=max_wait_us)
         self._check(self._L.opir_serve_start(self._ctx, ctypes.byref(cfg)))

@@ -1,0 +1,68 @@
+"""The autotuner (opir_autotune): it measures every scan tile configuration
+and every first-dimension engine on the device, adopts the fastest, and the
+responses stay bit-identical to the oracle's and to the untuned ones."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _argmin(ms):
+    ok = [(m, i) for i, m in enumerate(ms) if m >= 0]
+    return min(ok)[1] if ok else -1
+
+
+@pytest.mark.parametrize("shape", [(4096, 256), (1 << 13, 64), (1 << 14, 1024)])
+def test_autotune_choices_and_parity(gpu_lib, oracle_lib, shape):
+    from onionpirv2_gb300 import PirClient, PirParams, PirServer
+    params = PirParams(num_entries=shape[0], max_fst_dim=shape[1])
+    server = PirServer(params)
+    server.gen_data(777)
+    clients = [PirClient(params, i, secret_seed=50 + i) for i in range(8)]
+    for c in clients:
+        server.set_client_galois_key(c.get_client_id(), c.create_galois_keys(seed=1))
+        server.set_client_gsw_key(c.get_client_id(), c.generate_gsw_from_key(seed=2))
+    entries = [(i * 977 + 5) % params.get_num_entries() for i in range(8)]
+    queries = np.stack([c.fast_generate_query(e, seed=3) for c, e in zip(clients, entries)])
+    ids = [c.get_client_id() for c in clients]
+    before = [server.make_query(i, q) for i, q in zip(ids, queries)]
+    rep = server.autotune(max_batch=8, reps=2)
+    # the choices are the fastest measurements
+    scan_ms = [c["ms"] for c in rep["scan_configs"]]
+    assert len(scan_ms) >= 1 and any(m > 0 for m in scan_ms)
+    assert rep["scan_choice"] == _argmin(scan_ms)
+    assert [b["batch"] for b in rep["batches"]] == [2, 4, 8]
+    for b in rep["batches"]:
+        ms = [b["ms"][k] for k in ("scan", "imad", "tensor")]
+        assert b["ms"]["scan"] > 0
+        assert b["engine"] == ("scan", "imad", "tensor")[_argmin(ms)]
+    # same bits after tuning: single queries and batches of every size
+    o = oracle_lib.Oracle(*shape)
+    db = o.build_db(777)
+    for j in (0, 5):
+        c = clients[j]
+        ref, _, _, _ = o.make_query_server(db, c.create_galois_keys(seed=1),
+                                           o.gsw_key_to_ntt(c.generate_gsw_from_key(seed=2)),
+                                           queries[j])
+        assert np.array_equal(before[j], ref)
+    for i, q, r in zip(ids, queries, before):
+        assert np.array_equal(server.make_query(i, q), r)
+    for B in (2, 3, 5, 8):
+        resps, packed = server.make_query_batch(ids[:B], queries[:B])
+        for j in range(B):
+            assert np.array_equal(resps[j], before[j]), (B, j)
+            entry, _ = clients[j].decode_response(entries[j], packed[j].tobytes())
+            assert np.array_equal(entry, server.direct_get_entry(entries[j]))
+    server.close()
+
+
+def test_autotune_refused_while_serving(gpu_lib):
+    from onionpirv2_gb300 import OpirError, PirParams, PirServer
+    server = PirServer(PirParams(num_entries=4096, max_fst_dim=256))
+    server.gen_data(1)
+    server.serve_start(max_batch=4)
+    with pytest.raises(OpirError):
+        server.autotune(max_batch=4)
+    server.serve_stop()
+    server.autotune(max_batch=4, reps=1)
+    server.close()
