@@ -149,7 +149,18 @@ __device__ __forceinline__ void gs_bf(uint64_t &x, uint64_t &y, ulonglong2 w, ui
   y = mul_shoup_lazy4(u - v + q4, w.x, w.y, q);
 }
 
+// Twiddle reads: from global memory through the read-only path, or from a
+// copy staged in shared memory (prefetch_tw), which latency-bound kernels
+// with few CTAs per SM use -- an L2 round trip per register pass otherwise
+// sits on the critical path of every transform.
+template <bool kSmemTw>
+__device__ __forceinline__ ulonglong2 tw_ld(const ulonglong2 *p) {
+  if constexpr (kSmemTw) return *p;
+  else return __ldg(p);
+}
+
 // Three CT stages (bits lo+2, lo+1, lo).  Stage on bit b: twiddle m + (idx >> (b+1)), m = 2^(10-b).
+template <bool kSmemTw = false>
 __device__ __forceinline__ void ct_pass3(uint64_t r[8], int tid, int lo, const ulonglong2 *tw,
                                          uint64_t q, uint64_t q4) {
   const int base = pass_index(tid, 0, lo);
@@ -162,10 +173,11 @@ __device__ __forceinline__ void ct_pass3(uint64_t r[8], int tid, int lo, const u
     for (int e = 0; e < 8; ++e) {
       if (e & half) continue;
       const int idx = base | (e << lo);
-      ct_bf(r[e], r[e | half], __ldg(tw + m + (idx >> (b + 1))), q, q4);
+      ct_bf(r[e], r[e | half], tw_ld<kSmemTw>(tw + m + (idx >> (b + 1))), q, q4);
     }
   }
 }
+template <bool kSmemTw = false>
 __device__ __forceinline__ void gs_pass3(uint64_t r[8], int tid, int lo, const ulonglong2 *tw,
                                          uint64_t q, uint64_t q4) {
   const int base = pass_index(tid, 0, lo);
@@ -178,34 +190,36 @@ __device__ __forceinline__ void gs_pass3(uint64_t r[8], int tid, int lo, const u
     for (int e = 0; e < 8; ++e) {
       if (e & half) continue;
       const int idx = base | (e << lo);
-      gs_bf(r[e], r[e | half], __ldg(tw + m + (idx >> (b + 1))), q, q4);
+      gs_bf(r[e], r[e | half], tw_ld<kSmemTw>(tw + m + (idx >> (b + 1))), q, q4);
     }
   }
 }
 // Stages on bits 1 and 0: the thread's slots 8 tid .. 8 tid + 7 form the
 // radix-4 groups g = 2 tid and 2 tid + 1.
+template <bool kSmemTw = false>
 __device__ __forceinline__ void ct_pass2(uint64_t r[8], int tid, const ulonglong2 *tw, uint64_t q,
                                          uint64_t q4) {
 #pragma unroll
   for (int gsub = 0; gsub < 2; ++gsub) {
     const int g = 2 * tid + gsub;
     uint64_t *x = r + 4 * gsub;
-    const ulonglong2 w1 = __ldg(tw + 512 + g);
+    const ulonglong2 w1 = tw_ld<kSmemTw>(tw + 512 + g);
     ct_bf(x[0], x[2], w1, q, q4);
     ct_bf(x[1], x[3], w1, q, q4);
-    ct_bf(x[0], x[1], __ldg(tw + 1024 + 2 * g), q, q4);
-    ct_bf(x[2], x[3], __ldg(tw + 1024 + 2 * g + 1), q, q4);
+    ct_bf(x[0], x[1], tw_ld<kSmemTw>(tw + 1024 + 2 * g), q, q4);
+    ct_bf(x[2], x[3], tw_ld<kSmemTw>(tw + 1024 + 2 * g + 1), q, q4);
   }
 }
+template <bool kSmemTw = false>
 __device__ __forceinline__ void gs_pass2(uint64_t r[8], int tid, const ulonglong2 *tw, uint64_t q,
                                          uint64_t q4) {
 #pragma unroll
   for (int gsub = 0; gsub < 2; ++gsub) {
     const int g = 2 * tid + gsub;
     uint64_t *x = r + 4 * gsub;
-    gs_bf(x[0], x[1], __ldg(tw + 1024 + 2 * g), q, q4);
-    gs_bf(x[2], x[3], __ldg(tw + 1024 + 2 * g + 1), q, q4);
-    const ulonglong2 w1 = __ldg(tw + 512 + g);
+    gs_bf(x[0], x[1], tw_ld<kSmemTw>(tw + 1024 + 2 * g), q, q4);
+    gs_bf(x[2], x[3], tw_ld<kSmemTw>(tw + 1024 + 2 * g + 1), q, q4);
+    const ulonglong2 w1 = tw_ld<kSmemTw>(tw + 512 + g);
     gs_bf(x[0], x[2], w1, q, q4);
     gs_bf(x[1], x[3], w1, q, q4);
   }
@@ -252,23 +266,24 @@ __device__ __forceinline__ void stg_slot8(uint64_t *base, const uint64_t v[8]) {
 // Forward NTT: r strided (values < 8q) -> r slot (fully reduced).  sa, sb:
 // two shared buffers of kSmemPoly words; all 256 threads of the group take
 // part; ends with a barrier so sa/sb may be reused at once.
+template <bool kSmemTw = false>
 __device__ __forceinline__ void ntt_fwd(uint64_t r[8], uint64_t *sa, uint64_t *sb,
                                         const ulonglong2 *tw, uint64_t q) {
   const int tid = threadIdx.x & (kNttThreads - 1);
   const uint64_t q2 = 2 * q, q4 = 4 * q;
-  ct_pass3(r, tid, 8, tw, q, q4);
+  ct_pass3<kSmemTw>(r, tid, 8, tw, q, q4);
   store_pass(sa, r, tid, 8);
   __syncthreads();
   load_pass(sa, r, tid, 5);
-  ct_pass3(r, tid, 5, tw, q, q4);
+  ct_pass3<kSmemTw>(r, tid, 5, tw, q, q4);
   store_pass(sb, r, tid, 5);
   __syncthreads();
   load_pass(sb, r, tid, 2);
-  ct_pass3(r, tid, 2, tw, q, q4);
+  ct_pass3<kSmemTw>(r, tid, 2, tw, q, q4);
   store_pass(sa, r, tid, 2);
   __syncthreads();
   load_slots(sa, r, tid);
-  ct_pass2(r, tid, tw, q, q4);
+  ct_pass2<kSmemTw>(r, tid, tw, q, q4);
 #pragma unroll
   for (int e = 0; e < 8; ++e) {
     uint64_t v = r[e] >= q4 ? r[e] - q4 : r[e];
@@ -279,24 +294,25 @@ __device__ __forceinline__ void ntt_fwd(uint64_t r[8], uint64_t *sa, uint64_t *s
 }
 
 // Inverse NTT: r slot (values < 4q) -> r strided (fully reduced), scaled by N^-1.
+template <bool kSmemTw = false>
 __device__ __forceinline__ void ntt_inv(uint64_t r[8], uint64_t *sa, uint64_t *sb,
                                         const ulonglong2 *tw, uint64_t q, uint64_t n_inv,
                                         uint64_t n_inv_s) {
   const int tid = threadIdx.x & (kNttThreads - 1);
   const uint64_t q2 = 2 * q, q4 = 4 * q;
-  gs_pass2(r, tid, tw, q, q4);
+  gs_pass2<kSmemTw>(r, tid, tw, q, q4);
   store_slots(sa, r, tid);
   __syncthreads();
   load_pass(sa, r, tid, 2);
-  gs_pass3(r, tid, 2, tw, q, q4);
+  gs_pass3<kSmemTw>(r, tid, 2, tw, q, q4);
   store_pass(sb, r, tid, 2);
   __syncthreads();
   load_pass(sb, r, tid, 5);
-  gs_pass3(r, tid, 5, tw, q, q4);
+  gs_pass3<kSmemTw>(r, tid, 5, tw, q, q4);
   store_pass(sa, r, tid, 5);
   __syncthreads();
   load_pass(sa, r, tid, 8);
-  gs_pass3(r, tid, 8, tw, q, q4);
+  gs_pass3<kSmemTw>(r, tid, 8, tw, q, q4);
 #pragma unroll
   for (int e = 0; e < 8; ++e) {
     uint64_t v = mul_shoup_lazy4(r[e], n_inv, n_inv_s, q);
@@ -311,6 +327,25 @@ __device__ __forceinline__ void ntt_fwd(uint64_t r[8], uint64_t *sa, uint64_t *s
 }
 __device__ __forceinline__ void ntt_inv(uint64_t r[8], uint64_t *sa, uint64_t *sb, const ModTab &M) {
   ntt_inv(r, sa, sb, M.inv, M.q, M.n_inv, M.n_inv_s);
+}
+// forward transform with M's twiddle table staged in shared memory at s_fwd
+__device__ __forceinline__ void ntt_fwd_s(uint64_t r[8], uint64_t *sa, uint64_t *sb,
+                                          const ulonglong2 *s_fwd, const ModTab &M) {
+  ntt_fwd<true>(r, sa, sb, s_fwd, M.q);
+}
+// Stage a 2048-entry twiddle table in shared memory: one 16-byte cp.async
+// per entry, issued now; tw_wait() completes it (every thread of the CTA
+// must call tw_wait before the first transform that reads the copy).
+__device__ __forceinline__ void prefetch_tw(ulonglong2 *dst, const ulonglong2 *src) {
+  for (int i = threadIdx.x; i < kN; i += blockDim.x) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst + i);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src + i) : "memory");
+  }
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+__device__ __forceinline__ void tw_wait() {
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+  __syncthreads();
 }
 
 }  // namespace opir

@@ -140,7 +140,8 @@ __global__ void __launch_bounds__(T, 2) expand_level_kernel(const uint64_t *cur,
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void ext_product_core(const uint64_t *src, const uint64_t *gsw, int l,
                                                  int base_log2, uint64_t *sa, uint64_t *sb,
-                                                 const ModTab &M, uint64_t out[2][8]) {
+                                                 const ulonglong2 *s_fwd, const ModTab &M,
+                                                 uint64_t out[2][8]) {
   const int tid = threadIdx.x;
   const uint64_t mask = (1ULL << base_log2) - 1;
   U128 acc0[8], acc1[8];
@@ -155,7 +156,7 @@ __device__ __forceinline__ void ext_product_core(const uint64_t *src, const uint
       uint64_t d[8];
 #pragma unroll
       for (int e = 0; e < 8; ++e) d[e] = (src[poly * kN + strided_idx(tid, e)] >> sh) & mask;
-      ntt_fwd(d, sa, sb, M);
+      ntt_fwd_s(d, sa, sb, s_fwd, M);
       const uint64_t *g0 = gsw + (size_t)j * 2 * kN, *g1 = g0 + kN;
       uint64_t w0[8], w1[8];
       ldg_slot8(g0, w0);
@@ -183,6 +184,8 @@ __global__ void __launch_bounds__(T, 2) query_to_gsw_kernel(const uint64_t *leav
                                                             int n1, ModTab M, Consts C) {
   extern __shared__ uint64_t smem[];
   uint64_t *sa = smem, *sb = smem + kSmemPoly, *sx = smem + 2 * kSmemPoly;  // sx: [2][N]
+  ulonglong2 *s_fwd = reinterpret_cast<ulonglong2 *>(sx + 2 * kN);
+  prefetch_tw(s_fwd, M.fwd);
   const int tid = threadIdx.x;
   const int j = blockIdx.x, b = blockIdx.y;
   const int l = C.l;
@@ -191,6 +194,7 @@ __global__ void __launch_bounds__(T, 2) query_to_gsw_kernel(const uint64_t *leav
   uint64_t *rgsw = gsw_out + b * gsw_stride + (size_t)dim * 2 * l * 2 * kN;
   // first half: the ciphertext itself in NTT form
   uint64_t *row0 = rgsw + (size_t)kk * 2 * kN;
+  tw_wait();
 #pragma unroll 1
   for (int poly = 0; poly < 2; ++poly) {
     uint64_t r[8];
@@ -200,12 +204,12 @@ __global__ void __launch_bounds__(T, 2) query_to_gsw_kernel(const uint64_t *leav
       r[e] = ct[i];
       sx[i] = r[e];  // own slots only
     }
-    ntt_fwd(r, sa, sb, M);
+    ntt_fwd_s(r, sa, sb, s_fwd, M);
     stg_slot8(row0 + poly * kN, r);
   }
   // second half: external product with RGSW(sk) under the key gadget
   uint64_t out[2][8];
-  ext_product_core(sx, kb.q[b].gsw_key, C.l_key, C.base_log2_key, sa, sb, M, out);
+  ext_product_core(sx, kb.q[b].gsw_key, C.l_key, C.base_log2_key, sa, sb, s_fwd, M, out);
   uint64_t *row1 = rgsw + (size_t)(l + kk) * 2 * kN;
 #pragma unroll
   for (int poly = 0; poly < 2; ++poly) stg_slot8(row1 + poly * kN, out[poly]);
@@ -218,6 +222,8 @@ __global__ void __launch_bounds__(T, 2) fold_kernel(uint64_t *res, size_t res_st
                                                     int half, ModTab M, Consts C) {
   extern __shared__ uint64_t smem[];
   uint64_t *sa = smem, *sb = smem + kSmemPoly, *sd = smem + 2 * kSmemPoly;  // sd: [2][N]
+  ulonglong2 *s_fwd = reinterpret_cast<ulonglong2 *>(sd + 2 * kN);
+  prefetch_tw(s_fwd, M.fwd);
   const int tid = threadIdx.x;
   const int j = blockIdx.x, b = blockIdx.y;
   const uint64_t q = C.q;
@@ -228,8 +234,9 @@ __global__ void __launch_bounds__(T, 2) fold_kernel(uint64_t *res, size_t res_st
     const int i = (i2 >> 3) * kN + strided_idx(tid, i2 & 7);
     sd[i] = sub_mod(yp[i], xp[i], q);  // own slots only
   }
+  tw_wait();
   uint64_t out[2][8];
-  ext_product_core(sd, gsw + b * gsw_stride, C.l, C.base_log2, sa, sb, M, out);
+  ext_product_core(sd, gsw + b * gsw_stride, C.l, C.base_log2, sa, sb, s_fwd, M, out);
   // polynomial 1 waits in shared memory (sd is no longer read) while
   // polynomial 0 is transformed back
 #pragma unroll
@@ -269,6 +276,8 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(T)
   uint64_t *sa = smem, *sb = smem + kSmemPoly;
   uint64_t *s_sig = smem + 2 * kSmemPoly;  // sigma(c1), then sigma(c0) (natural index)
   uint64_t *s_out = s_sig + kN;            // p-CTAs: their inverse transform (natural index)
+  ulonglong2 *s_fwd = reinterpret_cast<ulonglong2 *>(s_out + kN);
+  prefetch_tw(s_fwd, m ? Mp.fwd : Mq.fwd);
   const int tid = threadIdx.x;
   const int node = blockIdx.x >> 2, b = blockIdx.y;
   const int k = 1 << level;
@@ -285,7 +294,7 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(T)
     else
       s_sig[j - kN] = neg_mod(v, q);
   }
-  __syncthreads();
+  tw_wait();
   const ModTab &M = m ? Mp : Mq;
   uint64_t t[8];
 #pragma unroll
@@ -293,7 +302,7 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(T)
     const uint64_t v = s_sig[strided_idx(tid, e)];
     t[e] = (m && v >= p) ? v - p : v;  // q < 2p
   }
-  ntt_fwd(t, sa, sb, M);
+  ntt_fwd_s(t, sa, sb, s_fwd, M);
   const size_t key_off = (size_t)level * 4 * kN + (size_t)(2 * kk + m) * kN;
   {
     // Shoup product with the key's companion: [0, 4 mod), which the inverse
@@ -348,9 +357,9 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(T)
 // MAC of digit polynomials (coefficient form, strided distribution, NTT'd
 // here) with RGSW rows, for both output polynomials; 128-bit sums.
 __device__ __forceinline__ void digit_mac(uint64_t d[8], const uint64_t *row, uint64_t *sa,
-                                          uint64_t *sb, const ModTab &M, U128 acc0[8],
-                                          U128 acc1[8]) {
-  ntt_fwd(d, sa, sb, M);
+                                          uint64_t *sb, const ulonglong2 *s_fwd, const ModTab &M,
+                                          U128 acc0[8], U128 acc1[8]) {
+  ntt_fwd_s(d, sa, sb, s_fwd, M);
   uint64_t w0[8], w1[8];
   ldg_slot8(row, w0);
   ldg_slot8(row + kN, w1);
@@ -358,6 +367,34 @@ __device__ __forceinline__ void digit_mac(uint64_t d[8], const uint64_t *row, ui
   for (int e = 0; e < 8; ++e) {
     mac_to(acc0[e], d[e], w0[e]);
     mac_to(acc1[e], d[e], w1[e]);
+  }
+}
+
+// Sum over cluster ranks 0 .. R-1 of the 8 slots 8 tid .. 8 tid + 7 of
+// `src` (a shared-memory array at the same offset in every CTA), mod q.  All
+// 4R 16-byte remote loads are in flight before the first addition: summing
+// element by element serialised the distributed-shared-memory latency.
+template <int R>
+__device__ __forceinline__ void cluster_sum8(cg::cluster_group &cluster, uint64_t *src, uint64_t q,
+                                             uint64_t sum[8]) {
+  ulonglong2 v[R][4];
+#pragma unroll
+  for (int rr = 0; rr < R; ++rr) {
+    const ulonglong2 *pr = reinterpret_cast<const ulonglong2 *>(
+        cluster.map_shared_rank(src, rr) + slot_idx(threadIdx.x, 0));
+#pragma unroll
+    for (int h = 0; h < 4; ++h) v[rr][h] = pr[h];
+  }
+#pragma unroll
+  for (int h = 0; h < 4; ++h) {
+    uint64_t s0 = v[0][h].x, s1 = v[0][h].y;
+#pragma unroll
+    for (int rr = 1; rr < R; ++rr) {
+      s0 = add_mod(s0, v[rr][h].x, q);
+      s1 = add_mod(s1, v[rr][h].y, q);
+    }
+    sum[2 * h] = s0;
+    sum[2 * h + 1] = s1;
   }
 }
 
@@ -375,6 +412,8 @@ __global__ void __cluster_dims__(kFoldCluster, 1, 1) __launch_bounds__(T)
   extern __shared__ uint64_t smem[];
   uint64_t *sa = smem, *sb = smem + kSmemPoly;
   uint64_t *part = smem + 2 * kSmemPoly;  // [kk][slot]
+  ulonglong2 *s_fwd = reinterpret_cast<ulonglong2 *>(part + 2 * kN);
+  prefetch_tw(s_fwd, M.fwd);
   const int tid = threadIdx.x;
   const int j = blockIdx.x / kFoldCluster, b = blockIdx.y;
   const uint64_t q = C.q;
@@ -395,7 +434,8 @@ __global__ void __cluster_dims__(kFoldCluster, 1, 1) __launch_bounds__(T)
       const int i = poly * kN + strided_idx(tid, e);
       d[e] = (sub_mod(yp[i], xp[i], q) >> sh) & mask;
     }
-    digit_mac(d, rgsw + (size_t)(poly * l + r) * 2 * kN, sa, sb, M, acc0, acc1);
+    if (poly == 0) tw_wait();
+    digit_mac(d, rgsw + (size_t)(poly * l + r) * 2 * kN, sa, sb, s_fwd, M, acc0, acc1);
   }
 #pragma unroll
   for (int e = 0; e < 8; ++e) {
@@ -406,13 +446,7 @@ __global__ void __cluster_dims__(kFoldCluster, 1, 1) __launch_bounds__(T)
   cluster.sync();
   if (r < 2) {
     uint64_t sum[8];
-#pragma unroll
-    for (int e = 0; e < 8; ++e) sum[e] = 0;
-    for (int rr = 0; rr < kFoldCluster; ++rr) {
-      const uint64_t *pr = cluster.map_shared_rank(part, rr) + (size_t)r * kN;
-#pragma unroll
-      for (int e = 0; e < 8; ++e) sum[e] = add_mod(sum[e], pr[slot_idx(tid, e)], q);
-    }
+    cluster_sum8<kFoldCluster>(cluster, part + (size_t)r * kN, q, sum);
     ntt_inv(sum, sa, sb, M);
 #pragma unroll
     for (int e = 0; e < 8; ++e) {
@@ -437,6 +471,8 @@ __global__ void __cluster_dims__(kQtgCluster, 1, 1) __launch_bounds__(T)
   extern __shared__ uint64_t smem[];
   uint64_t *sa = smem, *sb = smem + kSmemPoly;
   uint64_t *part = smem + 2 * kSmemPoly;
+  ulonglong2 *s_fwd = reinterpret_cast<ulonglong2 *>(part + 2 * kN);
+  prefetch_tw(s_fwd, M.fwd);
   const int tid = threadIdx.x;
   const int jct = blockIdx.x / kQtgCluster, b = blockIdx.y;
   const int l = C.l, lk = C.l_key;
@@ -444,6 +480,7 @@ __global__ void __cluster_dims__(kQtgCluster, 1, 1) __launch_bounds__(T)
   const uint64_t q = C.q;
   const uint64_t *ct = leaves + b * leaves_stride + (size_t)(n1 + jct) * 2 * kN;
   uint64_t *rgsw = gsw_out + b * gsw_stride + (size_t)dim * 2 * l * 2 * kN;
+  tw_wait();
   if (r == kQtgCluster - 1) {
     uint64_t *row0 = rgsw + (size_t)kk * 2 * kN;
 #pragma unroll
@@ -451,8 +488,7 @@ __global__ void __cluster_dims__(kQtgCluster, 1, 1) __launch_bounds__(T)
       uint64_t v[8];
 #pragma unroll
       for (int e = 0; e < 8; ++e) v[e] = ct[poly * kN + strided_idx(tid, e)];
-      ntt_fwd(v, sa, sb, M);
-#pragma unroll
+      ntt_fwd_s(v, sa, sb, s_fwd, M);
       stg_slot8(row0 + poly * kN, v);
     }
   } else {
@@ -470,7 +506,7 @@ __global__ void __cluster_dims__(kQtgCluster, 1, 1) __launch_bounds__(T)
         uint64_t d[8];
 #pragma unroll
         for (int e = 0; e < 8; ++e) d[e] = (ct[poly * kN + strided_idx(tid, e)] >> sh) & mask;
-        digit_mac(d, key + (size_t)(poly * lk + level) * 2 * kN, sa, sb, M, acc0, acc1);
+        digit_mac(d, key + (size_t)(poly * lk + level) * 2 * kN, sa, sb, s_fwd, M, acc0, acc1);
       }
     }
 #pragma unroll
@@ -483,14 +519,9 @@ __global__ void __cluster_dims__(kQtgCluster, 1, 1) __launch_bounds__(T)
   cluster.sync();
   if (r < 2) {
     uint64_t *row1 = rgsw + (size_t)(l + kk) * 2 * kN + (size_t)r * kN;
-#pragma unroll
-    for (int e = 0; e < 8; ++e) {
-      const int si = slot_idx(tid, e);
-      uint64_t sum = 0;
-      for (int rr = 0; rr < kQtgCluster - 1; ++rr)
-        sum = add_mod(sum, cluster.map_shared_rank(part, rr)[(size_t)r * kN + si], q);
-      row1[si] = sum;
-    }
+    uint64_t sum[8];
+    cluster_sum8<kQtgCluster - 1>(cluster, part + (size_t)r * kN, q, sum);
+    stg_slot8(row1, sum);
   }
   cluster.sync();
 }
@@ -508,9 +539,10 @@ int g_qtg_threshold = 40;
 
 constexpr size_t kExpandSmem = (2 * kSmemPoly + 4 * kN) * sizeof(uint64_t);
 
-constexpr size_t kClusterSmem = (2 * kSmemPoly + 2 * kN) * sizeof(uint64_t);
+// plus the staged forward twiddle table (2048 x 16 bytes) at the end
+constexpr size_t kClusterSmem = (2 * kSmemPoly + 2 * kN) * sizeof(uint64_t) + kN * sizeof(ulonglong2);
 // one-CTA fold and RGSW reconstruction: transform buffers + the source ciphertext
-constexpr size_t kExtSmem = (2 * kSmemPoly + 2 * kN) * sizeof(uint64_t);
+constexpr size_t kExtSmem = (2 * kSmemPoly + 2 * kN) * sizeof(uint64_t) + kN * sizeof(ulonglong2);
 
 cudaError_t init_kernel_attributes() {
   cudaError_t e;
