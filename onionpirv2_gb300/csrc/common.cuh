@@ -257,6 +257,16 @@ __device__ __forceinline__ void ldg_slot8(const uint64_t *base, uint64_t v[8]) {
     v[2 * j + 1] = t.y;
   }
 }
+// the slot layout of ldg_slot8 from shared memory
+__device__ __forceinline__ void lds_slot8(const uint64_t *base, uint64_t v[8]) {
+  const ulonglong2 *p = reinterpret_cast<const ulonglong2 *>(base) + 4 * (threadIdx.x & (kNttThreads - 1));
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const ulonglong2 t = p[j];
+    v[2 * j] = t.x;
+    v[2 * j + 1] = t.y;
+  }
+}
 __device__ __forceinline__ void stg_slot8(uint64_t *base, const uint64_t v[8]) {
   ulonglong2 *p = reinterpret_cast<ulonglong2 *>(base) + 4 * (threadIdx.x & (kNttThreads - 1));
 #pragma unroll
@@ -343,8 +353,29 @@ __device__ __forceinline__ void prefetch_tw(ulonglong2 *dst, const ulonglong2 *s
   }
   asm volatile("cp.async.commit_group;\n" ::: "memory");
 }
+// the same for `words` 64-bit words (even, both addresses 16-byte aligned)
+__device__ __forceinline__ void prefetch_words(uint64_t *dst, const uint64_t *src, int words) {
+  for (int i = 2 * threadIdx.x; i < words; i += 2 * blockDim.x) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst + i);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src + i) : "memory");
+  }
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+// inverse transform with M's inverse twiddle table staged at s_inv
+__device__ __forceinline__ void ntt_inv_s(uint64_t r[8], uint64_t *sa, uint64_t *sb,
+                                          const ulonglong2 *s_inv, const ModTab &M) {
+  ntt_inv<true>(r, sa, sb, s_inv, M.q, M.n_inv, M.n_inv_s);
+}
 __device__ __forceinline__ void tw_wait() {
   asm volatile("cp.async.wait_all;\n" ::: "memory");
+  __syncthreads();
+}
+// wait until at most `Pending` of this thread's most recent staging groups
+// are still in flight (groups complete in commit order), then make every
+// thread's completed copies visible to the CTA
+template <int Pending>
+__device__ __forceinline__ void stage_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(Pending) : "memory");
   __syncthreads();
 }
 

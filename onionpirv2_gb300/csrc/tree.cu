@@ -265,6 +265,9 @@ __global__ void __launch_bounds__(T, 2) fold_kernel(uint64_t *res, size_t res_st
 // The q-CTA kk then combines with the p-CTA kk through distributed shared
 // memory and writes polynomial kk of both children (polynomial kk of c'
 // depends on key polynomial kk only).
+// kStage: also stage the inverse twiddles and the key polynomial with its
+// companions in shared memory (one CTA per SM; for launches of one wave).
+template <bool kStage>
 __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(T)
     expand_cluster_kernel(const uint64_t *cur, uint64_t *nxt, size_t in_stride, size_t out_stride,
                           const __grid_constant__ KeyBatch kb, int level, ModTab Mq, ModTab Mp,
@@ -276,10 +279,19 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(T)
   uint64_t *sa = smem, *sb = smem + kSmemPoly;
   uint64_t *s_sig = smem + 2 * kSmemPoly;  // sigma(c1), then sigma(c0) (natural index)
   uint64_t *s_out = s_sig + kN;            // p-CTAs: their inverse transform (natural index)
-  ulonglong2 *s_fwd = reinterpret_cast<ulonglong2 *>(s_out + kN);
-  prefetch_tw(s_fwd, m ? Mp.fwd : Mq.fwd);
-  const int tid = threadIdx.x;
+  ulonglong2 *s_fwd = reinterpret_cast<ulonglong2 *>(s_out + kN), *s_inv = s_fwd + kN;
+  uint64_t *s_key = reinterpret_cast<uint64_t *>(s_inv + kN);  // key polynomial, companions
   const int node = blockIdx.x >> 2, b = blockIdx.y;
+  const size_t key_off = (size_t)level * 4 * kN + (size_t)(2 * kk + m) * kN;
+  // staging groups, completed in this order: forward twiddles, key,
+  // companions, inverse twiddles
+  prefetch_tw(s_fwd, m ? Mp.fwd : Mq.fwd);
+  if constexpr (kStage) {
+    prefetch_words(s_key, kb.q[b].galois + key_off, kN);
+    prefetch_words(s_key + kN, kb.q[b].galois_s + key_off, kN);
+    prefetch_tw(s_inv, m ? Mp.inv : Mq.inv);
+  }
+  const int tid = threadIdx.x;
   const int k = 1 << level;
   const uint64_t g = (uint64_t)(kN / k + 1);
   const uint64_t q = C.q, p = C.p;
@@ -294,7 +306,10 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(T)
     else
       s_sig[j - kN] = neg_mod(v, q);
   }
-  tw_wait();
+  if constexpr (kStage)
+    stage_wait<3>();
+  else
+    tw_wait();
   const ModTab &M = m ? Mp : Mq;
   uint64_t t[8];
 #pragma unroll
@@ -303,17 +318,27 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(T)
     t[e] = (m && v >= p) ? v - p : v;  // q < 2p
   }
   ntt_fwd_s(t, sa, sb, s_fwd, M);
-  const size_t key_off = (size_t)level * 4 * kN + (size_t)(2 * kk + m) * kN;
   {
     // Shoup product with the key's companion: [0, 4 mod), which the inverse
     // transform takes
     uint64_t kv[8], ks[8];
-    ldg_slot8(kb.q[b].galois + key_off, kv);
-    ldg_slot8(kb.q[b].galois_s + key_off, ks);
+    if constexpr (kStage) {
+      stage_wait<1>();
+      lds_slot8(s_key, kv);
+      lds_slot8(s_key + kN, ks);
+    } else {
+      ldg_slot8(kb.q[b].galois + key_off, kv);
+      ldg_slot8(kb.q[b].galois_s + key_off, ks);
+    }
 #pragma unroll
     for (int e = 0; e < 8; ++e) t[e] = mul_shoup_lazy4(t[e], kv[e], ks[e], M.q);
   }
-  ntt_inv(t, sa, sb, M);
+  if constexpr (kStage) {
+    stage_wait<0>();
+    ntt_inv_s(t, sa, sb, s_inv, M);
+  } else {
+    ntt_inv(t, sa, sb, M);
+  }
   if (m == 1) {
 #pragma unroll
     for (int e = 0; e < 8; ++e) s_out[strided_idx(tid, e)] = t[e];
@@ -412,8 +437,7 @@ __global__ void __cluster_dims__(kFoldCluster, 1, 1) __launch_bounds__(T)
   extern __shared__ uint64_t smem[];
   uint64_t *sa = smem, *sb = smem + kSmemPoly;
   uint64_t *part = smem + 2 * kSmemPoly;  // [kk][slot]
-  ulonglong2 *s_fwd = reinterpret_cast<ulonglong2 *>(part + 2 * kN);
-  prefetch_tw(s_fwd, M.fwd);
+  ulonglong2 *s_fwd = reinterpret_cast<ulonglong2 *>(part + 2 * kN);  // staged by cp.async
   const int tid = threadIdx.x;
   const int j = blockIdx.x / kFoldCluster, b = blockIdx.y;
   const uint64_t q = C.q;
@@ -421,6 +445,7 @@ __global__ void __cluster_dims__(kFoldCluster, 1, 1) __launch_bounds__(T)
   uint64_t *xp = res + b * res_stride + (size_t)j * 2 * kN;
   const uint64_t *yp = res + b * res_stride + (size_t)(j + half) * 2 * kN;
   const uint64_t *rgsw = gsw + b * gsw_stride;
+  prefetch_tw(s_fwd, M.fwd);
   const int sh = (l - 1 - r) * C.base_log2;
   const uint64_t mask = (1ULL << C.base_log2) - 1;
   U128 acc0[8], acc1[8];
@@ -541,7 +566,13 @@ constexpr size_t kExpandSmem = (2 * kSmemPoly + 4 * kN) * sizeof(uint64_t);
 
 // plus the staged forward twiddle table (2048 x 16 bytes) at the end
 constexpr size_t kClusterSmem = (2 * kSmemPoly + 2 * kN) * sizeof(uint64_t) + kN * sizeof(ulonglong2);
-// one-CTA fold and RGSW reconstruction: transform buffers + the source ciphertext
+// expansion cluster with kStage: plus the inverse table and a key polynomial
+// with its companions
+constexpr size_t kExpandClusterSmem = kClusterSmem + kN * sizeof(ulonglong2) + 2 * kN * sizeof(uint64_t);
+static_assert(kExpandClusterSmem <= 227 * 1024, "shared memory per CTA");
+int g_sms = 152;
+// one-CTA fold and RGSW reconstruction: transform buffers + the source
+// ciphertext + the staged forward twiddles
 constexpr size_t kExtSmem = (2 * kSmemPoly + 2 * kN) * sizeof(uint64_t) + kN * sizeof(ulonglong2);
 
 cudaError_t init_kernel_attributes() {
@@ -555,13 +586,22 @@ cudaError_t init_kernel_attributes() {
   if ((e = cudaFuncSetAttribute(query_to_gsw_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)kExtSmem)) != cudaSuccess)
     return e;
-  if ((e = cudaFuncSetAttribute(expand_cluster_kernel,
+  if ((e = cudaFuncSetAttribute(expand_cluster_kernel<true>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)kExpandClusterSmem)) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(expand_cluster_kernel<false>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)kClusterSmem)) != cudaSuccess)
     return e;
   if ((e = cudaFuncSetAttribute(fold_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)kClusterSmem)) != cudaSuccess)
     return e;
+  {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+  }
   if ((e = cudaFuncSetAttribute(query_to_gsw_cluster_kernel,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)kClusterSmem)) != cudaSuccess)
@@ -584,8 +624,12 @@ void launch_expand_level(const uint64_t *cur, uint64_t *nxt, size_t in_stride, s
     const int nb = batch - b0 < kMaxKeyBatch ? batch - b0 : kMaxKeyBatch;
     KeyBatch kb;
     for (int i = 0; i < nb; ++i) kb.q[i] = qd[b0 + i];
-    if (live_nodes * nb < g_expand_threshold)
-      expand_cluster_kernel<<<dim3(4 * live_nodes, nb), T, kClusterSmem, s>>>(
+    if (live_nodes * nb < g_expand_threshold && 4 * live_nodes * nb <= g_sms)
+      expand_cluster_kernel<true><<<dim3(4 * live_nodes, nb), T, kExpandClusterSmem, s>>>(
+          cur + b0 * in_stride, nxt + b0 * out_stride, in_stride, out_stride, kb, level, Mq, Mp,
+          C);
+    else if (live_nodes * nb < g_expand_threshold)
+      expand_cluster_kernel<false><<<dim3(4 * live_nodes, nb), T, kClusterSmem, s>>>(
           cur + b0 * in_stride, nxt + b0 * out_stride, in_stride, out_stride, kb, level, Mq, Mp,
           C);
     else
