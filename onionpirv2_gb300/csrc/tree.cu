@@ -487,7 +487,7 @@ __global__ void __cluster_dims__(kFoldCluster, 1, 1) __launch_bounds__(T)
 // handles key digit levels 2r and 2r+1 of both polynomials; CTAs 0 and 1 add
 // the partials of output polynomial 0 / 1 into the second-half row.
 constexpr int kQtgCluster = 6;
-__global__ void __cluster_dims__(kQtgCluster, 1, 1) __launch_bounds__(T)
+__global__ void __cluster_dims__(kQtgCluster, 1, 1) __launch_bounds__(T, 2)
     query_to_gsw_cluster_kernel(const uint64_t *leaves, size_t leaves_stride, uint64_t *gsw_out,
                                 size_t gsw_stride, const __grid_constant__ KeyBatch kb, int n1,
                                 ModTab M, Consts C) {
@@ -522,9 +522,9 @@ __global__ void __cluster_dims__(kQtgCluster, 1, 1) __launch_bounds__(T)
     U128 acc0[8], acc1[8];
 #pragma unroll
     for (int e = 0; e < 8; ++e) acc0[e] = acc1[e] = U128{0, 0};
-#pragma unroll
+#pragma unroll 1
     for (int poly = 0; poly < 2; ++poly) {
-#pragma unroll
+#pragma unroll 1
       for (int h = 0; h < 2; ++h) {
         const int level = 2 * r + h;          // row index within the poly's l_key rows
         const int sh = (lk - 1 - level) * C.base_log2_key;
@@ -555,10 +555,12 @@ __global__ void __cluster_dims__(kQtgCluster, 1, 1) __launch_bounds__(T)
 // one-CTA form at or above.  From per-launch timings on GB300 (the one-CTA
 // forms at two CTAs per SM): the cluster expansion wins below ~128 nodes
 // (128 and 256 measured alike, 1024 and 64 slower), the cluster fold on the
-// narrow levels (< 48 pairs), RGSW reconstruction is even.
+// narrow levels (< 48 pairs), the cluster RGSW reconstruction for one
+// query's 45 or 55 ciphertexts (80 -> 45 us; it needs two CTAs per SM so
+// that its 6-CTA clusters fit one wave).
 int g_expand_threshold = 128;
 int g_fold_threshold = 48;
-int g_qtg_threshold = 40;
+int g_qtg_threshold = 64;
 
 }  // namespace
 
@@ -608,7 +610,7 @@ cudaError_t init_kernel_attributes() {
     return e;
   g_expand_threshold = 128;
   g_fold_threshold = 48;
-  g_qtg_threshold = 40;
+  g_qtg_threshold = 64;
   if (const char *v = getenv("OPIR_CLUSTER_THRESHOLD"))  // one threshold for all (tests, sweeps)
     g_expand_threshold = g_fold_threshold = g_qtg_threshold = atoi(v);
   if (const char *v = getenv("OPIR_EXPAND_THRESHOLD")) g_expand_threshold = atoi(v);
