@@ -482,6 +482,68 @@ __global__ void __cluster_dims__(kFoldCluster, 1, 1) __launch_bounds__(T)
   cluster.sync();
 }
 
+// Folding, 2 CTAs per ciphertext pair (the wide levels of few queries): CTA
+// a decomposes polynomial a of y - x into its l digits, transforms them and
+// multiplies them with RGSW rows a l .. a l + l - 1, leaving partial sums of
+// both output polynomials (reduced mod q) in shared memory; CTA a then adds
+// the two partials of output polynomial a, transforms back and adds x.  Half
+// the dependent transforms of the one-CTA form per pair.
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(T, 2)
+    fold_pair_kernel(uint64_t *res, size_t res_stride, const uint64_t *gsw, size_t gsw_stride,
+                     int half, ModTab M, Consts C) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int a = (int)cluster.block_rank();
+  extern __shared__ uint64_t smem[];
+  uint64_t *sa = smem, *sb = smem + kSmemPoly;
+  uint64_t *part = smem + 2 * kSmemPoly;  // [output polynomial][slot]
+  ulonglong2 *s_fwd = reinterpret_cast<ulonglong2 *>(part + 2 * kN);  // staged by cp.async
+  prefetch_tw(s_fwd, M.fwd);
+  const int tid = threadIdx.x;
+  const int j = blockIdx.x >> 1, b = blockIdx.y;
+  const uint64_t q = C.q;
+  const int l = C.l;
+  uint64_t *xp = res + b * res_stride + (size_t)j * 2 * kN;
+  const uint64_t *yp = res + b * res_stride + (size_t)(j + half) * 2 * kN;
+  const uint64_t *rgsw = gsw + b * gsw_stride;
+  const uint64_t mask = (1ULL << C.base_log2) - 1;
+  // polynomial a of y - x in `part` (each thread reads back only its own
+  // strided slots; the transforms' barriers order the last reads before the
+  // partial sums overwrite it)
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const int i = strided_idx(tid, e);
+    part[i] = sub_mod(yp[a * kN + i], xp[a * kN + i], q);
+  }
+  U128 acc0[8], acc1[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) acc0[e] = acc1[e] = U128{0, 0};
+  tw_wait();
+#pragma unroll 1
+  for (int pp = l - 1; pp >= 0; --pp) {
+    const int sh = pp * C.base_log2;
+    uint64_t d[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) d[e] = (part[strided_idx(tid, e)] >> sh) & mask;
+    digit_mac(d, rgsw + (size_t)(a * l + (l - 1 - pp)) * 2 * kN, sa, sb, s_fwd, M, acc0, acc1);
+  }
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const int si = slot_idx(tid, e);
+    part[si] = barrett128(acc0[e], q, M.mu_lo, M.mu_hi);
+    part[kN + si] = barrett128(acc1[e], q, M.mu_lo, M.mu_hi);
+  }
+  cluster.sync();
+  uint64_t sum[8];
+  cluster_sum8<2>(cluster, part + (size_t)a * kN, q, sum);
+  ntt_inv(sum, sa, sb, M);
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const int i = a * kN + strided_idx(tid, e);
+    xp[i] = add_mod(xp[i], sum[e], q);
+  }
+  cluster.sync();
+}
+
 // RGSW reconstruction (query_to_gsw), 6 CTAs per ciphertext (l_key = 10):
 // CTA 5 writes the first-half row (the ciphertext in NTT form); CTA r < 5
 // handles key digit levels 2r and 2r+1 of both polynomials; CTAs 0 and 1 add
@@ -560,6 +622,10 @@ __global__ void __cluster_dims__(kQtgCluster, 1, 1) __launch_bounds__(T, 2)
 // that its 6-CTA clusters fit one wave).
 int g_expand_threshold = 128;
 int g_fold_threshold = 48;
+// pair form (2 CTAs per pair) from g_fold_threshold up to this many pairs:
+// one query's 64- and 128-pair levels (folding 0.314 -> 0.298 ms; the
+// 256-pair level and 32-query batches measured slower in the pair form)
+int g_pair_threshold = 130;
 int g_qtg_threshold = 64;
 
 }  // namespace
@@ -599,6 +665,9 @@ cudaError_t init_kernel_attributes() {
   if ((e = cudaFuncSetAttribute(fold_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)kClusterSmem)) != cudaSuccess)
     return e;
+  if ((e = cudaFuncSetAttribute(fold_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)kClusterSmem)) != cudaSuccess)
+    return e;
   {
     int dev = 0;
     cudaGetDevice(&dev);
@@ -610,12 +679,14 @@ cudaError_t init_kernel_attributes() {
     return e;
   g_expand_threshold = 128;
   g_fold_threshold = 48;
+  g_pair_threshold = 130;
   g_qtg_threshold = 64;
   if (const char *v = getenv("OPIR_CLUSTER_THRESHOLD"))  // one threshold for all (tests, sweeps)
     g_expand_threshold = g_fold_threshold = g_qtg_threshold = atoi(v);
   if (const char *v = getenv("OPIR_EXPAND_THRESHOLD")) g_expand_threshold = atoi(v);
   if (const char *v = getenv("OPIR_FOLD_THRESHOLD")) g_fold_threshold = atoi(v);
   if (const char *v = getenv("OPIR_QTG_THRESHOLD")) g_qtg_threshold = atoi(v);
+  if (const char *v = getenv("OPIR_PAIR_THRESHOLD")) g_pair_threshold = atoi(v);
   return cudaSuccess;
 }
 
@@ -665,6 +736,9 @@ void launch_fold(uint64_t *res, size_t res_stride, const uint64_t *gsw, size_t g
   if (C.l == kFoldCluster && half * batch < g_fold_threshold)
     fold_cluster_kernel<<<dim3(kFoldCluster * half, batch), T, kClusterSmem, s>>>(
         res, res_stride, gsw, gsw_stride, half, Mq, C);
+  else if (half * batch < g_pair_threshold)
+    fold_pair_kernel<<<dim3(2 * half, batch), T, kClusterSmem, s>>>(res, res_stride, gsw,
+                                                                     gsw_stride, half, Mq, C);
   else
     fold_kernel<<<dim3(half, batch), T, kExtSmem, s>>>(res, res_stride, gsw, gsw_stride, half, Mq,
                                                        C);

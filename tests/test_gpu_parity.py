@@ -192,12 +192,14 @@ def test_scan_configs_and_shapes(oracle_lib, gpu_lib, monkeypatch, shape, cfg):
     server.close()
 
 
-@pytest.mark.parametrize("threshold", [0, 1 << 30])
-def test_one_cta_and_cluster_tree_forms(oracle_lib, gpu_lib, monkeypatch, threshold):
+@pytest.mark.parametrize("threshold,pair", [(0, 0), (1 << 30, 0), (0, 1 << 30)])
+def test_one_cta_and_cluster_tree_forms(oracle_lib, gpu_lib, monkeypatch, threshold, pair):
     """Expansion, RGSW reconstruction and folding give the oracle's results
-    in both kernel forms (one CTA per ciphertext, or a cluster of CTAs)."""
+    in every kernel form (one CTA per ciphertext, a cluster of CTAs, and for
+    folding a pair of CTAs per ciphertext pair)."""
     from onionpirv2_gb300 import PirParams, PirServer
     monkeypatch.setenv("OPIR_CLUSTER_THRESHOLD", str(threshold))
+    monkeypatch.setenv("OPIR_PAIR_THRESHOLD", str(pair))
     o = oracle_lib.Oracle(4096, 256)
     P = o.P
     server = PirServer(PirParams(num_entries=4096, max_fst_dim=256))
