@@ -74,6 +74,8 @@ def parse():
                     help="serving benchmark alone: three resident databases (4096, 262,144 and "
                          "2,097,152 plaintexts), 512 clients under a key budget, Poisson arrivals")
     ap.add_argument("--serve-clients", type=int, default=512)
+    ap.add_argument("--serve-light-rate", type=float, default=700.0,
+                    help="--serve: a second leg at this offered rate, for latency below capacity")
     ap.add_argument("--batch-sweep", default=None,
                     help="comma-separated batch sizes: queries/s of every first-dimension "
                          "engine at each size (one JSON line per size)")
@@ -317,6 +319,15 @@ def serve_main(args):
     stats, n, same, decoded = serve_leg(server, qsets, args.serve_rate, args.serve_seconds,
                                         seed=11, threads=threads)
     t2 = time.time()
+    light = None
+    if args.serve_light_rate > 0:
+        lstats, ln, lsame, ldecoded = serve_leg(server, qsets, args.serve_light_rate,
+                                                args.serve_seconds, seed=12, threads=threads)
+        light = {"offered_qps": args.serve_light_rate, "arrivals": ln,
+                 "queries_per_s": lstats["queries_per_s"], "p50_ms": lstats["p50_ms"],
+                 "p99_ms": lstats["p99_ms"], "mean_batch": lstats["mean_batch"],
+                 "failed": lstats["failed"], "bit_exact_sample": lsame,
+                 "entries_decoded": f"{ldecoded}/{ln}"}
     clocks.stop()
     resident, nslots = server.resident_clients()
     line = {
@@ -336,6 +347,7 @@ def serve_main(args):
         "batches": stats["batches"], "mean_batch": stats["mean_batch"],
         "resident_clients": resident, "bit_exact_sample": same, "ingest_s": ingest_s,
         "entries_decoded": f"{decoded}/{n}",
+        "light_load": light,
         "client": {"threads": threads, "clients": args.serve_clients,
                    "keygen_s": keygen_s,
                    "keys_per_s": args.serve_clients / keygen_s,
@@ -451,6 +463,15 @@ def cpu_baseline(params, workload, clients, queries, gpu_resps, nq):
         times.append(time.perf_counter() - t)
         if gpu_resps is not None and i < len(gpu_resps):
             match &= bool(np.array_equal(resp, gpu_resps[i]))
+    # the reference itself is single-threaded: one more query on one thread
+    orc.set_threads(1)
+    gk = clients[0][0]
+    t = time.perf_counter()
+    resp1, _, _, _ = o.make_query_server(db, gk, gsw_ntt[0], queries[0])
+    one_s = time.perf_counter() - t
+    orc.set_threads(threads)
+    if gpu_resps is not None and len(gpu_resps):
+        match &= bool(np.array_equal(resp1, gpu_resps[0]))
     del db
     qps = nq / sum(times)
     return {
@@ -458,7 +479,28 @@ def cpu_baseline(params, workload, clients, queries, gpu_resps, nq):
         "sample": (f"{nq} full queries (all stages) on the {workload} database "
                    f"({params.get_num_pt()} plaintexts), {threads} threads; "
                    f"database build {build_s:.1f} s untimed"),
+        "single_thread_value": 1.0 / one_s,
+        "cpu": host_cpu_model(),
     }, match
+
+
+def host_cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
 
 
 def run_reference(args):
@@ -503,7 +545,8 @@ def run_reference(args):
         "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": threads, "kind": "port",
                          "sample": f"{steps} full queries after {warm} warm-up, "
                                    f"{threads} threads (CPU restatement of the reference "
-                                   "server; the reference needs the absent SEAL fork)"},
+                                   "server; the reference needs the absent SEAL fork)",
+                         "cpu": host_cpu_model()},
         "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
