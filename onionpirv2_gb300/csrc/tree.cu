@@ -379,6 +379,97 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(T)
   cluster.sync();
 }
 
+// Expansion, 2 CTAs per tree node (levels too wide for the 4-CTA cluster to
+// fit one wave, too narrow to fill the GPU with one CTA per node): CTA m
+// handles modulus m (0 = q, 1 = p) for both key polynomials:
+// INTT_m(NTT_m(sigma(c1)) * K[kk][m]), kk = 0, 1 -- three dependent transforms
+// instead of the one-CTA form's six.  CTA m then writes polynomial kk = m of
+// both children from its own and its peer's results (distributed shared
+// memory); sigma(c0) is gathered through the inverse automorphism.
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(T, 2)
+    expand_pair_kernel(const uint64_t *cur, uint64_t *nxt, size_t in_stride, size_t out_stride,
+                       const __grid_constant__ KeyBatch kb, int level, ModTab Mq, ModTab Mp,
+                       Consts C) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int m = (int)cluster.block_rank();
+  extern __shared__ uint64_t smem[];
+  uint64_t *sa = smem, *sb = smem + kSmemPoly;
+  uint64_t *s_sig = smem + 2 * kSmemPoly;  // sigma(c1), then the kk = 0 result (natural index)
+  ulonglong2 *s_fwd = reinterpret_cast<ulonglong2 *>(s_sig + kN);  // staged by cp.async
+  const ModTab &M = m ? Mp : Mq;
+  prefetch_tw(s_fwd, M.fwd);
+  const int tid = threadIdx.x;
+  const int node = blockIdx.x >> 1, b = blockIdx.y;
+  const int k = 1 << level;
+  const uint64_t g = (uint64_t)(kN / k + 1);
+  const uint64_t q = C.q, p = C.p;
+  const uint64_t *ci = cur + b * in_stride + (size_t)node * 2 * kN;
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const int i = strided_idx(tid, e);
+    const uint32_t j = (uint32_t)(((uint64_t)i * g) & (2 * kN - 1));
+    const uint64_t v = ci[kN + i];
+    if (j < (uint32_t)kN)
+      s_sig[j] = v;
+    else
+      s_sig[j - kN] = neg_mod(v, q);
+  }
+  tw_wait();
+  uint64_t t[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const uint64_t v = s_sig[strided_idx(tid, e)];
+    t[e] = (m && v >= p) ? v - p : v;  // q < 2p
+  }
+  ntt_fwd_s(t, sa, sb, s_fwd, M);  // its barriers end every read of sigma(c1)
+  const uint64_t *key = kb.q[b].galois + (size_t)level * 4 * kN;
+  const uint64_t *key_s = kb.q[b].galois_s + (size_t)level * 4 * kN;
+#pragma unroll 1
+  for (int kk = 0; kk < 2; ++kk) {
+    uint64_t a[8], as[8];
+    ldg_slot8(key + (size_t)(2 * kk + m) * kN, a);
+    ldg_slot8(key_s + (size_t)(2 * kk + m) * kN, as);
+#pragma unroll
+    for (int e = 0; e < 8; ++e) a[e] = mul_shoup_lazy4(t[e], a[e], as[e], M.q);
+    ntt_inv(a, sa, sb, M);  // ends with a barrier: sa is free afterwards
+    uint64_t *dst = kk == 0 ? s_sig : sa;  // result of key polynomial kk
+#pragma unroll
+    for (int e = 0; e < 8; ++e) dst[strided_idx(tid, e)] = a[e];
+  }
+  cluster.sync();
+  // this CTA writes polynomial kk = m of both children
+  const int kk = m;
+  const uint64_t *xq = kk == 0 ? cluster.map_shared_rank(s_sig, 0) : cluster.map_shared_rank(sa, 0);
+  const uint64_t *xp = kk == 0 ? cluster.map_shared_rank(s_sig, 1) : cluster.map_shared_rank(sa, 1);
+  uint64_t ginv = g;  // g^-1 mod 2N (g odd): Newton steps double the correct low bits
+#pragma unroll
+  for (int it = 0; it < 4; ++it) ginv *= 2 - g * ginv;
+  uint64_t *ce = nxt + b * out_stride + (size_t)(2 * node) * 2 * kN + (size_t)kk * kN;
+  uint64_t *co = ce + 2 * kN;
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const int i = strided_idx(tid, e);
+    const uint64_t rr = add_mod(xp[i], C.p_half, p);
+    const uint64_t v = mul_shoup(sub_mod(add_mod(xq[i], C.p_half_mod_q, q), rr, q), C.p_inv_q,
+                                 C.p_inv_q_s, q);
+    uint64_t cp = v;
+    if (kk == 0) {
+      // sigma(c0)[i]: coefficient s = i g^-1 mod 2N of c0, negated when s >= N
+      const uint32_t sidx = (uint32_t)(((uint64_t)i * ginv) & (2 * kN - 1));
+      const uint64_t s0 = sidx < (uint32_t)kN ? ci[sidx] : neg_mod(ci[sidx - kN], q);
+      cp = add_mod(s0, v, q);
+    }
+    const uint64_t x = ci[(size_t)kk * kN + i];
+    ce[i] = add_mod(x, cp, q);
+    const uint64_t d = sub_mod(x, cp, q);
+    if (i >= k)
+      co[i - k] = d;
+    else
+      co[kN - k + i] = neg_mod(d, q);
+  }
+  cluster.sync();
+}
+
 // MAC of digit polynomials (coefficient form, strided distribution, NTT'd
 // here) with RGSW rows, for both output polynomials; 128-bit sums.
 __device__ __forceinline__ void digit_mac(uint64_t d[8], const uint64_t *row, uint64_t *sa,
@@ -626,6 +717,10 @@ int g_fold_threshold = 48;
 // one query's 64- and 128-pair levels (folding 0.314 -> 0.298 ms; the
 // 256-pair level and 32-query batches measured slower in the pair form)
 int g_pair_threshold = 130;
+// expansion pair form (2 CTAs per node) from g_expand_threshold up to this
+// many nodes per launch: one query's 140-node level (expansion 0.223 ->
+// 0.212 ms; its 279-node level and 4- or 32-query batches were slower)
+int g_expand_pair_threshold = 150;
 int g_qtg_threshold = 64;
 
 }  // namespace
@@ -636,6 +731,8 @@ constexpr size_t kExpandSmem = (2 * kSmemPoly + 4 * kN) * sizeof(uint64_t);
 constexpr size_t kClusterSmem = (2 * kSmemPoly + 2 * kN) * sizeof(uint64_t) + kN * sizeof(ulonglong2);
 // expansion cluster with kStage: plus the inverse table and a key polynomial
 // with its companions
+// expansion pair: transform buffers, sigma(c1), the staged forward twiddles
+constexpr size_t kExpandPairSmem = (2 * kSmemPoly + kN) * sizeof(uint64_t) + kN * sizeof(ulonglong2);
 constexpr size_t kExpandClusterSmem = kClusterSmem + kN * sizeof(ulonglong2) + 2 * kN * sizeof(uint64_t);
 static_assert(kExpandClusterSmem <= 227 * 1024, "shared memory per CTA");
 int g_sms = 152;
@@ -668,6 +765,9 @@ cudaError_t init_kernel_attributes() {
   if ((e = cudaFuncSetAttribute(fold_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)kClusterSmem)) != cudaSuccess)
     return e;
+  if ((e = cudaFuncSetAttribute(expand_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)kExpandPairSmem)) != cudaSuccess)
+    return e;
   {
     int dev = 0;
     cudaGetDevice(&dev);
@@ -680,6 +780,7 @@ cudaError_t init_kernel_attributes() {
   g_expand_threshold = 128;
   g_fold_threshold = 48;
   g_pair_threshold = 130;
+  g_expand_pair_threshold = 150;
   g_qtg_threshold = 64;
   if (const char *v = getenv("OPIR_CLUSTER_THRESHOLD"))  // one threshold for all (tests, sweeps)
     g_expand_threshold = g_fold_threshold = g_qtg_threshold = atoi(v);
@@ -687,6 +788,7 @@ cudaError_t init_kernel_attributes() {
   if (const char *v = getenv("OPIR_FOLD_THRESHOLD")) g_fold_threshold = atoi(v);
   if (const char *v = getenv("OPIR_QTG_THRESHOLD")) g_qtg_threshold = atoi(v);
   if (const char *v = getenv("OPIR_PAIR_THRESHOLD")) g_pair_threshold = atoi(v);
+  if (const char *v = getenv("OPIR_EXPAND_PAIR_THRESHOLD")) g_expand_pair_threshold = atoi(v);
   return cudaSuccess;
 }
 
@@ -703,6 +805,10 @@ void launch_expand_level(const uint64_t *cur, uint64_t *nxt, size_t in_stride, s
           C);
     else if (live_nodes * nb < g_expand_threshold)
       expand_cluster_kernel<false><<<dim3(4 * live_nodes, nb), T, kClusterSmem, s>>>(
+          cur + b0 * in_stride, nxt + b0 * out_stride, in_stride, out_stride, kb, level, Mq, Mp,
+          C);
+    else if (live_nodes * nb < g_expand_pair_threshold)
+      expand_pair_kernel<<<dim3(2 * live_nodes, nb), T, kExpandPairSmem, s>>>(
           cur + b0 * in_stride, nxt + b0 * out_stride, in_stride, out_stride, kb, level, Mq, Mp,
           C);
     else

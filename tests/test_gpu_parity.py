@@ -196,10 +196,11 @@ def test_scan_configs_and_shapes(oracle_lib, gpu_lib, monkeypatch, shape, cfg):
 def test_one_cta_and_cluster_tree_forms(oracle_lib, gpu_lib, monkeypatch, threshold, pair):
     """Expansion, RGSW reconstruction and folding give the oracle's results
     in every kernel form (one CTA per ciphertext, a cluster of CTAs, and for
-    folding a pair of CTAs per ciphertext pair)."""
+    expansion and folding a pair of CTAs per node / ciphertext pair)."""
     from onionpirv2_gb300 import PirParams, PirServer
     monkeypatch.setenv("OPIR_CLUSTER_THRESHOLD", str(threshold))
     monkeypatch.setenv("OPIR_PAIR_THRESHOLD", str(pair))
+    monkeypatch.setenv("OPIR_EXPAND_PAIR_THRESHOLD", str(pair))
     o = oracle_lib.Oracle(4096, 256)
     P = o.P
     server = PirServer(PirParams(num_entries=4096, max_fst_dim=256))
