@@ -3,12 +3,15 @@
 // reconstruction (query_to_gsw, gsw_eval.cpp:254-286) and folding of the
 // further dimensions (other_dim_mux, server.cpp:295-334).
 //
-// Each stage has two forms.  The one-CTA form gives a whole ciphertext to one
-// CTA of 256 threads (least total work; used when a launch has many
-// ciphertexts).  The cluster form splits one ciphertext's independent NTTs
-// over a thread-block cluster and combines the partial results through
-// distributed shared memory, which shortens the dependent chain of NTTs per
-// tree level (used for the narrow levels, where latency dominates).
+// Each stage has a one-CTA form, which gives a whole ciphertext to one CTA of
+// 256 threads (least total work; used when a launch has many ciphertexts),
+// and cluster forms, which split one ciphertext's independent NTTs over a
+// thread-block cluster and combine the partial results through distributed
+// shared memory: that shortens the dependent chain of NTTs per tree level
+// where latency dominates.  Expansion and folding have a wide cluster (4 and
+// 5 CTAs, the narrowest levels) and a pair form (2 CTAs, levels in between);
+// a cluster launch pays off only while it fits one wave (a cluster's CTAs
+// share a GPC), which sets the thresholds below.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
