@@ -781,7 +781,7 @@ def main():
     clocks.stop()
     e2e_qps = e2e_steps * world / (e2e_ms / 1e3)
 
-    db_bytes = params.get_num_pt() * N * 8
+    db_bytes = db_bytes_cfg = params.get_num_pt() * N * 8
     peak, peak_kind = measured_peak()
     achieved = db_bytes / (mean["scan_kernel"] / 1e3) / 1e9
     traffic = read_traffic(args.workload)
@@ -794,7 +794,8 @@ def main():
                    "n1": params.get_fst_dim_sz(), "n_rest": params.get_other_dim_sz(),
                    "ndim": len(params.get_dims()), "batch": 1, "ntt_db_bytes": db_bytes,
                    "raw_db_mb": params.get_DBSize_MB(), "parallelism": f"replicas{world}",
-                   "l2": "inputs larger than L2 (NTT-form database 4.29 GB > 129 MB)"},
+                   "l2": (f"inputs larger than L2 (NTT-form database {db_bytes_cfg / 1e9:.2f} GB "
+                          "> 129 MB)")},
         "db_gbs_scanned": db_bytes * qps / 1e9,
         "raw_db_mbs": params.get_DBSize_MB() * qps,
         "stages_ms": mean,
