@@ -232,6 +232,12 @@ int opir_wait(opir_ctx *ctx, uint64_t ticket, uint32_t timeout_ms, uint64_t *res
 int opir_serve_stats_get(opir_ctx *ctx, opir_serve_stats *out);
 
 /* ---- timing and accounting ---- */
+/* Single queries on the synchronous calls (opir_make_query,
+ * opir_make_query_device) are captured into a CUDA graph and replayed
+ * (default on; OPIR_GRAPHS=0 in the environment turns it off at context
+ * creation).  The graph is not used with stage timing, traces or a key
+ * budget.  Results are the same either way. */
+int opir_set_graphs(opir_ctx *ctx, int enable);
 /* Enable per-stage CUDA-event timing of subsequent queries. */
 int opir_set_timing(opir_ctx *ctx, int enable);
 /* Device milliseconds of the last timed query for the reference's sections

@@ -39,7 +39,7 @@ EXPORTS = (
     "opir_launch_count", "opir_sync", "opir_ntt", "opir_ntt_device",
     "opir_set_key_budget", "opir_key_bytes_per_client", "opir_resident_clients",
     "opir_serve_start", "opir_serve_stop", "opir_submit", "opir_poll", "opir_wait",
-    "opir_serve_stats_get", "opir_set_batch_engine", "opir_autotune",
+    "opir_serve_stats_get", "opir_set_batch_engine", "opir_autotune", "opir_set_graphs",
 )
 
 ENGINES = {"auto": 0, "scan": 1, "imad": 2, "tensor": 3}
@@ -154,6 +154,7 @@ def load(path: str = LIB):
                                         _u64p, _u64p, _u8p]
     L.opir_first_dim_noalloc.argtypes = [_vp, ctypes.c_uint32, _vp, _vp]
     L.opir_set_timing.argtypes = [_vp, ctypes.c_int]
+    L.opir_set_graphs.argtypes = [_vp, ctypes.c_int]
     L.opir_stage_times.argtypes = [_vp, ctypes.POINTER(ctypes.c_float)]
     L.opir_launch_count.argtypes = [_vp]
     L.opir_launch_count.restype = ctypes.c_uint64

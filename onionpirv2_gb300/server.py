@@ -351,6 +351,10 @@ class PirServer:
         return {name: getattr(st, name) for name, _ in st._fields_}
 
     # ---- timing / accounting
+    def set_graphs(self, enable: bool = True):
+        """Replay single queries from a captured CUDA graph (default on)."""
+        self._check(self._L.opir_set_graphs(self._ctx, 1 if enable else 0))
+
     def set_timing(self, enable: bool = True):
         self._check(self._L.opir_set_timing(self._ctx, 1 if enable else 0))
 

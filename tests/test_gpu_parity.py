@@ -316,3 +316,32 @@ def test_tensor_core_first_dim_matches_single_queries(oracle_lib, gpu_lib, monke
         plain, _ = o.decrypt(sk, resp[j], 2)
         assert np.array_equal(o.entry_from_plain(idxs[j], plain), server.direct_get_entry(idxs[j]))
     server.close()
+
+
+def test_graph_replay_matches_direct_launches(oracle_lib, gpu_lib):
+    """Single queries replayed from the captured CUDA graph (updated for
+    every query: other clients, other queries) equal direct launches and the
+    oracle, on two databases of different shapes."""
+    from onionpirv2_gb300 import PirParams, PirServer
+    for shape in ((4096, 256), (1 << 13, 64)):
+        o = oracle_lib.Oracle(*shape)
+        server = PirServer(PirParams(num_entries=shape[0], max_fst_dim=shape[1]))
+        server.gen_data(21)
+        db = o.build_db(21)
+        clients = [make_client(o, 70 + j) for j in range(3)]
+        for j, (sk, gk, gswk) in enumerate(clients):
+            server.set_client_galois_key(j, gk)
+            server.set_client_gsw_key(j, gswk)
+        for it in range(6):
+            j = it % 3
+            sk, gk, gswk = clients[j]
+            qry = o.make_query(sk, 90 + it, (it * 1237) % o.P.num_entries)
+            server.set_graphs(True)
+            g = server.make_query(j, qry)
+            server.set_graphs(False)
+            d = server.make_query(j, qry)
+            assert np.array_equal(g, d) and g.packed == d.packed
+            if it < 2:
+                ref = o.make_query_server(db, gk, o.gsw_key_to_ntt(gswk), qry)[0]
+                assert np.array_equal(g, ref)
+        server.close()
