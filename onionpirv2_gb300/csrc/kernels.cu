@@ -121,22 +121,28 @@ __device__ __forceinline__ uint64_t mod_switch_coeff(uint64_t x, const Consts &C
   return (uint64_t)((P + (((unsigned __int128)1) << (s - 1))) >> s);
 }
 
+// One CTA per slice of kModSlices consecutive coefficient ranges of one
+// response: 2N / kModSlices coefficients (a multiple of 32, so every slice
+// starts on a 32-bit word of the packed stream), one per thread.
+constexpr int kModSlices = 16;
 __global__ void __launch_bounds__(T) modswitch_pack_kernel(const uint64_t *res, size_t res_stride,
                                                            uint64_t *resp, uint8_t *packed,
                                                            int packed_bytes, Consts C) {
   extern __shared__ uint32_t words[];
-  const int tid = threadIdx.x, b = blockIdx.x;
+  const int tid = threadIdx.x, slice = blockIdx.x, b = blockIdx.y;
   const int w = C.small_q_width;
-  const int nwords = (packed_bytes + 3) / 4;
+  const int per = 2 * kN / kModSlices;
+  const int i0 = slice * per;
+  const int nwords = per * w / 32;  // the slice's words of the packed stream
   for (int i = tid; i < nwords; i += T) words[i] = 0;
   __syncthreads();
   const uint64_t *ct = res + b * res_stride;
   const uint64_t mask = (1ULL << w) - 1;
-  for (int i = tid; i < 2 * kN; i += T) {
+  for (int i = i0 + tid; i < i0 + per; i += T) {
     const uint64_t v = mod_switch_coeff(ct[i], C);
     if (resp) resp[(size_t)b * 2 * kN + i] = v;
     const uint64_t m = v & mask;
-    const uint64_t bit = (uint64_t)i * w;
+    const uint64_t bit = (uint64_t)(i - i0) * w;
     const int wi = (int)(bit >> 5), sh = (int)(bit & 31);
     atomicOr(&words[wi], (uint32_t)(m << sh));
     if (sh + w > 32) atomicOr(&words[wi + 1], (uint32_t)(m >> (32 - sh)));
@@ -144,8 +150,8 @@ __global__ void __launch_bounds__(T) modswitch_pack_kernel(const uint64_t *res, 
   }
   __syncthreads();
   if (packed) {
-    uint8_t *dst = packed + (size_t)b * packed_bytes;
-    for (int i = tid; i < packed_bytes; i += T) dst[i] = (uint8_t)(words[i >> 2] >> (8 * (i & 3)));
+    uint8_t *dst = packed + (size_t)b * packed_bytes + (size_t)i0 * w / 8;
+    for (int i = tid; i < 4 * nwords; i += T) dst[i] = (uint8_t)(words[i >> 2] >> (8 * (i & 3)));
   }
 }
 
@@ -273,9 +279,10 @@ void launch_query_prep_plane(const uint64_t *leaves, size_t leaves_stride, uint6
 void launch_modswitch_pack(const uint64_t *res, size_t res_stride, uint64_t *resp,
                            uint8_t *packed, size_t packed_bytes, int batch, const Consts &C,
                            cudaStream_t s) {
-  const size_t smem = ((packed_bytes + 3) / 4 + 2) * sizeof(uint32_t);
-  modswitch_pack_kernel<<<batch, T, smem, s>>>(res, res_stride, resp, packed, (int)packed_bytes,
-                                               C);
+  // the packed stream is 2N w bits exactly; each slice fills its own words
+  const size_t smem = ((size_t)(2 * kN / kModSlices) * C.small_q_width / 32 + 2) * sizeof(uint32_t);
+  modswitch_pack_kernel<<<dim3(kModSlices, batch), T, smem, s>>>(res, res_stride, resp, packed,
+                                                                 (int)packed_bytes, C);
 }
 
 void launch_db_pack(const uint8_t *entries, uint64_t *coeffs, size_t num_pt, int entry_size,
