@@ -44,33 +44,26 @@ __global__ void __launch_bounds__(T) ntt_kernel(ModTab M, uint64_t *polys, int i
 
 // evaluate_first_dim's NTT of the selection vector (server.cpp:137-139) and
 // prep_query's transpose (server.cpp:80-118), into the scan operand:
-// qs[c * n1 + k] = {lo30(Q0), hi30(Q0), lo30(Q1), hi30(Q1)} of leaf k.
+// qs[c * n1 + k] = {lo30(Q0), hi30(Q0), lo30(Q1), hi30(Q1)} of leaf k.  One
+// CTA per leaf and polynomial (blockIdx.z): each writes its half of the
+// 16-byte operand words.
 __global__ void __launch_bounds__(T) query_prep_kernel(const uint64_t *leaves,
                                                        size_t leaves_stride, uint4 *qs,
                                                        size_t stride_b, size_t stride_c,
                                                        size_t stride_k, ModTab M) {
   __shared__ uint64_t sa[kSmemPoly], sb[kSmemPoly];
   const int tid = threadIdx.x;
-  const int k = blockIdx.x, b = blockIdx.y;
-  const uint64_t *ct = leaves + b * leaves_stride + (size_t)k * 2 * kN;
-  uint64_t r0[8], r1[8];
+  const int k = blockIdx.x, b = blockIdx.y, poly = blockIdx.z;
+  const uint64_t *ct = leaves + b * leaves_stride + (size_t)k * 2 * kN + (size_t)poly * kN;
+  uint64_t r[8];
 #pragma unroll
-  for (int e = 0; e < 8; ++e) {
-    r0[e] = ct[strided_idx(tid, e)];
-    r1[e] = ct[kN + strided_idx(tid, e)];
-  }
-  ntt_fwd(r0, sa, sb, M);
-  ntt_fwd(r1, sa, sb, M);
-  uint4 *dst = qs + b * stride_b + k * stride_k;
+  for (int e = 0; e < 8; ++e) r[e] = ct[strided_idx(tid, e)];
+  ntt_fwd(r, sa, sb, M);
+  uint2 *dst = reinterpret_cast<uint2 *>(qs + b * stride_b + k * stride_k) + poly;
 #pragma unroll
   for (int e = 0; e < 8; ++e) {
     const int c = slot_idx(tid, e);
-    uint4 v;
-    v.x = (uint32_t)(r0[e] & 0x3FFFFFFFu);
-    v.y = (uint32_t)(r0[e] >> 30);
-    v.z = (uint32_t)(r1[e] & 0x3FFFFFFFu);
-    v.w = (uint32_t)(r1[e] >> 30);
-    dst[(size_t)c * stride_c] = v;
+    dst[(size_t)c * stride_c * 2] = make_uint2((uint32_t)(r[e] & 0x3FFFFFFFu), (uint32_t)(r[e] >> 30));
   }
 }
 
@@ -82,19 +75,13 @@ __global__ void __launch_bounds__(T) query_prep_plane_kernel(const uint64_t *lea
                                                              uint64_t *plane, int n1, ModTab M) {
   __shared__ uint64_t sa[kSmemPoly], sb[kSmemPoly];
   const int tid = threadIdx.x;
-  const int k = blockIdx.x, b = blockIdx.y;
-  const uint64_t *ct = leaves + b * leaves_stride + (size_t)k * 2 * kN;
-  uint64_t r0[8], r1[8];
+  const int k = blockIdx.x, b = blockIdx.y, poly = blockIdx.z;  // one polynomial per CTA
+  const uint64_t *ct = leaves + b * leaves_stride + (size_t)k * 2 * kN + (size_t)poly * kN;
+  uint64_t r[8];
 #pragma unroll
-  for (int e = 0; e < 8; ++e) {
-    r0[e] = ct[strided_idx(tid, e)];
-    r1[e] = ct[kN + strided_idx(tid, e)];
-  }
-  ntt_fwd(r0, sa, sb, M);
-  ntt_fwd(r1, sa, sb, M);
-  uint64_t *dst = plane + ((size_t)b * n1 + k) * 2 * kN;
-  stg_slot8(dst, r0);
-  stg_slot8(dst + kN, r1);
+  for (int e = 0; e < 8; ++e) r[e] = ct[strided_idx(tid, e)];
+  ntt_fwd(r, sa, sb, M);
+  stg_slot8(plane + (((size_t)b * n1 + k) * 2 + poly) * kN, r);
 }
 
 // ---------------------------------------------------------------------------
@@ -261,19 +248,19 @@ void launch_ntt(const ModTab &M, uint64_t *polys, size_t count, bool inverse, cu
 
 void launch_query_prep(const uint64_t *leaves, size_t leaves_stride, uint4 *qs, size_t qs_stride,
                        int n1, int batch, const ModTab &Mq, cudaStream_t s) {
-  query_prep_kernel<<<dim3(n1, batch), T, 0, s>>>(leaves, leaves_stride, qs, qs_stride,
-                                                   (size_t)n1, 1, Mq);
+  query_prep_kernel<<<dim3(n1, batch, 2), T, 0, s>>>(leaves, leaves_stride, qs, qs_stride,
+                                                      (size_t)n1, 1, Mq);
 }
 
 void launch_query_prep_batched(const uint64_t *leaves, size_t leaves_stride, uint4 *qsb, int n1,
                                int batch, const ModTab &Mq, cudaStream_t s) {
-  query_prep_kernel<<<dim3(n1, batch), T, 0, s>>>(leaves, leaves_stride, qsb, 1,
+  query_prep_kernel<<<dim3(n1, batch, 2), T, 0, s>>>(leaves, leaves_stride, qsb, 1,
                                                    (size_t)n1 * batch, (size_t)batch, Mq);
 }
 
 void launch_query_prep_plane(const uint64_t *leaves, size_t leaves_stride, uint64_t *plane,
                              int n1, int batch, const ModTab &Mq, cudaStream_t s) {
-  query_prep_plane_kernel<<<dim3(n1, batch), T, 0, s>>>(leaves, leaves_stride, plane, n1, Mq);
+  query_prep_plane_kernel<<<dim3(n1, batch, 2), T, 0, s>>>(leaves, leaves_stride, plane, n1, Mq);
 }
 
 void launch_modswitch_pack(const uint64_t *res, size_t res_stride, uint64_t *resp,
