@@ -89,6 +89,11 @@ int opir_db_fill_synthetic(opir_ctx *ctx, uint32_t db_id, uint64_t seed);
  * db_aligned_[c*num_pt + row*n1 + col] (server.cpp:740). */
 int opir_db_upload_aligned(opir_ctx *ctx, uint32_t db_id, const uint64_t *db_aligned);
 
+/* PirServer::direct_get_entry (server.cpp:503-517): the entry's
+ * entry_size bytes, read back from the device database (its plaintext
+ * inverse-transformed and unpacked), for checking decrypted responses. */
+int opir_db_get_entry(opir_ctx *ctx, uint32_t db_id, uint64_t entry_index, uint8_t *entry);
+
 /* ---- per-client keys (server.cpp:480-500) ---- */
 /* set_client_galois_key: keys[level][k][mod][N], NTT form, level a is the
  * Galois element 1 + (N >> a) (client.cpp:235-237), mod 0 = q, 1 = p. */

@@ -64,6 +64,13 @@ class PirServer {
     check(opir_db_push_chunk(ctx_, db_, flat.data(), n, chunk_idx));
   }
 
+  // server.cpp:503-517: the entry read back from the device database
+  Entry direct_get_entry(size_t entry_idx) const {
+    Entry e(params_.entry_size);
+    check(opir_db_get_entry(ctx_, db_, entry_idx, e.data()));
+    return e;
+  }
+
   // server.cpp:480-484; keys [levels][2][2][N] in NTT form
   void set_client_galois_key(size_t client_id, const std::vector<uint64_t> &keys) {
     const size_t per = 4 * (size_t)params_.poly_degree;
@@ -162,7 +169,7 @@ class PirServer {
   uint32_t db_id() const { return db_; }
 
  private:
-  void check(int rc) {
+  void check(int rc) const {
     if (rc == OPIR_OK) return;
     const std::string msg = opir_last_error(ctx_);
     if (rc == OPIR_ERR_UNKNOWN_CLIENT) throw std::out_of_range(msg);

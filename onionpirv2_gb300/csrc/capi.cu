@@ -966,6 +966,47 @@ int opir_db_upload_aligned(opir_ctx *ctx, uint32_t db_id, const uint64_t *aligne
   return OPIR_OK;
 }
 
+int opir_db_get_entry(opir_ctx *ctx, uint32_t db_id, uint64_t entry_index, uint8_t *entry) {
+  if (!ctx || !entry) return OPIR_ERR_ARG;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  Db *db = find_db(ctx, db_id);
+  if (!db) return ctx->fail(OPIR_ERR_UNKNOWN_DB, "unknown database %u", db_id);
+  if (!db->dbs.p) return ctx->fail(OPIR_ERR_STATE, "database %u holds no data", db_id);
+  const opir_db_shape &S = db->shape;
+  if (entry_index >= db->num_pt * S.entries_per_pt)
+    return ctx->fail(OPIR_ERR_ARG, "entry %llu out of range", (unsigned long long)entry_index);
+  cudaSetDevice(ctx->device);
+  DevBuf d_plain;
+  CK(d_plain.alloc(kN * sizeof(uint64_t)), "alloc plaintext");
+  launch_db_plaintext(db->dbs.as<uint64_t>(), (int)S.fst_dim_sz, (int)S.other_dim_sz,
+                      (size_t)(entry_index / S.entries_per_pt), d_plain.as<uint64_t>(), ctx->Mq.tab,
+                      ctx->C, ctx->stream);
+  ctx->launches++;
+  std::vector<uint64_t> plain(kN);
+  CK(cudaMemcpyAsync(plain.data(), d_plain.p, kN * sizeof(uint64_t), cudaMemcpyDeviceToHost,
+                     ctx->stream),
+     "read plaintext");
+  CK(cudaStreamSynchronize(ctx->stream), "read plaintext");
+  // the entry's bytes, LSB first from bits_per_coeff-bit coefficients
+  // (push_database_chunk's packing, server.cpp:649-700, read back)
+  const uint64_t bpc = S.bits_per_coeff;
+  const uint64_t start = (entry_index % S.entries_per_pt) * (uint64_t)S.entry_size * 8;
+  uint64_t ci = start / bpc, have = bpc - start % bpc;
+  u128 buf = plain[ci] >> (start % bpc);
+  for (uint32_t n = 0; n < S.entry_size;) {
+    if (have >= 8) {
+      entry[n++] = (uint8_t)(buf & 0xFF);
+      buf >>= 8;
+      have -= 8;
+    } else {
+      ci++;
+      buf |= (u128)(ci < (uint64_t)kN ? plain[ci] : 0) << have;
+      have += bpc;
+    }
+  }
+  return OPIR_OK;
+}
+
 int opir_set_galois_key(opir_ctx *ctx, uint64_t client_id, const uint64_t *keys, uint32_t levels) {
   if (!ctx || !keys || !levels || levels > (uint32_t)kLogN) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);

@@ -222,6 +222,28 @@ __global__ void __launch_bounds__(T) db_ntt_scatter_kernel(const uint64_t *coeff
   }
 }
 
+// One plaintext back from the device database: its NTT slots gathered from
+// dbs, the inverse transform, and the plain lift of ingest undone (stored
+// coefficients are v or v + q - t for v >= (t + 1) / 2).  Natural order out.
+__global__ void __launch_bounds__(T) db_plaintext_kernel(const uint64_t *dbs, int n1, int n_rest,
+                                                         size_t pt, uint64_t *out, ModTab M,
+                                                         Consts C) {
+  __shared__ uint64_t sa[kSmemPoly], sb[kSmemPoly];
+  const int tid = threadIdx.x;
+  const size_t row = pt / n1, col = pt % n1;
+  const size_t plane = (size_t)n1 * n_rest;
+  uint64_t r[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const uint64_t w = dbs[(size_t)slot_idx(tid, e) * plane + col * n_rest + row];
+    r[e] = (w & 0x3FFFFFFFULL) | ((w >> 32) << 30);
+  }
+  ntt_inv(r, sa, sb, M);
+  const uint64_t thr = (C.t + 1) >> 1, inc = C.q - C.t;
+#pragma unroll
+  for (int e = 0; e < 8; ++e) out[strided_idx(tid, e)] = r[e] < thr ? r[e] : r[e] - inc;
+}
+
 __global__ void db_from_aligned_kernel(const uint64_t *aligned, uint64_t *dbs, int n1,
                                        int n_rest) {
   const size_t plane = (size_t)n1 * n_rest;
@@ -290,6 +312,11 @@ void launch_db_ntt_scatter(uint64_t *coeffs, size_t pt0, size_t count, uint64_t 
                            int n_rest, const ModTab &Mq, const Consts &C, cudaStream_t s) {
   if (!count) return;
   db_ntt_scatter_kernel<<<(unsigned)count, T, 0, s>>>(coeffs, pt0, dbs, n1, n_rest, Mq, C);
+}
+
+void launch_db_plaintext(const uint64_t *dbs, int n1, int n_rest, size_t pt, uint64_t *out,
+                         const ModTab &Mq, const Consts &C, cudaStream_t s) {
+  db_plaintext_kernel<<<1, T, 0, s>>>(dbs, n1, n_rest, pt, out, Mq, C);
 }
 
 void launch_db_from_aligned(const uint64_t *aligned, uint64_t *dbs, int n1, int n_rest,

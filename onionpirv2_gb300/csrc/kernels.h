@@ -128,6 +128,9 @@ void launch_db_gen_pack(uint64_t seed, size_t pt0, uint64_t *coeffs, size_t num_
 void launch_db_ntt_scatter(uint64_t *coeffs, size_t pt0, size_t count, uint64_t *dbs, int n1,
                            int n_rest, const ModTab &Mq, const Consts &C, cudaStream_t s);
 // reference layout db_aligned[c][row*n1+col] (NTT form) -> scan layout
+// plaintext `pt` of the database back in coefficient form (plain lift undone)
+void launch_db_plaintext(const uint64_t *dbs, int n1, int n_rest, size_t pt, uint64_t *out,
+                         const ModTab &Mq, const Consts &C, cudaStream_t s);
 void launch_db_from_aligned(const uint64_t *aligned, uint64_t *dbs, int n1, int n_rest,
                             cudaStream_t s);
 

@@ -83,8 +83,7 @@ class PirServer:
         db = ctypes.c_uint32()
         self._check(self._L.opir_db_create(self._ctx, ctypes.byref(shape), ctypes.byref(db)))
         self.db_id = db.value
-        self._seed: Optional[int] = None
-        self._raw_chunks = {}
+        self._db_entry_size = {}  # databases added with add_database
         self.resp_bytes = int(self._L.opir_response_bytes(self._ctx))
 
     # ---- plumbing
@@ -114,8 +113,6 @@ class PirServer:
     def gen_data(self, seed: int = 0x0B1A7):
         """Fill the whole database with seeded entries (server.cpp:47-78)."""
         self._check(self._L.opir_db_fill_synthetic(self._ctx, self.db_id, seed))
-        self._seed = seed
-        self._raw_chunks.clear()
 
     def push_database_chunk(self, chunk_entry, chunk_idx: int):
         """Pack, NTT and realign one chunk of fst_dim_sz plaintexts
@@ -142,8 +139,6 @@ class PirServer:
         arr = np.ascontiguousarray(arr)
         self._check(self._L.opir_db_push_chunk(self._ctx, self.db_id, _capi.p8(arr.reshape(-1)),
                                                n, chunk_idx))
-        self._raw_chunks[chunk_idx] = arr
-        self._seed = None
 
     def upload_ntt_db(self, db_aligned: np.ndarray):
         """Install an NTT-form database given in the reference layout
@@ -152,18 +147,16 @@ class PirServer:
         if a.size != self.pir_params.get_num_pt() * N:
             raise ValueError("database has the wrong size")
         self._check(self._L.opir_db_upload_aligned(self._ctx, self.db_id, _capi.p64(a.reshape(-1))))
-        self._seed = None
 
-    def direct_get_entry(self, entry_idx: int) -> np.ndarray:
-        """Non-private lookup of an entry, for testing (server.cpp:503-517)."""
-        P = self.pir_params
-        if self._seed is not None:
-            return synthetic_entries(self._seed, entry_idx, 1, P.get_entry_size())[0]
-        per_chunk = P.get_fst_dim_sz() * P.get_num_entries_per_plaintext()
-        chunk, off = divmod(entry_idx, per_chunk)
-        if chunk not in self._raw_chunks:
-            raise ValueError("Unable to open file for reading")
-        return self._raw_chunks[chunk][off].copy()
+    def direct_get_entry(self, entry_idx: int, db_id: Optional[int] = None) -> np.ndarray:
+        """Non-private lookup of an entry, for testing (server.cpp:503-517):
+        decoded from the device database (its plaintext inverse-transformed
+        and unpacked)."""
+        out = np.zeros(self.pir_params.get_entry_size() if db_id is None else
+                       self._db_entry_size.get(db_id, self.pir_params.get_entry_size()), np.uint8)
+        self._check(self._L.opir_db_get_entry(self._ctx, self.db_id if db_id is None else db_id,
+                                              entry_idx, _capi.p8(out)))
+        return out
 
     # ---- keys
     def set_client_galois_key(self, client_id: int, galois_keys):
@@ -265,6 +258,7 @@ class PirServer:
         self._check(self._L.opir_db_create(self._ctx, ctypes.byref(shape), ctypes.byref(db)))
         if seed is not None:
             self._check(self._L.opir_db_fill_synthetic(self._ctx, db.value, seed))
+        self._db_entry_size[db.value] = P.get_entry_size()
         return db.value
 
     # ---- key budget (client keys in a bounded pool, least recently used out)

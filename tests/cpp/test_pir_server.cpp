@@ -57,7 +57,8 @@ int main() {
         client.decrypt_mod_q(client.load_resp_from_stream(stream), &budget);
     const onionpir::Entry entry = client.get_entry_from_plaintext(idx, plain);
     orc_gen_entries(o, seed, idx, 1, expect.data());
-    const bool ok = n == ref_packed.size() && entry == expect;
+    const bool ok = n == ref_packed.size() && entry == expect &&
+                    server.direct_get_entry(idx) == expect;  // server.cpp:503-517
     orc_gsw_key_to_ntt(o, gsw.data(), 2 * P.l_key, gsw_ntt.data());
     orc_make_query_server(o, db.data(), gk.data(), gsw_ntt.data(), query.data(), ref.data(),
                           ref_packed.data(), nullptr);

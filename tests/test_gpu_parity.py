@@ -145,12 +145,36 @@ def test_push_chunk_matches_reference_layout(oracle_lib, gpu_lib):
         assert np.array_equal(resp, ref)
         plain, _ = o.decrypt(sk, resp, 2)
         assert np.array_equal(o.entry_from_plain(idx, plain), entries[idx])
+    # direct_get_entry decodes the pushed bytes back from the device database
+    for idx in (0, 1, 2222, P.num_entries - 1):
+        assert np.array_equal(server.direct_get_entry(idx), entries[idx])
     # the aligned-upload path gives the same database
     server.upload_ntt_db(db)
     query = o.make_query(sk, 8, 1234)
     resp = server.make_query(1, query)
     ref, _, _, _ = o.make_query_server(db, gk, o.gsw_key_to_ntt(gswk), query)
     assert np.array_equal(resp, ref)
+    assert np.array_equal(server.direct_get_entry(1234), entries[1234])
+
+
+@pytest.mark.parametrize("shape", [(4096, 256), (1 << 14, 1024), (100, 16)])
+def test_direct_get_entry_decodes_device_database(gpu_lib, shape):
+    """direct_get_entry (server.cpp:503-517) reads an entry back from the
+    device database: equal to the seeded generator's entries, for entry
+    sizes that fill a plaintext and for several entries per plaintext."""
+    from onionpirv2_gb300 import OpirError, PirParams, PirServer, synthetic_entries
+    for entry_size in (0, 100):
+        params = PirParams(num_entries=shape[0], max_fst_dim=shape[1], entry_size_cfg=entry_size)
+        server = PirServer(params)
+        server.gen_data(4321)
+        n = params.get_num_entries()
+        rng = np.random.default_rng(n)
+        for idx in [0, 1, n - 1] + [int(x) for x in rng.integers(0, n, size=5)]:
+            want = synthetic_entries(4321, idx, 1, params.get_entry_size())[0]
+            assert np.array_equal(server.direct_get_entry(idx), want), (entry_size, idx)
+        with pytest.raises(OpirError):
+            server.direct_get_entry(n)
+        server.close()
 
 
 SHAPES = [
