@@ -286,6 +286,10 @@ def serve_main(args):
     dbs = [server.add_database(params[0], seed=DB_SEED + 1), server.db_id,
            server.add_database(params[2], seed=DB_SEED + 2)]
     ingest_s = time.perf_counter() - t0
+    # per-database tuning: scan tiles and the engine per batch size
+    t = time.perf_counter()
+    tuned = {names[d]: server.autotune(max_batch=32, db_id=dbs[d]) for d in range(3)}
+    tune_s = time.perf_counter() - t
     per = server.key_bytes_per_client()
     slots = max(2, args.serve_clients // 2)
     server.set_key_budget(slots * per)  # half the clients' keys fit: LRU admission
@@ -348,6 +352,9 @@ def serve_main(args):
         "resident_clients": resident, "bit_exact_sample": same, "ingest_s": ingest_s,
         "entries_decoded": f"{decoded}/{n}",
         "light_load": light,
+        "autotune": {"seconds": tune_s,
+                     **{w: {b["batch"]: b["engine"] for b in t["batches"]}
+                        for w, t in tuned.items()}},
         "client": {"threads": threads, "clients": args.serve_clients,
                    "keygen_s": keygen_s,
                    "keys_per_s": args.serve_clients / keygen_s,
