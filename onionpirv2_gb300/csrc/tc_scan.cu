@@ -25,7 +25,7 @@
 //   database  dbl[c][rb][k/8][r%16][i][k%8]      (rb = r / 16)
 //   queries   ql [c][h][k/8][b'][j][k%8]         (b' = 2 b + poly - 32 h)
 // (h: column half of at most 32 query polynomials = 256 TMEM columns), so the
-// slice of a pipeline stage (32 k) of either operand is contiguous and
+// slice of a pipeline stage (32 or 64 k) of either operand is contiguous and
 // lands in shared memory in the K-major, no-swizzle canonical layout that the
 // tcgen05 shared-memory descriptors below describe (leading byte offset =
 // stride between core matrices along k, stride byte offset = 128 between
@@ -40,14 +40,18 @@ namespace opir {
 namespace {
 
 constexpr int kTcRows = 16;                 // database rows per tile
-constexpr int kTcKC = 32;                   // k per pipeline stage
-constexpr int kTcKB = kTcKC / 8;            // core matrices along k per stage
-constexpr int kTcStages = 8;
+constexpr int kTcKC = 32;                   // k granularity of the first dimension
 constexpr int kTcMaxNB = 64;                // query polynomials per pass (32 queries)
 constexpr int kTcHalfNB = 32;               // query polynomials per tile (256 TMEM columns)
-constexpr uint32_t kTcABytes = kTcKB * kTcRows * 128;        // 8 KB
-constexpr uint32_t kTcBBytesMax = kTcKB * kTcHalfNB * 128;   // 16 KB
-constexpr uint32_t kTcStageBytes = kTcABytes + kTcBBytesMax;
+// pipeline stages: KC k per stage (64, or 32 when the segment length is an
+// odd multiple of 32), STAGES stages; the 64-k ring (4 x 48 KB) measured
+// 25 % faster than the 32-k ring (8 x 24 KB) and 5 % faster than 2 x 96 KB
+template <int KC>
+__host__ __device__ constexpr uint32_t tc_a_bytes() { return KC / 8 * kTcRows * 128; }
+template <int KC>
+__host__ __device__ constexpr uint32_t tc_stage_bytes() {
+  return tc_a_bytes<KC>() + KC / 8 * kTcHalfNB * 128;
+}
 constexpr int kTcYStride = 168;             // int32 words per (warp, row) block of Y staging
 constexpr int kTcEpiWarps = 8;              // two per TMEM lane quadrant
 constexpr int kTcThreads = (kTcEpiWarps + 2) * 32;  // epilogue warps, producer, MMA
@@ -134,22 +138,25 @@ __device__ __forceinline__ uint64_t tc_combine(const int (&y)[16], uint64_t q, u
   return barrett128(acc, q, mu_lo, mu_hi);
 }
 
+template <int KC, int STAGES>
 __global__ void __launch_bounds__(kTcThreads, 1)
     tc_scan_kernel(const uint16_t *__restrict__ dbl, const uint16_t *__restrict__ ql, uint64_t *out,
                    size_t out_stride, int b_base, TcGeom G, uint64_t q, uint64_t mu_lo,
                    uint64_t mu_hi, uint64_t r64, uint64_t r128, uint32_t *status) {
+  constexpr int kTcKB = KC / 8;  // core matrices along k per stage
+  constexpr uint32_t kTcABytes = tc_a_bytes<KC>(), kTcStageBytes = tc_stage_bytes<KC>();
   extern __shared__ __align__(1024) unsigned char smem[];
-  int *ysm = reinterpret_cast<int *>(smem + kTcStages * kTcStageBytes);
+  int *ysm = reinterpret_cast<int *>(smem + STAGES * kTcStageBytes);
   uint64_t *bars = reinterpret_cast<uint64_t *>(ysm + kTcEpiWarps * 4 * kTcYStride);
-  uint64_t *full = bars, *empty = bars + kTcStages;
-  uint64_t *acc_full = bars + 2 * kTcStages;  // [2]
+  uint64_t *full = bars, *empty = bars + STAGES;
+  uint64_t *acc_full = bars + 2 * STAGES;  // [2]
   uint64_t *acc_empty = acc_full + 2;         // [2]
   uint64_t *drained = acc_full + 4;
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * kTcStages + 5);
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * STAGES + 5);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kTcStages; ++s) {
+    for (int s = 0; s < STAGES; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
@@ -187,8 +194,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             dbl + ((size_t)(c * G.n_rb + rb) * kblk + G.k0 / 8) * (kTcRows * 64);
         const uint16_t *b_src = ql + ((size_t)(c * G.nh + hf) * kblk + G.k0 / 8) * G.nbh * 64;
         for (int kc = 0; kc < G.nkc; ++kc, ++it) {
-          const int s = (int)(it % kTcStages);
-          const long long round = it / kTcStages;
+          const int s = (int)(it % STAGES);
+          const long long round = it / STAGES;
           if (round > 0 && !mbar_wait(&empty[s], (uint32_t)((round - 1) & 1))) {
             report_error(status, kErrTcWaitEmpty);
             ok = false;
@@ -201,9 +208,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         }
       }
       // never leave the CTA with copies still landing in its shared memory
-      const long long first = it > kTcStages ? it - kTcStages : 0;
+      const long long first = it > STAGES ? it - STAGES : 0;
       for (long long j = first; j < it; ++j)
-        if (!mbar_wait(&full[j % kTcStages], (uint32_t)((j / kTcStages) & 1))) {
+        if (!mbar_wait(&full[j % STAGES], (uint32_t)((j / STAGES) & 1))) {
           report_error(status, kErrTcDrain);
           break;
         }
@@ -224,8 +231,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         tc_fence_after();
         const uint32_t d = tmem + (uint32_t)buf * 256;
         for (int kc = 0; kc < G.nkc; ++kc, ++it) {
-          const int s = (int)(it % kTcStages);
-          if (!mbar_wait(&full[s], (uint32_t)((it / kTcStages) & 1))) {
+          const int s = (int)(it % STAGES);
+          if (!mbar_wait(&full[s], (uint32_t)((it / STAGES) & 1))) {
             report_error(status, kErrTcWaitFull);
             ok = false;
             break;
@@ -233,7 +240,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           tc_fence_after();
           const uint32_t sa = smem_base + (uint32_t)s * kTcStageBytes, sb = sa + kTcABytes;
 #pragma unroll
-          for (int ks = 0; ks < kTcKC / 16; ++ks)
+          for (int ks = 0; ks < KC / 16; ++ks)
             tc_mma(d, smem_desc(sa + ks * 2 * lbo_a, lbo_a, 128),
                    smem_desc(sb + ks * 2 * lbo_b, lbo_b, 128), G.idesc,
                    (kc > 0 || ks > 0) ? 1u : 0u);
@@ -411,9 +418,13 @@ __global__ void query_limb_kernel(const uint64_t *__restrict__ plane, uint16_t *
   }
 }
 
-constexpr size_t kTcSmem = kTcStages * kTcStageBytes + kTcEpiWarps * 4 * kTcYStride * sizeof(int) +
-                           (2 * kTcStages + 6) * 8;
-static_assert(kTcSmem <= 227 * 1024, "shared memory per CTA");
+template <int KC, int STAGES>
+constexpr size_t tc_smem() {
+  return STAGES * tc_stage_bytes<KC>() + kTcEpiWarps * 4 * kTcYStride * sizeof(int) +
+         (2 * STAGES + 6) * 8;
+}
+static_assert(tc_smem<64, 4>() <= 227 * 1024, "shared memory per CTA");
+static_assert(tc_smem<32, 8>() <= 227 * 1024, "shared memory per CTA");
 
 int g_tc_sms = 0;
 
@@ -445,7 +456,7 @@ TcGeom pass_geom(int n1, int n_rest, int pb) {
   G.nbh = 2 * padded / G.nh;
   G.n_rb = n_rest / kTcRows;
   G.units = (long long)kN * G.n_rb * G.nh;
-  G.b_bytes = (uint32_t)(kTcKB * G.nbh * 128);
+  G.b_bytes = 0;  // per stage: set by the launcher for its stage size
   G.idesc = make_idesc(G.nbh * 8);
   G.k0 = 0;
   G.nkc = 0;
@@ -470,8 +481,12 @@ cudaError_t init_tc_attributes() {
   int dev;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&g_tc_sms, cudaDevAttrMultiProcessorCount, dev);
-  return cudaFuncSetAttribute(tc_scan_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)kTcSmem);
+  cudaError_t e = cudaFuncSetAttribute(tc_scan_kernel<64, 4>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)tc_smem<64, 4>());
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(tc_scan_kernel<32, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)tc_smem<32, 8>());
 }
 
 void launch_db_limbs(const uint64_t *dbs, uint16_t *dbl, int n1, int n_rest, cudaStream_t s) {
@@ -507,10 +522,18 @@ int launch_tc_scan(const uint16_t *dbl, const uint16_t *ql, uint64_t *out, size_
     for (int k0 = 0; k0 < n1; k0 += kTcMaxSegment) {
       const int klen = n1 - k0 < kTcMaxSegment ? n1 - k0 : kTcMaxSegment;
       G.k0 = k0;
-      G.nkc = klen / kTcKC;
       G.accumulate = k0 > 0;
-      tc_scan_kernel<<<(unsigned)grid, kTcThreads, kTcSmem, s>>>(
-          dbl, ql + off, out, out_stride, b0, G, q, mu_lo, mu_hi, r64, r128, status);
+      if (klen % 64 == 0) {
+        G.nkc = klen / 64;
+        G.b_bytes = (uint32_t)(64 / 8 * G.nbh * 128);
+        tc_scan_kernel<64, 4><<<(unsigned)grid, kTcThreads, tc_smem<64, 4>(), s>>>(
+            dbl, ql + off, out, out_stride, b0, G, q, mu_lo, mu_hi, r64, r128, status);
+      } else {
+        G.nkc = klen / 32;
+        G.b_bytes = (uint32_t)(32 / 8 * G.nbh * 128);
+        tc_scan_kernel<32, 8><<<(unsigned)grid, kTcThreads, tc_smem<32, 8>(), s>>>(
+            dbl, ql + off, out, out_stride, b0, G, q, mu_lo, mu_hi, r64, r128, status);
+      }
       launches++;
     }
     off += pass_limb_elems(n1, pb);
