@@ -385,20 +385,26 @@ __global__ void db_limb_kernel(const uint64_t *__restrict__ dbs, uint16_t *__res
 
 // one thread: 8 consecutive k of one (slot, query polynomial) of the pass,
 // from plane[b][k][poly][c] (consecutive threads read consecutive slots) to
-// ql[c][h][k/8][b' - nbh h][j][k%8] (one 128-byte core matrix per thread)
-__global__ void query_limb_kernel(const uint64_t *__restrict__ plane, uint16_t *__restrict__ ql,
-                                  int n1, int b_base, int nh, int nbh, int pass_batch) {
+// ql[c][h][k/8][b' - nbh h][j][k%8].  A warp covers 8 slots x 4 query
+// polynomials: its output is 8 runs of 512 bytes, which it writes through a
+// 4 KB shared-memory transpose so that every store instruction fills one run.
+__global__ void __launch_bounds__(256) query_limb_kernel(const uint64_t *__restrict__ plane,
+                                                         uint16_t *__restrict__ ql, int n1,
+                                                         int b_base, int nh, int nbh,
+                                                         int pass_batch) {
+  __shared__ uint4 stage[8][8 * 4 * 8];  // [warp][slot][polynomial][limb]
   const int kblk = n1 / 8;
-  const long long total = (long long)kN * nh * kblk * nbh;
-  // a warp covers 8 consecutive slots x 4 consecutive query polynomials:
-  // 64-byte runs of the plane per read, 512-byte runs of ql per write
+  const long long total = (long long)kN * nh * kblk * nbh;  // a multiple of 32
+  uint4 *st = stage[threadIdx.x >> 5];
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
        t += (long long)gridDim.x * blockDim.x) {
     const int lane = (int)(t & 31);
     long long rest = t >> 5;
-    const int c = (int)(rest % (kN / 8)) * 8 + (lane & 7);
+    const int c0 = (int)(rest % (kN / 8)) * 8;
+    const int c = c0 + (lane & 7);
     rest /= kN / 8;
-    const int bl = (int)(rest % (nbh / 4)) * 4 + (lane >> 3);
+    const int bl0 = (int)(rest % (nbh / 4)) * 4;
+    const int bl = bl0 + (lane >> 3);
     rest /= nbh / 4;
     const int kb = (int)(rest % kblk);
     const int hf = (int)(rest / kblk);
@@ -409,12 +415,19 @@ __global__ void query_limb_kernel(const uint64_t *__restrict__ plane, uint16_t *
         plane + (((size_t)(b_base + b) * n1 + kb * 8) * 2 + (bq & 1)) * kN + c;
 #pragma unroll
     for (int kk = 0; kk < 8; ++kk) limbs8(b < pass_batch ? src[(size_t)kk * 2 * kN] : 0, d[kk]);
-    uint4 *dst = reinterpret_cast<uint4 *>(
-        ql + ((((size_t)c * nh + hf) * kblk + kb) * nbh + bl) * 64);
+    __syncwarp();  // the previous iteration's reads of the staging buffer are done
 #pragma unroll
     for (int i = 0; i < 8; ++i)
-      dst[i] = make_uint4(d[0][i] | (uint32_t)d[1][i] << 16, d[2][i] | (uint32_t)d[3][i] << 16,
-                          d[4][i] | (uint32_t)d[5][i] << 16, d[6][i] | (uint32_t)d[7][i] << 16);
+      st[((lane & 7) * 4 + (lane >> 3)) * 8 + i] =
+          make_uint4(d[0][i] | (uint32_t)d[1][i] << 16, d[2][i] | (uint32_t)d[3][i] << 16,
+                     d[4][i] | (uint32_t)d[5][i] << 16, d[6][i] | (uint32_t)d[7][i] << 16);
+    __syncwarp();
+#pragma unroll
+    for (int cs = 0; cs < 8; ++cs) {
+      uint4 *dst = reinterpret_cast<uint4 *>(
+          ql + ((((size_t)(c0 + cs) * nh + hf) * kblk + kb) * nbh + bl0) * 64);
+      dst[lane] = st[cs * 32 + lane];  // polynomial bl0 + lane / 8, limb lane % 8
+    }
   }
 }
 
