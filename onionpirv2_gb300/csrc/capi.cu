@@ -144,6 +144,8 @@ struct ModTables {
   uint64_t psi = 0;
 };
 
+constexpr int kGraphKey = 14;  // words identifying a captured single-query graph
+
 struct Db {
   opir_db_shape shape{};
   uint64_t num_pt = 0;
@@ -159,7 +161,7 @@ struct Db {
   // by everything their kernel parameters hold (client keys, buffers, tile
   // configuration); the least recently used one is updated in place on a miss
   struct Graph {
-    uint64_t key[12];
+    uint64_t key[kGraphKey];
     cudaGraphExec_t exec = nullptr;
     uint64_t used = 0;
     uint64_t launches = 0;  // kernels in the graph
@@ -640,11 +642,13 @@ int run_sync(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
   rc = resolve_keys(ctx, client_ids[0], db, s, &qd);  // no budget: pointers only
   if (rc) return rc;
   const Workspace &W = *E.W;
-  const uint64_t key[12] = {
-      client_ids[0], (uint64_t)qd.galois, (uint64_t)qd.gsw_key, (uint64_t)d_queries,
-      (uint64_t)d_resp, (uint64_t)d_packed, (uint64_t)W.exp0.p, (uint64_t)W.exp1.p,
-      (uint64_t)W.gsw.p ^ ((uint64_t)W.qs.p << 1), (uint64_t)W.res.p, (uint64_t)db.dbs.p,
-      (uint64_t)(int64_t)db.scan_cfg};
+  // every value a kernel parameter of the captured pipeline holds (the
+  // context's tables and the database shape are fixed for its lifetime)
+  const uint64_t key[kGraphKey] = {
+      client_ids[0],      (uint64_t)qd.galois, (uint64_t)qd.galois_s, (uint64_t)qd.gsw_key,
+      (uint64_t)d_queries, (uint64_t)d_resp,   (uint64_t)d_packed,    (uint64_t)W.exp0.p,
+      (uint64_t)W.exp1.p,  (uint64_t)W.gsw.p,  (uint64_t)W.qs.p,      (uint64_t)W.res.p,
+      (uint64_t)db.dbs.p,  (uint64_t)(int64_t)db.scan_cfg};
   Db::Graph *hit = nullptr, *lru = nullptr;
   for (auto &g : db.graphs) {
     if (std::memcmp(g.key, key, sizeof key) == 0) hit = &g;
