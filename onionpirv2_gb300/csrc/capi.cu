@@ -633,7 +633,13 @@ int run_sync(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
              const uint64_t *d_queries, uint64_t *d_resp, uint8_t *d_packed, const Trace *trace) {
   const PipeEnv E = sync_env(ctx);
   cudaStream_t s = E.s;
-  const bool capturable = s != nullptr && s != cudaStreamLegacy && s != cudaStreamPerThread;
+  bool capturable = s != nullptr && s != cudaStreamLegacy && s != cudaStreamPerThread;
+  if (capturable) {
+    // a caller capturing the stream into a graph of its own records the
+    // launches themselves
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    capturable = cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusNone;
+  }
   if (batch != 1 || trace || E.timed || !ctx->graphs || ctx->key_budget || !capturable)
     return run_pipeline(ctx, db, batch, client_ids, d_queries, d_resp, d_packed, trace, E);
   int rc = ensure_workspace(ctx, db, batch, *E.W);  // no allocation inside the capture
