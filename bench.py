@@ -59,7 +59,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="db262144")
-    ap.add_argument("--cpu-queries", type=int, default=2)
+    ap.add_argument("--cpu-queries", type=int, default=10,
+                    help="timed queries of the CPU baseline (after 3 untimed ones, as tests.cpp:16)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch", type=int, default=32,
                     help="batch size of the batched measurement (0 = skip)")
@@ -462,7 +463,11 @@ def cpu_baseline(params, workload, clients, queries, gpu_resps, nq):
     db = o.build_db(DB_SEED)
     build_s = time.perf_counter() - t
     times, match = [], True
+    nq = max(1, min(nq, len(queries)))
     gsw_ntt = [o.gsw_key_to_ntt(c[1]) for c in clients]
+    for i in range(3):  # warm-up (EXPERIMENT_ITERATIONS = 10 timed + 3)
+        j = i % len(queries)
+        o.make_query_server(db, clients[j % NUM_CLIENTS][0], gsw_ntt[j % NUM_CLIENTS], queries[j])
     for i in range(nq):
         gk = clients[i % NUM_CLIENTS][0]
         t = time.perf_counter()
@@ -483,8 +488,8 @@ def cpu_baseline(params, workload, clients, queries, gpu_resps, nq):
     qps = nq / sum(times)
     return {
         "value": qps, "unit": "queries/s", "cores": threads, "kind": "port",
-        "sample": (f"{nq} full queries (all stages) on the {workload} database "
-                   f"({params.get_num_pt()} plaintexts), {threads} threads; "
+        "sample": (f"{nq} full queries (all stages) after 3 untimed on the {workload} "
+                   f"database ({params.get_num_pt()} plaintexts), {threads} threads; "
                    f"database build {build_s:.1f} s untimed"),
         "single_thread_value": 1.0 / one_s,
         "cpu": host_cpu_model(),
