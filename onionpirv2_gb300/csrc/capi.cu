@@ -210,6 +210,7 @@ struct PipeEnv {
   uint32_t *status;  // device status word (bounded-wait timeouts)
   bool timed;        // record the stage events
   bool keep_pins;    // leave the batch's clients pinned (serving: until the batch completes)
+  bool graph = false;  // launches recorded into a CUDA graph
 };
 
 // ---- serving (continuous batching)
@@ -510,6 +511,11 @@ int run_pipeline(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
   const size_t w = (size_t)1 << h;
   const size_t n1 = db.shape.fst_dim_sz, nr = db.shape.other_dim_sz;
   const int l = (int)ctx->prm.gsw_l;
+  // Programmatic launches (a kernel stages its constant tables while its
+  // predecessor runs) of the kinds g_pdl_* select, never across stage events
+  // or trace copies; the first kernel follows host copies and launches
+  // normally.
+  const int pdl = E.timed || trace ? 0 : E.graph ? g_pdl_graph : g_pdl_direct;
 
   record(ctx, E, 0);
   // ---- expansion
@@ -520,7 +526,7 @@ int run_pipeline(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
     const int live = (int)((u + ((size_t)1 << (h - a)) - 1) >> (h - a));
     uint64_t *nxt = bufs[a & 1];
     launch_expand_level(cur, nxt, cur_stride, w * CTW, qd, a, live, batch, ctx->Mq.tab,
-                        ctx->Mp.tab, ctx->C, s);
+                        ctx->Mp.tab, ctx->C, s, (pdl & kPdlExpand) && a > 0);
     ctx->launches++;
     cur = nxt;
     cur_stride = w * CTW;
@@ -532,7 +538,8 @@ int run_pipeline(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
   const size_t gsw_stride = (size_t)(db.ndim > 1 ? db.ndim - 1 : 1) * 2 * l * CTW;
   if (db.ndim > 1) {
     launch_query_to_gsw(leaves, leaves_stride, W.gsw.as<uint64_t>(), gsw_stride, qd, (int)n1,
-                        (db.ndim - 1) * l, batch, ctx->Mq.tab, ctx->C, s);
+                        (db.ndim - 1) * l, batch, ctx->Mq.tab, ctx->C, s,
+                        (pdl & kPdlQtg) && h > 0);
     ctx->launches++;
   }
   record(ctx, E, 2);
@@ -542,6 +549,7 @@ int run_pipeline(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
   // a batch of queries shares one pass over the database (batched GEMM);
   // a single query (or an unsupported shape) streams it once per query
   const int use = engine_for(ctx, db, batch);
+  const bool pdl_prep = (pdl & kPdlPrep) && (h > 0 || db.ndim > 1);  // a kernel precedes
   const bool tensor = use == OPIR_ENGINE_TENSOR, batched = use == OPIR_ENGINE_IMAD;
   if (tensor) {
     if (!db.dbl_valid) {
@@ -554,7 +562,7 @@ int run_pipeline(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
     }
     CK(W.ql.alloc(tc_query_limb_bytes((int)n1, batch)), "alloc query limbs");
     launch_query_prep_plane(leaves, leaves_stride, W.qs.as<uint64_t>(), (int)n1, batch,
-                            ctx->Mq.tab, s);
+                            ctx->Mq.tab, s, pdl_prep);
     launch_tc_query_limbs(W.qs.as<uint64_t>(), W.ql.as<uint16_t>(), (int)n1, batch, s);
     ctx->launches += (batch + 31) / 32;
     record(ctx, E, 6);
@@ -564,21 +572,22 @@ int run_pipeline(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
                                     E.status, s) - 1;
   } else if (batched) {
     launch_query_prep_batched(leaves, leaves_stride, W.qs.as<uint4>(), (int)n1, batch,
-                              ctx->Mq.tab, s);
+                              ctx->Mq.tab, s, pdl_prep);
     record(ctx, E, 6);
     launch_scan_batched(db.dbs.as<uint64_t>(), W.qs.as<uint4>(), W.res.as<uint64_t>(), res_stride,
                         (int)n1, (int)nr, batch, ctx->C, ctx->Mq.tab.mu_lo, ctx->Mq.tab.mu_hi,
                         E.status, s);
   } else {
     launch_query_prep(leaves, leaves_stride, W.qs.as<uint4>(), qs_stride, (int)n1, batch,
-                      ctx->Mq.tab, s);
+                      ctx->Mq.tab, s, pdl_prep);
     record(ctx, E, 6);
     launch_scan(db.dbs.as<uint64_t>(), W.qs.as<uint4>(), qs_stride, W.res.as<uint64_t>(),
                 res_stride, (int)n1, (int)nr, batch, ctx->C, ctx->Mq.tab.mu_lo,
                 ctx->Mq.tab.mu_hi, E.status, s, db.scan_cfg);
   }
   record(ctx, E, 7);
-  launch_ntt(ctx->Mq.tab, W.res.as<uint64_t>(), (size_t)batch * nr * 2, true, s);
+  launch_ntt(ctx->Mq.tab, W.res.as<uint64_t>(), (size_t)batch * nr * 2, true, s,
+             (pdl & kPdlNtt) != 0);
   ctx->launches += 3;
   record(ctx, E, 3);
   if (trace && trace->first_dim)
@@ -589,14 +598,14 @@ int run_pipeline(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
   for (int i = 1; i < db.ndim; i++) {
     const int half = (int)(cnt / 2);
     launch_fold(W.res.as<uint64_t>(), res_stride, W.gsw.as<uint64_t>() + (size_t)(i - 1) * 2 * l * CTW,
-                gsw_stride, half, batch, ctx->Mq.tab, ctx->C, s);
+                gsw_stride, half, batch, ctx->Mq.tab, ctx->C, s, (pdl & kPdlFold) != 0);
     ctx->launches++;
     cnt = half;
   }
   record(ctx, E, 4);
   // ---- mod switch + pack
   launch_modswitch_pack(W.res.as<uint64_t>(), res_stride, d_resp, d_packed, ctx->resp_bytes, batch,
-                        ctx->C, s);
+                        ctx->C, s, (pdl & kPdlModswitch) != 0);
   ctx->launches++;
   record(ctx, E, 5);
   CK(cudaGetLastError(), "kernel launch");
@@ -668,15 +677,14 @@ int run_sync(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
   }
   const uint64_t launches0 = ctx->launches;
   CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin graph capture");
-  rc = run_pipeline(ctx, db, 1, client_ids, d_queries, d_resp, d_packed, nullptr, E);
+  PipeEnv Eg = E;
+  Eg.graph = true;
+  rc = run_pipeline(ctx, db, 1, client_ids, d_queries, d_resp, d_packed, nullptr, Eg);
   cudaGraph_t g = nullptr;
   const cudaError_t ce = cudaStreamEndCapture(s, &g);
-  if (rc) {
-    if (g) cudaGraphDestroy(g);
-    cudaGetLastError();
-    return rc;
-  }
-  bool ok = ce == cudaSuccess && g != nullptr;
+  // a launch the capture did not take also ends here: direct launches below
+  // then report the error of the launch itself, if it persists
+  bool ok = rc == OPIR_OK && ce == cudaSuccess && g != nullptr;
   Db::Graph *slot = nullptr;
   if (ok && db.graphs.size() < kGraphs) {
     db.graphs.push_back(Db::Graph{});

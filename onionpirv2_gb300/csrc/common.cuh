@@ -379,4 +379,25 @@ __device__ __forceinline__ void stage_wait() {
   __syncthreads();
 }
 
+// Programmatic dependent launch (PTX griddepcontrol).  A kernel launched with
+// programmatic stream serialization may become resident while the previous
+// kernel of its stream still runs: what it does before grid_dep_wait() may
+// read only data that no launch of the current pipeline writes (twiddle
+// tables, client keys).  grid_dep_wait() returns once the previous kernel has
+// completed and its writes are visible -- at once for a normal launch.
+// grid_dep_launch(), called after the wait, lets the next programmatic launch
+// become resident; every kernel that calls it has passed its own wait, so
+// when a kernel starts, all launches before the previous one are complete.
+__device__ __forceinline__ void grid_dep_wait() {
+  asm volatile("griddepcontrol.wait;\n" ::: "memory");
+}
+__device__ __forceinline__ void grid_dep_launch() {
+  asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+}
+// both, at the point where a kernel starts reading its predecessor's output
+__device__ __forceinline__ void grid_dep_sync() {
+  grid_dep_wait();
+  grid_dep_launch();
+}
+
 }  // namespace opir

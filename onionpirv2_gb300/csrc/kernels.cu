@@ -24,6 +24,7 @@ __global__ void __launch_bounds__(T) ntt_kernel(ModTab M, uint64_t *polys, int i
   __shared__ uint64_t sa[kSmemPoly], sb[kSmemPoly];
   uint64_t *p = polys + (size_t)blockIdx.x * kN;
   const int tid = threadIdx.x;
+  grid_dep_sync();
   uint64_t r[8];
   if (!inverse) {
 #pragma unroll
@@ -55,6 +56,7 @@ __global__ void __launch_bounds__(T) query_prep_kernel(const uint64_t *leaves,
   const int tid = threadIdx.x;
   const int k = blockIdx.x, b = blockIdx.y, poly = blockIdx.z;
   const uint64_t *ct = leaves + b * leaves_stride + (size_t)k * 2 * kN + (size_t)poly * kN;
+  grid_dep_sync();
   uint64_t r[8];
 #pragma unroll
   for (int e = 0; e < 8; ++e) r[e] = ct[strided_idx(tid, e)];
@@ -77,6 +79,7 @@ __global__ void __launch_bounds__(T) query_prep_plane_kernel(const uint64_t *lea
   const int tid = threadIdx.x;
   const int k = blockIdx.x, b = blockIdx.y, poly = blockIdx.z;  // one polynomial per CTA
   const uint64_t *ct = leaves + b * leaves_stride + (size_t)k * 2 * kN + (size_t)poly * kN;
+  grid_dep_sync();
   uint64_t r[8];
 #pragma unroll
   for (int e = 0; e < 8; ++e) r[e] = ct[strided_idx(tid, e)];
@@ -123,6 +126,7 @@ __global__ void __launch_bounds__(T) modswitch_pack_kernel(const uint64_t *res, 
   const int nwords = per * w / 32;  // the slice's words of the packed stream
   for (int i = tid; i < nwords; i += T) words[i] = 0;
   __syncthreads();
+  grid_dep_sync();
   const uint64_t *ct = res + b * res_stride;
   const uint64_t mask = (1ULL << w) - 1;
   for (int i = i0 + tid; i < i0 + per; i += T) {
@@ -263,35 +267,37 @@ __global__ void db_from_aligned_kernel(const uint64_t *aligned, uint64_t *dbs, i
 // launchers
 // ---------------------------------------------------------------------------
 
-void launch_ntt(const ModTab &M, uint64_t *polys, size_t count, bool inverse, cudaStream_t s) {
+void launch_ntt(const ModTab &M, uint64_t *polys, size_t count, bool inverse, cudaStream_t s,
+                bool pdl) {
   if (!count) return;
-  ntt_kernel<<<(unsigned)count, T, 0, s>>>(M, polys, inverse ? 1 : 0);
+  launch_kernel(pdl, ntt_kernel, dim3((unsigned)count), dim3(T), 0, s, M, polys, inverse ? 1 : 0);
 }
 
 void launch_query_prep(const uint64_t *leaves, size_t leaves_stride, uint4 *qs, size_t qs_stride,
-                       int n1, int batch, const ModTab &Mq, cudaStream_t s) {
-  query_prep_kernel<<<dim3(n1, batch, 2), T, 0, s>>>(leaves, leaves_stride, qs, qs_stride,
-                                                      (size_t)n1, 1, Mq);
+                       int n1, int batch, const ModTab &Mq, cudaStream_t s, bool pdl) {
+  launch_kernel(pdl, query_prep_kernel, dim3(n1, batch, 2), dim3(T), 0, s,
+                leaves, leaves_stride, qs, qs_stride, (size_t)n1, (size_t)1, Mq);
 }
 
 void launch_query_prep_batched(const uint64_t *leaves, size_t leaves_stride, uint4 *qsb, int n1,
-                               int batch, const ModTab &Mq, cudaStream_t s) {
-  query_prep_kernel<<<dim3(n1, batch, 2), T, 0, s>>>(leaves, leaves_stride, qsb, 1,
-                                                   (size_t)n1 * batch, (size_t)batch, Mq);
+                               int batch, const ModTab &Mq, cudaStream_t s, bool pdl) {
+  launch_kernel(pdl, query_prep_kernel, dim3(n1, batch, 2), dim3(T), 0, s,
+                leaves, leaves_stride, qsb, (size_t)1, (size_t)n1 * batch, (size_t)batch, Mq);
 }
 
 void launch_query_prep_plane(const uint64_t *leaves, size_t leaves_stride, uint64_t *plane,
-                             int n1, int batch, const ModTab &Mq, cudaStream_t s) {
-  query_prep_plane_kernel<<<dim3(n1, batch, 2), T, 0, s>>>(leaves, leaves_stride, plane, n1, Mq);
+                             int n1, int batch, const ModTab &Mq, cudaStream_t s, bool pdl) {
+  launch_kernel(pdl, query_prep_plane_kernel, dim3(n1, batch, 2), dim3(T), 0, s, leaves,
+                leaves_stride, plane, n1, Mq);
 }
 
 void launch_modswitch_pack(const uint64_t *res, size_t res_stride, uint64_t *resp,
                            uint8_t *packed, size_t packed_bytes, int batch, const Consts &C,
-                           cudaStream_t s) {
+                           cudaStream_t s, bool pdl) {
   // the packed stream is 2N w bits exactly; each slice fills its own words
   const size_t smem = ((size_t)(2 * kN / kModSlices) * C.small_q_width / 32 + 2) * sizeof(uint32_t);
-  modswitch_pack_kernel<<<dim3(kModSlices, batch), T, smem, s>>>(res, res_stride, resp, packed,
-                                                                 (int)packed_bytes, C);
+  launch_kernel(pdl, modswitch_pack_kernel, dim3(kModSlices, batch), dim3(T), smem, s, res,
+                res_stride, resp, packed, (int)packed_bytes, C);
 }
 
 void launch_db_pack(const uint8_t *entries, uint64_t *coeffs, size_t num_pt, int entry_size,

@@ -43,29 +43,59 @@ struct Consts {
 // device before the first launch.
 cudaError_t init_kernel_attributes();
 
+// Which dependent kernels of the query pipeline are programmatic launches, a
+// bit per launch kind: in a captured CUDA graph (g_pdl_graph, OPIR_PDL_GRAPH)
+// and in direct launches (g_pdl_direct, OPIR_PDL); set by
+// init_kernel_attributes.
+enum { kPdlExpand = 1, kPdlQtg = 2, kPdlPrep = 4, kPdlNtt = 8, kPdlFold = 16, kPdlModswitch = 32 };
+extern int g_pdl_graph, g_pdl_direct;
+
+// Launch `k` on stream s; with `pdl` the launch may become
+// resident while the previous kernel of the stream still runs, so `k` must
+// call grid_dep_wait() (common.cuh) before touching what earlier launches
+// write.  Errors surface through cudaGetLastError like <<< >>> launches.
+template <typename... P, typename... A>
+inline void launch_kernel(bool pdl, void (*k)(P...), dim3 grid, dim3 block, size_t smem,
+                          cudaStream_t s, A &&...args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, k, static_cast<A &&>(args)...);
+}
+
 // ---- batched transforms on polynomials in global memory (natural order in,
 // NTT slot order out for forward; slot order in, natural out for inverse)
-void launch_ntt(const ModTab &M, uint64_t *polys, size_t count, bool inverse, cudaStream_t s);
+// (pdl: a programmatic launch after the previous kernel of the pipeline)
+void launch_ntt(const ModTab &M, uint64_t *polys, size_t count, bool inverse, cudaStream_t s,
+                bool pdl = false);
 
 // ---- query expansion, one tree level for every query of the batch
 // cur: [B][nodes_in][2][N], nxt: [B][2*nodes_in][2][N]
 void launch_expand_level(const uint64_t *cur, uint64_t *nxt, size_t in_stride, size_t out_stride,
                          const QueryDesc *qd, int level, int live_nodes, int batch,
-                         const ModTab &Mq, const ModTab &Mp, const Consts &C, cudaStream_t s);
+                         const ModTab &Mq, const ModTab &Mp, const Consts &C, cudaStream_t s,
+                         bool pdl = false);
 
 // ---- RGSW reconstruction (query_to_gsw) for all further dimensions
 // leaves: [B][u][2][N] (coefficient form), gsw_out: [B][ndim-1][2l][2][N]
 void launch_query_to_gsw(const uint64_t *leaves, size_t leaves_stride, uint64_t *gsw_out,
                          size_t gsw_stride, const QueryDesc *qd, int n1, int num_cts, int batch,
-                         const ModTab &Mq, const Consts &C, cudaStream_t s);
+                         const ModTab &Mq, const Consts &C, cudaStream_t s, bool pdl = false);
 
 // ---- first dimension
 // NTT the first n1 leaves and transpose to the scan operand Qs[b][c][k]
 void launch_query_prep(const uint64_t *leaves, size_t leaves_stride, uint4 *qs, size_t qs_stride,
-                       int n1, int batch, const ModTab &Mq, cudaStream_t s);
+                       int n1, int batch, const ModTab &Mq, cudaStream_t s, bool pdl = false);
 // the same into the batched operand layout qsb[c][k][b]
 void launch_query_prep_batched(const uint64_t *leaves, size_t leaves_stride, uint4 *qsb, int n1,
-                               int batch, const ModTab &Mq, cudaStream_t s);
+                               int batch, const ModTab &Mq, cudaStream_t s, bool pdl = false);
 // out[b][row][poly][c] = sum_k DB[c][k][row] * Q[b][c][k][poly] mod q  (NTT form)
 // (bulk-copy pipelined kernel in tile configuration `cfg` -- < 0: the
 // default -- when the shape fits it, else a plain kernel; status collects
@@ -89,7 +119,8 @@ bool launch_scan_batched(const uint64_t *dbs, const uint4 *qsb, uint64_t *out, s
 // NTT the first n1 leaves into a plain plane[b][k][poly][c] of residues
 // (query operand of the tensor-core path)
 void launch_query_prep_plane(const uint64_t *leaves, size_t leaves_stride, uint64_t *plane,
-                             int n1, int batch, const ModTab &Mq, cudaStream_t s);
+                             int n1, int batch, const ModTab &Mq, cudaStream_t s,
+                             bool pdl = false);
 // Batched product on the tcgen05 tensor cores (tc_scan.cu): residues split
 // into 8-bit limbs held as bf16, exact fp32 accumulation in tensor memory.
 // The database needs its limb plane dbl (tc_db_limb_bytes, built by
@@ -110,12 +141,13 @@ int launch_tc_scan(const uint16_t *dbl, const uint16_t *ql, uint64_t *out, size_
 
 // ---- one folding level (other_dim_mux): res[b][j] += INTT(RGSW x (res[j+half]-res[j]))
 void launch_fold(uint64_t *res, size_t res_stride, const uint64_t *gsw, size_t gsw_stride,
-                 int half, int batch, const ModTab &Mq, const Consts &C, cudaStream_t s);
+                 int half, int batch, const ModTab &Mq, const Consts &C, cudaStream_t s,
+                 bool pdl = false);
 
 // ---- mod switch to small_q + response bit packing
 void launch_modswitch_pack(const uint64_t *res, size_t res_stride, uint64_t *resp,
                            uint8_t *packed, size_t packed_bytes, int batch, const Consts &C,
-                           cudaStream_t s);
+                           cudaStream_t s, bool pdl = false);
 
 // ---- database ingest
 // entry bytes (device) -> plaintext coefficients (bits_per_coeff LSB-first)

@@ -55,6 +55,7 @@ __global__ void __launch_bounds__(T, 2) expand_level_kernel(const uint64_t *cur,
   const uint64_t g = (uint64_t)(kN / k + 1);
   const uint64_t q = C.q, p = C.p;
   const uint64_t *ci = cur + b * in_stride + (size_t)node * 2 * kN;
+  grid_dep_sync();
 
   // automorphism x -> x^g on both polynomials (scatter to shared memory)
 #pragma unroll
@@ -189,6 +190,7 @@ __global__ void __launch_bounds__(T, 2) query_to_gsw_kernel(const uint64_t *leav
   uint64_t *sa = smem, *sb = smem + kSmemPoly, *sx = smem + 2 * kSmemPoly;  // sx: [2][N]
   ulonglong2 *s_fwd = reinterpret_cast<ulonglong2 *>(sx + 2 * kN);
   prefetch_tw(s_fwd, M.fwd);
+  grid_dep_sync();
   const int tid = threadIdx.x;
   const int j = blockIdx.x, b = blockIdx.y;
   const int l = C.l;
@@ -227,6 +229,7 @@ __global__ void __launch_bounds__(T, 2) fold_kernel(uint64_t *res, size_t res_st
   uint64_t *sa = smem, *sb = smem + kSmemPoly, *sd = smem + 2 * kSmemPoly;  // sd: [2][N]
   ulonglong2 *s_fwd = reinterpret_cast<ulonglong2 *>(sd + 2 * kN);
   prefetch_tw(s_fwd, M.fwd);
+  grid_dep_sync();
   const int tid = threadIdx.x;
   const int j = blockIdx.x, b = blockIdx.y;
   const uint64_t q = C.q;
@@ -294,6 +297,7 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(T)
     prefetch_words(s_key + kN, kb.q[b].galois_s + key_off, kN);
     prefetch_tw(s_inv, m ? Mp.inv : Mq.inv);
   }
+  grid_dep_sync();  // the staged tables and keys are constant; the parent level is not
   const int tid = threadIdx.x;
   const int k = 1 << level;
   const uint64_t g = (uint64_t)(kN / k + 1);
@@ -401,6 +405,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(T, 2)
   ulonglong2 *s_fwd = reinterpret_cast<ulonglong2 *>(s_sig + kN);  // staged by cp.async
   const ModTab &M = m ? Mp : Mq;
   prefetch_tw(s_fwd, M.fwd);
+  grid_dep_sync();
   const int tid = threadIdx.x;
   const int node = blockIdx.x >> 1, b = blockIdx.y;
   const int k = 1 << level;
@@ -540,6 +545,7 @@ __global__ void __cluster_dims__(kFoldCluster, 1, 1) __launch_bounds__(T)
   const uint64_t *yp = res + b * res_stride + (size_t)(j + half) * 2 * kN;
   const uint64_t *rgsw = gsw + b * gsw_stride;
   prefetch_tw(s_fwd, M.fwd);
+  grid_dep_sync();
   const int sh = (l - 1 - r) * C.base_log2;
   const uint64_t mask = (1ULL << C.base_log2) - 1;
   U128 acc0[8], acc1[8];
@@ -592,6 +598,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(T, 2)
   uint64_t *part = smem + 2 * kSmemPoly;  // [output polynomial][slot]
   ulonglong2 *s_fwd = reinterpret_cast<ulonglong2 *>(part + 2 * kN);  // staged by cp.async
   prefetch_tw(s_fwd, M.fwd);
+  grid_dep_sync();
   const int tid = threadIdx.x;
   const int j = blockIdx.x >> 1, b = blockIdx.y;
   const uint64_t q = C.q;
@@ -654,6 +661,7 @@ __global__ void __cluster_dims__(kQtgCluster, 1, 1) __launch_bounds__(T, 2)
   uint64_t *part = smem + 2 * kSmemPoly;
   ulonglong2 *s_fwd = reinterpret_cast<ulonglong2 *>(part + 2 * kN);
   prefetch_tw(s_fwd, M.fwd);
+  grid_dep_sync();
   const int tid = threadIdx.x;
   const int jct = blockIdx.x / kQtgCluster, b = blockIdx.y;
   const int l = C.l, lk = C.l_key;
@@ -739,6 +747,12 @@ constexpr size_t kExpandPairSmem = (2 * kSmemPoly + kN) * sizeof(uint64_t) + kN 
 constexpr size_t kExpandClusterSmem = kClusterSmem + kN * sizeof(ulonglong2) + 2 * kN * sizeof(uint64_t);
 static_assert(kExpandClusterSmem <= 227 * 1024, "shared memory per CTA");
 int g_sms = 152;
+// Measured on one query of the 262,144-plaintext database: in a graph, the
+// expansion levels gain (836 -> 841 queries/s, their kernels stage 96 KB of
+// twiddles and keys), folding loses (-> 819), the other kinds are neutral;
+// direct launches gain with every kind (797 -> 814).
+int g_pdl_graph = kPdlExpand;
+int g_pdl_direct = kPdlExpand | kPdlQtg | kPdlPrep | kPdlNtt | kPdlFold | kPdlModswitch;
 // one-CTA fold and RGSW reconstruction: transform buffers + the source
 // ciphertext + the staged forward twiddles
 constexpr size_t kExtSmem = (2 * kSmemPoly + 2 * kN) * sizeof(uint64_t) + kN * sizeof(ulonglong2);
@@ -792,65 +806,69 @@ cudaError_t init_kernel_attributes() {
   if (const char *v = getenv("OPIR_QTG_THRESHOLD")) g_qtg_threshold = atoi(v);
   if (const char *v = getenv("OPIR_PAIR_THRESHOLD")) g_pair_threshold = atoi(v);
   if (const char *v = getenv("OPIR_EXPAND_PAIR_THRESHOLD")) g_expand_pair_threshold = atoi(v);
+  g_pdl_graph = kPdlExpand;
+  g_pdl_direct = kPdlExpand | kPdlQtg | kPdlPrep | kPdlNtt | kPdlFold | kPdlModswitch;
+  if (const char *v = getenv("OPIR_PDL_GRAPH")) g_pdl_graph = atoi(v);
+  if (const char *v = getenv("OPIR_PDL")) g_pdl_direct = atoi(v);
   return cudaSuccess;
 }
 
 void launch_expand_level(const uint64_t *cur, uint64_t *nxt, size_t in_stride, size_t out_stride,
                          const QueryDesc *qd, int level, int live_nodes, int batch,
-                         const ModTab &Mq, const ModTab &Mp, const Consts &C, cudaStream_t s) {
+                         const ModTab &Mq, const ModTab &Mp, const Consts &C, cudaStream_t s,
+                         bool pdl) {
   for (int b0 = 0; b0 < batch; b0 += kMaxKeyBatch) {
     const int nb = batch - b0 < kMaxKeyBatch ? batch - b0 : kMaxKeyBatch;
     KeyBatch kb;
     for (int i = 0; i < nb; ++i) kb.q[i] = qd[b0 + i];
+    const uint64_t *in = cur + b0 * in_stride;
+    uint64_t *out = nxt + b0 * out_stride;
     if (live_nodes * nb < g_expand_threshold && 4 * live_nodes * nb <= g_sms)
-      expand_cluster_kernel<true><<<dim3(4 * live_nodes, nb), T, kExpandClusterSmem, s>>>(
-          cur + b0 * in_stride, nxt + b0 * out_stride, in_stride, out_stride, kb, level, Mq, Mp,
-          C);
+      launch_kernel(pdl, expand_cluster_kernel<true>, dim3(4 * live_nodes, nb), dim3(T),
+                    kExpandClusterSmem, s, in, out, in_stride, out_stride, kb, level, Mq, Mp, C);
     else if (live_nodes * nb < g_expand_threshold)
-      expand_cluster_kernel<false><<<dim3(4 * live_nodes, nb), T, kClusterSmem, s>>>(
-          cur + b0 * in_stride, nxt + b0 * out_stride, in_stride, out_stride, kb, level, Mq, Mp,
-          C);
+      launch_kernel(pdl, expand_cluster_kernel<false>, dim3(4 * live_nodes, nb), dim3(T),
+                    kClusterSmem, s, in, out, in_stride, out_stride, kb, level, Mq, Mp, C);
     else if (live_nodes * nb < g_expand_pair_threshold)
-      expand_pair_kernel<<<dim3(2 * live_nodes, nb), T, kExpandPairSmem, s>>>(
-          cur + b0 * in_stride, nxt + b0 * out_stride, in_stride, out_stride, kb, level, Mq, Mp,
-          C);
+      launch_kernel(pdl, expand_pair_kernel, dim3(2 * live_nodes, nb), dim3(T), kExpandPairSmem,
+                    s, in, out, in_stride, out_stride, kb, level, Mq, Mp, C);
     else
-      expand_level_kernel<<<dim3(live_nodes, nb), T, kExpandSmem, s>>>(
-          cur + b0 * in_stride, nxt + b0 * out_stride, in_stride, out_stride, kb, level, Mq, Mp,
-          C);
+      launch_kernel(pdl, expand_level_kernel, dim3(live_nodes, nb), dim3(T), kExpandSmem, s, in,
+                    out, in_stride, out_stride, kb, level, Mq, Mp, C);
   }
 }
 
 void launch_query_to_gsw(const uint64_t *leaves, size_t leaves_stride, uint64_t *gsw_out,
                          size_t gsw_stride, const QueryDesc *qd, int n1, int num_cts, int batch,
-                         const ModTab &Mq, const Consts &C, cudaStream_t s) {
+                         const ModTab &Mq, const Consts &C, cudaStream_t s, bool pdl) {
   if (num_cts <= 0) return;
   for (int b0 = 0; b0 < batch; b0 += kMaxKeyBatch) {
     const int nb = batch - b0 < kMaxKeyBatch ? batch - b0 : kMaxKeyBatch;
     KeyBatch kb;
     for (int i = 0; i < nb; ++i) kb.q[i] = qd[b0 + i];
+    const uint64_t *in = leaves + b0 * leaves_stride;
+    uint64_t *out = gsw_out + b0 * gsw_stride;
     if (C.l_key == 2 * (kQtgCluster - 1) && num_cts * nb < g_qtg_threshold)
-      query_to_gsw_cluster_kernel<<<dim3(kQtgCluster * num_cts, nb), T, kClusterSmem, s>>>(
-          leaves + b0 * leaves_stride, leaves_stride, gsw_out + b0 * gsw_stride, gsw_stride, kb,
-          n1, Mq, C);
+      launch_kernel(pdl, query_to_gsw_cluster_kernel, dim3(kQtgCluster * num_cts, nb), dim3(T),
+                    kClusterSmem, s, in, leaves_stride, out, gsw_stride, kb, n1, Mq, C);
     else
-      query_to_gsw_kernel<<<dim3(num_cts, nb), T, kExtSmem, s>>>(
-          leaves + b0 * leaves_stride, leaves_stride, gsw_out + b0 * gsw_stride, gsw_stride, kb,
-          n1, Mq, C);
+      launch_kernel(pdl, query_to_gsw_kernel, dim3(num_cts, nb), dim3(T), kExtSmem, s, in,
+                    leaves_stride, out, gsw_stride, kb, n1, Mq, C);
   }
 }
 
 void launch_fold(uint64_t *res, size_t res_stride, const uint64_t *gsw, size_t gsw_stride,
-                 int half, int batch, const ModTab &Mq, const Consts &C, cudaStream_t s) {
+                 int half, int batch, const ModTab &Mq, const Consts &C, cudaStream_t s,
+                 bool pdl) {
   if (C.l == kFoldCluster && half * batch < g_fold_threshold)
-    fold_cluster_kernel<<<dim3(kFoldCluster * half, batch), T, kClusterSmem, s>>>(
-        res, res_stride, gsw, gsw_stride, half, Mq, C);
+    launch_kernel(pdl, fold_cluster_kernel, dim3(kFoldCluster * half, batch), dim3(T),
+                  kClusterSmem, s, res, res_stride, gsw, gsw_stride, half, Mq, C);
   else if (half * batch < g_pair_threshold)
-    fold_pair_kernel<<<dim3(2 * half, batch), T, kClusterSmem, s>>>(res, res_stride, gsw,
-                                                                     gsw_stride, half, Mq, C);
+    launch_kernel(pdl, fold_pair_kernel, dim3(2 * half, batch), dim3(T), kClusterSmem, s, res,
+                  res_stride, gsw, gsw_stride, half, Mq, C);
   else
-    fold_kernel<<<dim3(half, batch), T, kExtSmem, s>>>(res, res_stride, gsw, gsw_stride, half, Mq,
-                                                       C);
+    launch_kernel(pdl, fold_kernel, dim3(half, batch), dim3(T), kExtSmem, s, res, res_stride,
+                  gsw, gsw_stride, half, Mq, C);
 }
 
 }  // namespace opir
