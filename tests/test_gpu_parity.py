@@ -378,6 +378,38 @@ def test_tensor_core_first_dim_matches_single_queries(oracle_lib, gpu_lib, monke
     server.close()
 
 
+@pytest.mark.parametrize("pdl", ["63", "0"])
+def test_batch_over_key_chunk_matches_oracle(oracle_lib, gpu_lib, monkeypatch, pdl):
+    """70 queries in one batch: the tree kernels take client keys in chunks
+    of 64 queries, so the batch launches each level twice (programmatic
+    launches on and off); every response equals the oracle's."""
+    from onionpirv2_gb300 import PirParams, PirServer
+    monkeypatch.setenv("OPIR_PDL", pdl)
+    o = oracle_lib.Oracle(4096, 256)
+    server = PirServer(PirParams(num_entries=4096, max_fst_dim=256))
+    server.gen_data(5)
+    db = o.build_db(5)
+    clients = [make_client(o, 800 + 3 * j) for j in range(5)]
+    for j, (sk, gk, gswk) in enumerate(clients):
+        server.set_client_galois_key(j, gk)
+        server.set_client_gsw_key(j, gswk)
+    B = 70
+    ids = [(7 * b) % 5 for b in range(B)]
+    idxs = [(b * 601 + 11) % 4096 for b in range(B)]
+    queries = np.stack([o.make_query(clients[ids[b]][0], 300 + b, idxs[b]) for b in range(B)])
+    resp, packed = server.make_query_batch(ids, queries)
+    gsw_ntt = [o.gsw_key_to_ntt(c[2]) for c in clients]
+    for b in list(range(0, B, 9)) + [63, 64, 65, B - 1]:
+        ref, ref_packed, _, _ = o.make_query_server(db, clients[ids[b]][1], gsw_ntt[ids[b]],
+                                                    queries[b])
+        assert np.array_equal(resp[b], ref), b
+        assert np.array_equal(packed[b], ref_packed), b
+    for b in range(B):
+        plain, _ = o.decrypt(clients[ids[b]][0], resp[b], 2)
+        assert np.array_equal(o.entry_from_plain(idxs[b], plain), server.direct_get_entry(idxs[b]))
+    server.close()
+
+
 def test_graph_replay_matches_direct_launches(oracle_lib, gpu_lib):
     """Single queries replayed from the captured CUDA graph (updated for
     every query: other clients, other queries) equal direct launches and the
