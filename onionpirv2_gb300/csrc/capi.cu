@@ -304,6 +304,7 @@ struct opir_ctx {
   std::unique_ptr<Serving> serving;
   bool timing = false;
   bool graphs = true;  // single queries on the synchronous path replay a CUDA graph
+  bool host_copies = false;  // host calls stage through device buffers (else mapped pinned memory)
   cudaEvent_t ev[8] = {};
   float stage_ms[6] = {};
   bool stage_valid = false;
@@ -808,6 +809,7 @@ int opir_ctx_create(const opir_params *P, int device, opir_ctx **out) {
   // test and sweep overrides of the engine choice
   if (const char *v = getenv("OPIR_TC")) c->engine = atoi(v) ? OPIR_ENGINE_TENSOR : OPIR_ENGINE_IMAD;
   if (const char *v = getenv("OPIR_GRAPHS")) c->graphs = atoi(v) != 0;
+  if (const char *v = getenv("OPIR_HOST_COPIES")) c->host_copies = atoi(v) != 0;
   if (const char *v = getenv("OPIR_BATCH_SCAN"))
     if (!atoi(v)) c->engine = OPIR_ENGINE_SCAN;
   if (const char *v = getenv("OPIR_TC_MIN_BATCH")) c->tc_min_batch = atoi(v);
@@ -1146,17 +1148,34 @@ static int query_host(opir_ctx *ctx, uint32_t db_id, uint32_t batch, const uint6
   CK(W.h_out.alloc(status_off + 16), "alloc pinned");
   CK(cudaStreamSynchronize(ctx->stream), "sync");
   std::memcpy(W.h_in.p, queries, batch * CTB);
-  CK(cudaMemcpyAsync(W.queries.p, W.h_in.p, batch * CTB, cudaMemcpyHostToDevice, ctx->stream),
-     "upload queries");
-  int rc = run_sync(ctx, *db, (int)batch, client_ids, W.queries.as<uint64_t>(),
-                    W.resp.as<uint64_t>(), W.packed.as<uint8_t>(), trace);
-  if (rc) return rc;
   uint8_t *h_resp = static_cast<uint8_t *>(W.h_out.p);
   uint8_t *h_packed = h_resp + batch * CTB;
-  if (resps)
+  // The staging buffers are mapped pinned memory: the first expansion level
+  // reads the queries and the mod-switch kernel writes the responses across
+  // the host link themselves, which saves the copy engine's three round trips
+  // (set OPIR_HOST_COPIES=1 for copies through device buffers).
+  uint64_t *d_in = nullptr;
+  uint8_t *d_out = nullptr;
+  const bool mapped =
+      !ctx->host_copies &&
+      cudaHostGetDevicePointer(reinterpret_cast<void **>(&d_in), W.h_in.p, 0) == cudaSuccess &&
+      cudaHostGetDevicePointer(reinterpret_cast<void **>(&d_out), W.h_out.p, 0) == cudaSuccess;
+  int rc;
+  if (mapped) {
+    rc = run_sync(ctx, *db, (int)batch, client_ids, d_in, reinterpret_cast<uint64_t *>(d_out),
+                  d_out + batch * CTB, trace);
+  } else {
+    cudaGetLastError();
+    CK(cudaMemcpyAsync(W.queries.p, W.h_in.p, batch * CTB, cudaMemcpyHostToDevice, ctx->stream),
+       "upload queries");
+    rc = run_sync(ctx, *db, (int)batch, client_ids, W.queries.as<uint64_t>(),
+                  W.resp.as<uint64_t>(), W.packed.as<uint8_t>(), trace);
+  }
+  if (rc) return rc;
+  if (resps && !mapped)
     CK(cudaMemcpyAsync(h_resp, W.resp.p, batch * CTB, cudaMemcpyDeviceToHost, ctx->stream),
        "download responses");
-  if (packed)
+  if (packed && !mapped)
     CK(cudaMemcpyAsync(h_packed, W.packed.p, batch * ctx->resp_bytes, cudaMemcpyDeviceToHost,
                        ctx->stream),
        "download responses");

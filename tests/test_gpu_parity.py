@@ -378,6 +378,43 @@ def test_tensor_core_first_dim_matches_single_queries(oracle_lib, gpu_lib, monke
     server.close()
 
 
+@pytest.mark.parametrize("copies", ["0", "1"])
+def test_host_staging_matches_oracle(oracle_lib, gpu_lib, monkeypatch, copies):
+    """Host-buffer calls, with the kernels reading queries from and writing
+    responses to mapped pinned memory (default) or through device buffers
+    and copies: single queries (graph replay and direct launches), a batch
+    and a trace equal the oracle."""
+    from onionpirv2_gb300 import PirParams, PirServer
+    monkeypatch.setenv("OPIR_HOST_COPIES", copies)
+    o = oracle_lib.Oracle(4096, 256)
+    server = PirServer(PirParams(num_entries=4096, max_fst_dim=256))
+    server.gen_data(33)
+    db = o.build_db(33)
+    ids, queries, refs = [], [], []
+    for j in range(3):
+        sk, gk, gswk = make_client(o, 200 + 3 * j)
+        server.set_client_galois_key(j, gk)
+        server.set_client_gsw_key(j, gswk)
+        qry = o.make_query(sk, 40 + j, 1311 * j + 5)
+        ids.append(j)
+        queries.append(qry)
+        refs.append(o.make_query_server(db, gk, o.gsw_key_to_ntt(gswk), qry))
+    for graphs in (True, False):
+        server.set_graphs(graphs)
+        for j in range(3):
+            r = server.make_query(j, queries[j])
+            assert np.array_equal(np.asarray(r), refs[j][0]), (graphs, j)
+            assert r.packed == refs[j][1].tobytes(), (graphs, j)
+    resp, packed = server.make_query_batch(ids, np.stack(queries))
+    for j in range(3):
+        assert np.array_equal(resp[j], refs[j][0])
+        assert np.array_equal(packed[j], refs[j][1])
+    tr = server.make_query_trace(0, queries[0])
+    assert np.array_equal(tr["resp"], refs[0][0])
+    assert np.array_equal(tr["packed"], refs[0][1])
+    server.close()
+
+
 @pytest.mark.parametrize("pdl", ["63", "0"])
 def test_batch_over_key_chunk_matches_oracle(oracle_lib, gpu_lib, monkeypatch, pdl):
     """70 queries in one batch: the tree kernels take client keys in chunks
