@@ -86,9 +86,27 @@ __device__ __forceinline__ void acc3_flush_mid(Acc3 &a) {
   add_to(a.MID, U128{a.mid, 0});
   a.mid = 0;
 }
+// Karatsuba form of the same sums: `mid` takes (a0 + a1)(b0 + b1) (< 2^62,
+// so it is flushed every 4 k-steps) and the cross terms are recovered at the
+// end as MID - LL - HH (exact, >= 0): three products per step instead of four.
+__device__ __forceinline__ void acc3_mac_k(Acc3 &a, uint32_t a0, uint32_t a1, uint32_t sa,
+                                           uint32_t b0, uint32_t b1, uint32_t sb) {
+  mad_cc(a.ll, a0, b0);
+  mad_cc(a.mid, sa, sb);
+  mad_cc(a.hh, a1, b1);
+}
+__device__ __forceinline__ void acc3_unkaratsuba(Acc3 &a) {
+  asm("sub.cc.u64 %0, %0, %2;\n\tsubc.u64 %1, %1, %3;"
+      : "+l"(a.MID.lo), "+l"(a.MID.hi)
+      : "l"(a.LL.lo), "l"(a.LL.hi));
+  asm("sub.cc.u64 %0, %0, %2;\n\tsubc.u64 %1, %1, %3;"
+      : "+l"(a.MID.lo), "+l"(a.MID.hi)
+      : "l"(a.HH.lo), "l"(a.HH.hi));
+}
 __device__ __forceinline__ uint64_t acc3_reduce(Acc3 &a, const Consts &C, uint64_t mu_lo,
-                                                uint64_t mu_hi) {
+                                                uint64_t mu_hi, bool karatsuba = false) {
   acc3_flush(a);
+  if (karatsuba) acc3_unkaratsuba(a);
   const uint64_t q = C.q;
   const uint64_t rl = barrett128(a.LL, q, mu_lo, mu_hi);
   const uint64_t rm = barrett128(a.MID, q, mu_lo, mu_hi);
@@ -188,8 +206,9 @@ struct ScanGeom {
 };
 
 // kRows rows per consumer thread, kWarps consumer warps (kRows * kWarps * 32
-// == 512), kStepK k-steps per stage, kStages stages, kMinBlocks CTAs per SM.
-template <int kRows, int kWarps, int kStepK, int kStages, int kMinBlocks>
+// == 512), kStepK k-steps per stage, kStages stages, kMinBlocks CTAs per SM;
+// kKara: Karatsuba products (acc3_mac_k).
+template <int kRows, int kWarps, int kStepK, int kStages, int kMinBlocks, int kKara>
 __global__ void __launch_bounds__(kWarps * 32 + 32, kMinBlocks)
     scan_bulk_kernel(const uint64_t *__restrict__ dbs, const uint4 *__restrict__ qs,
                      size_t qs_stride, uint64_t *out, size_t out_stride, ScanGeom G, Consts C,
@@ -197,6 +216,7 @@ __global__ void __launch_bounds__(kWarps * 32 + 32, kMinBlocks)
   constexpr int kTileRows = kRows * kWarps * 32;  // rows (of one or more planes) per tile
   static_assert(kStepK == 1 || kStepK == 2 || kStepK == 4 || kStepK == 8 || kStepK % 16 == 0,
                 "flush cadence: middle partial every 8 k-steps, outer ones every 16");
+  static_assert(!kKara || kStepK % 16 == 0, "Karatsuba form: middle partial every 4 k-steps");
   constexpr int kStageDbBytes = kStepK * kTileRows * 8;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const int stage_bytes = kStageDbBytes + G.q_bytes;
@@ -318,6 +338,30 @@ __global__ void __launch_bounds__(kWarps * 32 + 32, kMinBlocks)
           a[0] = sdb[(size_t)k * G.rt];
         }
         const uint4 bq = sq[k];
+        if constexpr (kKara) {
+          const uint32_t sb0 = bq.x + bq.y, sb1 = bq.z + bq.w;
+#pragma unroll
+          for (int rr = 0; rr < kRows; ++rr) {
+            const uint32_t a0 = (uint32_t)a[rr], a1 = (uint32_t)(a[rr] >> 32);
+            const uint32_t sa = a0 + a1;
+            acc3_mac_k(acc[rr][0], a0, a1, sa, bq.x, bq.y, sb0);
+            acc3_mac_k(acc[rr][1], a0, a1, sa, bq.z, bq.w, sb1);
+          }
+          if ((k & 15) == 15) {
+#pragma unroll
+            for (int rr = 0; rr < kRows; ++rr) {
+              acc3_flush(acc[rr][0]);
+              acc3_flush(acc[rr][1]);
+            }
+          } else if ((k & 3) == 3) {
+#pragma unroll
+            for (int rr = 0; rr < kRows; ++rr) {
+              acc3_flush_mid(acc[rr][0]);
+              acc3_flush_mid(acc[rr][1]);
+            }
+          }
+          continue;
+        }
 #pragma unroll
         for (int rr = 0; rr < kRows; ++rr) {
           const uint32_t a0 = (uint32_t)a[rr], a1 = (uint32_t)(a[rr] >> 32);
@@ -364,8 +408,8 @@ __global__ void __launch_bounds__(kWarps * 32 + 32, kMinBlocks)
 #pragma unroll
     for (int rr = 0; rr < kRows; ++rr) {
       const size_t row = (size_t)rt * G.rt + r + rr;
-      o[row * 2 * kN + c] = acc3_reduce(acc[rr][0], C, mu_lo, mu_hi);
-      o[row * 2 * kN + kN + c] = acc3_reduce(acc[rr][1], C, mu_lo, mu_hi);
+      o[row * 2 * kN + c] = acc3_reduce(acc[rr][0], C, mu_lo, mu_hi, kKara != 0);
+      o[row * 2 * kN + kN + c] = acc3_reduce(acc[rr][1], C, mu_lo, mu_hi, kKara != 0);
     }
   }
 }
@@ -630,16 +674,16 @@ int g_num_sms = 0;
 int g_cfg = 0;
 int g_batch_form = 3;  // accumulate spelling of scan_batch_kernel (OPIR_BATCH_MAC)
 
-template <int R, int W, int K, int S, int B>
+template <int R, int W, int K, int S, int B, int KA>
 cudaError_t set_attr() {
   constexpr int kTileRows = R * W * 32;
   const int max_smem = S * (K * kTileRows * 8 + (kTileRows / 2) * K * 16) + 2 * S * 8;
-  return cudaFuncSetAttribute(scan_bulk_kernel<R, W, K, S, B>,
+  return cudaFuncSetAttribute(scan_bulk_kernel<R, W, K, S, B, KA>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize,
                               max_smem > 227 * 1024 ? 227 * 1024 : max_smem);
 }
 
-template <int R, int W, int K, int S, int B>
+template <int R, int W, int K, int S, int B, int KA>
 bool launch_bulk(const uint64_t *dbs, const uint4 *qs, size_t qs_stride, uint64_t *out,
                  size_t out_stride, int n1, int n_rest, int batch, const Consts &C,
                  uint64_t mu_lo, uint64_t mu_hi, uint32_t *status, cudaStream_t s) {
@@ -658,35 +702,37 @@ bool launch_bulk(const uint64_t *dbs, const uint4 *qs, size_t qs_stride, uint64_
   const int smem = S * (K * kTileRows * 8 + G.q_bytes) + 2 * S * 8;
   if (smem > 227 * 1024) return false;  // tiny planes: many query runs per stage
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, scan_bulk_kernel<R, W, K, S, B>,
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, scan_bulk_kernel<R, W, K, S, B, KA>,
                                                 W * 32 + 32, smem);
   if (per_sm < 1) per_sm = 1;
   const int sms = g_num_sms > 0 ? g_num_sms : 152;
   long long grid = (long long)per_sm * sms;
   if (grid > G.items) grid = G.items;
-  scan_bulk_kernel<R, W, K, S, B><<<(unsigned)grid, W * 32 + 32, smem, s>>>(
+  scan_bulk_kernel<R, W, K, S, B, KA><<<(unsigned)grid, W * 32 + 32, smem, s>>>(
       dbs, qs, qs_stride, out, out_stride, G, C, mu_lo, mu_hi, status);
   return true;
 }
 
-// compiled configurations {rows, warps, k-steps, stages, CTAs/SM};
+// compiled configurations {rows, warps, k-steps, stages, CTAs/SM, Karatsuba};
 // OPIR_SCAN_CFG selects one by index (tuning sweeps)
 #define OPIR_SCAN_CONFIGS(X) \
-  X(0, 1, 16, 16, 3, 1)      \
-  X(1, 1, 16, 8, 6, 1)       \
-  X(2, 1, 16, 16, 2, 1)      \
-  X(3, 1, 16, 8, 5, 1)       \
-  X(4, 1, 16, 4, 12, 1)      \
-  X(5, 2, 8, 16, 3, 1)       \
-  X(6, 1, 8, 16, 3, 2)
-constexpr int kNumCfgs = 7;
+  X(0, 1, 16, 16, 3, 1, 0)   \
+  X(1, 1, 16, 8, 6, 1, 0)    \
+  X(2, 1, 16, 16, 2, 1, 0)   \
+  X(3, 1, 16, 8, 5, 1, 0)    \
+  X(4, 1, 16, 4, 12, 1, 0)   \
+  X(5, 2, 8, 16, 3, 1, 0)    \
+  X(6, 1, 8, 16, 3, 2, 0)    \
+  X(7, 1, 16, 16, 3, 1, 1)   \
+  X(8, 2, 8, 16, 3, 1, 1)
+constexpr int kNumCfgs = 9;
 
 }  // namespace
 
 cudaError_t init_scan_attributes() {
   cudaError_t e = cudaSuccess;
-#define OPIR_SET(i, R, W, K, S, B) \
-  if (e == cudaSuccess) e = set_attr<R, W, K, S, B>();
+#define OPIR_SET(i, R, W, K, S, B, KA) \
+  if (e == cudaSuccess) e = set_attr<R, W, K, S, B, KA>();
   OPIR_SCAN_CONFIGS(OPIR_SET)
 #undef OPIR_SET
   if (e != cudaSuccess) return e;
@@ -747,7 +793,7 @@ int scan_config_count() { return kNumCfgs; }
 
 void scan_config_desc(int i, uint32_t out[5]) {
   uint32_t d[kNumCfgs][5] = {
-#define OPIR_DESC(i, R, W, K, S, B) {R, W, K, S, B},
+#define OPIR_DESC(i, R, W, K, S, B, KA) {R, W, K, S, B},
       OPIR_SCAN_CONFIGS(OPIR_DESC)
 #undef OPIR_DESC
   };
@@ -761,10 +807,10 @@ int launch_scan(const uint64_t *dbs, const uint4 *qs, size_t qs_stride, uint64_t
   if (n_rest >= 2 && n1 % 8 == 0) {
     bool done = false;
     switch (cfg) {
-#define OPIR_CASE(i, R, W, K, S, B)                                                            \
-  case i:                                                                                      \
-    done = launch_bulk<R, W, K, S, B>(dbs, qs, qs_stride, out, out_stride, n1, n_rest, batch, \
-                                      C, mu_lo, mu_hi, status, s);                             \
+#define OPIR_CASE(i, R, W, K, S, B, KA)                                                      \
+  case i:                                                                                    \
+    done = launch_bulk<R, W, K, S, B, KA>(dbs, qs, qs_stride, out, out_stride, n1, n_rest,   \
+                                          batch, C, mu_lo, mu_hi, status, s);                \
     break;
       OPIR_SCAN_CONFIGS(OPIR_CASE)
 #undef OPIR_CASE

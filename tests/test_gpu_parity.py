@@ -187,7 +187,7 @@ SHAPES = [
 
 
 @pytest.mark.parametrize("shape", SHAPES)
-@pytest.mark.parametrize("cfg", [0, 1, 2, 3, 4, 5, 6])
+@pytest.mark.parametrize("cfg", [0, 1, 2, 3, 4, 5, 6, 7, 8])
 def test_scan_configs_and_shapes(oracle_lib, gpu_lib, monkeypatch, shape, cfg):
     """Every compiled scan pipeline configuration and every tile geometry
     gives the oracle's first-dimension result and response."""
