@@ -184,7 +184,8 @@ int opir_set_batch_engine(opir_ctx *ctx, int engine, uint32_t tensor_min_batch);
  * times in ms of one first-dimension product; < 0: cannot run this shape. */
 typedef struct opir_tune_report {
   uint32_t scan_configs;   /* compiled scan configurations (<= 16) */
-  uint32_t scan_desc[16][5]; /* rows per thread, warps, k-steps, stages, CTAs per SM */
+  uint32_t scan_desc[16][6]; /* rows per thread, warps, k-steps, stages, CTAs per SM,
+                                Karatsuba products (0/1) */
   float scan_ms[16];
   int32_t scan_choice;     /* chosen configuration, -1: the plain kernel */
   uint32_t batch_points;   /* number of batch sizes measured (<= 8) */

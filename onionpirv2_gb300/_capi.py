@@ -97,7 +97,7 @@ class OpirServeStats(ctypes.Structure):
 class OpirTuneReport(ctypes.Structure):
     _fields_ = [
         ("scan_configs", ctypes.c_uint32),
-        ("scan_desc", (ctypes.c_uint32 * 5) * 16),
+        ("scan_desc", (ctypes.c_uint32 * 6) * 16),
         ("scan_ms", ctypes.c_float * 16),
         ("scan_choice", ctypes.c_int32),
         ("batch_points", ctypes.c_uint32),

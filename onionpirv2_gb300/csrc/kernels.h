@@ -105,9 +105,9 @@ int launch_scan(const uint64_t *dbs, const uint4 *qs, size_t qs_stride, uint64_t
                 size_t out_stride, int n1, int n_rest, int batch, const Consts &C,
                 uint64_t mu_lo, uint64_t mu_hi, uint32_t *status, cudaStream_t s, int cfg = -1);
 // compiled tile configurations of the bulk scan: {rows per thread, warps,
-// k-steps per stage, stages, CTAs per SM}
+// k-steps per stage, stages, CTAs per SM, Karatsuba products}
 int scan_config_count();
-void scan_config_desc(int i, uint32_t out[5]);
+void scan_config_desc(int i, uint32_t out[6]);
 cudaError_t init_scan_attributes();
 // Batched product: one pass over the database for up to 32 queries at a time
 // (qsb[c][k][b], out as launch_scan).  Returns false if the shape is not

@@ -791,13 +791,13 @@ bool launch_scan_batched(const uint64_t *dbs, const uint4 *qsb, uint64_t *out, s
 
 int scan_config_count() { return kNumCfgs; }
 
-void scan_config_desc(int i, uint32_t out[5]) {
-  uint32_t d[kNumCfgs][5] = {
-#define OPIR_DESC(i, R, W, K, S, B, KA) {R, W, K, S, B},
+void scan_config_desc(int i, uint32_t out[6]) {
+  uint32_t d[kNumCfgs][6] = {
+#define OPIR_DESC(i, R, W, K, S, B, KA) {R, W, K, S, B, KA},
       OPIR_SCAN_CONFIGS(OPIR_DESC)
 #undef OPIR_DESC
   };
-  for (int k = 0; k < 5; k++) out[k] = (i >= 0 && i < kNumCfgs) ? d[i][k] : 0;
+  for (int k = 0; k < 6; k++) out[k] = (i >= 0 && i < kNumCfgs) ? d[i][k] : 0;
 }
 
 int launch_scan(const uint64_t *dbs, const uint4 *qs, size_t qs_stride, uint64_t *out,

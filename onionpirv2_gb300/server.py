@@ -290,7 +290,7 @@ class PirServer:
         self._check(self._L.opir_autotune(self._ctx, self.db_id if db_id is None else db_id,
                                           max_batch, reps, ctypes.byref(r)))
         names = {1: "scan", 2: "imad", 3: "tensor"}
-        keys = ("rows", "warps", "ksteps", "stages", "ctas_per_sm")
+        keys = ("rows", "warps", "ksteps", "stages", "ctas_per_sm", "karatsuba")
         return {
             "scan_configs": [dict(zip(keys, list(r.scan_desc[i])), ms=float(r.scan_ms[i]))
                              for i in range(r.scan_configs)],

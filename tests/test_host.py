@@ -25,6 +25,40 @@ def test_library_exports_every_declared_symbol(gpu_lib):
         assert hasattr(lib, s), s
 
 
+def test_ctypes_structs_match_the_c_header(tmp_path):
+    """Every ctypes mirror of an include/onionpir_gpu.h struct has the C
+    layout: size and each field's offset, from a program gcc compiles
+    against the header."""
+    import shutil
+    import subprocess
+    from onionpirv2_gb300 import _capi
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    mirrors = {"opir_params": _capi.OpirParams, "opir_db_shape": _capi.OpirDbShape,
+               "opir_serve_config": _capi.OpirServeConfig,
+               "opir_serve_stats": _capi.OpirServeStats,
+               "opir_tune_report": _capi.OpirTuneReport}
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "onionpir_gpu.h"',
+             "int main(void) {"]
+    for cname, cls in mirrors.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in cls._fields_:
+            lines.append(f'  printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                   check=True, capture_output=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {tuple(line.split()[:2]): int(line.split()[2]) for line in out if line.strip()}
+    for cname, cls in mirrors.items():
+        assert got[(cname, "size")] == ctypes.sizeof(cls), cname
+        for fname, _ in cls._fields_:
+            assert got[(cname, fname)] == getattr(cls, fname).offset, (cname, fname)
+
+
 def test_ctx_create_without_gpu_fails_cleanly(gpu_lib):
     import torch
     if torch.cuda.is_available():
