@@ -47,6 +47,27 @@ def test_single_rank_needs_no_process_group():
     assert bench.aggregate_replicas(20.0, 50, 1) == (20.0, 2500.0)
 
 
+def test_reference_arm_prints_the_contract_line():
+    """`bench.py --impl reference` (no GPU) prints one JSON line with the
+    metric, the CPU sample it timed and an e2e without device copies."""
+    import json
+    import subprocess
+    env = dict(os.environ, RANK="0", WORLD_SIZE="1")
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
+                          "--workload", "db4096", "--steps", "2", "--warmup", "1"],
+                         cwd=ROOT, env=env, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [x for x in out.stdout.splitlines() if x.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["unit"] == "queries/s" and d["value"] > 0
+    assert d["steps"] == 2 and d["warmup"] == 1 and d["higher_is_better"] is True
+    assert d["config"]["workload"] == "db4096"
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    assert d["e2e"] == {"value": d["value"], "unit": "queries/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}
+
+
 def test_reference_arm_runs_on_rank_zero_only(monkeypatch):
     sys.path.insert(0, ROOT)
     import bench
