@@ -139,16 +139,39 @@ int opir_make_query_trace(opir_ctx *ctx, uint32_t db_id, uint64_t client_id,
                           const uint64_t *query, uint64_t *leaves, uint64_t *gsw,
                           uint64_t *first_dim, uint64_t *resp, uint8_t *packed);
 
-/* First dimension only, without allocating device memory (no counterpart
- * in the reference; there it is the inside of evaluate_first_dim,
- * server.cpp:124-175).  d_fst_cts: the n1 expanded selection ciphertexts
+/* PirServer::save_resp_to_stream (server.cpp:581-633) for any responses:
+ * resps[count][2][N] (host; coefficients mod small_q, of which the low
+ * ceil(log2 small_q) bits are kept, as the reference masks them) ->
+ * packed[count][opir_response_bytes()] (host), each the reference's
+ * LSB-first bit stream of c0 then c1.  opir_make_query* already return the
+ * packed bytes of their own responses; this packs responses held elsewhere
+ * (batches, served tickets, stored ciphertexts).  Blocking. */
+int opir_pack_response(opir_ctx *ctx, const uint64_t *resps, uint32_t count, uint8_t *packed);
+
+/* PirServer::other_dim_mux (server.h:39, server.cpp:295-334): one folding
+ * level.  result[count][2][N] (host, coefficient form, fully reduced mod q;
+ * count even) and the RGSW selection ciphertext sel[2l][2][N] (host, NTT
+ * form: the layout query_to_gsw produces, gsw_eval.h:8).  For
+ * i < count/2: result[i] = result[i] + INTT(sel (x) (result[i + count/2] -
+ * result[i])); afterwards result[0 .. count/2) holds the folded ciphertexts
+ * (the reference resizes its vector to that half).  Blocking. */
+int opir_other_dim_mux(opir_ctx *ctx, uint64_t *result, uint64_t count, const uint64_t *sel);
+
+/* First dimension only, without allocating device memory.  No counterpart
+ * in the reference.  d_fst_cts: the n1 expanded selection ciphertexts
  * [n1][2][N] (device, coefficient form); d_out: the n_rest results
  * [n_rest][2][N] (device, coefficient form).  For callers that cannot call
- * cudaMalloc: the scan's query operand lives in a 16 MiB static device
- * array, so n1 <= 512 (larger databases get OPIR_ERR_ARG).  The first call
- * on a device looks up that array's address (cudaGetSymbolAddress), so make
- * it before any stream capture.  Asynchronous on the context stream; all
- * calls share the array, so calls that overlap on the GPU race. */
+ * cudaMalloc during a request (a request thread with a latency budget, since
+ * allocation synchronises the device, or a process whose device memory is
+ * reserved up front by another allocator): the scan's query operand lives in
+ * a 16 MiB static device array, so n1 <= 512 (larger databases get
+ * OPIR_ERR_ARG).  The first call on each context looks up that array's
+ * address (cudaGetSymbolAddress) with the context's device current, so make
+ * it before any stream capture.  Asynchronous on the context stream: a scan
+ * that gives up on a bounded device wait records it in the context's status
+ * word, which the next opir_sync reports as OPIR_ERR_TIMEOUT.  All calls (of
+ * every context on a device) share the array, so calls that overlap on the
+ * GPU race. */
 int opir_first_dim_noalloc(opir_ctx *ctx, uint32_t db_id, const uint64_t *d_fst_cts,
                            uint64_t *d_out);
 

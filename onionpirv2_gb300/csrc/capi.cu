@@ -309,6 +309,7 @@ struct opir_ctx {
   float stage_ms[6] = {};
   bool stage_valid = false;
   uint64_t launches = 0;
+  void *noalloc_scratch = nullptr;  // device address of the static scratch (opir_first_dim_noalloc)
   std::string err;
 
   int fail(int code, const char *fmt, ...) {
@@ -1429,6 +1430,51 @@ int opir_ntt_device(opir_ctx *ctx, int mod, int inverse, uint64_t *d_polys, uint
   return OPIR_OK;
 }
 
+// save_resp_to_stream (server.cpp:581-633) for responses the caller holds:
+// the bit packing of the pipeline's last kernel without its modulus switch.
+int opir_pack_response(opir_ctx *ctx, const uint64_t *resps, uint32_t count, uint8_t *packed) {
+  if (!ctx || !resps || !packed || !count) return OPIR_ERR_ARG;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  cudaSetDevice(ctx->device);
+  const size_t in_bytes = (size_t)count * 2 * kN * 8, out_bytes = (size_t)count * ctx->resp_bytes;
+  DevBuf din, dout;
+  CK(din.alloc(in_bytes), "alloc");
+  CK(dout.alloc(out_bytes), "alloc");
+  CK(cudaMemcpyAsync(din.p, resps, in_bytes, cudaMemcpyHostToDevice, ctx->stream), "upload");
+  launch_pack_response(din.as<uint64_t>(), 2 * (size_t)kN, dout.as<uint8_t>(), ctx->resp_bytes,
+                       (int)count, ctx->C, ctx->stream);
+  ctx->launches++;
+  CK(cudaGetLastError(), "pack launch");
+  CK(cudaMemcpyAsync(packed, dout.p, out_bytes, cudaMemcpyDeviceToHost, ctx->stream), "download");
+  CK(cudaStreamSynchronize(ctx->stream), "pack");
+  return OPIR_OK;
+}
+
+// other_dim_mux (server.cpp:295-334): one folding level of `count`
+// ciphertexts with one RGSW selection ciphertext, on the device.
+int opir_other_dim_mux(opir_ctx *ctx, uint64_t *result, uint64_t count, const uint64_t *sel) {
+  if (!ctx || !result || !sel) return OPIR_ERR_ARG;
+  if (count < 2 || count % 2 || count / 2 > 0x7fffffff)
+    return ctx->fail(OPIR_ERR_ARG, "other_dim_mux folds an even number (>= 2) of ciphertexts");
+  std::lock_guard<std::mutex> g(ctx->mu);
+  cudaSetDevice(ctx->device);
+  const size_t CTW = 2 * (size_t)kN;
+  const size_t res_bytes = count * CTW * 8, sel_bytes = 2 * (size_t)ctx->prm.gsw_l * CTW * 8;
+  DevBuf dres, dsel;
+  CK(dres.alloc(res_bytes), "alloc");
+  CK(dsel.alloc(sel_bytes), "alloc");
+  CK(cudaMemcpyAsync(dres.p, result, res_bytes, cudaMemcpyHostToDevice, ctx->stream), "upload");
+  CK(cudaMemcpyAsync(dsel.p, sel, sel_bytes, cudaMemcpyHostToDevice, ctx->stream), "upload");
+  launch_fold(dres.as<uint64_t>(), count * CTW, dsel.as<uint64_t>(), 2 * (size_t)ctx->prm.gsw_l * CTW,
+              (int)(count / 2), 1, ctx->Mq.tab, ctx->C, ctx->stream);
+  ctx->launches++;
+  CK(cudaGetLastError(), "fold launch");
+  CK(cudaMemcpyAsync(result, dres.p, res_bytes / 2, cudaMemcpyDeviceToHost, ctx->stream),
+     "download");
+  CK(cudaStreamSynchronize(ctx->stream), "other_dim_mux");
+  return OPIR_OK;
+}
+
 }  // extern "C"
 
 
@@ -1830,38 +1876,16 @@ int opir_serve_stats_get(opir_ctx *ctx, opir_serve_stats *out) {
 // First dimension without allocation
 //
 // For callers that must not allocate device memory during a call: a request
-// thread with a latency budget (cudaMalloc/cudaFree synchronise the device),
-// a host process whose device memory is pre-reserved by another allocator,
-// or code that later records the work into a CUDA graph.  The query operand
-// of the scan lives in the file-scope array below instead of context
-// workspace.  Every GPU that loads this library holds the array until the
-// process exits.
+// thread with a latency budget (cudaMalloc/cudaFree synchronise the device)
+// or a host process whose device memory is reserved up front by another
+// allocator.  The query operand of the scan lives in the file-scope array
+// below instead of context workspace.  Every GPU that loads this library
+// holds the array until the process exits.
 // ===========================================================================
 
 // Room for the transposed query operand: n1 * N * 16 bytes, so n1 <= 512.
 constexpr size_t kNoAllocScratchBytes = size_t(16) << 20;  // 16 MiB
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
-
-namespace {
-std::mutex g_noalloc_mu;
-constexpr int kMaxDevices = 64;
-void *g_noalloc_ptr[kMaxDevices] = {};
-
-// Device address of g_noalloc_scratch on the current device (looked up once
-// per device; the host-side symbol is not a device address).
-cudaError_t noalloc_scratch(int device, void **out) {
-  std::lock_guard<std::mutex> g(g_noalloc_mu);
-  if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
-  if (!g_noalloc_ptr[device]) {
-    void *p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) return e;
-    g_noalloc_ptr[device] = p;
-  }
-  *out = g_noalloc_ptr[device];
-  return cudaSuccess;
-}
-}  // namespace
 
 extern "C" int opir_first_dim_noalloc(opir_ctx *ctx, uint32_t db_id, const uint64_t *d_fst_cts,
                                       uint64_t *d_out) {
@@ -1877,12 +1901,21 @@ extern "C" int opir_first_dim_noalloc(opir_ctx *ctx, uint32_t db_id, const uint6
                      "%zu (first dimension <= %zu)",
                      n1, need, kNoAllocScratchBytes, kNoAllocScratchBytes / (kN * sizeof(uint4)));
   CK(cudaSetDevice(ctx->device), "set device");
-  void *scratch = nullptr;
-  CK(noalloc_scratch(ctx->device, &scratch), "cudaGetSymbolAddress(static scratch)");
-  uint4 *qs = static_cast<uint4 *>(scratch);
+  // The host-side symbol is not a device address: look the array up once per
+  // context, with the context's device current (a context never outlives the
+  // CUDA context its device buffers live in, so the address stays valid).
+  if (!ctx->noalloc_scratch) {
+    void *p = nullptr;
+    CK(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress(static scratch)");
+    ctx->noalloc_scratch = p;
+  }
+  uint4 *qs = static_cast<uint4 *>(ctx->noalloc_scratch);
   cudaStream_t s = ctx->stream;
   const size_t CTW = 2 * (size_t)kN;
-  // the operand is fully rewritten before the scan reads it: nothing to clear
+  // One query, so this is the plain streaming scan (engine_for picks it for
+  // batch 1 too); the batched engines' operand buffers and the tensor
+  // engine's limb planes, which are allocated on demand, are never touched.
+  // The operand is fully rewritten before the scan reads it: nothing to clear.
   launch_query_prep(d_fst_cts, n1 * CTW, qs, (size_t)kN * n1, (int)n1, 1, ctx->Mq.tab, s);
   launch_scan(db->dbs.as<uint64_t>(), qs, (size_t)kN * n1, d_out, nr * CTW, (int)n1, (int)nr, 1,
               ctx->C, ctx->Mq.tab.mu_lo, ctx->Mq.tab.mu_hi, ctx->status.as<uint32_t>(), s,

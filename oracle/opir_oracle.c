@@ -967,7 +967,9 @@ int orc_first_dim(const orc_ctx *ctx, const uint64_t *db, const uint64_t *fst, u
 }
 
 /* Same as orc_first_dim but with the reference's wrapping uint128 sums
- * (mat_mat_128, matrix.cpp:220-235): the loop that the CPU baseline times. */
+ * (mat_mat_128, matrix.cpp:220-235), for the exact-vs-wrapping tests.  The
+ * CPU baseline times orc_make_query_server, whose first dimension is the
+ * exact orc_first_dim: the same loop nest plus one carry count per MAC. */
 void orc_first_dim_wrapping(const orc_ctx *ctx, const uint64_t *db, const uint64_t *fst,
                             uint64_t *out) {
   const orc_params *P = &ctx->P;
