@@ -17,6 +17,12 @@ switch, packing).
   cpu_baseline  the CPU restatement of the reference server (oracle/), all
          host threads, full queries on the same database and inputs; its
          responses are also compared bit for bit with the GPU's.
+  batched  32 queries per step sharing one pass over the database on the
+         tensor-core engine (and the integer engine beside it).
+  large  the 2,097,152-plaintext database (1024 x 2048, 34.4 GB in NTT form):
+         64 queries per batch on the tensor-core engine against the same
+         queries one at a time, the tensor kernel's roofline, every response
+         decoded.
 
 Inputs: the database is seeded entries ingested on the GPU; four seeded
 PirClients (the CPU client library) make the Galois keys, RGSW keys and the
@@ -77,6 +83,13 @@ def parse():
     ap.add_argument("--serve-clients", type=int, default=512)
     ap.add_argument("--serve-light-rate", type=float, default=700.0,
                     help="--serve: a second leg at this offered rate, for latency below capacity")
+    ap.add_argument("--large-workload", default="db2097152",
+                    help="database of the large batched leg (2,097,152 plaintexts, 1024 x 2048)")
+    ap.add_argument("--large-batch", type=int, default=64,
+                    help="queries per batch of the large leg (0 = skip the leg)")
+    ap.add_argument("--large-steps", type=int, default=4, help="timed batches of the large leg")
+    ap.add_argument("--only-large", action="store_true",
+                    help="run the large batched leg alone and print its object")
     ap.add_argument("--batch-sweep", default=None,
                     help="comma-separated batch sizes: queries/s of every first-dimension "
                          "engine at each size (one JSON line per size)")
@@ -220,6 +233,135 @@ def serve_leg(server, qsets, rate, seconds, seed=7, max_batch=32, lanes=2, max_w
                                [resps[j].packed for j in sel], qs.db_seed,
                                qs.params.get_entry_size(), threads)[0]
     return stats, n, same, ok
+
+
+def tensor_roofline(params, B, ms, workload):
+    """Roofline of tc_scan_kernel: algorithmic bf16 flops of the limb GEMM
+    (64 limb products of 2 flops per 60x60-bit MAC, N * n_rest * n1 * 2B
+    MACs) over the kernel's time, against the measured burst bf16 peak (the
+    kernel is timed per launch, not over a seconds-long loop)."""
+    n1, nrest = params.get_fst_dim_sz(), params.get_other_dim_sz()
+    flops = 2.0 * 64 * nrest * 2 * B * n1 * N
+    peak, kind = measured_peak("bf16_tflops")
+    ach = flops / (ms / 1e3) / 1e12
+    return {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
+            "frac": ach / peak, "traffic": read_traffic(f"{workload}_b{B}", "tc_scan_kernel"),
+            "kernel": "tc_scan_kernel (first dimension of the batch)",
+            "flops_per_step": flops, "kernel_ms": ms,
+            "peak_source": f"{kind} bf16_tflops (burst)"}
+
+
+def large_leg(args, local, clocks=None):
+    """The 2,097,152-plaintext database (1024 x 2048: 34.4 GB in NTT form,
+    68.7 GB of tensor-engine limbs), B queries per batch on the tensor engine,
+    and the same queries one at a time.  Every response is decoded by its
+    client; the batch must equal the single queries bit for bit."""
+    import torch
+    from onionpirv2_gb300 import PirParams, PirServer
+    params = PirParams.preset(args.large_workload)
+    B = args.large_batch
+    dev = f"cuda:{local}"
+    server = PirServer(params, device=local)
+    stream = torch.cuda.Stream(device=local)
+    server.set_stream(stream.cuda_stream)
+    seed = DB_SEED + 2
+    t = time.perf_counter()
+    server.gen_data(seed)
+    ingest_s = time.perf_counter() - t
+    inp = Inputs(params, 2 * B, seed=3)
+    for cid, (gk, gsw) in enumerate(inp.keys):
+        server.set_client_galois_key(cid, gk)
+        server.set_client_gsw_key(cid, gsw)
+    nq = 2 * B
+    qbytes, rb = 2 * N * 8, server.resp_bytes
+    dq = torch.from_numpy(inp.queries.view(np.int64)).to(dev)
+    dresp = torch.empty((nq, 2, N), dtype=torch.int64, device=dev)
+    dpack = torch.empty((nq, rb), dtype=torch.uint8, device=dev)
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+
+    def one(i):
+        server.make_query_device([i % NUM_CLIENTS], dq.data_ptr() + i * qbytes,
+                                 dresp.data_ptr() + i * qbytes, dpack.data_ptr() + i * rb)
+
+    def batch(k):  # batch k holds queries [k B, (k + 1) B)
+        ids = [(k * B + j) % NUM_CLIENTS for j in range(B)]
+        server.make_query_device(ids, dq.data_ptr() + k * B * qbytes,
+                                 dresp.data_ptr() + k * B * qbytes, dpack.data_ptr() + k * B * rb)
+
+    with torch.cuda.stream(stream):
+        # single queries: every query once (the first B are the batch's reference)
+        for i in range(3):
+            one(i)
+        stream.synchronize()
+        e0, e1 = ev(), ev()
+        e0.record(stream)
+        for i in range(nq):
+            one(i)
+        e1.record(stream)
+        e1.synchronize()
+        single_ms = e0.elapsed_time(e1) / nq
+        single = dresp.cpu().numpy().view(np.uint64).reshape(nq, -1).copy()
+        server.set_batch_engine("tensor")
+        batch(0)  # builds the limb plane
+        batch(1)
+        stream.synchronize()
+        t1 = time.time()
+        e0.record(stream)
+        for k in range(args.large_steps):
+            batch(k % 2)
+        e1.record(stream)
+        e1.synchronize()
+        t2 = time.time()
+        bms = e0.elapsed_time(e1) / args.large_steps
+        server.set_timing(True)
+        st = []
+        for k in range(2):
+            batch(k)
+            stream.synchronize()
+            st.append(server.stage_times())
+        server.set_timing(False)
+        server.set_batch_engine("auto")
+    got = dresp.cpu().numpy().view(np.uint64).reshape(nq, -1)
+    same = bool(np.array_equal(got, single))
+    decoded, budget, _ = decode_check(inp.clients, inp.owners[:nq], inp.entries[:nq],
+                                      dpack.cpu().numpy(), seed, params.get_entry_size(),
+                                      threads=os.cpu_count() or 1)
+    stages = {k: statistics.mean(x[k] for x in st) for k in st[0]}
+    db_bytes = params.get_num_pt() * N * 8
+    out = {
+        "workload": args.large_workload, "db_plaintexts": params.get_num_pt(),
+        "n1": params.get_fst_dim_sz(), "n_rest": params.get_other_dim_sz(),
+        "ndim": len(params.get_dims()), "ntt_db_bytes": db_bytes, "batch": B,
+        "engine": "tensor (tcgen05, 8-bit limbs in bf16, exact)",
+        "value": B / (bms / 1e3), "unit": "queries/s", "ms_per_batch": bms,
+        "steps": args.large_steps, "stages_ms": stages,
+        "single_query": {"value": 1e3 / single_ms, "unit": "queries/s", "ms_per_query": single_ms,
+                         "queries": nq},
+        "speedup_vs_single": single_ms * B / bms,
+        "roofline": tensor_roofline(params, B, stages["scan_kernel"], args.large_workload),
+        "matches_single_query_responses": same,
+        "entries_decoded": f"{decoded}/{nq}", "min_noise_budget": budget,
+        "ingest_s": ingest_s,
+        "l2": f"inputs larger than L2 (NTT-form database {db_bytes / 1e9:.1f} GB > 129 MB)",
+    }
+    if clocks is not None:
+        out["clocks"] = clocks.summary(t1, t2)
+    server.close()
+    return out
+
+
+def large_main(args):
+    """The large batched leg alone (one JSON object)."""
+    import torch
+    _, _, local = dist_env()
+    torch.cuda.set_device(local)
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.5)
+    out = large_leg(args, local, clocks)
+    clocks.stop()
+    print(json.dumps(out), flush=True)
+    return 0
 
 
 def sweep_main(args):
@@ -490,7 +632,8 @@ def cpu_baseline(params, workload, clients, queries, gpu_resps, nq):
         "value": qps, "unit": "queries/s", "cores": threads, "kind": "port",
         "sample": (f"{nq} full queries (all stages) after 3 untimed on the {workload} "
                    f"database ({params.get_num_pt()} plaintexts), {threads} threads; "
-                   f"database build {build_s:.1f} s untimed"),
+                   f"database build {build_s:.1f} s untimed; first dimension: the "
+                   "mat_mat_128 loop nest with exact sums (orc_first_dim)"),
         "single_thread_value": 1.0 / one_s,
         "cpu": host_cpu_model(),
     }, match
@@ -606,6 +749,8 @@ def main():
         return serve_main(args)
     if args.batch_sweep:
         return sweep_main(args)
+    if args.only_large:
+        return large_main(args)
     rank, world, local = dist_env()
     import torch
     if not torch.cuda.is_available():
@@ -748,21 +893,11 @@ def main():
         single_resps = dresp[:B].cpu().numpy().view(np.uint64).reshape(B, -1).copy()
         tensor = run_batched("tensor")
         imad = run_batched("imad")
-        # tensor-core kernel roofline: algorithmic bf16 flops of the limb GEMM
-        # (64 limb products per 60x60-bit MAC) / its launch time (stage events)
-        n1, nrest = params.get_fst_dim_sz(), params.get_other_dim_sz()
-        flops = 2.0 * 64 * nrest * 2 * B * n1 * N
-        tms = tensor["stages_ms"]["scan_kernel"]
-        tpeak, tkind = measured_peak("bf16_tflops_sustained")
-        tach = flops / (tms / 1e3) / 1e12
+        # tensor-core kernel roofline (limb-GEMM flops / kernel time, burst peak)
         batched = dict(tensor, batch=B, engine="tensor (tcgen05, 8-bit limbs in bf16, exact)",
                        speedup_vs_single=tensor["value"] / qps,
-                       roofline={"bound": "tensor", "achieved": tach, "peak": tpeak,
-                                 "unit": "TFLOP/s", "frac": tach / tpeak,
-                                 "traffic": read_traffic(f"{args.workload}_b{B}", "tc_scan_kernel"),
-                                 "kernel": "tc_scan_kernel (first dimension of the batch)",
-                                 "flops_per_step": flops,
-                                 "peak_source": f"{tkind} bf16_tflops_sustained"},
+                       roofline=tensor_roofline(params, B, tensor["stages_ms"]["scan_kernel"],
+                                                args.workload),
                        imad=dict(imad, engine="integer multiply-add GEMM"))
     # ---- client side: every response of the timed queries (rewritten by
     # the batched passes, which equal them) decodes to its database entry
@@ -790,8 +925,14 @@ def main():
                    "failed": sstats["failed"], "bit_exact_sample": ssame,
                    "entries_decoded": f"{sok}/{sn}",
                    "policy": "max_batch 32, 2 lanes, max_wait 2 ms"}
-    clocks.stop()
     e2e_qps = e2e_steps * world / (e2e_ms / 1e3)
+    # ---- large: the 2,097,152-plaintext database, batches on the tensor
+    # engine (this database's device memory released first)
+    server.close()
+    large = None
+    if args.large_batch > 1 and world == 1:
+        large = large_leg(args, local, clocks)
+    clocks.stop()
 
     db_bytes = db_bytes_cfg = params.get_num_pt() * N * 8
     peak, peak_kind = measured_peak()
@@ -833,6 +974,7 @@ def main():
                    "what": "PirClient (CPU) per client: Galois keys + RGSW(sk); per query: "
                            "generation; per response: unpack, decrypt, entry"},
         "batched": batched,
+        "large": large,
         "serving": serving,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -842,7 +984,6 @@ def main():
         line["full_size_parity"] = "bit-exact vs oracle" if match else "MISMATCH vs oracle"
     if rank == 0:
         print(json.dumps(line), flush=True)
-    server.close()
     if pg:
         import torch.distributed as dist
         dist.destroy_process_group()

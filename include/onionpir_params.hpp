@@ -15,6 +15,9 @@ namespace onionpir {
 
 using Ciphertext = std::vector<uint64_t>;  // [2][N], coefficient form
 using Entry = std::vector<uint8_t>;
+// One RGSW ciphertext (GSWCiphertext, gsw_eval.h:8): 2l rows [row][2][N]
+// flattened, NTT form.
+using GSWCiphertext = std::vector<uint64_t>;
 
 struct PirParams {
   uint64_t q = 0, p = 0, t = 0, small_q = 0;  // CoeffModulus::Create / generate_prime results

@@ -95,12 +95,41 @@ class PirServer {
     return resp;
   }
 
-  // server.cpp:581-633: writes the packed response; returns its size
+  // server.cpp:581-633: writes the packed response; returns its size.  Any
+  // response mod small_q is accepted; the last make_query response reuses
+  // the bytes the GPU packed with it, others are packed on the GPU.
   size_t save_resp_to_stream(const Ciphertext &response, std::ostream &stream) {
-    if (response != last_resp_) throw std::invalid_argument("not the last response of make_query");
-    stream.write(reinterpret_cast<const char *>(last_packed_.data()),
-                 (std::streamsize)last_packed_.size());
-    return last_packed_.size();
+    if (response.size() != 2 * (size_t)params_.poly_degree)
+      throw std::invalid_argument("response must be one ciphertext");
+    const std::vector<uint8_t> *bytes = &last_packed_;
+    std::vector<uint8_t> packed;
+    if (response != last_resp_ || last_packed_.empty()) {
+      packed.assign(resp_bytes_, 0);
+      check(opir_pack_response(ctx_, response.data(), 1, packed.data()));
+      bytes = &packed;
+    }
+    stream.write(reinterpret_cast<const char *>(bytes->data()), (std::streamsize)bytes->size());
+    return bytes->size();
+  }
+
+  // server.h:39, server.cpp:295-334: folds result = [x || y] to
+  // x + RGSW(b) (x) (y - x) with one RGSW selection ciphertext ([2l][2][N],
+  // NTT form) and resizes result to its first half, as the reference does.
+  void other_dim_mux(std::vector<Ciphertext> &result, const GSWCiphertext &selection_cipher) {
+    const size_t ct = 2 * (size_t)params_.poly_degree;
+    if (result.empty() || result.size() % 2)
+      throw std::invalid_argument("other_dim_mux folds an even number of ciphertexts");
+    if (selection_cipher.size() != 2 * (size_t)params_.l * ct)
+      throw std::invalid_argument("selection_cipher must be one RGSW ciphertext");
+    std::vector<uint64_t> flat(result.size() * ct);
+    for (size_t i = 0; i < result.size(); ++i) {
+      if (result[i].size() != ct) throw std::invalid_argument("result must hold ciphertexts");
+      std::copy(result[i].begin(), result[i].end(), flat.begin() + i * ct);
+    }
+    check(opir_other_dim_mux(ctx_, flat.data(), result.size(), selection_cipher.data()));
+    result.resize(result.size() / 2);
+    for (size_t i = 0; i < result.size(); ++i)
+      result[i].assign(flat.begin() + i * ct, flat.begin() + (i + 1) * ct);
   }
 
   // Many queries at once, one pass over the database; each response equals

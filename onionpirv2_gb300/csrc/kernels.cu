@@ -113,8 +113,11 @@ __device__ __forceinline__ uint64_t mod_switch_coeff(uint64_t x, const Consts &C
 
 // One CTA per slice of kModSlices consecutive coefficient ranges of one
 // response: 2N / kModSlices coefficients (a multiple of 32, so every slice
-// starts on a 32-bit word of the packed stream), one per thread.
+// starts on a 32-bit word of the packed stream), one per thread.  kSwitch:
+// mod-switch each coefficient first (the query pipeline); else pack the
+// coefficients as given (save_resp_to_stream of any response).
 constexpr int kModSlices = 16;
+template <bool kSwitch>
 __global__ void __launch_bounds__(T) modswitch_pack_kernel(const uint64_t *res, size_t res_stride,
                                                            uint64_t *resp, uint8_t *packed,
                                                            int packed_bytes, Consts C) {
@@ -130,7 +133,7 @@ __global__ void __launch_bounds__(T) modswitch_pack_kernel(const uint64_t *res, 
   const uint64_t *ct = res + b * res_stride;
   const uint64_t mask = (1ULL << w) - 1;
   for (int i = i0 + tid; i < i0 + per; i += T) {
-    const uint64_t v = mod_switch_coeff(ct[i], C);
+    const uint64_t v = kSwitch ? mod_switch_coeff(ct[i], C) : ct[i];
     if (resp) resp[(size_t)b * 2 * kN + i] = v;
     const uint64_t m = v & mask;
     const uint64_t bit = (uint64_t)(i - i0) * w;
@@ -296,8 +299,15 @@ void launch_modswitch_pack(const uint64_t *res, size_t res_stride, uint64_t *res
                            cudaStream_t s, bool pdl) {
   // the packed stream is 2N w bits exactly; each slice fills its own words
   const size_t smem = ((size_t)(2 * kN / kModSlices) * C.small_q_width / 32 + 2) * sizeof(uint32_t);
-  launch_kernel(pdl, modswitch_pack_kernel, dim3(kModSlices, batch), dim3(T), smem, s, res,
+  launch_kernel(pdl, modswitch_pack_kernel<true>, dim3(kModSlices, batch), dim3(T), smem, s, res,
                 res_stride, resp, packed, (int)packed_bytes, C);
+}
+
+void launch_pack_response(const uint64_t *resps, size_t stride, uint8_t *packed,
+                          size_t packed_bytes, int batch, const Consts &C, cudaStream_t s) {
+  const size_t smem = ((size_t)(2 * kN / kModSlices) * C.small_q_width / 32 + 2) * sizeof(uint32_t);
+  launch_kernel(false, modswitch_pack_kernel<false>, dim3(kModSlices, batch), dim3(T), smem, s,
+                resps, stride, (uint64_t *)nullptr, packed, (int)packed_bytes, C);
 }
 
 void launch_db_pack(const uint8_t *entries, uint64_t *coeffs, size_t num_pt, int entry_size,

@@ -149,6 +149,11 @@ void launch_modswitch_pack(const uint64_t *res, size_t res_stride, uint64_t *res
                            uint8_t *packed, size_t packed_bytes, int batch, const Consts &C,
                            cudaStream_t s, bool pdl = false);
 
+// ---- response bit packing alone (save_resp_to_stream of any response
+// mod small_q): resps[b] at stride words -> packed[b][packed_bytes]
+void launch_pack_response(const uint64_t *resps, size_t stride, uint8_t *packed,
+                          size_t packed_bytes, int batch, const Consts &C, cudaStream_t s);
+
 // ---- database ingest
 // entry bytes (device) -> plaintext coefficients (bits_per_coeff LSB-first)
 void launch_db_pack(const uint8_t *entries, uint64_t *coeffs, size_t num_pt, int entry_size,

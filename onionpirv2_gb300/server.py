@@ -232,14 +232,45 @@ class PirServer:
                     gsw=gsw.reshape(max(ndim - 1, 1), 2 * P.get_l(), 2, N),
                     first_dim=fd.reshape(-1, 2, N), resp=resp.reshape(2, N), packed=packed)
 
-    def save_resp_to_stream(self, response: ResponseCiphertext, stream: io.IOBase) -> int:
+    def save_resp_to_stream(self, response, stream: io.IOBase) -> int:
         """Write the response's packed bytes (server.cpp:581-633); returns the
-        number of bytes written."""
+        number of bytes written.  Any response ciphertext mod small_q ((2, N)
+        uint64) is accepted: one that carries the bytes the GPU packed with it
+        (make_query, poll, wait) is written as is, any other (a row of a
+        batch, a stored ciphertext) is packed on the GPU (opir_pack_response)."""
         packed = getattr(response, "packed", None)
         if packed is None:
-            raise ValueError("response was not produced by make_query")
+            packed = self.pack_responses(np.asarray(response).reshape(1, 2, N))[0].tobytes()
         stream.write(packed)
         return len(packed)
+
+    def pack_responses(self, responses) -> np.ndarray:
+        """The reference's packed wire bytes of every response
+        ([count][2][N] mod small_q) -> uint8 [count][resp_bytes]."""
+        r = np.ascontiguousarray(responses, np.uint64)
+        if r.size == 0 or r.size % (2 * N):
+            raise ValueError("responses must be [count][2][N] uint64")
+        count = r.size // (2 * N)
+        out = np.zeros(count * self.resp_bytes, np.uint8)
+        self._check(self._L.opir_pack_response(self._ctx, _capi.p64(r.reshape(-1)), count,
+                                               _capi.p8(out)))
+        return out.reshape(count, self.resp_bytes)
+
+    def other_dim_mux(self, result, selection_cipher) -> np.ndarray:
+        """One folding level (server.cpp:295-334): result [count][2][N]
+        (coefficient form mod q, count even) and the RGSW selection
+        ciphertext [2l][2][N] (NTT form) -> the count/2 ciphertexts
+        result[i] + INTT(RGSW(b) x (result[i + count/2] - result[i]))."""
+        r = np.ascontiguousarray(result, np.uint64).copy()
+        sel = np.ascontiguousarray(selection_cipher, np.uint64)
+        if r.size % (2 * N) or (r.size // (2 * N)) % 2:
+            raise ValueError("result must hold an even number of ciphertexts [count][2][N]")
+        if sel.size != 2 * self.pir_params.get_l() * 2 * N:
+            raise ValueError("selection_cipher must be one RGSW ciphertext [2l][2][N]")
+        count = r.size // (2 * N)
+        self._check(self._L.opir_other_dim_mux(self._ctx, _capi.p64(r.reshape(-1)), count,
+                                               _capi.p64(sel.reshape(-1))))
+        return r.reshape(count, 2, N)[: count // 2].copy()
 
     # ---- further databases on this context (served side by side)
     def add_database(self, pir_params: PirParams, seed: Optional[int] = None) -> int:

@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstring>
 #include <sstream>
+#include <string>
 #include <stdexcept>
 #include <vector>
 
@@ -33,6 +34,7 @@ int main() {
   std::vector<uint8_t> ref_packed(orc_response_bytes(o)), expect(P.entry_size);
   std::vector<size_t> all_clients;
   std::vector<onionpir::Ciphertext> all_queries, all_resps;
+  std::vector<std::string> all_bytes;
   for (size_t i = 0; i < iters; ++i) {
     const uint64_t client_id = 1000 + i, idx = (i * 2654435761ULL + 17) % P.num_entries;
     // odd iterations: keys and queries from OS entropy; even: seeded
@@ -52,6 +54,7 @@ int main() {
     std::stringstream stream;
     const size_t n = server.save_resp_to_stream(resp, stream);
     const std::string bytes = stream.str();
+    all_bytes.push_back(bytes);
     int budget = 0;
     const onionpir::Plaintext plain =
         client.decrypt_mod_q(client.load_resp_from_stream(stream), &budget);
@@ -77,12 +80,23 @@ int main() {
   }
   // the same queries as one batch, and through the serving loop
   const std::vector<onionpir::Ciphertext> batch = server.make_query_batch(all_clients, all_queries);
+  // save_resp_to_stream packs any response: every batch row and served
+  // response must stream the bytes of the single query's response
   int batch_same = 0, served_same = 0;
-  for (size_t i = 0; i < iters; ++i) batch_same += batch[i] == all_resps[i];
+  for (size_t i = 0; i < iters; ++i) {
+    std::stringstream st;
+    server.save_resp_to_stream(batch[i], st);
+    batch_same += batch[i] == all_resps[i] && st.str() == all_bytes[i];
+  }
   server.serve_start(4, 2, 500);
   std::vector<uint64_t> tickets;
   for (size_t i = 0; i < iters; ++i) tickets.push_back(server.submit(all_clients[i], all_queries[i]));
-  for (size_t i = 0; i < iters; ++i) served_same += server.wait(tickets[i]) == all_resps[i];
+  for (size_t i = 0; i < iters; ++i) {
+    const onionpir::Ciphertext r = server.wait(tickets[i]);
+    std::stringstream st;
+    server.save_resp_to_stream(r, st);
+    served_same += r == all_resps[i] && st.str() == all_bytes[i];
+  }
   const opir_serve_stats st = server.serve_stats();
   server.serve_stop();
   std::printf("Success rate: %d/%zu, bit-identical: %d/%zu, unknown client -> out_of_range: %s\n",
