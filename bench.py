@@ -570,12 +570,14 @@ class ClockSampler:
 
 
 def read_traffic(workload, kernel="scan_kernel"):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+    """DRAM bytes of `kernel` per launch -- or per batch, where a batch is
+    several launches -- from the committed ncu summary, if any."""
     path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
     try:
         with open(path) as f:
             for line in f:
-                if line.strip().startswith("traffic_bytes_per_launch:"):
+                if line.strip().startswith(("traffic_bytes_per_launch:",
+                                            "traffic_bytes_per_batch:")):
                     return float(line.split(":", 1)[1])
     except OSError:
         pass

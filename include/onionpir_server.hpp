@@ -89,8 +89,10 @@ class PirServer {
     if (query.size() != 2 * (size_t)params_.poly_degree)
       throw std::invalid_argument("query must be one ciphertext");
     Ciphertext resp(query.size());
-    last_packed_.assign(resp_bytes_, 0);
-    check(opir_make_query(ctx_, db_, client_id, query.data(), resp.data(), last_packed_.data()));
+    std::vector<uint8_t> packed(resp_bytes_, 0);
+    check(opir_make_query(ctx_, db_, client_id, query.data(), resp.data(), packed.data()));
+    // the packed bytes are kept only for a query that succeeded
+    last_packed_.swap(packed);
     last_resp_ = resp;
     return resp;
   }
