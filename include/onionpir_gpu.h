@@ -279,6 +279,15 @@ uint64_t opir_launch_count(const opir_ctx *ctx);
  * error recorded by asynchronous queries (OPIR_ERR_TIMEOUT). */
 int opir_sync(opir_ctx *ctx);
 
+/* Test hook of the bounded device waits (no reference counterpart).  With
+ * polls > 0 the single-query scan of this context's synchronous calls
+ * withholds the copies of one pipeline stage in its first CTA and gives up
+ * waiting for that stage after `polls` polls (at most 2^20; the production
+ * limit is 2^22): the call then returns OPIR_ERR_TIMEOUT with the status
+ * bits in opir_last_error, and the next call on the context runs normally.
+ * 0 turns it off.  Not for production use. */
+int opir_debug_withhold_scan_stage(opir_ctx *ctx, uint32_t polls);
+
 /* ---- primitives (tests) ---- */
 /* Negacyclic NTT of `count` polynomials mod q (mod = 0) or p (mod = 1),
  * host buffers, in place. */

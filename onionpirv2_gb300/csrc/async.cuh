@@ -18,6 +18,13 @@ constexpr uint32_t kErrDrain = 4u;      // producer gave up draining its copies
 constexpr uint32_t kSpinLimit = 1u << 22;
 constexpr uint32_t kSuspendHintNs = 2000;  // per try_wait; the wait stays bounded by kSpinLimit tries
 
+// A kernel's status area is kStatusWords words: [0] the error bits above,
+// [1] a test hook read by the single-query scan -- nonzero: its first CTA
+// withholds the copies of its first pipeline stage and its waits give up
+// after that many polls, so a test can make a consumer wait run out (the
+// host sets it through opir_debug_withhold_scan_stage; 0 in production).
+constexpr int kStatusWords = 4;
+
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
@@ -68,15 +75,17 @@ __device__ __forceinline__ bool mbar_try_wait_hint(uint64_t *bar, uint32_t parit
 }
 
 // Bounded wait for the phase with the given parity to complete.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-  for (uint32_t i = 0; i < kSpinLimit; ++i)
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity,
+                                          uint32_t limit = kSpinLimit) {
+  for (uint32_t i = 0; i < limit; ++i)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
 
 // Bounded wait that sleeps between polls (consumer side of a pipeline).
-__device__ __forceinline__ bool mbar_wait_sleep(uint64_t *bar, uint32_t parity) {
-  for (uint32_t i = 0; i < kSpinLimit; ++i)
+__device__ __forceinline__ bool mbar_wait_sleep(uint64_t *bar, uint32_t parity,
+                                                uint32_t limit = kSpinLimit) {
+  for (uint32_t i = 0; i < limit; ++i)
     if (mbar_try_wait_hint(bar, parity)) return true;
   return false;
 }

@@ -29,6 +29,7 @@
 #include <vector>
 
 #include "../../include/onionpir_gpu.h"
+#include "async.cuh"
 #include "kernels.h"
 #include "serve_core.h"
 #include "tune_core.h"
@@ -801,8 +802,8 @@ int opir_ctx_create(const opir_params *P, int device, opir_ctx **out) {
   if (init_kernel_attributes() != cudaSuccess || init_scan_attributes() != cudaSuccess ||
       init_tc_attributes() != cudaSuccess)
     return OPIR_ERR_CUDA;
-  if (c->status.alloc(sizeof(uint32_t)) != cudaSuccess ||
-      cudaMemset(c->status.p, 0, sizeof(uint32_t)) != cudaSuccess)
+  if (c->status.alloc(kStatusWords * sizeof(uint32_t)) != cudaSuccess ||
+      cudaMemset(c->status.p, 0, kStatusWords * sizeof(uint32_t)) != cudaSuccess)
     return OPIR_ERR_CUDA;
   if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess)
     return OPIR_ERR_CUDA;
@@ -1430,6 +1431,21 @@ int opir_ntt_device(opir_ctx *ctx, int mod, int inverse, uint64_t *d_polys, uint
   return OPIR_OK;
 }
 
+// Test hook of the bounded-wait failure path (async.cuh): the single-query
+// scans of this context's synchronous calls withhold one pipeline stage in
+// their first CTA and give up waiting for it after `polls` polls (0: off).
+int opir_debug_withhold_scan_stage(opir_ctx *ctx, uint32_t polls) {
+  if (!ctx) return OPIR_ERR_ARG;
+  if (polls > (1u << 20))
+    return ctx->fail(OPIR_ERR_ARG, "at most 2^20 polls (the production limit is 2^22)");
+  std::lock_guard<std::mutex> g(ctx->mu);
+  cudaSetDevice(ctx->device);
+  CK(cudaStreamSynchronize(ctx->stream), "sync");
+  CK(cudaMemcpy(ctx->status.as<uint32_t>() + 1, &polls, sizeof polls, cudaMemcpyHostToDevice),
+     "set scan test hook");
+  return OPIR_OK;
+}
+
 // save_resp_to_stream (server.cpp:581-633) for responses the caller holds:
 // the bit packing of the pipeline's last kernel without its modulus switch.
 int opir_pack_response(opir_ctx *ctx, const uint64_t *resps, uint32_t count, uint8_t *packed) {
@@ -1740,8 +1756,8 @@ int opir_serve_start(opir_ctx *ctx, const opir_serve_config *cfg) {
     L->owner = S.get();
     CK(cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking), "lane stream");
     CK(cudaEventCreateWithFlags(&L->done, cudaEventDisableTiming), "lane event");
-    CK(L->status.alloc(sizeof(uint32_t)), "lane status");
-    CK(cudaMemset(L->status.p, 0, sizeof(uint32_t)), "lane status");
+    CK(L->status.alloc(kStatusWords * sizeof(uint32_t)), "lane status");
+    CK(cudaMemset(L->status.p, 0, kStatusWords * sizeof(uint32_t)), "lane status");
     CK(L->h_status.alloc(sizeof(uint32_t)), "lane status");
     const int rc = presize_lane(ctx, *L, (int)cfg->max_batch);
     if (rc) return rc;

@@ -235,6 +235,12 @@ __global__ void __launch_bounds__(kWarps * 32 + 32, kMinBlocks)
 
   const size_t plane_words = (size_t)G.n1 * G.n_rest;
   const long long per_b = (long long)(kN / G.pc) * G.row_tiles;
+  // test hook (async.cuh): CTA 0 withholds its first stage, and its waits
+  // for stages give up after `limit` polls; the drain below keeps the
+  // production limit, since every copy it waits for was issued
+  const uint32_t hook = status ? status[1] : 0u;
+  const bool withhold = hook != 0 && blockIdx.x == 0;
+  const uint32_t limit = withhold ? hook : kSpinLimit;
 
   if (warp == kWarps) {
     // ------------------------------ producer ------------------------------
@@ -257,7 +263,7 @@ __global__ void __launch_bounds__(kWarps * 32 + 32, kMinBlocks)
         }
         if (reuse) {
           bool w = true;
-          if (lane == 0) w = mbar_wait(&empty[s], ephase);
+          if (lane == 0) w = mbar_wait(&empty[s], ephase, limit);
           w = __shfl_sync(0xffffffffu, w, 0);
           if (!w) {
             if (lane == 0) report_error(status, kErrWaitEmpty);
@@ -265,6 +271,7 @@ __global__ void __launch_bounds__(kWarps * 32 + 32, kMinBlocks)
             break;
           }
         }
+        if (withhold && it == 0) continue;  // stage 0 never arrives (test hook)
         unsigned char *st = smem_raw + (size_t)s * stage_bytes;
         uint64_t *sdb = reinterpret_cast<uint64_t *>(st);
         uint4 *sq = reinterpret_cast<uint4 *>(st + kStageDbBytes);
@@ -295,6 +302,7 @@ __global__ void __launch_bounds__(kWarps * 32 + 32, kMinBlocks)
     if (lane == 0) {
       const long long first = it > kStages ? it - kStages : 0;
       for (long long j = first; j < it; ++j) {
+        if (withhold && j == 0) continue;  // issued nothing
         if (!mbar_wait(&full[j % kStages], (uint32_t)((j / kStages) & 1))) {
           report_error(status, kErrDrain);
           break;
@@ -320,7 +328,7 @@ __global__ void __launch_bounds__(kWarps * 32 + 32, kMinBlocks)
       acc3_zero(acc[rr][1]);
     }
     for (int kb = 0; kb < G.nkb; ++kb) {
-      if (!mbar_wait_sleep(&full[s], phase)) {
+      if (!mbar_wait_sleep(&full[s], phase, limit)) {
         report_error(status, kErrWaitFull);
         return;
       }

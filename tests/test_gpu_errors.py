@@ -83,3 +83,44 @@ def test_misuse_returns_codes_and_the_context_stays_usable(oracle_lib, gpu_lib):
     ref, _, _, _ = o.make_query_server(db_ref, gk, o.gsw_key_to_ntt(gswk), q1)
     assert np.array_equal(server.make_query(1, q1), ref)
     server.close()
+
+
+def test_scan_wait_timeout_is_reported_and_the_context_recovers(oracle_lib, gpu_lib):
+    """The bounded-wait failure path of the pipelined scan (async.cuh): the
+    producer of the scan's first CTA withholds one stage, its consumers give
+    up after a few thousand polls, the query returns OPIR_ERR_TIMEOUT with
+    the status bits, and the next query on the same context is bit-exact
+    against the oracle again (directly launched and replayed from a CUDA
+    graph alike)."""
+    from onionpirv2_gb300 import PirParams, PirServer, _capi
+    L = _capi.load()
+    o = oracle_lib.Oracle(4096, 256)
+    server = PirServer(PirParams(num_entries=4096, max_fst_dim=256))
+    seed = 4321
+    server.gen_data(seed)
+    db = o.build_db(seed)
+    sk = o.keygen(61)
+    gk, gswk = o.galois_keys(sk, 62), o.gsw_key(sk, 63)
+    server.set_client_galois_key(1, gk)
+    server.set_client_gsw_key(1, gswk)
+    gsw_ntt = o.gsw_key_to_ntt(gswk)
+    queries = [o.make_query(sk, 70 + j, i) for j, i in enumerate((5, 3000, 4095))]
+    want = [o.make_query_server(db, gk, gsw_ntt, q)[0] for q in queries]
+    for graphs in (True, False):
+        server.set_graphs(graphs)
+        assert np.array_equal(server.make_query(1, queries[0]), want[0])
+        _capi.check(server.ctx, L.opir_debug_withhold_scan_stage(server.ctx, 4096))
+        with pytest.raises(_capi.OpirError) as e:
+            server.make_query(1, queries[1])
+        assert e.value.code == -8  # OPIR_ERR_TIMEOUT
+        msg = L.opir_last_error(server.ctx).decode()
+        assert "timed out" in msg and "0x" in msg
+        st = int(msg.split("0x")[1].split(")")[0], 16)
+        assert st & 1, "a consumer wait ran out (kErrWaitFull)"
+        assert not st & 4, "the producer drained every copy it issued"
+        _capi.check(server.ctx, L.opir_debug_withhold_scan_stage(server.ctx, 0))
+        assert np.array_equal(server.make_query(1, queries[1]), want[1])
+        assert np.array_equal(server.make_query(1, queries[2]), want[2])
+        _capi.check(server.ctx, L.opir_sync(server.ctx))
+    assert L.opir_debug_withhold_scan_stage(server.ctx, (1 << 20) + 1) == -1
+    server.close()
