@@ -72,6 +72,35 @@ int opir_ctx_set_stream(opir_ctx *ctx, void *cuda_stream);
 const char *opir_last_error(const opir_ctx *ctx);
 uint64_t opir_response_bytes(const opir_ctx *ctx);
 
+/* Multi-modulus parameter sets (rns_mod_cnt > 1: the PolyDegree = 4096,
+ * CoeffMods = {60, 60, 60} presets of database_constants.h:13-172), and any
+ * power-of-two N from 1024 to 4096 with one or two ciphertext primes.
+ * Replaces PirServer::PirServer for those presets (server.cpp:25-39).
+ * On such a context a ciphertext is uint64_t[2][R][N] (SEAL's layout: poly,
+ * prime, coefficient); Galois keys are [level][R][2][R+1][N] (decomposition
+ * prime j, key polynomial, modulus q_0 .. q_{R-1}, p; NTT form), the RGSW
+ * key [2 l_key][2][R][N] (coefficient form), the reference-layout database
+ * [R N][num_pt]; responses stay [2][N] mod small_q after the switch to q_0
+ * (server.cpp:567-570) and to small_q.  Supported: the database calls but
+ * push_chunk and get_entry, the key calls, opir_make_query, _batch (one
+ * query after another) and _trace (leaves [u][2][R][N], gsw
+ * [ndim-1][2l][2][R][N], first_dim [n_rest][2][R][N]), opir_pack_response,
+ * opir_ntt (mod 0 .. R-1 = q_i, R = p), timing, opir_sync.  The others return
+ * OPIR_ERR_STATE. */
+typedef struct opir_rns_params {
+  uint32_t poly_degree;        /* N                                           */
+  uint32_t rns_count;          /* ciphertext primes R: 1 or 2                 */
+  uint64_t coeff_moduli[2];    /* q_0 .. q_{R-1} (CoeffModulus::Create order) */
+  uint64_t special_modulus;    /* p                                           */
+  uint64_t plain_modulus;      /* t                                           */
+  uint64_t small_modulus;      /* small_q                                     */
+  uint32_t gsw_l;              /* l      (GSW_L)                              */
+  uint32_t gsw_base_log2;      /* ceil(log2 Q / l)       (pir.cpp:53)         */
+  uint32_t gsw_l_key;          /* l_key  (GSW_L_KEY)                          */
+  uint32_t gsw_base_log2_key;  /* ceil(log2 Q / l_key)   (pir.cpp:54)         */
+} opir_rns_params;
+int opir_ctx_create_rns(const opir_rns_params *params, int device, opir_ctx **out);
+
 /* ---- database (server.h:22-25; server.cpp:47-78, 635-748) ---- */
 int opir_db_create(opir_ctx *ctx, const opir_db_shape *shape, uint32_t *db_id);
 int opir_db_destroy(opir_ctx *ctx, uint32_t db_id);

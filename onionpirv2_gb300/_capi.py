@@ -41,7 +41,7 @@ EXPORTS = (
     "opir_serve_start", "opir_serve_stop", "opir_submit", "opir_poll", "opir_wait",
     "opir_serve_stats_get", "opir_set_batch_engine", "opir_autotune", "opir_set_graphs",
     "opir_db_get_entry", "opir_pack_response", "opir_other_dim_mux",
-    "opir_debug_withhold_scan_stage",
+    "opir_debug_withhold_scan_stage", "opir_ctx_create_rns",
 )
 
 ENGINES = {"auto": 0, "scan": 1, "imad": 2, "tensor": 3}
@@ -51,6 +51,21 @@ class OpirParams(ctypes.Structure):
     _fields_ = [
         ("poly_degree", ctypes.c_uint32),
         ("coeff_modulus", ctypes.c_uint64),
+        ("special_modulus", ctypes.c_uint64),
+        ("plain_modulus", ctypes.c_uint64),
+        ("small_modulus", ctypes.c_uint64),
+        ("gsw_l", ctypes.c_uint32),
+        ("gsw_base_log2", ctypes.c_uint32),
+        ("gsw_l_key", ctypes.c_uint32),
+        ("gsw_base_log2_key", ctypes.c_uint32),
+    ]
+
+
+class OpirRnsParams(ctypes.Structure):
+    _fields_ = [
+        ("poly_degree", ctypes.c_uint32),
+        ("rns_count", ctypes.c_uint32),
+        ("coeff_moduli", ctypes.c_uint64 * 2),
         ("special_modulus", ctypes.c_uint64),
         ("plain_modulus", ctypes.c_uint64),
         ("small_modulus", ctypes.c_uint64),
@@ -132,6 +147,8 @@ def load(path: str = LIB):
             "(python -c 'import __graft_entry__ as g; g.build()')")
     L = ctypes.CDLL(path)
     L.opir_ctx_create.argtypes = [ctypes.POINTER(OpirParams), ctypes.c_int, ctypes.POINTER(_vp)]
+    L.opir_ctx_create_rns.argtypes = [ctypes.POINTER(OpirRnsParams), ctypes.c_int,
+                                      ctypes.POINTER(_vp)]
     L.opir_ctx_destroy.argtypes = [_vp]
     L.opir_ctx_destroy.restype = None
     L.opir_ctx_set_stream.argtypes = [_vp, _vp]

@@ -30,7 +30,9 @@
 
 #include "../../include/onionpir_gpu.h"
 #include "async.cuh"
+#include "hostmath.h"
 #include "kernels.h"
+#include "rns.h"
 #include "serve_core.h"
 #include "tune_core.h"
 
@@ -39,63 +41,15 @@ using namespace opir;
 namespace {
 
 using u128 = unsigned __int128;
+using hostmath::bitlen;
+using hostmath::brv;
+using hostmath::is_prime;
+using hostmath::mulmod;
+using hostmath::powmod;
+using hostmath::shoup;
 
-uint64_t mulmod(uint64_t a, uint64_t b, uint64_t q) { return (uint64_t)(((u128)a * b) % q); }
-uint64_t powmod(uint64_t b, uint64_t e, uint64_t q) {
-  uint64_t r = 1 % q;
-  b %= q;
-  while (e) {
-    if (e & 1) r = mulmod(r, b, q);
-    b = mulmod(b, b, q);
-    e >>= 1;
-  }
-  return r;
-}
-bool is_prime(uint64_t n) {
-  static const uint64_t bases[] = {2, 3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 37};
-  if (n < 2) return false;
-  for (uint64_t b : bases) {
-    if (n == b) return true;
-    if (n % b == 0) return false;
-  }
-  uint64_t d = n - 1;
-  int s = 0;
-  while (!(d & 1)) d >>= 1, s++;
-  for (uint64_t b : bases) {
-    uint64_t x = powmod(b, d, n);
-    if (x == 1 || x == n - 1) continue;
-    bool comp = true;
-    for (int r = 1; r < s && comp; r++) {
-      x = mulmod(x, x, n);
-      if (x == n - 1) comp = false;
-    }
-    if (comp) return false;
-  }
-  return true;
-}
-uint64_t shoup(uint64_t w, uint64_t q) { return (uint64_t)(((u128)w << 64) / q); }
-unsigned bitlen(uint64_t x) { return x ? 64 - __builtin_clzll(x) : 0; }
-uint64_t brv(uint64_t x, unsigned bits) {
-  uint64_t y = 0;
-  for (unsigned i = 0; i < bits; i++) y = (y << 1) | ((x >> i) & 1);
-  return y;
-}
 // smallest primitive 2N-th root of unity mod q
-uint64_t minimal_root(uint64_t q) {
-  const uint64_t two_n = 2 * kN, cof = (q - 1) / two_n;
-  uint64_t psi = 0;
-  for (uint64_t g = 2; g < q && !psi; g++) {
-    uint64_t c = powmod(g, cof, q);
-    if (powmod(c, two_n / 2, q) == q - 1) psi = c;
-  }
-  if (!psi) return 0;
-  uint64_t best = psi, sq = mulmod(psi, psi, q), cur = psi;
-  for (uint64_t k = 1; k < two_n / 2; k++) {
-    cur = mulmod(cur, sq, q);
-    if (cur < best) best = cur;
-  }
-  return best;
-}
+uint64_t minimal_root(uint64_t q) { return hostmath::minimal_root(q, 2 * kN); }
 
 struct DevBuf {
   void *p = nullptr;
@@ -311,6 +265,10 @@ struct opir_ctx {
   bool stage_valid = false;
   uint64_t launches = 0;
   void *noalloc_scratch = nullptr;  // device address of the static scratch (opir_first_dim_noalloc)
+  // multi-modulus parameter sets (opir_ctx_create_rns): the entry points that
+  // support them dispatch here, the others return OPIR_ERR_STATE
+  std::unique_ptr<RnsServer> rns;
+  uint32_t rns_count = 1;
   std::string err;
 
   int fail(int code, const char *fmt, ...) {
@@ -336,6 +294,20 @@ struct opir_ctx {
     cudaError_t e_ = (call);                             \
     if (e_ != cudaSuccess) return ctx->cuda_fail(e_, what); \
   } while (0)
+
+// Entry points of a multi-modulus context (opir_ctx_create_rns) run on its
+// RnsServer, under the context's lock and with its error message copied.
+#define RNS_DISPATCH(call)                          \
+  if (ctx && ctx->rns) {                            \
+    std::lock_guard<std::mutex> g_(ctx->mu);        \
+    cudaSetDevice(ctx->device);                     \
+    const int rc_ = (call);                         \
+    if (rc_ != OPIR_OK) ctx->err = ctx->rns->error(); \
+    return rc_;                                     \
+  }
+#define RNS_UNSUPPORTED(what)                                                         \
+  if (ctx && ctx->rns)                                                                \
+    return ctx->fail(OPIR_ERR_STATE, "%s is not available for multi-modulus parameter sets", what);
 
 namespace {
 
@@ -763,6 +735,20 @@ int ingest_chunk_coeffs(opir_ctx *ctx, Db &db, size_t pt0, size_t count) {
   return OPIR_OK;
 }
 
+// make_query_batch on a multi-modulus context: the queries one after another
+// (queries [batch][2][R][N], resps [batch][2][N], packed [batch][bytes]).
+int rns_batch(opir_ctx *ctx, uint32_t db_id, uint32_t batch, const uint64_t *ids,
+              const uint64_t *queries, uint64_t *resps, uint8_t *packed) {
+  const size_t qw = 2 * (size_t)ctx->prm.poly_degree * ctx->rns_count;
+  const size_t rw = 2 * (size_t)ctx->prm.poly_degree, pb = ctx->resp_bytes;
+  for (uint32_t b = 0; b < batch; b++) {
+    const int rc = ctx->rns->make_query(db_id, ids[b], queries + b * qw, resps ? resps + b * rw : nullptr,
+                                        packed ? packed + b * pb : nullptr, nullptr, ctx->stream);
+    if (rc) return rc;
+  }
+  return OPIR_OK;
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -770,6 +756,40 @@ int ingest_chunk_coeffs(opir_ctx *ctx, Db &db, size_t pt0, size_t count) {
 // ===========================================================================
 
 extern "C" {
+
+int opir_ctx_create_rns(const opir_rns_params *P, int device, opir_ctx **out) {
+  if (!P || !out) return OPIR_ERR_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return OPIR_ERR_NO_DEVICE;
+  if (device < 0 || device >= ndev) return OPIR_ERR_ARG;
+  std::unique_ptr<opir_ctx> ctx(new opir_ctx());
+  ctx->device = device;
+  std::string err;
+  const int rc = RnsServer::create(*P, device, &ctx->rns, &err);
+  if (rc) return rc;
+  opir_params &prm = ctx->prm;  // the fields the shared entry points read
+  prm.poly_degree = P->poly_degree;
+  prm.coeff_modulus = P->coeff_moduli[0];
+  prm.special_modulus = P->special_modulus;
+  prm.plain_modulus = P->plain_modulus;
+  prm.small_modulus = P->small_modulus;
+  prm.gsw_l = P->gsw_l;
+  prm.gsw_base_log2 = P->gsw_base_log2;
+  prm.gsw_l_key = P->gsw_l_key;
+  prm.gsw_base_log2_key = P->gsw_base_log2_key;
+  ctx->rns_count = P->rns_count;
+  ctx->resp_bytes = ctx->rns->response_bytes();
+  ctx->graphs = false;
+  if (ctx->status.alloc(kStatusWords * sizeof(uint32_t)) != cudaSuccess ||
+      cudaMemset(ctx->status.p, 0, kStatusWords * sizeof(uint32_t)) != cudaSuccess)
+    return OPIR_ERR_CUDA;
+  if (cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess)
+    return OPIR_ERR_CUDA;
+  ctx->stream = ctx->own_stream;
+  *out = ctx.release();
+  return OPIR_OK;
+}
 
 int opir_ctx_create(const opir_params *P, int device, opir_ctx **out) {
   if (!P || !out) return OPIR_ERR_ARG;
@@ -877,6 +897,7 @@ const char *opir_last_error(const opir_ctx *ctx) { return ctx ? ctx->err.c_str()
 uint64_t opir_response_bytes(const opir_ctx *ctx) { return ctx ? ctx->resp_bytes : 0; }
 
 int opir_db_create(opir_ctx *ctx, const opir_db_shape *shape, uint32_t *db_id) {
+  RNS_DISPATCH(shape && db_id ? ctx->rns->db_create(*shape, db_id) : OPIR_ERR_ARG)
   if (!ctx || !shape || !db_id) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
   const opir_db_shape &S = *shape;
@@ -907,6 +928,7 @@ int opir_db_create(opir_ctx *ctx, const opir_db_shape *shape, uint32_t *db_id) {
 }
 
 int opir_db_destroy(opir_ctx *ctx, uint32_t db_id) {
+  RNS_DISPATCH(ctx->rns->db_destroy(db_id))
   if (!ctx) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
   if (serving_active(ctx)) return ctx->fail(OPIR_ERR_STATE, "serving is active");
@@ -918,6 +940,7 @@ int opir_db_destroy(opir_ctx *ctx, uint32_t db_id) {
 
 int opir_db_push_chunk(opir_ctx *ctx, uint32_t db_id, const uint8_t *entries, uint64_t num_entries,
                        uint64_t chunk_idx) {
+  RNS_UNSUPPORTED("push_database_chunk")
   if (!ctx || !entries) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
   if (serving_active(ctx)) return ctx->fail(OPIR_ERR_STATE, "serving is active");
@@ -947,6 +970,7 @@ int opir_db_push_chunk(opir_ctx *ctx, uint32_t db_id, const uint8_t *entries, ui
 }
 
 int opir_db_fill_synthetic(opir_ctx *ctx, uint32_t db_id, uint64_t seed) {
+  RNS_DISPATCH(ctx->rns->db_fill_synthetic(db_id, seed, ctx->stream))
   if (!ctx) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
   if (serving_active(ctx)) return ctx->fail(OPIR_ERR_STATE, "serving is active");
@@ -969,6 +993,7 @@ int opir_db_fill_synthetic(opir_ctx *ctx, uint32_t db_id, uint64_t seed) {
 }
 
 int opir_db_upload_aligned(opir_ctx *ctx, uint32_t db_id, const uint64_t *aligned) {
+  RNS_DISPATCH(aligned ? ctx->rns->db_upload_aligned(db_id, aligned, ctx->stream) : OPIR_ERR_ARG)
   if (!ctx || !aligned) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
   if (serving_active(ctx)) return ctx->fail(OPIR_ERR_STATE, "serving is active");
@@ -989,6 +1014,7 @@ int opir_db_upload_aligned(opir_ctx *ctx, uint32_t db_id, const uint64_t *aligne
 }
 
 int opir_db_get_entry(opir_ctx *ctx, uint32_t db_id, uint64_t entry_index, uint8_t *entry) {
+  RNS_UNSUPPORTED("direct_get_entry")
   if (!ctx || !entry) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
   Db *db = find_db(ctx, db_id);
@@ -1030,6 +1056,7 @@ int opir_db_get_entry(opir_ctx *ctx, uint32_t db_id, uint64_t entry_index, uint8
 }
 
 int opir_set_galois_key(opir_ctx *ctx, uint64_t client_id, const uint64_t *keys, uint32_t levels) {
+  RNS_DISPATCH(keys ? ctx->rns->set_galois_key(client_id, keys, levels, ctx->stream) : OPIR_ERR_ARG)
   if (!ctx || !keys || !levels || levels > (uint32_t)kLogN) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
   cudaSetDevice(ctx->device);
@@ -1064,6 +1091,7 @@ int opir_set_galois_key(opir_ctx *ctx, uint64_t client_id, const uint64_t *keys,
 }
 
 int opir_set_gsw_key(opir_ctx *ctx, uint64_t client_id, const uint64_t *rows) {
+  RNS_DISPATCH(rows ? ctx->rns->set_gsw_key(client_id, rows, ctx->stream) : OPIR_ERR_ARG)
   if (!ctx || !rows) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
   cudaSetDevice(ctx->device);
@@ -1090,6 +1118,7 @@ int opir_set_gsw_key(opir_ctx *ctx, uint64_t client_id, const uint64_t *rows) {
 }
 
 int opir_erase_client(opir_ctx *ctx, uint64_t client_id) {
+  RNS_DISPATCH(ctx->rns->erase_client(client_id))
   if (!ctx) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
   cudaSetDevice(ctx->device);
@@ -1106,6 +1135,7 @@ int opir_erase_client(opir_ctx *ctx, uint64_t client_id) {
 }
 
 int opir_set_key_budget(opir_ctx *ctx, uint64_t bytes) {
+  RNS_UNSUPPORTED("a key budget")
   if (!ctx) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
   if (!ctx->clients.empty() || serving_active(ctx))
@@ -1126,6 +1156,7 @@ int opir_set_key_budget(opir_ctx *ctx, uint64_t bytes) {
 uint64_t opir_key_bytes_per_client(const opir_ctx *ctx) { return ctx ? ctx->slot_words * 8 : 0; }
 
 int opir_resident_clients(opir_ctx *ctx, uint32_t *resident, uint32_t *slots) {
+  RNS_UNSUPPORTED("a key budget")
   if (!ctx || !resident || !slots) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
   *resident = ctx->key_budget ? (uint32_t)ctx->lru.used() : (uint32_t)ctx->clients.size();
@@ -1199,6 +1230,7 @@ static int query_host(opir_ctx *ctx, uint32_t db_id, uint32_t batch, const uint6
 
 int opir_make_query(opir_ctx *ctx, uint32_t db_id, uint64_t client_id, const uint64_t *query,
                     uint64_t *resp, uint8_t *packed) {
+  RNS_DISPATCH(query ? ctx->rns->make_query(db_id, client_id, query, resp, packed, nullptr, ctx->stream) : OPIR_ERR_ARG)
   if (!ctx || !query) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
   if (serving_active(ctx))
@@ -1208,6 +1240,7 @@ int opir_make_query(opir_ctx *ctx, uint32_t db_id, uint64_t client_id, const uin
 
 int opir_make_query_batch(opir_ctx *ctx, uint32_t db_id, uint32_t batch, const uint64_t *client_ids,
                           const uint64_t *queries, uint64_t *resps, uint8_t *packed) {
+  RNS_DISPATCH(queries && client_ids && batch ? rns_batch(ctx, db_id, batch, client_ids, queries, resps, packed) : OPIR_ERR_ARG)
   if (!ctx || !queries || !client_ids || !batch) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
   if (serving_active(ctx))
@@ -1217,6 +1250,7 @@ int opir_make_query_batch(opir_ctx *ctx, uint32_t db_id, uint32_t batch, const u
 
 int opir_make_query_device(opir_ctx *ctx, uint32_t db_id, uint32_t batch, const uint64_t *client_ids,
                            const uint64_t *d_queries, uint64_t *d_resps, uint8_t *d_packed) {
+  RNS_UNSUPPORTED("make_query on device buffers")
   if (!ctx || !d_queries || !client_ids || !batch) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
   if (serving_active(ctx))
@@ -1230,6 +1264,13 @@ int opir_make_query_device(opir_ctx *ctx, uint32_t db_id, uint32_t batch, const 
 int opir_make_query_trace(opir_ctx *ctx, uint32_t db_id, uint64_t client_id, const uint64_t *query,
                           uint64_t *leaves, uint64_t *gsw, uint64_t *first_dim, uint64_t *resp,
                           uint8_t *packed) {
+  if (ctx && ctx->rns) {
+    RnsTrace t;
+    t.leaves = leaves;
+    t.gsw = gsw;
+    t.first_dim = first_dim;
+    RNS_DISPATCH(query ? ctx->rns->make_query(db_id, client_id, query, resp, packed, &t, ctx->stream) : OPIR_ERR_ARG)
+  }
   if (!ctx || !query) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
   if (serving_active(ctx))
@@ -1242,6 +1283,7 @@ int opir_make_query_trace(opir_ctx *ctx, uint32_t db_id, uint64_t client_id, con
 }
 
 int opir_set_batch_engine(opir_ctx *ctx, int engine, uint32_t tensor_min_batch) {
+  RNS_UNSUPPORTED("the batch engines")
   if (!ctx || engine < OPIR_ENGINE_AUTO || engine > OPIR_ENGINE_TENSOR) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
   if (serving_active(ctx)) return ctx->fail(OPIR_ERR_STATE, "serving is active");
@@ -1252,6 +1294,7 @@ int opir_set_batch_engine(opir_ctx *ctx, int engine, uint32_t tensor_min_batch) 
 
 int opir_autotune(opir_ctx *ctx, uint32_t db_id, uint32_t max_batch, uint32_t reps,
                   opir_tune_report *report) {
+  RNS_UNSUPPORTED("the autotuner")
   if (!ctx) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
   if (serving_active(ctx)) return ctx->fail(OPIR_ERR_STATE, "serving is active");
@@ -1380,6 +1423,7 @@ int opir_set_graphs(opir_ctx *ctx, int enable) {
 int opir_set_timing(opir_ctx *ctx, int enable) {
   if (!ctx) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
+  if (ctx->rns) ctx->rns->set_timing(enable != 0);
   ctx->timing = enable != 0;
   ctx->stage_valid = false;
   return OPIR_OK;
@@ -1388,6 +1432,8 @@ int opir_set_timing(opir_ctx *ctx, int enable) {
 int opir_stage_times(opir_ctx *ctx, float *ms6) {
   if (!ctx || !ms6) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
+  if (ctx->rns)
+    return ctx->rns->stage_times(ms6) ? OPIR_OK : ctx->fail(OPIR_ERR_STATE, "no timed query");
   if (!ctx->timing || !ctx->stage_valid) return ctx->fail(OPIR_ERR_STATE, "no timed query");
   int rc = collect_times(ctx);
   if (rc) return rc;
@@ -1395,7 +1441,9 @@ int opir_stage_times(opir_ctx *ctx, float *ms6) {
   return OPIR_OK;
 }
 
-uint64_t opir_launch_count(const opir_ctx *ctx) { return ctx ? ctx->launches : 0; }
+uint64_t opir_launch_count(const opir_ctx *ctx) {
+  return ctx ? ctx->launches + (ctx->rns ? ctx->rns->launches() : 0) : 0;
+}
 
 int opir_sync(opir_ctx *ctx) {
   if (!ctx) return OPIR_ERR_ARG;
@@ -1406,6 +1454,7 @@ int opir_sync(opir_ctx *ctx) {
 }
 
 int opir_ntt(opir_ctx *ctx, int mod, int inverse, uint64_t *polys, uint64_t count) {
+  RNS_DISPATCH(polys ? ctx->rns->ntt(mod, inverse != 0, polys, count, ctx->stream) : OPIR_ERR_ARG)
   if (!ctx || !polys || (mod != 0 && mod != 1)) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
   cudaSetDevice(ctx->device);
@@ -1422,6 +1471,7 @@ int opir_ntt(opir_ctx *ctx, int mod, int inverse, uint64_t *polys, uint64_t coun
 }
 
 int opir_ntt_device(opir_ctx *ctx, int mod, int inverse, uint64_t *d_polys, uint64_t count) {
+  RNS_UNSUPPORTED("opir_ntt_device")
   if (!ctx || !d_polys || (mod != 0 && mod != 1)) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
   cudaSetDevice(ctx->device);
@@ -1435,6 +1485,7 @@ int opir_ntt_device(opir_ctx *ctx, int mod, int inverse, uint64_t *d_polys, uint
 // scans of this context's synchronous calls withhold one pipeline stage in
 // their first CTA and give up waiting for it after `polls` polls (0: off).
 int opir_debug_withhold_scan_stage(opir_ctx *ctx, uint32_t polls) {
+  RNS_UNSUPPORTED("the scan test hook")
   if (!ctx) return OPIR_ERR_ARG;
   if (polls > (1u << 20))
     return ctx->fail(OPIR_ERR_ARG, "at most 2^20 polls (the production limit is 2^22)");
@@ -1449,6 +1500,7 @@ int opir_debug_withhold_scan_stage(opir_ctx *ctx, uint32_t polls) {
 // save_resp_to_stream (server.cpp:581-633) for responses the caller holds:
 // the bit packing of the pipeline's last kernel without its modulus switch.
 int opir_pack_response(opir_ctx *ctx, const uint64_t *resps, uint32_t count, uint8_t *packed) {
+  RNS_DISPATCH(resps && packed && count ? ctx->rns->pack_response(resps, count, packed, ctx->stream) : OPIR_ERR_ARG)
   if (!ctx || !resps || !packed || !count) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
   cudaSetDevice(ctx->device);
@@ -1469,6 +1521,7 @@ int opir_pack_response(opir_ctx *ctx, const uint64_t *resps, uint32_t count, uin
 // other_dim_mux (server.cpp:295-334): one folding level of `count`
 // ciphertexts with one RGSW selection ciphertext, on the device.
 int opir_other_dim_mux(opir_ctx *ctx, uint64_t *result, uint64_t count, const uint64_t *sel) {
+  RNS_UNSUPPORTED("other_dim_mux")
   if (!ctx || !result || !sel) return OPIR_ERR_ARG;
   if (count < 2 || count % 2 || count / 2 > 0x7fffffff)
     return ctx->fail(OPIR_ERR_ARG, "other_dim_mux folds an even number (>= 2) of ciphertexts");
@@ -1743,6 +1796,7 @@ int presize_lane(opir_ctx *ctx, Lane &L, int max_batch) {
 extern "C" {
 
 int opir_serve_start(opir_ctx *ctx, const opir_serve_config *cfg) {
+  RNS_UNSUPPORTED("serving")
   if (!ctx || !cfg || !cfg->max_batch || cfg->lanes < 1 || cfg->lanes > 4) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
   if (serving_active(ctx)) return ctx->fail(OPIR_ERR_STATE, "serving is already active");
@@ -1905,6 +1959,7 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 
 extern "C" int opir_first_dim_noalloc(opir_ctx *ctx, uint32_t db_id, const uint64_t *d_fst_cts,
                                       uint64_t *d_out) {
+  RNS_UNSUPPORTED("the allocation-free first dimension")
   if (!ctx || !d_fst_cts || !d_out) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
   Db *db = find_db(ctx, db_id);

@@ -95,6 +95,15 @@ PRESETS: Dict[str, dict] = {
     "8GB_best_throughput": dict(max_fst_dim=512, num_entries=1 << 21),
 }
 
+# The N = 4096 presets with two ciphertext primes (CoeffMods = {60, 60, 60},
+# database_constants.h:13-172) share these ciphertext parameters; the
+# "2^14 * 24KB = 384MB" preset (database_constants.h:92-101) is the one the
+# tests and the benchmark use.
+RNS4096 = dict(poly_degree=4096, gsw_l=4, gsw_l_key=8, plain_mod_bits=46, small_q_width=57,
+               coeff_mods=(60, 60, 60))
+PRESETS["n4096_384MB"] = dict(max_fst_dim=256, num_entries=1 << 14, **RNS4096)
+PRESETS["n4096_1GB"] = dict(max_fst_dim=256, num_entries=1 << 20, entry_size_cfg=1024, **RNS4096)
+
 # Workloads used by the tests and the benchmark (sizes as named).
 WORKLOADS: Dict[str, dict] = {
     # 256 x 2^4 = 4096 plaintexts (CPU-runnable reference case)
@@ -109,6 +118,12 @@ WORKLOADS: Dict[str, dict] = {
     "db262144": dict(max_fst_dim=512, num_entries=1 << 18),
     # 1024 x 2^11 = 2,097,152 plaintexts, ~8 GB raw entries, 34.4 GB NTT form
     "db2097152": dict(max_fst_dim=1024, num_entries=1 << 21),
+    # N = 4096 with two ciphertext primes: 256 x 2^2 = 1024 plaintexts of
+    # 23,040-byte entries (parity-test case)
+    "rns1024": dict(max_fst_dim=256, num_entries=1024, **RNS4096),
+    # 256 x 2^6 = 16,384 plaintexts: the "2^14 * 24KB = 384MB" preset,
+    # 1.07 GB in NTT form over the two primes
+    "rns16384": dict(max_fst_dim=256, num_entries=1 << 14, **RNS4096),
 }
 
 
@@ -148,8 +163,11 @@ class PirParams:
         self.num_entries = self.num_pt * self.get_num_entries_per_plaintext()
         ndim = 1 + int(math.log2(other))                                       # pir.cpp:89
         self.dims = [first] + [2] * (ndim - 1)
-        if self.get_rns_mod_cnt() != 1:
-            raise ValueError("only one ciphertext prime (CoeffMods = {60, 60}) is supported")
+        if not 1 <= self.get_rns_mod_cnt() <= 2:
+            raise ValueError("one or two ciphertext primes (CoeffMods of length 2 or 3) are "
+                             "supported")
+        if n not in (1024, 2048, 4096):
+            raise ValueError("poly_degree must be 1024, 2048 or 4096")
 
     @classmethod
     def preset(cls, name: str, **kw) -> "PirParams":
@@ -217,6 +235,11 @@ class PirParams:
 
     def get_DBSize_MB(self) -> float:
         return self.num_entries * self.entry_size / 1024 / 1024
+
+    def is_multi_modulus(self) -> bool:
+        """True for parameter sets served by the multi-modulus path
+        (opir_ctx_create_rns): more than one ciphertext prime, or N != 2048."""
+        return self.get_rns_mod_cnt() > 1 or self.poly_degree != POLY_DEGREE
 
     def get_physical_storage_MB(self) -> float:
         return self.get_coeff_val_cnt() * self.num_pt * 8 / 1024 / 1024

@@ -66,13 +66,24 @@ class PirServer:
         self.pir_params = pir_params
         self._L = _capi.load()
         P = pir_params
-        prm = _capi.OpirParams(
-            poly_degree=P.poly_degree, coeff_modulus=P.coeff_modulus[0],
-            special_modulus=P.coeff_modulus[-1], plain_modulus=P.plain_mod,
-            small_modulus=P.small_q, gsw_l=P.gsw_l, gsw_base_log2=P.base_log2,
-            gsw_l_key=P.gsw_l_key, gsw_base_log2_key=P.base_log2_key)
+        self.n, self.R = P.poly_degree, P.get_rns_mod_cnt()
         ctx = ctypes.c_void_p()
-        rc = self._L.opir_ctx_create(ctypes.byref(prm), device, ctypes.byref(ctx))
+        if P.is_multi_modulus():
+            qs = P.get_coeff_modulus()
+            prm = _capi.OpirRnsParams(
+                poly_degree=P.poly_degree, rns_count=self.R,
+                coeff_moduli=(ctypes.c_uint64 * 2)(*(qs + [0] * (2 - len(qs)))),
+                special_modulus=P.coeff_modulus[-1], plain_modulus=P.plain_mod,
+                small_modulus=P.small_q, gsw_l=P.gsw_l, gsw_base_log2=P.base_log2,
+                gsw_l_key=P.gsw_l_key, gsw_base_log2_key=P.base_log2_key)
+            rc = self._L.opir_ctx_create_rns(ctypes.byref(prm), device, ctypes.byref(ctx))
+        else:
+            prm = _capi.OpirParams(
+                poly_degree=P.poly_degree, coeff_modulus=P.coeff_modulus[0],
+                special_modulus=P.coeff_modulus[-1], plain_modulus=P.plain_mod,
+                small_modulus=P.small_q, gsw_l=P.gsw_l, gsw_base_log2=P.base_log2,
+                gsw_l_key=P.gsw_l_key, gsw_base_log2_key=P.base_log2_key)
+            rc = self._L.opir_ctx_create(ctypes.byref(prm), device, ctypes.byref(ctx))
         if rc != 0:
             raise _capi.OpirError(rc, "opir_ctx_create failed")
         self._ctx = ctx
@@ -85,6 +96,11 @@ class PirServer:
         self.db_id = db.value
         self._db_entry_size = {}  # databases added with add_database
         self.resp_bytes = int(self._L.opir_response_bytes(self._ctx))
+
+    @property
+    def ct_words(self) -> int:
+        """uint64 words of one query ciphertext: 2 R N (SEAL's [2][R][N])."""
+        return 2 * self.R * self.n
 
     # ---- plumbing
     def _check(self, rc: int):
@@ -144,7 +160,7 @@ class PirServer:
         """Install an NTT-form database given in the reference layout
         db_aligned_[c * num_pt + row * n1 + col] (server.cpp:740)."""
         a = np.ascontiguousarray(db_aligned, np.uint64)
-        if a.size != self.pir_params.get_num_pt() * N:
+        if a.size != self.pir_params.get_num_pt() * self.n * self.R:
             raise ValueError("database has the wrong size")
         self._check(self._L.opir_db_upload_aligned(self._ctx, self.db_id, _capi.p64(a.reshape(-1))))
 
@@ -161,15 +177,16 @@ class PirServer:
     # ---- keys
     def set_client_galois_key(self, client_id: int, galois_keys):
         keys = _read_u64(galois_keys)
-        levels = keys.size // (4 * N)
-        if levels * 4 * N != keys.size or levels == 0:
-            raise ValueError("Galois keys must be [levels][2][2][N] uint64")
+        per = self.R * 2 * (self.R + 1) * self.n  # [R][2][R+1][N] per level
+        levels = keys.size // per
+        if levels * per != keys.size or levels == 0:
+            raise ValueError("Galois keys must be [levels][R][2][R+1][N] uint64")
         self._check(self._L.opir_set_galois_key(self._ctx, client_id, _capi.p64(keys), levels))
 
     def set_client_gsw_key(self, client_id: int, gsw_rows):
         rows = _read_u64(gsw_rows)
-        if rows.size != 2 * self.pir_params.get_l_key() * 2 * N:
-            raise ValueError("RGSW key must be [2*l_key][2][N] uint64")
+        if rows.size != 2 * self.pir_params.get_l_key() * self.ct_words:
+            raise ValueError("RGSW key must be [2*l_key][2][R][N] uint64")
         self._check(self._L.opir_set_gsw_key(self._ctx, client_id, _capi.p64(rows)))
 
     def erase_client(self, client_id: int):
@@ -181,14 +198,14 @@ class PirServer:
         ciphertext mod small_q with its packed bytes attached.  `db_id`
         selects a database added with add_database (default: this server's)."""
         q = _read_u64(query)
-        if q.size != 2 * N:
-            raise ValueError("query must be one ciphertext [2][N]")
-        resp = np.zeros(2 * N, np.uint64)
+        if q.size != self.ct_words:
+            raise ValueError("query must be one ciphertext [2][R][N]")
+        resp = np.zeros(2 * self.n, np.uint64)
         packed = np.zeros(self.resp_bytes, np.uint8)
         self._check(self._L.opir_make_query(self._ctx, self.db_id if db_id is None else db_id,
                                             client_id, _capi.p64(q), _capi.p64(resp),
                                             _capi.p8(packed)))
-        out = resp.reshape(2, N).view(ResponseCiphertext)
+        out = resp.reshape(2, self.n).view(ResponseCiphertext)
         out.packed = packed.tobytes()
         return out
 
@@ -197,13 +214,13 @@ class PirServer:
         ids = np.ascontiguousarray(np.asarray(client_ids, dtype=np.uint64))
         q = np.ascontiguousarray(queries, np.uint64).reshape(-1)
         B = ids.size
-        if q.size != B * 2 * N:
-            raise ValueError("queries must be [batch][2][N]")
-        resp = np.zeros(B * 2 * N, np.uint64)
+        if q.size != B * self.ct_words:
+            raise ValueError("queries must be [batch][2][R][N]")
+        resp = np.zeros(B * 2 * self.n, np.uint64)
         packed = np.zeros(B * self.resp_bytes, np.uint8)
         self._check(self._L.opir_make_query_batch(self._ctx, self.db_id, B, _capi.p64(ids),
                                                   _capi.p64(q), _capi.p64(resp), _capi.p8(packed)))
-        return resp.reshape(B, 2, N), packed.reshape(B, self.resp_bytes)
+        return resp.reshape(B, 2, self.n), packed.reshape(B, self.resp_bytes)
 
     def make_query_device(self, client_ids: Sequence[int], d_queries: int, d_resps: int,
                           d_packed: int):
@@ -215,22 +232,27 @@ class PirServer:
             ctypes.c_void_p(d_resps), ctypes.c_void_p(d_packed)))
 
     def make_query_trace(self, client_id: int, query):
-        """make_query returning every intermediate (parity tests)."""
+        """make_query returning every intermediate (parity tests); shapes
+        [u][2][R][N], [ndim-1][2l][2][R][N], [n_rest][2][R][N] (R = 1: the
+        prime axis is dropped)."""
         P = self.pir_params
         q = _read_u64(query)
         ndim = len(P.get_dims())
         u = P.get_fst_dim_sz() + P.get_l() * (ndim - 1)
-        leaves = np.zeros(u * 2 * N, np.uint64)
-        gsw = np.zeros(max(ndim - 1, 1) * 2 * P.get_l() * 2 * N, np.uint64)
-        fd = np.zeros(P.get_other_dim_sz() * 2 * N, np.uint64)
-        resp = np.zeros(2 * N, np.uint64)
+        cw = self.ct_words
+        leaves = np.zeros(u * cw, np.uint64)
+        gsw = np.zeros(max(ndim - 1, 1) * 2 * P.get_l() * cw, np.uint64)
+        fd = np.zeros(P.get_other_dim_sz() * cw, np.uint64)
+        resp = np.zeros(2 * self.n, np.uint64)
         packed = np.zeros(self.resp_bytes, np.uint8)
         self._check(self._L.opir_make_query_trace(
             self._ctx, self.db_id, client_id, _capi.p64(q), _capi.p64(leaves), _capi.p64(gsw),
             _capi.p64(fd), _capi.p64(resp), _capi.p8(packed)))
-        return dict(leaves=leaves.reshape(u, 2, N),
-                    gsw=gsw.reshape(max(ndim - 1, 1), 2 * P.get_l(), 2, N),
-                    first_dim=fd.reshape(-1, 2, N), resp=resp.reshape(2, N), packed=packed)
+        ct = (2, self.n) if self.R == 1 else (2, self.R, self.n)
+        return dict(leaves=leaves.reshape((u,) + ct),
+                    gsw=gsw.reshape((max(ndim - 1, 1), 2 * P.get_l()) + ct),
+                    first_dim=fd.reshape((-1,) + ct), resp=resp.reshape(2, self.n),
+                    packed=packed)
 
     def save_resp_to_stream(self, response, stream: io.IOBase) -> int:
         """Write the response's packed bytes (server.cpp:581-633); returns the
@@ -240,7 +262,7 @@ class PirServer:
         batch, a stored ciphertext) is packed on the GPU (opir_pack_response)."""
         packed = getattr(response, "packed", None)
         if packed is None:
-            packed = self.pack_responses(np.asarray(response).reshape(1, 2, N))[0].tobytes()
+            packed = self.pack_responses(np.asarray(response).reshape(1, 2, self.n))[0].tobytes()
         stream.write(packed)
         return len(packed)
 
@@ -248,9 +270,9 @@ class PirServer:
         """The reference's packed wire bytes of every response
         ([count][2][N] mod small_q) -> uint8 [count][resp_bytes]."""
         r = np.ascontiguousarray(responses, np.uint64)
-        if r.size == 0 or r.size % (2 * N):
+        if r.size == 0 or r.size % (2 * self.n):
             raise ValueError("responses must be [count][2][N] uint64")
-        count = r.size // (2 * N)
+        count = r.size // (2 * self.n)
         out = np.zeros(count * self.resp_bytes, np.uint8)
         self._check(self._L.opir_pack_response(self._ctx, _capi.p64(r.reshape(-1)), count,
                                                _capi.p8(out)))
@@ -397,7 +419,7 @@ class PirServer:
     def ntt(self, polys: np.ndarray, mod: int = 0, inverse: bool = False) -> np.ndarray:
         a = np.ascontiguousarray(polys, np.uint64).copy()
         self._check(self._L.opir_ntt(self._ctx, mod, 1 if inverse else 0, _capi.p64(a.reshape(-1)),
-                                     a.size // N))
+                                     a.size // self.n))
         return a
 
 

@@ -38,7 +38,8 @@ def test_ctypes_structs_match_the_c_header(tmp_path):
     mirrors = {"opir_params": _capi.OpirParams, "opir_db_shape": _capi.OpirDbShape,
                "opir_serve_config": _capi.OpirServeConfig,
                "opir_serve_stats": _capi.OpirServeStats,
-               "opir_tune_report": _capi.OpirTuneReport}
+               "opir_tune_report": _capi.OpirTuneReport,
+               "opir_rns_params": _capi.OpirRnsParams}
     lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "onionpir_gpu.h"',
              "int main(void) {"]
     for cname, cls in mirrors.items():

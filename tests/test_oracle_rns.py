@@ -86,3 +86,23 @@ def test_crt_decomposition_and_modulus_switch_follow_big_integers(rns2):
             x0, x1 = int(ct[poly, 0, c]), int(ct[poly, 1, c])
             X = x1 + q1 * (((x0 - x1) * pow(q1, -1, q0)) % q0)
             assert int(nxt[poly, 0, c]) == ((X + q1 // 2) // q1) % q0  # round(X / q1) mod q0
+
+
+def test_product_parameters_match_the_oracle(oracle_lib):
+    """onionpirv2_gb300.PirParams for the N = 4096 presets derives what the
+    oracle derives (pir.cpp:9-95)."""
+    from onionpirv2_gb300 import PirParams
+    for name in ("n4096_384MB", "rns1024", "rns16384"):
+        p = PirParams.preset(name)
+        r = oracle_lib.RnsOracle(p.poly_degree, p.num_entries, p.max_fst_dim, l=p.gsw_l,
+                                 l_key=p.gsw_l_key, plain_bits=p.plain_mod_bits,
+                                 small_q_width=p.small_q_width, coeff_bits=tuple(p.coeff_mods))
+        P = r.P
+        assert p.is_multi_modulus() and p.get_rns_mod_cnt() == P.rns == 2
+        assert tuple(p.get_coeff_modulus()) == P.q and p.coeff_modulus[-1] == P.p
+        assert (p.plain_mod, p.small_q, p.base_log2, p.base_log2_key) == (
+            P.t, P.small_q, P.base_log2, P.base_log2_key)
+        assert (p.get_entry_size(), p.get_num_pt(), p.get_fst_dim_sz(), p.get_other_dim_sz(),
+                len(p.get_dims()), p.get_expan_height()) == (
+            P.entry_size, P.num_pt, P.n1, P.n_rest, P.ndim, P.h)
+        assert p.response_bytes() == r.response_bytes()
