@@ -23,6 +23,10 @@ switch, packing).
          64 queries per batch on the tensor-core engine against the same
          queries one at a time, the tensor kernel's roofline, every response
          decoded.
+  rns    the multi-modulus path: N = 4096 with two ciphertext primes on the
+         "2^14 * 24KB = 384MB" preset (1.07 GB in NTT form), one query per
+         call through the host API, with the multi-modulus CPU restatement
+         timed beside it.
 
 Inputs: the database is seeded entries ingested on the GPU; four seeded
 PirClients (the CPU client library) make the Galois keys, RGSW keys and the
@@ -90,6 +94,12 @@ def parse():
     ap.add_argument("--large-steps", type=int, default=4, help="timed batches of the large leg")
     ap.add_argument("--only-large", action="store_true",
                     help="run the large batched leg alone and print its object")
+    ap.add_argument("--rns-workload", default="rns16384",
+                    help="database of the multi-modulus leg (N = 4096, two ciphertext primes)")
+    ap.add_argument("--rns-steps", type=int, default=20,
+                    help="timed queries of the multi-modulus leg (0 = skip the leg)")
+    ap.add_argument("--only-rns", action="store_true",
+                    help="run the multi-modulus leg alone and print its object")
     ap.add_argument("--batch-sweep", default=None,
                     help="comma-separated batch sizes: queries/s of every first-dimension "
                          "engine at each size (one JSON line per size)")
@@ -348,6 +358,120 @@ def large_leg(args, local, clocks=None):
         out["clocks"] = clocks.summary(t1, t2)
     server.close()
     return out
+
+
+def rns_inputs(params, count, seed=11):
+    """Seeded synthetic client material of a multi-modulus database: Galois
+    keys [h][R][2][R+1][N], RGSW rows [2 l_key][2][R][N] and `count` queries
+    [2][R][N] of uniform residues (the server's work does not depend on the
+    values; the parity tests check real keys and queries against the oracle)."""
+    rng = np.random.default_rng(seed)
+    n, R = params.poly_degree, params.get_rns_mod_cnt()
+    qs = params.get_coeff_modulus()
+    mods = np.array(qs + [params.coeff_modulus[-1]], dtype=np.uint64)
+    h = params.get_expan_height()
+    gk = rng.integers(0, 2**62, size=(h, R, 2, R + 1, n), dtype=np.uint64) % mods[None, None, None, :, None]
+    data = np.array(qs, dtype=np.uint64)[None, None, :, None]
+    gsw = rng.integers(0, 2**62, size=(2 * params.get_l_key(), 2, R, n), dtype=np.uint64) % data
+    queries = rng.integers(0, 2**62, size=(count, 2, R, n), dtype=np.uint64) % data
+    return gk, gsw, queries
+
+
+def rns_leg(args, local, clocks=None, cpu=True):
+    """The multi-modulus path (N = 4096, two ciphertext primes; the
+    "2^14 * 24KB = 384MB" preset of database_constants.h) through the public
+    host API: one query per step, host buffers, stage times, the scan
+    kernel's HBM roofline, and the multi-modulus CPU restatement of the
+    reference timed on the host cores beside it."""
+    from onionpirv2_gb300 import PirParams, PirServer
+    params = PirParams.preset(args.rns_workload)
+    server = PirServer(params, device=local)
+    t = time.perf_counter()
+    server.gen_data(DB_SEED + 3)
+    ingest_s = time.perf_counter() - t
+    steps = args.rns_steps
+    gk, gsw, queries = rns_inputs(params, steps + 3)
+    server.set_client_galois_key(0, gk)
+    server.set_client_gsw_key(0, gsw)
+    for i in range(3):
+        server.make_query(0, queries[i])
+    t1 = time.time()
+    t = time.perf_counter()
+    for i in range(steps):
+        server.make_query(0, queries[3 + i])
+    el = time.perf_counter() - t
+    t2 = time.time()
+    server.set_timing(True)
+    st = []
+    for i in range(5):
+        server.make_query(0, queries[i])
+        st.append(server.stage_times())
+    server.set_timing(False)
+    stages = {k: statistics.mean(x[k] for x in st) for k in st[0]}
+    server.close()
+    R, n = params.get_rns_mod_cnt(), params.poly_degree
+    db_bytes = params.get_num_pt() * n * R * 8
+    peak, kind = measured_peak()
+    ach = db_bytes / (stages["scan_kernel"] / 1e3) / 1e9
+    out = {
+        "workload": args.rns_workload, "poly_degree": n, "ciphertext_primes": R,
+        "db_plaintexts": params.get_num_pt(), "n1": params.get_fst_dim_sz(),
+        "n_rest": params.get_other_dim_sz(), "ndim": len(params.get_dims()),
+        "entry_size": params.get_entry_size(), "raw_db_mb": params.get_DBSize_MB(),
+        "ntt_db_bytes": db_bytes,
+        "value": steps / el, "unit": "queries/s", "ms_per_query": el / steps * 1e3,
+        "timing": "wall clock around blocking opir_make_query calls (host query in, "
+                  "response and packed bytes out)",
+        "stages_ms": stages,
+        "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                     "frac": ach / peak, "traffic": None,
+                     "kernel": "rns_scan_kernel (first dimension, every prime)",
+                     "peak_source": f"{kind} hbm_gbs"},
+        "inputs": "seeded uniform residues as keys and queries (value-independent work; "
+                  "bit-exactness against the oracle is the -m gpu tests' job)",
+        "ingest_s": ingest_s,
+    }
+    if clocks is not None:
+        out["clocks"] = clocks.summary(t1, t2)
+    if cpu:
+        from oracle import oracle as orc
+        orc.build()
+        threads = os.cpu_count() or 1
+        orc.set_threads(threads)
+        P = params
+        o = orc.RnsOracle(P.poly_degree, P.num_entries, P.max_fst_dim, l=P.gsw_l,
+                          l_key=P.gsw_l_key, plain_bits=P.plain_mod_bits,
+                          small_q_width=P.small_q_width, coeff_bits=tuple(P.coeff_mods))
+        db = o.build_db(DB_SEED + 3)
+        gsn = o.gsw_to_ntt(gsw)
+        o.make_query_server(db, gk, gsn, queries[0])
+        nq = 3
+        t = time.perf_counter()
+        for i in range(nq):
+            o.make_query_server(db, gk, gsn, queries[1 + i])
+        cpu_s = (time.perf_counter() - t) / nq
+        out["cpu_baseline"] = {"value": 1.0 / cpu_s, "unit": "queries/s", "cores": threads,
+                               "kind": "port",
+                               "sample": f"{nq} full queries after 1 untimed on the same database "
+                                         f"and inputs, {threads} threads (multi-modulus CPU "
+                                         "restatement of the reference server)",
+                               "cpu": host_cpu_model()}
+        del db
+    return out
+
+
+def rns_main(args):
+    """The multi-modulus leg alone (one JSON object)."""
+    import torch
+    _, _, local = dist_env()
+    torch.cuda.set_device(local)
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.5)
+    out = rns_leg(args, local, clocks, cpu=not args.no_cpu_baseline)
+    clocks.stop()
+    print(json.dumps(out), flush=True)
+    return 0
 
 
 def large_main(args):
@@ -753,6 +877,8 @@ def main():
         return sweep_main(args)
     if args.only_large:
         return large_main(args)
+    if args.only_rns:
+        return rns_main(args)
     rank, world, local = dist_env()
     import torch
     if not torch.cuda.is_available():
@@ -934,6 +1060,10 @@ def main():
     large = None
     if args.large_batch > 1 and world == 1:
         large = large_leg(args, local, clocks)
+    # ---- rns: the multi-modulus path (N = 4096, two ciphertext primes)
+    rns = None
+    if args.rns_steps > 0 and world == 1:
+        rns = rns_leg(args, local, clocks, cpu=rank == 0 and not args.no_cpu_baseline)
     clocks.stop()
 
     db_bytes = db_bytes_cfg = params.get_num_pt() * N * 8
@@ -977,6 +1107,7 @@ def main():
                            "generation; per response: unpack, decrypt, entry"},
         "batched": batched,
         "large": large,
+        "rns": rns,
         "serving": serving,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

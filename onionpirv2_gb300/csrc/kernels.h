@@ -135,9 +135,14 @@ cudaError_t init_tc_attributes();
 void launch_db_limbs(const uint64_t *dbs, uint16_t *dbl, int n1, int n_rest, cudaStream_t s);
 void launch_tc_query_limbs(const uint64_t *plane, uint16_t *ql, int n1, int batch,
                            cudaStream_t s);
+// ring: the shared-memory pipeline of the tensor kernel, 64 k x 4 stages
+// (n1 a multiple of 64) or 32 k x 8 stages; an invalid choice (or -1) takes
+// the first that fits.
+enum { kTcRing64x4 = 0, kTcRing32x8 = 1 };
+bool tc_ring_valid(int ring, int n1);
 int launch_tc_scan(const uint16_t *dbl, const uint16_t *ql, uint64_t *out, size_t out_stride,
                    int n1, int n_rest, int batch, uint64_t q, uint64_t mu_lo, uint64_t mu_hi,
-                   uint64_t r64, uint64_t r128, uint32_t *status, cudaStream_t s);
+                   uint64_t r64, uint64_t r128, uint32_t *status, cudaStream_t s, int ring = -1);
 
 // ---- one folding level (other_dim_mux): res[b][j] += INTT(RGSW x (res[j+half]-res[j]))
 void launch_fold(uint64_t *res, size_t res_stride, const uint64_t *gsw, size_t gsw_stride,

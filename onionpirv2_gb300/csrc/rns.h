@@ -132,7 +132,7 @@ class RnsServer {
   uint64_t resp_bytes_ = 0;
   uint64_t launches_ = 0;
   bool timing_ = false, stage_valid_ = false;
-  cudaEvent_t ev_[6] = {};
+  cudaEvent_t ev_[8] = {};  // stage boundaries 0-5, scan kernel 6-7
   std::string err_;
 };
 

@@ -8,8 +8,10 @@
 // [-128, 127] (the top limb in [0, 16]); each limb is exact in bf16, a limb
 // product is at most 2^14 in magnitude and a sum of 512 of them at most 2^23,
 // so the fp32 accumulation of tcgen05.mma kind::f16 is exact.  Longer first
-// dimensions run as segments of at most 512 k, each reduced mod q and added
-// to the previous segments' result.
+// dimensions run as segments of at most 512 k inside one launch: the MMAs of
+// each segment fill an accumulator of their own, the epilogue reduces it mod
+// q and keeps the running sum in registers, and a tile's result is stored
+// once, after its last segment.
 //
 // MMA shape per tile: M = 16 database rows x 8 limbs = 128 (TMEM lanes),
 // N = 2B query polynomials x 8 limbs <= 512 (TMEM columns, two MMAs of <= 256),
@@ -31,6 +33,8 @@
 // stride between core matrices along k, stride byte offset = 128 between
 // 8-row groups).
 #include <cuda_bf16.h>
+
+#include <cstdlib>
 
 #include "async.cuh"
 #include "common.cuh"
@@ -64,16 +68,25 @@ constexpr uint32_t kErrTcWaitAcc = 32u;
 constexpr uint32_t kErrTcDrain = 64u;
 constexpr uint32_t kErrTcRange = 128u;
 
+constexpr int kTcMaxSegment = 512;  // k per exact fp32 accumulation
+int g_tc_ring = -1;                 // OPIR_TC_RING: force a ring shape (tests, sweeps)
+
 struct TcGeom {
   int n1, n_rest, batch;      // batch: queries of the pass
-  int k0;                     // first k of this segment (multiple of 32)
-  int accumulate;             // add to the result of the previous segments
   int nh, nbh;                // column halves, query polynomials per half (multiple of 8)
-  int n_rb, nkc;              // row tiles, 32-k chunks of the segment
+  int n_rb;                   // row tiles
+  int nseg;                   // k segments of at most kTcMaxSegment
   long long units;            // N * n_rb * nh tiles
   uint32_t b_bytes;           // query bytes per stage
   uint32_t idesc;             // instruction descriptor (M = 128, N = 8 nbh)
 };
+
+// pipeline stages (of KC k) in segment s
+template <int KC>
+__device__ __forceinline__ int seg_chunks(const TcGeom &G, int s) {
+  const int len = G.n1 - s * kTcMaxSegment;
+  return (len < kTcMaxSegment ? len : kTcMaxSegment) / KC;
+}
 
 // Shared-memory matrix descriptor (tcgen05): start address, leading byte
 // offset (k direction), stride byte offset (8-row groups), version 1, no
@@ -190,10 +203,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       for (long long u = blockIdx.x; u < G.units && ok; u += gridDim.x) {
         const long long c = u / per_c, rem = u % per_c;
         const long long rb = rem / G.nh, hf = rem % G.nh;
-        const uint16_t *a_src =
-            dbl + ((size_t)(c * G.n_rb + rb) * kblk + G.k0 / 8) * (kTcRows * 64);
-        const uint16_t *b_src = ql + ((size_t)(c * G.nh + hf) * kblk + G.k0 / 8) * G.nbh * 64;
-        for (int kc = 0; kc < G.nkc; ++kc, ++it) {
+        const uint16_t *a_src = dbl + (size_t)(c * G.n_rb + rb) * kblk * (kTcRows * 64);
+        const uint16_t *b_src = ql + (size_t)(c * G.nh + hf) * kblk * G.nbh * 64;
+        for (int kc = 0; kc < G.n1 / KC; ++kc, ++it) {
           const int s = (int)(it % STAGES);
           const long long round = it / STAGES;
           if (round > 0 && !mbar_wait(&empty[s], (uint32_t)((round - 1) & 1))) {
@@ -219,34 +231,38 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     // ------------------------------ MMA issue ------------------------------
     if (lane == 0) {
       const uint32_t lbo_a = kTcRows * 128, lbo_b = (uint32_t)G.nbh * 128;
-      long long it = 0, j = 0;
+      long long it = 0, j = 0;  // j: accumulators filled, one per (tile, segment)
       bool ok = true;
-      for (long long u = blockIdx.x; u < G.units && ok; u += gridDim.x, ++j) {
-        const int buf = (int)(j & 1);
-        // accumulator buf was last used by tile j - 2
-        if (j >= 2 && !mbar_wait(&acc_empty[buf], (uint32_t)(((j >> 1) - 1) & 1))) {
-          report_error(status, kErrTcWaitAcc);
-          break;
-        }
-        tc_fence_after();
-        const uint32_t d = tmem + (uint32_t)buf * 256;
-        for (int kc = 0; kc < G.nkc; ++kc, ++it) {
-          const int s = (int)(it % STAGES);
-          if (!mbar_wait(&full[s], (uint32_t)((it / STAGES) & 1))) {
-            report_error(status, kErrTcWaitFull);
+      for (long long u = blockIdx.x; u < G.units && ok; u += gridDim.x) {
+        for (int sg = 0; sg < G.nseg && ok; ++sg, ++j) {
+          const int buf = (int)(j & 1);
+          // accumulator buf was last used by accumulator j - 2
+          if (j >= 2 && !mbar_wait(&acc_empty[buf], (uint32_t)(((j >> 1) - 1) & 1))) {
+            report_error(status, kErrTcWaitAcc);
             ok = false;
             break;
           }
           tc_fence_after();
-          const uint32_t sa = smem_base + (uint32_t)s * kTcStageBytes, sb = sa + kTcABytes;
+          const uint32_t d = tmem + (uint32_t)buf * 256;
+          const int nkc = seg_chunks<KC>(G, sg);
+          for (int kc = 0; kc < nkc; ++kc, ++it) {
+            const int s = (int)(it % STAGES);
+            if (!mbar_wait(&full[s], (uint32_t)((it / STAGES) & 1))) {
+              report_error(status, kErrTcWaitFull);
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint32_t sa = smem_base + (uint32_t)s * kTcStageBytes, sb = sa + kTcABytes;
 #pragma unroll
-          for (int ks = 0; ks < KC / 16; ++ks)
-            tc_mma(d, smem_desc(sa + ks * 2 * lbo_a, lbo_a, 128),
-                   smem_desc(sb + ks * 2 * lbo_b, lbo_b, 128), G.idesc,
-                   (kc > 0 || ks > 0) ? 1u : 0u);
-          tc_commit(&empty[s]);  // the stage is free once these MMAs have read it
+            for (int ks = 0; ks < KC / 16; ++ks)
+              tc_mma(d, smem_desc(sa + ks * 2 * lbo_a, lbo_a, 128),
+                     smem_desc(sb + ks * 2 * lbo_b, lbo_b, 128), G.idesc,
+                     (kc > 0 || ks > 0) ? 1u : 0u);
+            tc_commit(&empty[s]);  // the stage is free once these MMAs have read it
+          }
+          if (ok) tc_commit(&acc_full[buf]);
         }
-        if (ok) tc_commit(&acc_full[buf]);
       }
       // wait for every MMA issued so far before the columns are released
       tc_commit(drained);
@@ -262,72 +278,84 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     const uint32_t lane_bits = (uint32_t)(qd * 32) << 16;
     const int groups = G.nbh / 8;
     long long j = 0;
-    bool range_ok = true;
-    for (long long u = blockIdx.x; u < G.units; u += gridDim.x, ++j) {
-      const int buf = (int)(j & 1);
-      bool got = true;
-      if (lane == 0) got = mbar_wait_sleep(&acc_full[buf], (uint32_t)((j >> 1) & 1));
-      got = __shfl_sync(0xffffffffu, got, 0);
-      if (!got) {
-        if (lane == 0) report_error(status, kErrTcWaitAcc);
-        break;
-      }
-      tc_fence_after();
+    bool range_ok = true, alive = true;
+    for (long long u = blockIdx.x; u < G.units && alive; u += gridDim.x) {
       const long long c = u / per_c, rem = u % per_c;
       const long long rb = rem / G.nh, hf = rem % G.nh;
       const size_t row = (size_t)rb * kTcRows + qd * 4 + rsub;
-      const uint32_t acc_addr = tmem + lane_bits + (uint32_t)buf * 256;
-      for (int grp = part; grp < groups; grp += 2) {
+      uint64_t sum[4] = {0, 0, 0, 0};  // this lane's cell of groups part, part + 2, ...
+      for (int sg = 0; sg < G.nseg; ++sg, ++j) {
+        const int buf = (int)(j & 1);
+        bool got = true;
+        if (lane == 0) got = mbar_wait_sleep(&acc_full[buf], (uint32_t)((j >> 1) & 1));
+        got = __shfl_sync(0xffffffffu, got, 0);
+        if (!got) {
+          if (lane == 0) report_error(status, kErrTcWaitAcc);
+          alive = false;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t acc_addr = tmem + lane_bits + (uint32_t)buf * 256;
 #pragma unroll
-        for (int hc = 0; hc < 2; ++hc) {
-          uint32_t r[32];
-          tmem_ld32(acc_addr + (uint32_t)((grp * 2 + hc) * 32), r);
+        for (int gi = 0; gi < 4; ++gi) {
+          const int grp = part + 2 * gi;
+          if (grp >= groups) break;
 #pragma unroll
-          for (int bl = 0; bl < 4; ++bl) {
-            int x[8];
+          for (int hc = 0; hc < 2; ++hc) {
+            uint32_t r[32];
+            tmem_ld32(acc_addr + (uint32_t)((grp * 2 + hc) * 32), r);
 #pragma unroll
-            for (int d = 0; d < 8; ++d) x[d] = __float2int_rn(__uint_as_float(r[bl * 8 + d]));
-            // skewed exchange: lane t8 collects Y_t8 and Y_(t8+8) of its row
-            int ylo = x[0], yhi = 0;
+            for (int bl = 0; bl < 4; ++bl) {
+              int x[8];
 #pragma unroll
-            for (int d = 1; d < 8; ++d) {
-              const int v = __shfl_sync(0xffffffffu, x[d], (lane & ~7) | ((lane - d) & 7));
-              if (d <= t8)
-                ylo += v;
-              else
-                yhi += v;
+              for (int d = 0; d < 8; ++d) x[d] = __float2int_rn(__uint_as_float(r[bl * 8 + d]));
+              // skewed exchange: lane t8 collects Y_t8 and Y_(t8+8) of its row
+              int ylo = x[0], yhi = 0;
+#pragma unroll
+              for (int d = 1; d < 8; ++d) {
+                const int v = __shfl_sync(0xffffffffu, x[d], (lane & ~7) | ((lane - d) & 7));
+                if (d <= t8)
+                  ylo += v;
+                else
+                  yhi += v;
+              }
+              int *yb = yw + (hc * 4 + bl) * 20;
+              yb[t8] = ylo;
+              yb[t8 + 8] = yhi;
             }
-            int *yb = yw + (hc * 4 + bl) * 20;
-            yb[t8] = ylo;
-            yb[t8 + 8] = yhi;
           }
-        }
-        __syncwarp();
-        int y[16];
-        const int4 *src = reinterpret_cast<const int4 *>(yw + t8 * 20);
+          __syncwarp();
+          int y[16];
+          const int4 *src = reinterpret_cast<const int4 *>(yw + t8 * 20);
 #pragma unroll
-        for (int v = 0; v < 4; ++v) {
-          const int4 t = src[v];
-          y[4 * v] = t.x;
-          y[4 * v + 1] = t.y;
-          y[4 * v + 2] = t.z;
-          y[4 * v + 3] = t.w;
+          for (int v = 0; v < 4; ++v) {
+            const int4 t = src[v];
+            y[4 * v] = t.x;
+            y[4 * v + 1] = t.y;
+            y[4 * v + 2] = t.z;
+            y[4 * v + 3] = t.w;
+          }
+          __syncwarp();
+          bool ok_one = true;
+          const uint64_t val = tc_combine(y, q, mu_lo, mu_hi, r64, r128, ok_one);
+          range_ok &= ok_one;
+          sum[gi] = sg == 0 ? val : add_mod(sum[gi], val, q);
         }
+        tc_fence_before();
         __syncwarp();
-        bool ok_one = true;
-        uint64_t val = tc_combine(y, q, mu_lo, mu_hi, r64, r128, ok_one);
-        range_ok &= ok_one;
+        if (lane == 0) mbar_arrive(&acc_empty[buf]);
+      }
+      if (!alive) break;
+      // the tile's results, once
+#pragma unroll
+      for (int gi = 0; gi < 4; ++gi) {
+        const int grp = part + 2 * gi;
+        if (grp >= groups) break;
         const int bq = (int)hf * kTcHalfNB + grp * 8 + t8;  // query polynomial in the pass
         const int b = bq >> 1;
-        if (b < G.batch) {
-          uint64_t *o = out + (size_t)(b_base + b) * out_stride + (row * 2 + (bq & 1)) * kN + c;
-          if (G.accumulate) val = add_mod(val, *o, q);
-          *o = val;
-        }
+        if (b < G.batch)
+          out[(size_t)(b_base + b) * out_stride + (row * 2 + (bq & 1)) * kN + c] = sum[gi];
       }
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&acc_empty[buf]);
     }
     if (!range_ok) report_error(status, kErrTcRange);
   }
@@ -449,8 +477,6 @@ uint32_t make_idesc(int n) {
 
 }  // namespace
 
-constexpr int kTcMaxSegment = 512;  // k per exact fp32 accumulation
-
 bool tc_scan_supported(int n1, int n_rest) {
   return n1 % kTcKC == 0 && n1 > 0 && n_rest % kTcRows == 0 && n_rest >= kTcRows;
 }
@@ -469,11 +495,9 @@ TcGeom pass_geom(int n1, int n_rest, int pb) {
   G.nbh = 2 * padded / G.nh;
   G.n_rb = n_rest / kTcRows;
   G.units = (long long)kN * G.n_rb * G.nh;
+  G.nseg = (n1 + kTcMaxSegment - 1) / kTcMaxSegment;
   G.b_bytes = 0;  // per stage: set by the launcher for its stage size
   G.idesc = make_idesc(G.nbh * 8);
-  G.k0 = 0;
-  G.nkc = 0;
-  G.accumulate = 0;
   return G;
 }
 // query limbs of one pass (elements); passes follow each other in ql
@@ -491,6 +515,8 @@ size_t tc_query_limb_bytes(int n1, int batch) {
 }
 
 cudaError_t init_tc_attributes() {
+  g_tc_ring = -1;
+  if (const char *v = getenv("OPIR_TC_RING")) g_tc_ring = atoi(v);
   int dev;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&g_tc_sms, cudaDevAttrMultiProcessorCount, dev);
@@ -522,9 +548,14 @@ void launch_tc_query_limbs(const uint64_t *plane, uint16_t *ql, int n1, int batc
   }
 }
 
+bool tc_ring_valid(int ring, int n1) { return ring == kTcRing32x8 || (ring == kTcRing64x4 && n1 % 64 == 0); }
+
 int launch_tc_scan(const uint16_t *dbl, const uint16_t *ql, uint64_t *out, size_t out_stride,
                    int n1, int n_rest, int batch, uint64_t q, uint64_t mu_lo, uint64_t mu_hi,
-                   uint64_t r64, uint64_t r128, uint32_t *status, cudaStream_t s) {
+                   uint64_t r64, uint64_t r128, uint32_t *status, cudaStream_t s, int ring) {
+  if (g_tc_ring >= 0) ring = g_tc_ring;
+  // every segment length is a multiple of 64 when n1 is (segments of 512)
+  if (!tc_ring_valid(ring, n1)) ring = n1 % 64 == 0 ? kTcRing64x4 : kTcRing32x8;
   int launches = 0;
   size_t off = 0;
   for (int b0 = 0; b0 < batch; b0 += kTcMaxNB / 2) {
@@ -532,23 +563,16 @@ int launch_tc_scan(const uint16_t *dbl, const uint16_t *ql, uint64_t *out, size_
     TcGeom G = pass_geom(n1, n_rest, pb);
     const int sms = g_tc_sms > 0 ? g_tc_sms : 152;
     const long long grid = G.units < sms ? G.units : sms;
-    for (int k0 = 0; k0 < n1; k0 += kTcMaxSegment) {
-      const int klen = n1 - k0 < kTcMaxSegment ? n1 - k0 : kTcMaxSegment;
-      G.k0 = k0;
-      G.accumulate = k0 > 0;
-      if (klen % 64 == 0) {
-        G.nkc = klen / 64;
-        G.b_bytes = (uint32_t)(64 / 8 * G.nbh * 128);
-        tc_scan_kernel<64, 4><<<(unsigned)grid, kTcThreads, tc_smem<64, 4>(), s>>>(
-            dbl, ql + off, out, out_stride, b0, G, q, mu_lo, mu_hi, r64, r128, status);
-      } else {
-        G.nkc = klen / 32;
-        G.b_bytes = (uint32_t)(32 / 8 * G.nbh * 128);
-        tc_scan_kernel<32, 8><<<(unsigned)grid, kTcThreads, tc_smem<32, 8>(), s>>>(
-            dbl, ql + off, out, out_stride, b0, G, q, mu_lo, mu_hi, r64, r128, status);
-      }
-      launches++;
+    if (ring == kTcRing64x4) {
+      G.b_bytes = (uint32_t)(64 / 8 * G.nbh * 128);
+      tc_scan_kernel<64, 4><<<(unsigned)grid, kTcThreads, tc_smem<64, 4>(), s>>>(
+          dbl, ql + off, out, out_stride, b0, G, q, mu_lo, mu_hi, r64, r128, status);
+    } else {
+      G.b_bytes = (uint32_t)(32 / 8 * G.nbh * 128);
+      tc_scan_kernel<32, 8><<<(unsigned)grid, kTcThreads, tc_smem<32, 8>(), s>>>(
+          dbl, ql + off, out, out_stride, b0, G, q, mu_lo, mu_hi, r64, r128, status);
     }
+    launches++;
     off += pass_limb_elems(n1, pb);
   }
   return launches;

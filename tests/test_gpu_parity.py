@@ -341,9 +341,10 @@ def test_batched_scan_matches_single_and_oracle(oracle_lib, gpu_lib, monkeypatch
     ((4096, 256), 20),      # 40 query polynomials: a 256 + 64 column split
     ((1 << 15, 512), 5),    # 512 x 64
     ((1 << 15, 512), 32),   # a full pass: 512 tensor-memory columns
-    ((1 << 14, 1024), 6),   # 1024 x 16: two k segments of 512, the second accumulating
+    ((1 << 14, 1024), 6),   # 1024 x 16: two k segments of 512 summed in the epilogue
+    ((1 << 14, 1024), 40),  # the same in two passes (32 + 8 queries)
     ((1536, 128), 4),       # 96 x 16: 32-k pipeline stages (96 is not a multiple of 64)
-    ((8704, 1024), 3),      # 544 x 16: a 64-k segment of 512, then a 32-k segment of 32
+    ((8704, 1024), 3),      # 544 x 16: k segments of 512 and 32, 32-k pipeline stages
 ])
 def test_tensor_core_first_dim_matches_single_queries(oracle_lib, gpu_lib, monkeypatch, shape,
                                                       batch):
