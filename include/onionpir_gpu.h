@@ -224,16 +224,22 @@ int opir_set_batch_engine(opir_ctx *ctx, int engine, uint32_t tensor_min_batch);
 
 /* ---- autotuner (no reference counterpart) ----
  * Times, on this GPU and for database db_id, every compiled tile
- * configuration of the single-query scan, and the first-dimension product
- * of every engine (one scan per query, integer GEMM, tensor-core limb GEMM)
- * at the batch sizes 2, 4, ..., max_batch (at most 256), each after a
+ * configuration of the single-query scan, the first-dimension product of
+ * every engine (one scan per query, integer GEMM, tensor-core limb GEMM) at
+ * the batch sizes 2, 4, ..., max_batch (at most 256), the tensor kernel's
+ * two shared-memory ring shapes at the largest of them, and every launch
+ * form (one CTA per ciphertext, two CTAs, a thread-block cluster) of every
+ * expansion, RGSW-reconstruction and folding launch of this database's
+ * pipeline at one query and at each batch size up to 64 -- each after a
  * warm-up, over `reps` repetitions (0: 3), on operands of valid residues.
- * The database then scans with the fastest configuration, and under
- * OPIR_ENGINE_AUTO a batch of B queries takes the engine that was fastest at
- * the largest measured size <= B.  Builds the database's limb plane if the
- * tensor engine can run on it.  Results are unchanged (every configuration
- * and engine gives the same bits).  Not while serving (OPIR_ERR_STATE).
- * times in ms of one first-dimension product; < 0: cannot run this shape. */
+ * The database then scans with the fastest configuration, runs the tensor
+ * kernel with the faster ring, launches each tree stage in the form that was
+ * fastest for its work count, and under OPIR_ENGINE_AUTO a batch of B
+ * queries takes the engine that was fastest at the largest measured size
+ * <= B.  Builds the database's limb plane if the tensor engine can run on
+ * it.  Results are unchanged (every configuration, ring, form and engine
+ * gives the same bits).  Not while serving (OPIR_ERR_STATE).
+ * Times in ms of one launch or product; < 0: cannot run this shape. */
 typedef struct opir_tune_report {
   uint32_t scan_configs;   /* compiled scan configurations (<= 16) */
   uint32_t scan_desc[16][6]; /* rows per thread, warps, k-steps, stages, CTAs per SM,
@@ -244,6 +250,14 @@ typedef struct opir_tune_report {
   uint32_t batch[8];
   float engine_ms[8][3];   /* [point][OPIR_ENGINE_SCAN - 1 .. OPIR_ENGINE_TENSOR - 1] */
   int32_t engine[8];       /* chosen OPIR_ENGINE_* per point */
+  uint32_t tc_ring_desc[2][2]; /* tensor kernel rings: {k per stage, stages} */
+  float tc_ring_ms[2];     /* at the largest batch size; < 0: not measured */
+  int32_t tc_ring_choice;  /* -1: not tuned */
+  uint32_t form_points;    /* distinct tree-stage launches measured (<= 128) */
+  uint32_t form_stage[128]; /* 0 expansion, 1 RGSW reconstruction, 2 folding */
+  uint32_t form_count[128]; /* work items: nodes / ciphertexts / pairs x queries */
+  float form_ms[128][3];   /* one CTA, two CTAs, cluster per ciphertext */
+  int32_t form_choice[128];
 } opir_tune_report;
 int opir_autotune(opir_ctx *ctx, uint32_t db_id, uint32_t max_batch, uint32_t reps,
                   opir_tune_report *report);

@@ -120,6 +120,14 @@ class OpirTuneReport(ctypes.Structure):
         ("batch", ctypes.c_uint32 * 8),
         ("engine_ms", (ctypes.c_float * 3) * 8),
         ("engine", ctypes.c_int32 * 8),
+        ("tc_ring_desc", (ctypes.c_uint32 * 2) * 2),
+        ("tc_ring_ms", ctypes.c_float * 2),
+        ("tc_ring_choice", ctypes.c_int32),
+        ("form_points", ctypes.c_uint32),
+        ("form_stage", ctypes.c_uint32 * 128),
+        ("form_count", ctypes.c_uint32 * 128),
+        ("form_ms", (ctypes.c_float * 3) * 128),
+        ("form_choice", ctypes.c_int32 * 128),
     ]
 
 

@@ -112,6 +112,8 @@ struct Db {
   // the engine per batch size (empty: the fixed crossovers)
   int scan_cfg = -1;
   tune::EngineTable engines;
+  int tc_ring = -1;  // tensor kernel ring shape (kTcRing*), -1: the default
+  TreeForms forms;   // tuned launch form per tree-stage work count
   // the synchronous single-query pipeline as CUDA graphs: executables keyed
   // by everything their kernel parameters hold (client keys, buffers, tile
   // configuration); the least recently used one is updated in place on a miss
@@ -501,7 +503,7 @@ int run_pipeline(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
     const int live = (int)((u + ((size_t)1 << (h - a)) - 1) >> (h - a));
     uint64_t *nxt = bufs[a & 1];
     launch_expand_level(cur, nxt, cur_stride, w * CTW, qd, a, live, batch, ctx->Mq.tab,
-                        ctx->Mp.tab, ctx->C, s, (pdl & kPdlExpand) && a > 0);
+                        ctx->Mp.tab, ctx->C, s, (pdl & kPdlExpand) && a > 0, &db.forms);
     ctx->launches++;
     cur = nxt;
     cur_stride = w * CTW;
@@ -514,7 +516,7 @@ int run_pipeline(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
   if (db.ndim > 1) {
     launch_query_to_gsw(leaves, leaves_stride, W.gsw.as<uint64_t>(), gsw_stride, qd, (int)n1,
                         (db.ndim - 1) * l, batch, ctx->Mq.tab, ctx->C, s,
-                        (pdl & kPdlQtg) && h > 0);
+                        (pdl & kPdlQtg) && h > 0, &db.forms);
     ctx->launches++;
   }
   record(ctx, E, 2);
@@ -544,7 +546,7 @@ int run_pipeline(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
     ctx->launches += launch_tc_scan(db.dbl.as<uint16_t>(), W.ql.as<uint16_t>(), W.res.as<uint64_t>(),
                                     res_stride, (int)n1, (int)nr, batch, ctx->Mq.tab.q,
                                     ctx->Mq.tab.mu_lo, ctx->Mq.tab.mu_hi, ctx->r64, ctx->r128,
-                                    E.status, s) - 1;
+                                    E.status, s, db.tc_ring) - 1;
   } else if (batched) {
     launch_query_prep_batched(leaves, leaves_stride, W.qs.as<uint4>(), (int)n1, batch,
                               ctx->Mq.tab, s, pdl_prep);
@@ -573,7 +575,7 @@ int run_pipeline(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
   for (int i = 1; i < db.ndim; i++) {
     const int half = (int)(cnt / 2);
     launch_fold(W.res.as<uint64_t>(), res_stride, W.gsw.as<uint64_t>() + (size_t)(i - 1) * 2 * l * CTW,
-                gsw_stride, half, batch, ctx->Mq.tab, ctx->C, s, (pdl & kPdlFold) != 0);
+                gsw_stride, half, batch, ctx->Mq.tab, ctx->C, s, (pdl & kPdlFold) != 0, &db.forms);
     ctx->launches++;
     cnt = half;
   }
@@ -732,6 +734,111 @@ int ingest_chunk_coeffs(opir_ctx *ctx, Db &db, size_t pt0, size_t count) {
                         ctx->stream);
   ctx->launches++;
   CK(cudaGetLastError(), "ingest launch");
+  return OPIR_OK;
+}
+
+// The tree-stage part of opir_autotune: for one query and for every batch
+// size of the report up to one key chunk (64 queries), every expansion level,
+// the RGSW reconstruction and every folding level of database db, each form
+// the parameter set allows, on operands of valid residues (the database's)
+// and synthetic keys reduced mod their modulus with correct companions.  The
+// fastest form per (stage, work count) goes into `out`; the report lists
+// every measurement.
+template <class TimeIt>
+int tune_tree_forms(opir_ctx *ctx, const Db &db, opir_tune_report &R, TreeForms &out,
+                    TimeIt &time_it, const DevBuf &leaves_src, const DevBuf &res) {
+  std::vector<int> batches{1};
+  for (uint32_t i = 0; i < R.batch_points; i++)
+    if (R.batch[i] <= (uint32_t)kMaxKeyBatch) batches.push_back((int)R.batch[i]);
+  const int bmax = batches.back();
+  const size_t CTW = 2 * (size_t)kN, w = (size_t)1 << db.h;
+  const int n1 = (int)db.shape.fst_dim_sz, nr = (int)db.shape.other_dim_sz, l = ctx->C.l;
+  const int num_cts = (db.ndim - 1) * l;
+  const size_t gsw_stride = (size_t)(db.ndim > 1 ? db.ndim - 1 : 1) * 2 * l * CTW;
+  cudaStream_t s = ctx->stream;
+  // keys: one set for every query, [kLogN][k][q, p][N] then the companions
+  const size_t gwords = (size_t)kLogN * 4 * kN;
+  std::vector<uint64_t> hk(2 * gwords);
+  uint64_t x = 0x9E3779B97F4A7C15ULL;
+  for (size_t i = 0; i < gwords; i++) {
+    x ^= x << 13, x ^= x >> 7, x ^= x << 17;
+    const uint64_t mod = ((i / kN) & 1) ? ctx->Mp.tab.q : ctx->Mq.tab.q;
+    hk[i] = x % mod;
+    hk[gwords + i] = shoup(hk[i], mod);
+  }
+  DevBuf keys, gswk, exp0, exp1, gsw;
+  CK(keys.alloc(hk.size() * 8), "autotune keys");
+  CK(cudaMemcpyAsync(keys.p, hk.data(), hk.size() * 8, cudaMemcpyHostToDevice, s), "autotune keys");
+  const size_t kwords = 2 * (size_t)ctx->prm.gsw_l_key * CTW;
+  CK(gswk.alloc(kwords * 8), "autotune keys");
+  CK(exp0.alloc((size_t)bmax * w * CTW * 8), "autotune expansion");
+  CK(exp1.alloc((size_t)bmax * w * CTW * 8), "autotune expansion");
+  CK(gsw.alloc((size_t)bmax * gsw_stride * 8), "autotune RGSW rows");
+  // fill `words` words of dst with copies of the operand residues
+  const size_t src_words = leaves_src.bytes / 8;
+  auto fill = [&](uint64_t *dst, size_t words) -> cudaError_t {
+    for (size_t off = 0; off < words; off += src_words) {
+      const size_t n = std::min(src_words, words - off);
+      const cudaError_t e =
+          cudaMemcpyAsync(dst + off, leaves_src.p, n * 8, cudaMemcpyDeviceToDevice, s);
+      if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+  };
+  CK(fill(gswk.as<uint64_t>(), kwords), "autotune keys");
+  CK(fill(exp0.as<uint64_t>(), (size_t)bmax * w * CTW), "autotune operands");
+  CK(fill(gsw.as<uint64_t>(), (size_t)bmax * gsw_stride), "autotune operands");
+  std::vector<QueryDesc> qd(bmax);
+  for (auto &d : qd) {
+    d.galois = keys.as<uint64_t>();
+    d.galois_s = keys.as<uint64_t>() + gwords;
+    d.gsw_key = gswk.as<uint64_t>();
+  }
+  R.form_points = 0;
+  auto measure = [&](int stage, int count, auto &&launch) {
+    if (out.pick(stage, count) != kFormDefault) return;  // measured already
+    if (R.form_points >= 128) return;
+    float ms[3];
+    for (int f = 0; f < 3; f++) {
+      if (!tree_form_valid(stage, f, ctx->C)) {
+        ms[f] = -1.0f;
+        continue;
+      }
+      TreeForms force;
+      force.set(stage, count, f);
+      ms[f] = time_it([&] {
+        launch(force);
+        return true;
+      });
+    }
+    const int best = tune::pick(ms, 3);
+    out.set(stage, count, best);
+    const uint32_t i = R.form_points++;
+    R.form_stage[i] = (uint32_t)stage;
+    R.form_count[i] = (uint32_t)count;
+    for (int f = 0; f < 3; f++) R.form_ms[i][f] = ms[f];
+    R.form_choice[i] = best;
+  };
+  for (int B : batches) {
+    for (int a = 0; a < db.h; a++) {
+      const int live = (int)((db.u + ((size_t)1 << (db.h - a)) - 1) >> (db.h - a));
+      measure(kStageExpand, live * B, [&](const TreeForms &f) {
+        launch_expand_level(exp0.as<uint64_t>(), exp1.as<uint64_t>(), w * CTW, w * CTW, qd.data(),
+                            a, live, B, ctx->Mq.tab, ctx->Mp.tab, ctx->C, s, false, &f);
+      });
+    }
+    if (db.ndim > 1)
+      measure(kStageQtg, num_cts * B, [&](const TreeForms &f) {
+        launch_query_to_gsw(exp0.as<uint64_t>(), w * CTW, gsw.as<uint64_t>(), gsw_stride, qd.data(),
+                            n1, num_cts, B, ctx->Mq.tab, ctx->C, s, false, &f);
+      });
+    for (int half = nr / 2; half >= 1; half /= 2)
+      measure(kStageFold, half * B, [&](const TreeForms &f) {
+        launch_fold(res.as<uint64_t>(), (size_t)nr * CTW, gsw.as<uint64_t>(), gsw_stride, half, B,
+                    ctx->Mq.tab, ctx->C, s, false, &f);
+      });
+  }
+  CK(cudaStreamSynchronize(s), "autotune tree stages");
   return OPIR_OK;
 }
 
@@ -1400,6 +1507,30 @@ int opir_autotune(opir_ctx *ctx, uint32_t db_id, uint32_t max_batch, uint32_t re
       return true;
     });
   }
+  // ---- tensor kernel: both shared-memory rings at the largest batch
+  R.tc_ring_choice = -1;
+  const uint32_t ring_desc[2][2] = {{64, 4}, {32, 8}};
+  std::memcpy(R.tc_ring_desc, ring_desc, sizeof ring_desc);
+  for (int ring = 0; ring < 2; ring++) {
+    R.tc_ring_ms[ring] = !(tc_ok && limbs && np && tc_ring_valid(ring, n1)) ? -1.0f : time_it([&] {
+      launch_tc_scan(db->dbl.as<uint16_t>(), ql.as<uint16_t>(), res.as<uint64_t>(), res_stride, n1,
+                     nr, bmax, ctx->Mq.tab.q, ctx->Mq.tab.mu_lo, ctx->Mq.tab.mu_hi, ctx->r64,
+                     ctx->r128, status, s, ring);
+      return true;
+    });
+  }
+  if (R.tc_ring_ms[0] >= 0 || R.tc_ring_ms[1] >= 0) R.tc_ring_choice = tune::pick(R.tc_ring_ms, 2);
+  // ---- tree stages: every form of every distinct launch of this database's
+  // pipeline, at one query and at the batch sizes up to one key chunk
+  TreeForms tuned;
+  {
+    const int trc = tune_tree_forms(ctx, *db, R, tuned, time_it, leaves, res);
+    if (trc) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      return trc;
+    }
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   CK(cudaGetLastError(), "autotune launches");
@@ -1407,6 +1538,12 @@ int opir_autotune(opir_ctx *ctx, uint32_t db_id, uint32_t max_batch, uint32_t re
   int rc = check_status(ctx);
   if (rc) return rc;
   db->scan_cfg = R.scan_choice;
+  db->tc_ring = R.tc_ring_choice;
+  db->forms = tuned;
+  // captured single-query graphs hold the launch forms of their capture
+  for (auto &gr : db->graphs)
+    if (gr.exec) cudaGraphExecDestroy(gr.exec);
+  db->graphs.clear();
   tune::build_table(db->engines, R.batch, np, R.engine_ms);
   for (int i = 0; i < np; i++) R.engine[i] = db->engines.engine[i];
   if (report) *report = R;

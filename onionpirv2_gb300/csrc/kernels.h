@@ -76,18 +76,54 @@ inline void launch_kernel(bool pdl, void (*k)(P...), dim3 grid, dim3 block, size
 void launch_ntt(const ModTab &M, uint64_t *polys, size_t count, bool inverse, cudaStream_t s,
                 bool pdl = false);
 
+// ---- launch forms of the tree stages
+// Every tree stage has a one-CTA form (a whole ciphertext per CTA), a
+// two-CTA form (expansion and folding: the two polynomials' transforms on two
+// CTAs) and a thread-block-cluster form (one ciphertext's independent
+// transforms spread over 4-6 CTAs).  Which is fastest depends on the launch's
+// work count (nodes, RGSW ciphertexts or fold pairs, times the queries of the
+// launch) and on the GPU: TreeForms holds the autotuner's choice per count;
+// a count it does not hold takes the measured default thresholds.
+enum { kStageExpand = 0, kStageQtg = 1, kStageFold = 2 };
+enum { kFormDefault = -1, kFormOne = 0, kFormPair = 1, kFormCluster = 2 };
+struct TreeForms {
+  static constexpr int kMax = 96;
+  int n[3] = {0, 0, 0};
+  int count[3][kMax] = {}, form[3][kMax] = {};
+  int pick(int stage, int cnt) const {
+    for (int i = 0; i < n[stage]; ++i)
+      if (count[stage][i] == cnt) return form[stage][i];
+    return kFormDefault;
+  }
+  bool set(int stage, int cnt, int f) {
+    for (int i = 0; i < n[stage]; ++i)
+      if (count[stage][i] == cnt) {
+        form[stage][i] = f;
+        return true;
+      }
+    if (n[stage] == kMax) return false;
+    count[stage][n[stage]] = cnt;
+    form[stage][n[stage]++] = f;
+    return true;
+  }
+};
+// whether `form` exists for this stage and parameter set (the cluster forms
+// are written for l = 5 data digits and l_key = 10 key digits)
+bool tree_form_valid(int stage, int form, const Consts &C);
+
 // ---- query expansion, one tree level for every query of the batch
 // cur: [B][nodes_in][2][N], nxt: [B][2*nodes_in][2][N]
 void launch_expand_level(const uint64_t *cur, uint64_t *nxt, size_t in_stride, size_t out_stride,
                          const QueryDesc *qd, int level, int live_nodes, int batch,
                          const ModTab &Mq, const ModTab &Mp, const Consts &C, cudaStream_t s,
-                         bool pdl = false);
+                         bool pdl = false, const TreeForms *forms = nullptr);
 
 // ---- RGSW reconstruction (query_to_gsw) for all further dimensions
 // leaves: [B][u][2][N] (coefficient form), gsw_out: [B][ndim-1][2l][2][N]
 void launch_query_to_gsw(const uint64_t *leaves, size_t leaves_stride, uint64_t *gsw_out,
                          size_t gsw_stride, const QueryDesc *qd, int n1, int num_cts, int batch,
-                         const ModTab &Mq, const Consts &C, cudaStream_t s, bool pdl = false);
+                         const ModTab &Mq, const Consts &C, cudaStream_t s, bool pdl = false,
+                         const TreeForms *forms = nullptr);
 
 // ---- first dimension
 // NTT the first n1 leaves and transpose to the scan operand Qs[b][c][k]
@@ -147,7 +183,7 @@ int launch_tc_scan(const uint16_t *dbl, const uint16_t *ql, uint64_t *out, size_
 // ---- one folding level (other_dim_mux): res[b][j] += INTT(RGSW x (res[j+half]-res[j]))
 void launch_fold(uint64_t *res, size_t res_stride, const uint64_t *gsw, size_t gsw_stride,
                  int half, int batch, const ModTab &Mq, const Consts &C, cudaStream_t s,
-                 bool pdl = false);
+                 bool pdl = false, const TreeForms *forms = nullptr);
 
 // ---- mod switch to small_q + response bit packing
 void launch_modswitch_pack(const uint64_t *res, size_t res_stride, uint64_t *resp,

@@ -813,23 +813,58 @@ cudaError_t init_kernel_attributes() {
   return cudaSuccess;
 }
 
+bool tree_form_valid(int stage, int form, const Consts &C) {
+  switch (form) {
+    case kFormOne:
+      return true;
+    case kFormPair:
+      return stage != kStageQtg;
+    case kFormCluster:
+      return stage == kStageExpand || (stage == kStageFold && C.l == kFoldCluster) ||
+             (stage == kStageQtg && C.l_key == 2 * (kQtgCluster - 1));
+    default:
+      return false;
+  }
+}
+
+namespace {
+// the tuned form for `count`, else the default thresholds
+int form_for(int stage, int count, const Consts &C, const TreeForms *forms) {
+  const int f = forms ? forms->pick(stage, count) : kFormDefault;
+  if (f != kFormDefault && tree_form_valid(stage, f, C)) return f;
+  switch (stage) {
+    case kStageExpand:
+      return count < g_expand_threshold ? kFormCluster
+             : count < g_expand_pair_threshold ? kFormPair : kFormOne;
+    case kStageQtg:
+      return tree_form_valid(kStageQtg, kFormCluster, C) && count < g_qtg_threshold ? kFormCluster
+                                                                                      : kFormOne;
+    default:
+      return tree_form_valid(kStageFold, kFormCluster, C) && count < g_fold_threshold
+                 ? kFormCluster
+                 : count < g_pair_threshold ? kFormPair : kFormOne;
+  }
+}
+}  // namespace
+
 void launch_expand_level(const uint64_t *cur, uint64_t *nxt, size_t in_stride, size_t out_stride,
                          const QueryDesc *qd, int level, int live_nodes, int batch,
                          const ModTab &Mq, const ModTab &Mp, const Consts &C, cudaStream_t s,
-                         bool pdl) {
+                         bool pdl, const TreeForms *forms) {
   for (int b0 = 0; b0 < batch; b0 += kMaxKeyBatch) {
     const int nb = batch - b0 < kMaxKeyBatch ? batch - b0 : kMaxKeyBatch;
     KeyBatch kb;
     for (int i = 0; i < nb; ++i) kb.q[i] = qd[b0 + i];
     const uint64_t *in = cur + b0 * in_stride;
     uint64_t *out = nxt + b0 * out_stride;
-    if (live_nodes * nb < g_expand_threshold && 4 * live_nodes * nb <= g_sms)
+    const int form = form_for(kStageExpand, live_nodes * nb, C, forms);
+    if (form == kFormCluster && 4 * live_nodes * nb <= g_sms)
       launch_kernel(pdl, expand_cluster_kernel<true>, dim3(4 * live_nodes, nb), dim3(T),
                     kExpandClusterSmem, s, in, out, in_stride, out_stride, kb, level, Mq, Mp, C);
-    else if (live_nodes * nb < g_expand_threshold)
+    else if (form == kFormCluster)
       launch_kernel(pdl, expand_cluster_kernel<false>, dim3(4 * live_nodes, nb), dim3(T),
                     kClusterSmem, s, in, out, in_stride, out_stride, kb, level, Mq, Mp, C);
-    else if (live_nodes * nb < g_expand_pair_threshold)
+    else if (form == kFormPair)
       launch_kernel(pdl, expand_pair_kernel, dim3(2 * live_nodes, nb), dim3(T), kExpandPairSmem,
                     s, in, out, in_stride, out_stride, kb, level, Mq, Mp, C);
     else
@@ -840,7 +875,8 @@ void launch_expand_level(const uint64_t *cur, uint64_t *nxt, size_t in_stride, s
 
 void launch_query_to_gsw(const uint64_t *leaves, size_t leaves_stride, uint64_t *gsw_out,
                          size_t gsw_stride, const QueryDesc *qd, int n1, int num_cts, int batch,
-                         const ModTab &Mq, const Consts &C, cudaStream_t s, bool pdl) {
+                         const ModTab &Mq, const Consts &C, cudaStream_t s, bool pdl,
+                         const TreeForms *forms) {
   if (num_cts <= 0) return;
   for (int b0 = 0; b0 < batch; b0 += kMaxKeyBatch) {
     const int nb = batch - b0 < kMaxKeyBatch ? batch - b0 : kMaxKeyBatch;
@@ -848,7 +884,7 @@ void launch_query_to_gsw(const uint64_t *leaves, size_t leaves_stride, uint64_t 
     for (int i = 0; i < nb; ++i) kb.q[i] = qd[b0 + i];
     const uint64_t *in = leaves + b0 * leaves_stride;
     uint64_t *out = gsw_out + b0 * gsw_stride;
-    if (C.l_key == 2 * (kQtgCluster - 1) && num_cts * nb < g_qtg_threshold)
+    if (form_for(kStageQtg, num_cts * nb, C, forms) == kFormCluster)
       launch_kernel(pdl, query_to_gsw_cluster_kernel, dim3(kQtgCluster * num_cts, nb), dim3(T),
                     kClusterSmem, s, in, leaves_stride, out, gsw_stride, kb, n1, Mq, C);
     else
@@ -859,11 +895,12 @@ void launch_query_to_gsw(const uint64_t *leaves, size_t leaves_stride, uint64_t 
 
 void launch_fold(uint64_t *res, size_t res_stride, const uint64_t *gsw, size_t gsw_stride,
                  int half, int batch, const ModTab &Mq, const Consts &C, cudaStream_t s,
-                 bool pdl) {
-  if (C.l == kFoldCluster && half * batch < g_fold_threshold)
+                 bool pdl, const TreeForms *forms) {
+  const int form = form_for(kStageFold, half * batch, C, forms);
+  if (form == kFormCluster)
     launch_kernel(pdl, fold_cluster_kernel, dim3(kFoldCluster * half, batch), dim3(T),
                   kClusterSmem, s, res, res_stride, gsw, gsw_stride, half, Mq, C);
-  else if (half * batch < g_pair_threshold)
+  else if (form == kFormPair)
     launch_kernel(pdl, fold_pair_kernel, dim3(2 * half, batch), dim3(T), kClusterSmem, s, res,
                   res_stride, gsw, gsw_stride, half, Mq, C);
   else

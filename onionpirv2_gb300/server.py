@@ -344,6 +344,8 @@ class PirServer:
                                           max_batch, reps, ctypes.byref(r)))
         names = {1: "scan", 2: "imad", 3: "tensor"}
         keys = ("rows", "warps", "ksteps", "stages", "ctas_per_sm", "karatsuba")
+        stages = ("expand", "query_to_gsw", "fold")
+        forms = ("one_cta", "two_cta", "cluster")
         return {
             "scan_configs": [dict(zip(keys, list(r.scan_desc[i])), ms=float(r.scan_ms[i]))
                              for i in range(r.scan_configs)],
@@ -352,6 +354,14 @@ class PirServer:
                          "ms": {names[e + 1]: float(r.engine_ms[i][e]) for e in range(3)},
                          "engine": names.get(int(r.engine[i]), "scan")}
                         for i in range(r.batch_points)],
+            "tc_rings": [{"k_per_stage": int(r.tc_ring_desc[i][0]),
+                          "stages": int(r.tc_ring_desc[i][1]), "ms": float(r.tc_ring_ms[i])}
+                         for i in range(2)],
+            "tc_ring_choice": int(r.tc_ring_choice),
+            "forms": [{"stage": stages[r.form_stage[i]], "count": int(r.form_count[i]),
+                       "ms": {forms[f]: float(r.form_ms[i][f]) for f in range(3)},
+                       "form": forms[r.form_choice[i]] if r.form_choice[i] >= 0 else None}
+                      for i in range(r.form_points)],
         }
 
     def serve_start(self, max_batch: int = 32, lanes: int = 2, max_wait_us: int = 2000):

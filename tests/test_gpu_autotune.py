@@ -36,6 +36,16 @@ def test_autotune_choices_and_parity(gpu_lib, oracle_lib, shape):
         ms = [b["ms"][k] for k in ("scan", "imad", "tensor")]
         assert b["ms"]["scan"] > 0
         assert b["engine"] == ("scan", "imad", "tensor")[_argmin(ms)]
+    # the tensor kernel's ring and every tree launch's form are the fastest
+    # measurements, and the tree launches of one query were measured
+    rings = [r["ms"] for r in rep["tc_rings"]]
+    if any(m >= 0 for m in rings):
+        assert rep["tc_ring_choice"] == _argmin(rings)
+    assert rep["forms"] and all(f["form"] is not None for f in rep["forms"])
+    for f in rep["forms"]:
+        ms = [f["ms"][k] for k in ("one_cta", "two_cta", "cluster")]
+        assert f["form"] == ("one_cta", "two_cta", "cluster")[_argmin(ms)]
+    assert {f["stage"] for f in rep["forms"]} >= {"expand", "fold"}
     # same bits after tuning: single queries and batches of every size
     o = oracle_lib.Oracle(*shape)
     db = o.build_db(777)
@@ -65,4 +75,39 @@ def test_autotune_refused_while_serving(gpu_lib):
         server.autotune(max_batch=4)
     server.serve_stop()
     server.autotune(max_batch=4, reps=1)
+    server.close()
+
+
+@pytest.mark.parametrize("shape", [(4096, 256), (1 << 14, 1024)])
+@pytest.mark.parametrize("ring,threshold,pair", [(0, 100000, 0), (1, 0, 100000), (0, 0, 0)])
+def test_every_tuning_candidate_is_bit_exact(oracle_lib, gpu_lib, monkeypatch, shape, ring,
+                                             threshold, pair):
+    """Every candidate the autotuner chooses among gives the oracle's bits:
+    both tensor-kernel rings (64 k x 4 stages, 32 k x 8 stages) and every
+    tree-stage form (all clusters, all two-CTA forms, all one-CTA forms),
+    on two database shapes, single queries and a batch on the tensor engine."""
+    from onionpirv2_gb300 import PirParams, PirServer
+    monkeypatch.setenv("OPIR_TC_RING", str(ring))
+    monkeypatch.setenv("OPIR_CLUSTER_THRESHOLD", str(threshold))
+    monkeypatch.setenv("OPIR_PAIR_THRESHOLD", str(pair))
+    monkeypatch.setenv("OPIR_EXPAND_PAIR_THRESHOLD", str(pair))
+    monkeypatch.setenv("OPIR_GRAPHS", "0")
+    o = oracle_lib.Oracle(*shape)
+    server = PirServer(PirParams(num_entries=shape[0], max_fst_dim=shape[1]))
+    server.gen_data(11)
+    db = o.build_db(11)
+    sk = o.keygen(12)
+    gk, gsw = o.galois_keys(sk, 13), o.gsw_key(sk, 14)
+    server.set_client_galois_key(0, gk)
+    server.set_client_gsw_key(0, gsw)
+    gsn = o.gsw_key_to_ntt(gsw)
+    idxs = [0, shape[0] // 3, shape[0] - 1]
+    queries = np.stack([o.make_query(sk, 20 + j, i) for j, i in enumerate(idxs)])
+    refs = [o.make_query_server(db, gk, gsn, q)[0] for q in queries]
+    for q, r in zip(queries, refs):
+        assert np.array_equal(server.make_query(0, q), r)
+    server.set_batch_engine("tensor")
+    resps, _ = server.make_query_batch([0, 0, 0], queries)
+    for j in range(3):
+        assert np.array_equal(resps[j], refs[j]), j
     server.close()
