@@ -1098,7 +1098,13 @@ def main():
                      "engine_by_batch": {str(b["batch"]): b["engine"] for b in tune["batches"]},
                      "first_dim_ms_by_batch": {str(b["batch"]): {k: round(v, 3) for k, v in
                                                                  b["ms"].items()}
-                                               for b in tune["batches"]}},
+                                               for b in tune["batches"]},
+                     "tc_ring": {"choice": tune["tc_ring_choice"],
+                                 "ms": {f'{r["k_per_stage"]}x{r["stages"]}': round(r["ms"], 4)
+                                        for r in tune["tc_rings"]}},
+                     "tree_forms": [{"stage": f["stage"], "count": f["count"], "form": f["form"],
+                                     "ms": {k: round(v, 4) for k, v in f["ms"].items()}}
+                                    for f in tune["forms"]]},
         "entries_decoded": f"{decoded}/{total}",
         "min_noise_budget": min_budget,
         "client": {"threads": 1, "keygen_ms": inp.keygen_s * 1e3, "query_ms": inp.query_s * 1e3,

@@ -811,7 +811,11 @@ int tune_tree_forms(opir_ctx *ctx, const Db &db, opir_tune_report &R, TreeForms 
         return true;
       });
     }
-    const int best = tune::pick(ms, 3);
+    // the default form was chosen from sweeps of the whole pipeline, where
+    // a launch follows its producer; a form timed on its own replaces it only
+    // when it is clearly faster
+    const int dflt = tree_default_form(stage, count, ctx->C);
+    const int best = tune::pick_over(ms, 3, dflt, tune::kTuneMargin);
     out.set(stage, count, best);
     const uint32_t i = R.form_points++;
     R.form_stage[i] = (uint32_t)stage;
@@ -1519,7 +1523,9 @@ int opir_autotune(opir_ctx *ctx, uint32_t db_id, uint32_t max_batch, uint32_t re
       return true;
     });
   }
-  if (R.tc_ring_ms[0] >= 0 || R.tc_ring_ms[1] >= 0) R.tc_ring_choice = tune::pick(R.tc_ring_ms, 2);
+  if (R.tc_ring_ms[0] >= 0 || R.tc_ring_ms[1] >= 0)
+    R.tc_ring_choice = tune::pick_over(R.tc_ring_ms, 2, n1 % 64 == 0 ? kTcRing64x4 : kTcRing32x8,
+                                       tune::kTuneMargin);
   // ---- tree stages: every form of every distinct launch of this database's
   // pipeline, at one query and at the batch sizes up to one key chunk
   TreeForms tuned;

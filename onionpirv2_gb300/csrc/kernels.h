@@ -110,6 +110,8 @@ struct TreeForms {
 // whether `form` exists for this stage and parameter set (the cluster forms
 // are written for l = 5 data digits and l_key = 10 key digits)
 bool tree_form_valid(int stage, int form, const Consts &C);
+// the form the measured default thresholds give a launch of `count` items
+int tree_default_form(int stage, int count, const Consts &C);
 
 // ---- query expansion, one tree level for every query of the batch
 // cur: [B][nodes_in][2][N], nxt: [B][2*nodes_in][2][N]

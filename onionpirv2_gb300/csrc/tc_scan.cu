@@ -47,6 +47,7 @@ constexpr int kTcRows = 16;                 // database rows per tile
 constexpr int kTcKC = 32;                   // k granularity of the first dimension
 constexpr int kTcMaxNB = 64;                // query polynomials per pass (32 queries)
 constexpr int kTcHalfNB = 32;               // query polynomials per tile (256 TMEM columns)
+static_assert(kTcHalfNB / 8 <= 4, "the epilogue holds two groups per warp part");
 // pipeline stages: KC k per stage (64, or 32 when the segment length is an
 // odd multiple of 32), STAGES stages; the 64-k ring (4 x 48 KB) measured
 // 25 % faster than the 32-k ring (8 x 24 KB) and 5 % faster than 2 x 96 KB
@@ -283,7 +284,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       const long long c = u / per_c, rem = u % per_c;
       const long long rb = rem / G.nh, hf = rem % G.nh;
       const size_t row = (size_t)rb * kTcRows + qd * 4 + rsub;
-      uint64_t sum[4] = {0, 0, 0, 0};  // this lane's cell of groups part, part + 2, ...
+      // this lane's cell of groups part and part + 2 (a tile has kTcHalfNB / 8
+      // <= 4 groups of 8 query polynomials over two warp parts)
+      uint64_t sum[2] = {0, 0};
       for (int sg = 0; sg < G.nseg; ++sg, ++j) {
         const int buf = (int)(j & 1);
         bool got = true;
@@ -297,7 +300,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         tc_fence_after();
         const uint32_t acc_addr = tmem + lane_bits + (uint32_t)buf * 256;
 #pragma unroll
-        for (int gi = 0; gi < 4; ++gi) {
+        for (int gi = 0; gi < 2; ++gi) {
           const int grp = part + 2 * gi;
           if (grp >= groups) break;
 #pragma unroll
@@ -348,7 +351,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       if (!alive) break;
       // the tile's results, once
 #pragma unroll
-      for (int gi = 0; gi < 4; ++gi) {
+      for (int gi = 0; gi < 2; ++gi) {
         const int grp = part + 2 * gi;
         if (grp >= groups) break;
         const int bq = (int)hf * kTcHalfNB + grp * 8 + t8;  // query polynomial in the pass

@@ -847,6 +847,10 @@ int form_for(int stage, int count, const Consts &C, const TreeForms *forms) {
 }
 }  // namespace
 
+int tree_default_form(int stage, int count, const Consts &C) {
+  return form_for(stage, count, C, nullptr);
+}
+
 void launch_expand_level(const uint64_t *cur, uint64_t *nxt, size_t in_stride, size_t out_stride,
                          const QueryDesc *qd, int level, int live_nodes, int batch,
                          const ModTab &Mq, const ModTab &Mp, const Consts &C, cudaStream_t s,

@@ -25,6 +25,19 @@ inline int pick(const float *ms, int n) {
   return best;
 }
 
+// Launch forms and ring shapes timed on their own, outside the pipeline,
+// replace the default only when at least this much faster.
+constexpr float kTuneMargin = 0.03f;
+
+// the fastest of n measurements if it beats measurement `dflt` by more than
+// `margin` (a fraction of dflt's time), else dflt; pick() when dflt is
+// unavailable
+inline int pick_over(const float *ms, int n, int dflt, float margin) {
+  const int best = pick(ms, n);
+  if (dflt < 0 || dflt >= n || ms[dflt] < 0 || best < 0) return best;
+  return ms[best] < ms[dflt] * (1.0f - margin) ? best : dflt;
+}
+
 // batch sizes measured for max_batch: 2, 4, ... up to the largest power of
 // two <= max_batch (at most kMaxPoints); returns how many
 inline int batch_points(uint32_t max_batch, uint32_t *out) {

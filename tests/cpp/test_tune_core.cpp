@@ -49,6 +49,15 @@ int main() {
   build_table(u, b, 1, dead);
   CHECK(engine_at(u, 2) == 1);
 
+  // a form or ring timed on its own replaces the default only when more than
+  // kTuneMargin faster
+  const float near[3] = {1.00f, 0.98f, 1.20f}, far[3] = {1.00f, 0.90f, 1.20f};
+  CHECK(pick_over(near, 3, 0, kTuneMargin) == 0);
+  CHECK(pick_over(far, 3, 0, kTuneMargin) == 1);
+  const float gone[3] = {-1.0f, 0.98f, 1.20f};
+  CHECK(pick_over(gone, 3, 0, kTuneMargin) == 1);  // default unavailable
+  CHECK(pick_over(near, 3, -1, kTuneMargin) == 1);
+
   if (failures) return 1;
   std::printf("all checks passed\n");
   return 0;

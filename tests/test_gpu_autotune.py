@@ -37,14 +37,19 @@ def test_autotune_choices_and_parity(gpu_lib, oracle_lib, shape):
         assert b["ms"]["scan"] > 0
         assert b["engine"] == ("scan", "imad", "tensor")[_argmin(ms)]
     # the tensor kernel's ring and every tree launch's form are the fastest
-    # measurements, and the tree launches of one query were measured
+    # measurement or within the 3 % by which a candidate timed on its own
+    # must beat the default; the tree launches of one query were measured
+    def near_best(ms, chosen):
+        best = min(m for m in ms if m >= 0)
+        return ms[chosen] >= 0 and ms[chosen] * 0.97 <= best + 1e-9
+
     rings = [r["ms"] for r in rep["tc_rings"]]
     if any(m >= 0 for m in rings):
-        assert rep["tc_ring_choice"] == _argmin(rings)
+        assert near_best(rings, rep["tc_ring_choice"])
     assert rep["forms"] and all(f["form"] is not None for f in rep["forms"])
+    names = ("one_cta", "two_cta", "cluster")
     for f in rep["forms"]:
-        ms = [f["ms"][k] for k in ("one_cta", "two_cta", "cluster")]
-        assert f["form"] == ("one_cta", "two_cta", "cluster")[_argmin(ms)]
+        assert near_best([f["ms"][k] for k in names], names.index(f["form"]))
     assert {f["stage"] for f in rep["forms"]} >= {"expand", "fold"}
     # same bits after tuning: single queries and batches of every size
     o = oracle_lib.Oracle(*shape)
