@@ -563,13 +563,20 @@ int run_pipeline(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
                 ctx->Mq.tab.mu_hi, E.status, s, db.scan_cfg);
   }
   record(ctx, E, 7);
-  launch_ntt(ctx->Mq.tab, W.res.as<uint64_t>(), (size_t)batch * nr * 2, true, s,
-             (pdl & kPdlNtt) != 0);
-  ctx->launches += 3;
+  // the n_rest results stay in NTT form: the folds transform only their
+  // differences back (evaluate_first_dim's inverse transforms, server.cpp:
+  // 239, 290, move into other_dim_mux)
+  ctx->launches += 2;
   record(ctx, E, 3);
-  if (trace && trace->first_dim)
-    CK(cudaMemcpyAsync(trace->first_dim, W.res.p, nr * CTW * 8, cudaMemcpyDeviceToHost, s),
+  if (trace && trace->first_dim) {
+    DevBuf fd;
+    CK(fd.alloc(nr * CTW * 8), "trace first dim");
+    CK(cudaMemcpyAsync(fd.p, W.res.p, nr * CTW * 8, cudaMemcpyDeviceToDevice, s), "trace first dim");
+    launch_ntt(ctx->Mq.tab, fd.as<uint64_t>(), nr * 2, true, s);
+    CK(cudaMemcpyAsync(trace->first_dim, fd.p, nr * CTW * 8, cudaMemcpyDeviceToHost, s),
        "trace first dim");
+    CK(cudaStreamSynchronize(s), "trace first dim");
+  }
   // ---- other dimensions
   size_t cnt = nr;
   for (int i = 1; i < db.ndim; i++) {
@@ -579,6 +586,10 @@ int run_pipeline(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
     ctx->launches++;
     cnt = half;
   }
+  // the folded ciphertext of every query back to coefficient form
+  launch_ntt_groups(ctx->Mq.tab, W.res.as<uint64_t>(), 2, batch, res_stride, true, s,
+                    (pdl & kPdlNtt) != 0);
+  ctx->launches++;
   record(ctx, E, 4);
   // ---- mod switch + pack
   launch_modswitch_pack(W.res.as<uint64_t>(), res_stride, d_resp, d_packed, ctx->resp_bytes, batch,
@@ -1677,9 +1688,12 @@ int opir_other_dim_mux(opir_ctx *ctx, uint64_t *result, uint64_t count, const ui
   CK(dsel.alloc(sel_bytes), "alloc");
   CK(cudaMemcpyAsync(dres.p, result, res_bytes, cudaMemcpyHostToDevice, ctx->stream), "upload");
   CK(cudaMemcpyAsync(dsel.p, sel, sel_bytes, cudaMemcpyHostToDevice, ctx->stream), "upload");
+  // the folds work on ciphertexts in NTT form
+  launch_ntt(ctx->Mq.tab, dres.as<uint64_t>(), count * 2, false, ctx->stream);
   launch_fold(dres.as<uint64_t>(), count * CTW, dsel.as<uint64_t>(), 2 * (size_t)ctx->prm.gsw_l * CTW,
               (int)(count / 2), 1, ctx->Mq.tab, ctx->C, ctx->stream);
-  ctx->launches++;
+  launch_ntt(ctx->Mq.tab, dres.as<uint64_t>(), count, true, ctx->stream);
+  ctx->launches += 3;
   CK(cudaGetLastError(), "fold launch");
   CK(cudaMemcpyAsync(result, dres.p, res_bytes / 2, cudaMemcpyDeviceToHost, ctx->stream),
      "download");

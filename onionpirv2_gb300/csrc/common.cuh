@@ -267,6 +267,17 @@ __device__ __forceinline__ void lds_slot8(const uint64_t *base, uint64_t v[8]) {
     v[2 * j + 1] = t.y;
   }
 }
+// the slot layout of ldg_slot8 through the coherent path (for data the
+// calling kernel itself writes later)
+__device__ __forceinline__ void ld_slot8(const uint64_t *base, uint64_t v[8]) {
+  const ulonglong2 *p = reinterpret_cast<const ulonglong2 *>(base) + 4 * (threadIdx.x & (kNttThreads - 1));
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const ulonglong2 t = p[j];
+    v[2 * j] = t.x;
+    v[2 * j + 1] = t.y;
+  }
+}
 __device__ __forceinline__ void stg_slot8(uint64_t *base, const uint64_t v[8]) {
   ulonglong2 *p = reinterpret_cast<ulonglong2 *>(base) + 4 * (threadIdx.x & (kNttThreads - 1));
 #pragma unroll

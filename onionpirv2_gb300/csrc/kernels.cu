@@ -21,9 +21,10 @@ constexpr int T = kNttThreads;
 // ---------------------------------------------------------------------------
 // generic batched NTT
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(T) ntt_kernel(ModTab M, uint64_t *polys, int inverse) {
+__global__ void __launch_bounds__(T) ntt_kernel(ModTab M, uint64_t *polys, int inverse,
+                                                size_t group_stride) {
   __shared__ uint64_t sa[kSmemPoly], sb[kSmemPoly];
-  uint64_t *p = polys + (size_t)blockIdx.x * kN;
+  uint64_t *p = polys + blockIdx.y * group_stride + (size_t)blockIdx.x * kN;
   const int tid = threadIdx.x;
   grid_dep_sync();
   uint64_t r[8];
@@ -245,7 +246,15 @@ __global__ void db_from_aligned_kernel(const uint64_t *aligned, uint64_t *dbs, i
 void launch_ntt(const ModTab &M, uint64_t *polys, size_t count, bool inverse, cudaStream_t s,
                 bool pdl) {
   if (!count) return;
-  launch_kernel(pdl, ntt_kernel, dim3((unsigned)count), dim3(T), 0, s, M, polys, inverse ? 1 : 0);
+  launch_kernel(pdl, ntt_kernel, dim3((unsigned)count), dim3(T), 0, s, M, polys, inverse ? 1 : 0,
+                (size_t)0);
+}
+
+void launch_ntt_groups(const ModTab &M, uint64_t *polys, int count, int groups,
+                       size_t group_stride, bool inverse, cudaStream_t s, bool pdl) {
+  if (count <= 0 || groups <= 0) return;
+  launch_kernel(pdl, ntt_kernel, dim3((unsigned)count, (unsigned)groups), dim3(T), 0, s, M, polys,
+                inverse ? 1 : 0, group_stride);
 }
 
 void launch_query_prep(const uint64_t *leaves, size_t leaves_stride, uint4 *qs, size_t qs_stride,

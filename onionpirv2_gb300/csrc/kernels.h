@@ -75,6 +75,10 @@ inline void launch_kernel(bool pdl, void (*k)(P...), dim3 grid, dim3 block, size
 // (pdl: a programmatic launch after the previous kernel of the pipeline)
 void launch_ntt(const ModTab &M, uint64_t *polys, size_t count, bool inverse, cudaStream_t s,
                 bool pdl = false);
+// `count` consecutive polynomials in each of `groups` groups group_stride
+// words apart (one per query of a batch)
+void launch_ntt_groups(const ModTab &M, uint64_t *polys, int count, int groups,
+                       size_t group_stride, bool inverse, cudaStream_t s, bool pdl = false);
 
 // ---- launch forms of the tree stages
 // Every tree stage has a one-CTA form (a whole ciphertext per CTA), a
@@ -182,7 +186,10 @@ int launch_tc_scan(const uint16_t *dbl, const uint16_t *ql, uint64_t *out, size_
                    int n1, int n_rest, int batch, uint64_t q, uint64_t mu_lo, uint64_t mu_hi,
                    uint64_t r64, uint64_t r128, uint32_t *status, cudaStream_t s, int ring = -1);
 
-// ---- one folding level (other_dim_mux): res[b][j] += INTT(RGSW x (res[j+half]-res[j]))
+// ---- one folding level (other_dim_mux) on ciphertexts held in NTT form:
+// res[b][j] += RGSW x INTT(res[j+half] - res[j]) for j < half (the
+// difference goes back to coefficient form for its gadget digits; the sum
+// stays in NTT form)
 void launch_fold(uint64_t *res, size_t res_stride, const uint64_t *gsw, size_t gsw_stride,
                  int half, int batch, const ModTab &Mq, const Consts &C, cudaStream_t s,
                  bool pdl = false, const TreeForms *forms = nullptr);

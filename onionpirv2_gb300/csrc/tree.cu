@@ -235,29 +235,29 @@ __global__ void __launch_bounds__(T, 2) fold_kernel(uint64_t *res, size_t res_st
   const uint64_t q = C.q;
   uint64_t *xp = res + b * res_stride + (size_t)j * 2 * kN;
   const uint64_t *yp = res + b * res_stride + (size_t)(j + half) * 2 * kN;
+  // y - x, held in NTT form, back to coefficient form for its digits
+#pragma unroll 1
+  for (int poly = 0; poly < 2; ++poly) {
+    uint64_t d[8], xv[8];
+    ldg_slot8(yp + poly * kN, d);
+    ld_slot8(xp + poly * kN, xv);
 #pragma unroll
-  for (int i2 = 0; i2 < 16; ++i2) {
-    const int i = (i2 >> 3) * kN + strided_idx(tid, i2 & 7);
-    sd[i] = sub_mod(yp[i], xp[i], q);  // own slots only
+    for (int e = 0; e < 8; ++e) d[e] = sub_mod(d[e], xv[e], q);
+    ntt_inv(d, sa, sb, M);
+#pragma unroll
+    for (int e = 0; e < 8; ++e) sd[poly * kN + strided_idx(tid, e)] = d[e];  // own slots only
   }
   tw_wait();
   uint64_t out[2][8];
   ext_product_core(sd, gsw + b * gsw_stride, C.l, C.base_log2, sa, sb, s_fwd, M, out);
-  // polynomial 1 waits in shared memory (sd is no longer read) while
-  // polynomial 0 is transformed back
+  // x + RGSW (x) (y - x), staying in NTT form
 #pragma unroll
-  for (int e = 0; e < 8; ++e) sd[slot_idx(tid, e)] = out[1][e];
-#pragma unroll 1
   for (int poly = 0; poly < 2; ++poly) {
-    uint64_t r[8];
+    uint64_t xv[8];
+    ld_slot8(xp + poly * kN, xv);
 #pragma unroll
-    for (int e = 0; e < 8; ++e) r[e] = poly ? sd[slot_idx(tid, e)] : out[0][e];
-    ntt_inv(r, sa, sb, M);
-#pragma unroll
-    for (int e = 0; e < 8; ++e) {
-      const int i = poly * kN + strided_idx(tid, e);
-      xp[i] = add_mod(xp[i], r[e], q);
-    }
+    for (int e = 0; e < 8; ++e) xv[e] = add_mod(xv[e], out[poly][e], q);
+    stg_slot8(xp + poly * kN, xv);
   }
 }
 
@@ -548,20 +548,32 @@ __global__ void __cluster_dims__(kFoldCluster, 1, 1) __launch_bounds__(T)
   grid_dep_sync();
   const int sh = (l - 1 - r) * C.base_log2;
   const uint64_t mask = (1ULL << C.base_log2) - 1;
+  // CTAs 0 and 1: polynomial r of y - x, held in NTT form, back to
+  // coefficient form in `part` for every CTA of the cluster to decompose
+  if (r < 2) {
+    uint64_t d[8], xv[8];
+    ldg_slot8(yp + (size_t)r * kN, d);
+    ld_slot8(xp + (size_t)r * kN, xv);
+#pragma unroll
+    for (int e = 0; e < 8; ++e) d[e] = sub_mod(d[e], xv[e], q);
+    ntt_inv(d, sa, sb, M);
+#pragma unroll
+    for (int e = 0; e < 8; ++e) part[strided_idx(tid, e)] = d[e];
+  }
+  cluster.sync();
   U128 acc0[8], acc1[8];
 #pragma unroll
   for (int e = 0; e < 8; ++e) acc0[e] = acc1[e] = U128{0, 0};
 #pragma unroll
   for (int poly = 0; poly < 2; ++poly) {
+    const uint64_t *src = cluster.map_shared_rank(part, poly);
     uint64_t d[8];
 #pragma unroll
-    for (int e = 0; e < 8; ++e) {
-      const int i = poly * kN + strided_idx(tid, e);
-      d[e] = (sub_mod(yp[i], xp[i], q) >> sh) & mask;
-    }
+    for (int e = 0; e < 8; ++e) d[e] = (src[strided_idx(tid, e)] >> sh) & mask;
     if (poly == 0) tw_wait();
     digit_mac(d, rgsw + (size_t)(poly * l + r) * 2 * kN, sa, sb, s_fwd, M, acc0, acc1);
   }
+  cluster.sync();  // every CTA has read the differences before `part` is reused
 #pragma unroll
   for (int e = 0; e < 8; ++e) {
     const int si = slot_idx(tid, e);
@@ -570,14 +582,13 @@ __global__ void __cluster_dims__(kFoldCluster, 1, 1) __launch_bounds__(T)
   }
   cluster.sync();
   if (r < 2) {
-    uint64_t sum[8];
+    // x + RGSW (x) (y - x), staying in NTT form
+    uint64_t sum[8], xv[8];
     cluster_sum8<kFoldCluster>(cluster, part + (size_t)r * kN, q, sum);
-    ntt_inv(sum, sa, sb, M);
+    ld_slot8(xp + (size_t)r * kN, xv);
 #pragma unroll
-    for (int e = 0; e < 8; ++e) {
-      const int i = r * kN + strided_idx(tid, e);
-      xp[i] = add_mod(xp[i], sum[e], q);
-    }
+    for (int e = 0; e < 8; ++e) xv[e] = add_mod(xv[e], sum[e], q);
+    stg_slot8(xp + (size_t)r * kN, xv);
   }
   cluster.sync();
 }
@@ -607,13 +618,19 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(T, 2)
   const uint64_t *yp = res + b * res_stride + (size_t)(j + half) * 2 * kN;
   const uint64_t *rgsw = gsw + b * gsw_stride;
   const uint64_t mask = (1ULL << C.base_log2) - 1;
-  // polynomial a of y - x in `part` (each thread reads back only its own
-  // strided slots; the transforms' barriers order the last reads before the
-  // partial sums overwrite it)
+  // polynomial a of y - x, held in NTT form, back to coefficient form in
+  // `part` (each thread reads back only its own strided slots; the
+  // transforms' barriers order the last reads before the partial sums
+  // overwrite it)
+  {
+    uint64_t d[8], xv[8];
+    ldg_slot8(yp + (size_t)a * kN, d);
+    ld_slot8(xp + (size_t)a * kN, xv);
 #pragma unroll
-  for (int e = 0; e < 8; ++e) {
-    const int i = strided_idx(tid, e);
-    part[i] = sub_mod(yp[a * kN + i], xp[a * kN + i], q);
+    for (int e = 0; e < 8; ++e) d[e] = sub_mod(d[e], xv[e], q);
+    ntt_inv(d, sa, sb, M);
+#pragma unroll
+    for (int e = 0; e < 8; ++e) part[strided_idx(tid, e)] = d[e];
   }
   U128 acc0[8], acc1[8];
 #pragma unroll
@@ -634,14 +651,13 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(T, 2)
     part[kN + si] = barrett128(acc1[e], q, M.mu_lo, M.mu_hi);
   }
   cluster.sync();
-  uint64_t sum[8];
+  // x + RGSW (x) (y - x), staying in NTT form
+  uint64_t sum[8], xv[8];
   cluster_sum8<2>(cluster, part + (size_t)a * kN, q, sum);
-  ntt_inv(sum, sa, sb, M);
+  ld_slot8(xp + (size_t)a * kN, xv);
 #pragma unroll
-  for (int e = 0; e < 8; ++e) {
-    const int i = a * kN + strided_idx(tid, e);
-    xp[i] = add_mod(xp[i], sum[e], q);
-  }
+  for (int e = 0; e < 8; ++e) xv[e] = add_mod(xv[e], sum[e], q);
+  stg_slot8(xp + (size_t)a * kN, xv);
   cluster.sync();
 }
 
