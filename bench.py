@@ -1102,6 +1102,9 @@ def main():
                      "tc_ring": {"choice": tune["tc_ring_choice"],
                                  "ms": {f'{r["k_per_stage"]}x{r["stages"]}': round(r["ms"], 4)
                                         for r in tune["tc_rings"]}},
+                     "tc_limbs": {"choice_bits": tune["tc_limbs_choice"],
+                                  "ms": {f'{r["bits"]}bit': round(r["ms"], 4)
+                                         for r in tune["tc_limbs"]}},
                      "tree_forms": [{"stage": f["stage"], "count": f["count"], "form": f["form"],
                                      "ms": {k: round(v, 4) for k, v in f["ms"].items()}}
                                     for f in tune["forms"]]},

@@ -258,6 +258,9 @@ typedef struct opir_tune_report {
   uint32_t form_count[128]; /* work items: nodes / ciphertexts / pairs x queries */
   float form_ms[128][3];   /* one CTA, two CTAs, cluster per ciphertext */
   int32_t form_choice[128];
+  float tc_limbs_ms[2];    /* query limbs of 8 and 9 bits at the largest batch size (the
+                              limb split plus the tensor kernel); < 0: not measured */
+  int32_t tc_limbs_choice; /* 0: 8-bit, 1: 9-bit, -1: not tuned */
 } opir_tune_report;
 int opir_autotune(opir_ctx *ctx, uint32_t db_id, uint32_t max_batch, uint32_t reps,
                   opir_tune_report *report);
@@ -330,6 +333,15 @@ int opir_sync(opir_ctx *ctx);
  * bits in opir_last_error, and the next call on the context runs normally.
  * 0 turns it off.  Not for production use. */
 int opir_debug_withhold_scan_stage(opir_ctx *ctx, uint32_t polls);
+/* Test hook of the first dimension (the inside of evaluate_first_dim; no
+ * public reference counterpart): `batch` queries' first-dimension leaves
+ * given directly, leaves[batch][n1][2][N] in coefficient form, multiplied
+ * with the database on the engine this batch size uses (opir_set_batch_engine,
+ * the tuned table or the crossovers; OPIR_TC_LIMBS forces the tensor
+ * engine's query limb width); out[batch][n_rest][2][N] in coefficient form.
+ * Lets tests drive the products with operands no query expansion produces. */
+int opir_debug_first_dim(opir_ctx *ctx, uint32_t db_id, uint32_t batch, const uint64_t *leaves,
+                         uint64_t *out);
 
 /* ---- primitives (tests) ---- */
 /* Negacyclic NTT of `count` polynomials mod q (mod = 0) or p (mod = 1),

@@ -41,7 +41,7 @@ EXPORTS = (
     "opir_serve_start", "opir_serve_stop", "opir_submit", "opir_poll", "opir_wait",
     "opir_serve_stats_get", "opir_set_batch_engine", "opir_autotune", "opir_set_graphs",
     "opir_db_get_entry", "opir_pack_response", "opir_other_dim_mux",
-    "opir_debug_withhold_scan_stage", "opir_ctx_create_rns",
+    "opir_debug_withhold_scan_stage", "opir_debug_first_dim", "opir_ctx_create_rns",
 )
 
 ENGINES = {"auto": 0, "scan": 1, "imad": 2, "tensor": 3}
@@ -128,6 +128,8 @@ class OpirTuneReport(ctypes.Structure):
         ("form_count", ctypes.c_uint32 * 128),
         ("form_ms", (ctypes.c_float * 3) * 128),
         ("form_choice", ctypes.c_int32 * 128),
+        ("tc_limbs_ms", ctypes.c_float * 2),
+        ("tc_limbs_choice", ctypes.c_int32),
     ]
 
 
@@ -183,6 +185,7 @@ def load(path: str = LIB):
     L.opir_pack_response.argtypes = [_vp, _u64p, ctypes.c_uint32, _u8p]
     L.opir_other_dim_mux.argtypes = [_vp, _u64p, ctypes.c_uint64, _u64p]
     L.opir_debug_withhold_scan_stage.argtypes = [_vp, ctypes.c_uint32]
+    L.opir_debug_first_dim.argtypes = [_vp, ctypes.c_uint32, ctypes.c_uint32, _u64p, _u64p]
     L.opir_set_timing.argtypes = [_vp, ctypes.c_int]
     L.opir_set_graphs.argtypes = [_vp, ctypes.c_int]
     L.opir_db_get_entry.argtypes = [_vp, ctypes.c_uint32, ctypes.c_uint64, _u8p]

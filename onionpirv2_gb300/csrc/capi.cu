@@ -112,7 +112,8 @@ struct Db {
   // the engine per batch size (empty: the fixed crossovers)
   int scan_cfg = -1;
   tune::EngineTable engines;
-  int tc_ring = -1;  // tensor kernel ring shape (kTcRing*), -1: the default
+  int tc_ring = -1;   // tensor kernel ring shape (kTcRing*), -1: the default
+  int tc_limbs = -1;  // query limb width (kTcLimbs*), -1: the default per pass
   TreeForms forms;   // tuned launch form per tree-stage work count
   // the synchronous single-query pipeline as CUDA graphs: executables keyed
   // by everything their kernel parameters hold (client keys, buffers, tile
@@ -451,6 +452,57 @@ int resolve_keys(opir_ctx *ctx, uint64_t id, const Db &db, cudaStream_t s, Query
   return OPIR_OK;
 }
 
+// First dimension (evaluate_first_dim, server.cpp:124-175) of `batch`
+// queries' n1 leaves (coefficient form) into W.res[b][n_rest][2][N], in NTT
+// form: one pass over the database per batch (batched GEMM on the tensor or
+// integer engine) or per query (the streaming scan), as engine_for decides.
+int enqueue_first_dim(opir_ctx *ctx, Db &db, Workspace &W, const uint64_t *leaves,
+                      size_t leaves_stride, int batch, bool pdl_prep, const PipeEnv &E) {
+  cudaStream_t s = E.s;
+  const size_t CTW = 2 * (size_t)kN;
+  const size_t n1 = db.shape.fst_dim_sz, nr = db.shape.other_dim_sz;
+  const size_t qs_stride = (size_t)kN * n1;
+  const size_t res_stride = nr * CTW;
+  const int use = engine_for(ctx, db, batch);
+  const bool tensor = use == OPIR_ENGINE_TENSOR, batched = use == OPIR_ENGINE_IMAD;
+  if (tensor) {
+    if (!db.dbl_valid) {
+      CK(db.dbl.alloc(tc_db_limb_bytes((int)n1, (int)nr)), "alloc database limb plane");
+      launch_db_limbs(db.dbs.as<uint64_t>(), db.dbl.as<uint16_t>(), (int)n1, (int)nr, s);
+      ctx->launches++;
+      // built once; batches on other streams read it afterwards
+      CK(cudaStreamSynchronize(s), "database limb plane");
+      db.dbl_valid = true;
+    }
+    CK(W.ql.alloc(tc_query_limb_bytes((int)n1, batch)), "alloc query limbs");
+    launch_query_prep_plane(leaves, leaves_stride, W.qs.as<uint64_t>(), (int)n1, batch,
+                            ctx->Mq.tab, s, pdl_prep);
+    launch_tc_query_limbs(W.qs.as<uint64_t>(), W.ql.as<uint16_t>(), (int)n1, batch, s,
+                          db.tc_limbs);
+    ctx->launches += (batch + 31) / 32;
+    record(ctx, E, 6);
+    ctx->launches += launch_tc_scan(db.dbl.as<uint16_t>(), W.ql.as<uint16_t>(), W.res.as<uint64_t>(),
+                                    res_stride, (int)n1, (int)nr, batch, ctx->Mq.tab.q,
+                                    ctx->Mq.tab.mu_lo, ctx->Mq.tab.mu_hi, ctx->r64, ctx->r128,
+                                    E.status, s, db.tc_ring, db.tc_limbs) - 1;
+  } else if (batched) {
+    launch_query_prep_batched(leaves, leaves_stride, W.qs.as<uint4>(), (int)n1, batch,
+                              ctx->Mq.tab, s, pdl_prep);
+    record(ctx, E, 6);
+    launch_scan_batched(db.dbs.as<uint64_t>(), W.qs.as<uint4>(), W.res.as<uint64_t>(), res_stride,
+                        (int)n1, (int)nr, batch, ctx->C, ctx->Mq.tab.mu_lo, ctx->Mq.tab.mu_hi,
+                        E.status, s);
+  } else {
+    launch_query_prep(leaves, leaves_stride, W.qs.as<uint4>(), qs_stride, (int)n1, batch,
+                      ctx->Mq.tab, s, pdl_prep);
+    record(ctx, E, 6);
+    launch_scan(db.dbs.as<uint64_t>(), W.qs.as<uint4>(), qs_stride, W.res.as<uint64_t>(),
+                res_stride, (int)n1, (int)nr, batch, ctx->C, ctx->Mq.tab.mu_lo,
+                ctx->Mq.tab.mu_hi, E.status, s, db.scan_cfg);
+  }
+  return OPIR_OK;
+}
+
 // Enqueue the whole query pipeline for `batch` queries already on the device.
 int run_pipeline(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
                  const uint64_t *d_queries, uint64_t *d_resp, uint8_t *d_packed,
@@ -521,47 +573,10 @@ int run_pipeline(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
   }
   record(ctx, E, 2);
   // ---- first dimension
-  const size_t qs_stride = (size_t)kN * n1;
   const size_t res_stride = nr * CTW;
-  // a batch of queries shares one pass over the database (batched GEMM);
-  // a single query (or an unsupported shape) streams it once per query
-  const int use = engine_for(ctx, db, batch);
   const bool pdl_prep = (pdl & kPdlPrep) && (h > 0 || db.ndim > 1);  // a kernel precedes
-  const bool tensor = use == OPIR_ENGINE_TENSOR, batched = use == OPIR_ENGINE_IMAD;
-  if (tensor) {
-    if (!db.dbl_valid) {
-      CK(db.dbl.alloc(tc_db_limb_bytes((int)n1, (int)nr)), "alloc database limb plane");
-      launch_db_limbs(db.dbs.as<uint64_t>(), db.dbl.as<uint16_t>(), (int)n1, (int)nr, s);
-      ctx->launches++;
-      // built once; batches on other streams read it afterwards
-      CK(cudaStreamSynchronize(s), "database limb plane");
-      db.dbl_valid = true;
-    }
-    CK(W.ql.alloc(tc_query_limb_bytes((int)n1, batch)), "alloc query limbs");
-    launch_query_prep_plane(leaves, leaves_stride, W.qs.as<uint64_t>(), (int)n1, batch,
-                            ctx->Mq.tab, s, pdl_prep);
-    launch_tc_query_limbs(W.qs.as<uint64_t>(), W.ql.as<uint16_t>(), (int)n1, batch, s);
-    ctx->launches += (batch + 31) / 32;
-    record(ctx, E, 6);
-    ctx->launches += launch_tc_scan(db.dbl.as<uint16_t>(), W.ql.as<uint16_t>(), W.res.as<uint64_t>(),
-                                    res_stride, (int)n1, (int)nr, batch, ctx->Mq.tab.q,
-                                    ctx->Mq.tab.mu_lo, ctx->Mq.tab.mu_hi, ctx->r64, ctx->r128,
-                                    E.status, s, db.tc_ring) - 1;
-  } else if (batched) {
-    launch_query_prep_batched(leaves, leaves_stride, W.qs.as<uint4>(), (int)n1, batch,
-                              ctx->Mq.tab, s, pdl_prep);
-    record(ctx, E, 6);
-    launch_scan_batched(db.dbs.as<uint64_t>(), W.qs.as<uint4>(), W.res.as<uint64_t>(), res_stride,
-                        (int)n1, (int)nr, batch, ctx->C, ctx->Mq.tab.mu_lo, ctx->Mq.tab.mu_hi,
-                        E.status, s);
-  } else {
-    launch_query_prep(leaves, leaves_stride, W.qs.as<uint4>(), qs_stride, (int)n1, batch,
-                      ctx->Mq.tab, s, pdl_prep);
-    record(ctx, E, 6);
-    launch_scan(db.dbs.as<uint64_t>(), W.qs.as<uint4>(), qs_stride, W.res.as<uint64_t>(),
-                res_stride, (int)n1, (int)nr, batch, ctx->C, ctx->Mq.tab.mu_lo,
-                ctx->Mq.tab.mu_hi, E.status, s, db.scan_cfg);
-  }
+  rc = enqueue_first_dim(ctx, db, W, leaves, leaves_stride, batch, pdl_prep, E);
+  if (rc) return rc;
   record(ctx, E, 7);
   // the n_rest results stay in NTT form: the folds transform only their
   // differences back (evaluate_first_dim's inverse transforms, server.cpp:
@@ -1537,6 +1552,22 @@ int opir_autotune(opir_ctx *ctx, uint32_t db_id, uint32_t max_batch, uint32_t re
   if (R.tc_ring_ms[0] >= 0 || R.tc_ring_ms[1] >= 0)
     R.tc_ring_choice = tune::pick_over(R.tc_ring_ms, 2, n1 % 64 == 0 ? kTcRing64x4 : kTcRing32x8,
                                        tune::kTuneMargin);
+  // ---- tensor kernel: both query limb widths (limb split and product) at the
+  // largest batch size, on the chosen ring
+  R.tc_limbs_choice = -1;
+  for (int lw = 0; lw < 2; lw++) {
+    R.tc_limbs_ms[lw] = !(tc_ok && limbs && np) ? -1.0f : time_it([&] {
+      launch_tc_query_limbs(qs.as<uint64_t>(), ql.as<uint16_t>(), n1, bmax, s, lw);
+      launch_tc_scan(db->dbl.as<uint16_t>(), ql.as<uint16_t>(), res.as<uint64_t>(), res_stride, n1,
+                     nr, bmax, ctx->Mq.tab.q, ctx->Mq.tab.mu_lo, ctx->Mq.tab.mu_hi, ctx->r64,
+                     ctx->r128, status, s, R.tc_ring_choice, lw);
+      return true;
+    });
+  }
+  if (R.tc_limbs_ms[0] >= 0 && R.tc_limbs_ms[1] >= 0)
+    R.tc_limbs_choice = tune::pick_over(
+        R.tc_limbs_ms, 2, tc_query_limb_width(bmax, -1) == 9 ? kTcLimbs9 : kTcLimbs8,
+        tune::kTuneMargin);
   // ---- tree stages: every form of every distinct launch of this database's
   // pipeline, at one query and at the batch sizes up to one key chunk
   TreeForms tuned;
@@ -1556,6 +1587,7 @@ int opir_autotune(opir_ctx *ctx, uint32_t db_id, uint32_t max_batch, uint32_t re
   if (rc) return rc;
   db->scan_cfg = R.scan_choice;
   db->tc_ring = R.tc_ring_choice;
+  db->tc_limbs = R.tc_limbs_choice;
   db->forms = tuned;
   // captured single-query graphs hold the launch forms of their capture
   for (auto &gr : db->graphs)
@@ -1649,6 +1681,44 @@ int opir_debug_withhold_scan_stage(opir_ctx *ctx, uint32_t polls) {
   CK(cudaMemcpy(ctx->status.as<uint32_t>() + 1, &polls, sizeof polls, cudaMemcpyHostToDevice),
      "set scan test hook");
   return OPIR_OK;
+}
+
+// Test hook: the first dimension of `batch` queries whose n1 leaves the
+// caller gives directly (leaves[b][n1][2][N], coefficient form), on the
+// engine this batch size uses; out[b][n_rest][2][N] in coefficient form, as
+// make_query_trace's first_dim.  Tests drive the products with operands that
+// no query expansion produces: the limb-range extremes of the tensor engine.
+int opir_debug_first_dim(opir_ctx *ctx, uint32_t db_id, uint32_t batch, const uint64_t *leaves,
+                         uint64_t *out) {
+  RNS_UNSUPPORTED("the first-dimension test hook")
+  if (!ctx || !leaves || !out || !batch) return OPIR_ERR_ARG;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  if (serving_active(ctx)) return ctx->fail(OPIR_ERR_STATE, "serving is active");
+  Db *db = find_db(ctx, db_id);
+  if (!db) return ctx->fail(OPIR_ERR_UNKNOWN_DB, "unknown database %u", db_id);
+  if (!db->dbs.p) return ctx->fail(OPIR_ERR_STATE, "database has no data");
+  cudaSetDevice(ctx->device);
+  const size_t CTW = 2 * (size_t)kN;
+  const size_t n1 = db->shape.fst_dim_sz, nr = db->shape.other_dim_sz;
+  cudaStream_t s = ctx->stream;
+  Workspace &W = ctx->ws;
+  int rc = ensure_workspace(ctx, *db, (int)batch, W);
+  if (rc) return rc;
+  DevBuf dl;
+  CK(dl.alloc(batch * n1 * CTW * 8), "alloc leaves");
+  CK(cudaMemcpyAsync(dl.p, leaves, batch * n1 * CTW * 8, cudaMemcpyHostToDevice, s),
+     "upload leaves");
+  const PipeEnv E{&W, s, ctx->status.as<uint32_t>(), false, false};
+  rc = enqueue_first_dim(ctx, *db, W, dl.as<uint64_t>(), n1 * CTW, (int)batch, false, E);
+  if (rc) return rc;
+  launch_ntt_groups(ctx->Mq.tab, W.res.as<uint64_t>(), (int)(nr * 2), (int)batch, nr * CTW,
+                    true, s, false);
+  ctx->launches++;
+  CK(cudaGetLastError(), "first dimension launches");
+  CK(cudaMemcpyAsync(out, W.res.p, batch * nr * CTW * 8, cudaMemcpyDeviceToHost, s),
+     "download first dimension");
+  CK(cudaStreamSynchronize(s), "first dimension");
+  return check_status(ctx);
 }
 
 // save_resp_to_stream (server.cpp:581-633) for responses the caller holds:

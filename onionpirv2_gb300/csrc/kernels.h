@@ -164,7 +164,8 @@ void launch_query_prep_plane(const uint64_t *leaves, size_t leaves_stride, uint6
                              int n1, int batch, const ModTab &Mq, cudaStream_t s,
                              bool pdl = false);
 // Batched product on the tcgen05 tensor cores (tc_scan.cu): residues split
-// into 8-bit limbs held as bf16, exact fp32 accumulation in tensor memory.
+// into 8-bit (database) and 8- or 9-bit (query) limbs held as bf16, exact
+// fp32 accumulation in tensor memory.
 // The database needs its limb plane dbl (tc_db_limb_bytes, built by
 // launch_db_limbs from dbs).  launch_tc_query_limbs splits the query plane
 // of launch_query_prep_plane into ql (tc_query_limb_bytes(n1, batch) bytes);
@@ -175,8 +176,15 @@ size_t tc_db_limb_bytes(int n1, int n_rest);
 size_t tc_query_limb_bytes(int n1, int batch);
 cudaError_t init_tc_attributes();
 void launch_db_limbs(const uint64_t *dbs, uint16_t *dbl, int n1, int n_rest, cudaStream_t s);
+// limbs: the width of the query limbs, 8 bits (eight limbs, 64 limb products
+// per modular multiply-add) or 9 bits (seven limbs, 56); -1 takes the one
+// with fewer MMA columns for each pass.  launch_tc_query_limbs and
+// launch_tc_scan must be given the same choice.
+enum { kTcLimbs8 = 0, kTcLimbs9 = 1 };
 void launch_tc_query_limbs(const uint64_t *plane, uint16_t *ql, int n1, int batch,
-                           cudaStream_t s);
+                           cudaStream_t s, int limbs = -1);
+// the query limb width (8 or 9) that a pass of min(batch, 32) queries uses
+int tc_query_limb_width(int batch, int limbs);
 // ring: the shared-memory pipeline of the tensor kernel, 64 k x 4 stages
 // (n1 a multiple of 64) or 32 k x 8 stages; an invalid choice (or -1) takes
 // the first that fits.
@@ -184,7 +192,8 @@ enum { kTcRing64x4 = 0, kTcRing32x8 = 1 };
 bool tc_ring_valid(int ring, int n1);
 int launch_tc_scan(const uint16_t *dbl, const uint16_t *ql, uint64_t *out, size_t out_stride,
                    int n1, int n_rest, int batch, uint64_t q, uint64_t mu_lo, uint64_t mu_hi,
-                   uint64_t r64, uint64_t r128, uint32_t *status, cudaStream_t s, int ring = -1);
+                   uint64_t r64, uint64_t r128, uint32_t *status, cudaStream_t s, int ring = -1,
+                   int limbs = -1);
 
 // ---- one folding level (other_dim_mux) on ciphertexts held in NTT form:
 // res[b][j] += RGSW x INTT(res[j+half] - res[j]) for j < half (the

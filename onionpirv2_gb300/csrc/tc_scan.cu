@@ -4,34 +4,40 @@
 // (n_rest x n1) . (n1 x 2B) of 60-bit residues, accumulated exactly
 // (matrix.cpp:79-97, 220-235 compute it with 64x64->128-bit multiply-adds,
 // server.cpp:178-293 reduce the 128-bit sums mod q).  Here every residue is
-// split into eight balanced 8-bit limbs, v = sum_i d_i 2^(8i) with d_i in
-// [-128, 127] (the top limb in [0, 16]); each limb is exact in bf16, a limb
-// product is at most 2^14 in magnitude and a sum of 512 of them at most 2^23,
-// so the fp32 accumulation of tcgen05.mma kind::f16 is exact.  Longer first
-// dimensions run as segments of at most 512 k inside one launch: the MMAs of
-// each segment fill an accumulator of their own, the epilogue reduces it mod
-// q and keeps the running sum in registers, and a tile's result is stored
-// once, after its last segment.
+// split into balanced limbs that are exact in bf16: a database residue into
+// eight 8-bit limbs, v = sum_i d_i 2^(8i) with d_i in [-128, 127] (the top
+// limb in [0, 16]), a query residue into eight such limbs or into seven
+// 9-bit limbs, v = sum_j e_j 2^(9j) with e_j in [-256, 255] (the top limb in
+// [0, 64]).  A limb product is at most 2^15 in magnitude and a sum of 512 of
+// them at most 2^24, so the fp32 accumulation of tcgen05.mma kind::f16 is
+// exact.  Longer first dimensions run as segments of at most 512 k inside
+// one launch: the MMAs of each segment fill an accumulator of their own, the
+// epilogue reduces it mod q and keeps the running sum in registers, and a
+// tile's result is stored once, after its last segment.
 //
 // MMA shape per tile: M = 16 database rows x 8 limbs = 128 (TMEM lanes),
-// N = 2B query polynomials x 8 limbs <= 512 (TMEM columns, two MMAs of <= 256),
-// K = n1.  Cell (row r, limb i ; query poly b', limb j) holds
-// x_ij = sum_k d_i(A[r,k]) d_j(Q[k,b']); the result is
-// sum_s Y_s 2^(8s), Y_s = sum_{i+j=s} x_ij.  The epilogue gathers the
-// anti-diagonal sums Y_s across the 8 lanes of a row with one skewed
-// shuffle pass, rebuilds the exact (<= 2^130) integer from them and reduces
-// it mod q -- the same value the 128-bit accumulation of the reference
-// reduces, without its wrap-around (the sum is exact here).
+// N = 2B query polynomials x QL limbs (QL = 8 or 7; two MMAs of <= 256
+// columns), K = n1.  Cell (row r, limb i ; query poly b', limb j) holds
+// x_ij = sum_k d_i(A[r,k]) e_j(Q[k,b']); the result is
+// sum_s Y_s 2^(8s), Y_s = sum_{i+j=s} x_ij w^j, with w = 1 for 8-bit query
+// limbs (weight 2^(8i+8j)) and w = 2 for 9-bit ones (2^(8i+9j) =
+// 2^(8(i+j)) 2^j).  The epilogue gathers the anti-diagonal sums Y_s across
+// the 8 lanes of a row with one skewed shuffle pass, rebuilds the exact
+// (<= 2^130) integer from them and reduces it mod q -- the same value the
+// 128-bit accumulation of the reference reduces, without its wrap-around
+// (the sum is exact here).  Seven query limbs do 56 limb products per
+// modular multiply-add instead of 64; the row side keeps eight limbs because
+// a tile's 128 TMEM lanes must hold whole rows of limbs.
 //
 // Data layout in HBM (bf16 limbs, "core matrices" of 8 rows x 8 k):
 //   database  dbl[c][rb][k/8][r%16][i][k%8]      (rb = r / 16)
 //   queries   ql [c][h][k/8][b'][j][k%8]         (b' = 2 b + poly - 32 h)
-// (h: column half of at most 32 query polynomials = 256 TMEM columns), so the
-// slice of a pipeline stage (32 or 64 k) of either operand is contiguous and
-// lands in shared memory in the K-major, no-swizzle canonical layout that the
-// tcgen05 shared-memory descriptors below describe (leading byte offset =
-// stride between core matrices along k, stride byte offset = 128 between
-// 8-row groups).
+// (h: column half of at most 32 query polynomials, <= 256 TMEM columns), so
+// the slice of a pipeline stage (32 or 64 k) of either operand is contiguous
+// and lands in shared memory in the K-major, no-swizzle canonical layout
+// that the tcgen05 shared-memory descriptors below describe (leading byte
+// offset = stride between core matrices along k, stride byte offset = 128
+// between 8-row groups).
 #include <cuda_bf16.h>
 
 #include <cstdlib>
@@ -74,12 +80,14 @@ int g_tc_ring = -1;                 // OPIR_TC_RING: force a ring shape (tests, 
 
 struct TcGeom {
   int n1, n_rest, batch;      // batch: queries of the pass
-  int nh, nbh;                // column halves, query polynomials per half (multiple of 8)
+  int nh, nbh;                // column halves, query polynomials per half (multiple of 8;
+                              // of 16 with 7 query limbs, so that N is a multiple of 16)
+  int ql;                     // limbs per query residue: 8 (8-bit) or 7 (9-bit)
   int n_rb;                   // row tiles
   int nseg;                   // k segments of at most kTcMaxSegment
   long long units;            // N * n_rb * nh tiles
   uint32_t b_bytes;           // query bytes per stage
-  uint32_t idesc;             // instruction descriptor (M = 128, N = 8 nbh)
+  uint32_t idesc;             // instruction descriptor (M = 128, N = ql nbh)
 };
 
 // pipeline stages (of KC k) in segment s
@@ -128,6 +136,21 @@ __device__ __forceinline__ void tmem_ld32(uint32_t addr, uint32_t (&r)[32]) {
       : "r"(addr));
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
+// 8 columns; the caller waits (tmem_ld_wait) before it reads r
+__device__ __forceinline__ void tmem_ld8(uint32_t addr, uint32_t *r) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+                 "=r"(r[6]), "=r"(r[7])
+               : "r"(addr));
+}
+// wait for the loads issued so far; the empty asm per register keeps every
+// read of r after the wait
+template <int NR>
+__device__ __forceinline__ void tmem_ld_wait(uint32_t (&r)[NR]) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < NR; ++i) asm volatile("" : "+r"(r[i]));
+}
 
 // sum_s y_s 2^(8s) (exact, >= 0 and < 2^132) mod q
 __device__ __forceinline__ uint64_t tc_combine(const int (&y)[16], uint64_t q, uint64_t mu_lo,
@@ -152,7 +175,7 @@ __device__ __forceinline__ uint64_t tc_combine(const int (&y)[16], uint64_t q, u
   return barrett128(acc, q, mu_lo, mu_hi);
 }
 
-template <int KC, int STAGES>
+template <int KC, int STAGES, int QL>
 __global__ void __launch_bounds__(kTcThreads, 1)
     tc_scan_kernel(const uint16_t *__restrict__ dbl, const uint16_t *__restrict__ ql, uint64_t *out,
                    size_t out_stride, int b_base, TcGeom G, uint64_t q, uint64_t mu_lo,
@@ -205,7 +228,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         const long long c = u / per_c, rem = u % per_c;
         const long long rb = rem / G.nh, hf = rem % G.nh;
         const uint16_t *a_src = dbl + (size_t)(c * G.n_rb + rb) * kblk * (kTcRows * 64);
-        const uint16_t *b_src = ql + (size_t)(c * G.nh + hf) * kblk * G.nbh * 64;
+        const uint16_t *b_src = ql + (size_t)(c * G.nh + hf) * kblk * G.nbh * (QL * 8);
         for (int kc = 0; kc < G.n1 / KC; ++kc, ++it) {
           const int s = (int)(it % STAGES);
           const long long round = it / STAGES;
@@ -217,7 +240,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           unsigned char *st = smem + (size_t)s * kTcStageBytes;
           mbar_arrive_expect_tx(&full[s], kTcABytes + G.b_bytes);
           bulk_g2s(st, a_src + (size_t)kc * kTcKB * (kTcRows * 64), kTcABytes, &full[s]);
-          bulk_g2s(st + kTcABytes, b_src + (size_t)kc * kTcKB * G.nbh * 64, G.b_bytes, &full[s]);
+          bulk_g2s(st + kTcABytes, b_src + (size_t)kc * kTcKB * G.nbh * (QL * 8), G.b_bytes,
+                   &full[s]);
         }
       }
       // never leave the CTA with copies still landing in its shared memory
@@ -231,7 +255,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   } else if (warp == kTcMma) {
     // ------------------------------ MMA issue ------------------------------
     if (lane == 0) {
-      const uint32_t lbo_a = kTcRows * 128, lbo_b = (uint32_t)G.nbh * 128;
+      const uint32_t lbo_a = kTcRows * 128, lbo_b = (uint32_t)G.nbh * (QL * 16);
       long long it = 0, j = 0;  // j: accumulators filled, one per (tile, segment)
       bool ok = true;
       for (long long u = blockIdx.x; u < G.units && ok; u += gridDim.x) {
@@ -303,28 +327,56 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         for (int gi = 0; gi < 2; ++gi) {
           const int grp = part + 2 * gi;
           if (grp >= groups) break;
+          if constexpr (QL == 8) {
 #pragma unroll
-          for (int hc = 0; hc < 2; ++hc) {
-            uint32_t r[32];
-            tmem_ld32(acc_addr + (uint32_t)((grp * 2 + hc) * 32), r);
+            for (int hc = 0; hc < 2; ++hc) {
+              uint32_t r[32];
+              tmem_ld32(acc_addr + (uint32_t)((grp * 2 + hc) * 32), r);
 #pragma unroll
-            for (int bl = 0; bl < 4; ++bl) {
-              int x[8];
+              for (int bl = 0; bl < 4; ++bl) {
+                int x[8];
 #pragma unroll
-              for (int d = 0; d < 8; ++d) x[d] = __float2int_rn(__uint_as_float(r[bl * 8 + d]));
-              // skewed exchange: lane t8 collects Y_t8 and Y_(t8+8) of its row
+                for (int d = 0; d < 8; ++d) x[d] = __float2int_rn(__uint_as_float(r[bl * 8 + d]));
+                // skewed exchange: lane t8 collects Y_t8 and Y_(t8+8) of its row
+                int ylo = x[0], yhi = 0;
+#pragma unroll
+                for (int d = 1; d < 8; ++d) {
+                  const int v = __shfl_sync(0xffffffffu, x[d], (lane & ~7) | ((lane - d) & 7));
+                  if (d <= t8)
+                    ylo += v;
+                  else
+                    yhi += v;
+                }
+                int *yb = yw + (hc * 4 + bl) * 20;
+                yb[t8] = ylo;
+                yb[t8 + 8] = yhi;
+              }
+            }
+          } else {
+            // 8 polynomials x 7 limbs = 56 columns from column 56 grp
+            uint32_t r[56];
+#pragma unroll
+            for (int m = 0; m < 7; ++m) tmem_ld8(acc_addr + (uint32_t)(grp * 56 + m * 8), r + m * 8);
+            tmem_ld_wait(r);
+#pragma unroll
+            for (int bl = 0; bl < 8; ++bl) {
+              // x_ij 2^j: |x_ij| <= 2^24, so |Y_s| <= 127 * 2^24 < 2^31
+              int x[7];
+#pragma unroll
+              for (int d = 0; d < 7; ++d)
+                x[d] = __float2int_rn(__uint_as_float(r[bl * 7 + d])) * (1 << d);
               int ylo = x[0], yhi = 0;
 #pragma unroll
-              for (int d = 1; d < 8; ++d) {
+              for (int d = 1; d < 7; ++d) {
                 const int v = __shfl_sync(0xffffffffu, x[d], (lane & ~7) | ((lane - d) & 7));
                 if (d <= t8)
                   ylo += v;
                 else
                   yhi += v;
               }
-              int *yb = yw + (hc * 4 + bl) * 20;
+              int *yb = yw + bl * 20;
               yb[t8] = ylo;
-              yb[t8 + 8] = yhi;
+              yb[t8 + 8] = yhi;  // Y_14 = Y_15 = 0
             }
           }
           __syncwarp();
@@ -385,6 +437,28 @@ __device__ __forceinline__ void limbs8(uint64_t v, uint16_t (&d)[8]) {
   }
 }
 
+// balanced 9-bit limbs of a residue < 2^60 (the top one in [0, 64]), as bf16
+// bit patterns; every |limb| <= 256 is exact in bf16
+__device__ __forceinline__ void limbs9(uint64_t v, uint16_t (&d)[7]) {
+  int carry = 0;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    int x = (int)(v & 511u) + carry;
+    v >>= 9;
+    carry = x >= 256;
+    x -= carry << 9;
+    d[i] = __bfloat16_as_ushort(__float2bfloat16_rn((float)x));
+  }
+  d[6] = __bfloat16_as_ushort(__float2bfloat16_rn((float)((int)v + carry)));
+}
+template <int QL>
+__device__ __forceinline__ void query_limbs(uint64_t v, uint16_t (&d)[QL]) {
+  if constexpr (QL == 8)
+    limbs8(v, d);
+  else
+    limbs9(v, d);
+}
+
 // one thread: 8 consecutive k of one (slot, row) -> one 128-byte core matrix
 __global__ void db_limb_kernel(const uint64_t *__restrict__ dbs, uint16_t *__restrict__ dbl,
                                int n1, int n_rest) {
@@ -417,13 +491,15 @@ __global__ void db_limb_kernel(const uint64_t *__restrict__ dbs, uint16_t *__res
 // one thread: 8 consecutive k of one (slot, query polynomial) of the pass,
 // from plane[b][k][poly][c] (consecutive threads read consecutive slots) to
 // ql[c][h][k/8][b' - nbh h][j][k%8].  A warp covers 8 slots x 4 query
-// polynomials: its output is 8 runs of 512 bytes, which it writes through a
-// 4 KB shared-memory transpose so that every store instruction fills one run.
+// polynomials: its output is 8 runs of QL x 64 bytes, which it writes
+// through a shared-memory transpose so that every store instruction fills
+// one run.
+template <int QL>
 __global__ void __launch_bounds__(256) query_limb_kernel(const uint64_t *__restrict__ plane,
                                                          uint16_t *__restrict__ ql, int n1,
                                                          int b_base, int nh, int nbh,
                                                          int pass_batch) {
-  __shared__ uint4 stage[8][8 * 4 * 8];  // [warp][slot][polynomial][limb]
+  __shared__ uint4 stage[8][8 * 4 * QL];  // [warp][slot][polynomial][limb]
   const int kblk = n1 / 8;
   const long long total = (long long)kN * nh * kblk * nbh;  // a multiple of 32
   uint4 *st = stage[threadIdx.x >> 5];
@@ -441,23 +517,25 @@ __global__ void __launch_bounds__(256) query_limb_kernel(const uint64_t *__restr
     const int hf = (int)(rest / kblk);
     const int bq = hf * kTcHalfNB + bl;
     const int b = bq >> 1;
-    uint16_t d[8][8];
+    uint16_t d[8][QL];
     const uint64_t *src =
         plane + (((size_t)(b_base + b) * n1 + kb * 8) * 2 + (bq & 1)) * kN + c;
 #pragma unroll
-    for (int kk = 0; kk < 8; ++kk) limbs8(b < pass_batch ? src[(size_t)kk * 2 * kN] : 0, d[kk]);
+    for (int kk = 0; kk < 8; ++kk)
+      query_limbs<QL>(b < pass_batch ? src[(size_t)kk * 2 * kN] : 0, d[kk]);
     __syncwarp();  // the previous iteration's reads of the staging buffer are done
 #pragma unroll
-    for (int i = 0; i < 8; ++i)
-      st[((lane & 7) * 4 + (lane >> 3)) * 8 + i] =
+    for (int i = 0; i < QL; ++i)
+      st[((lane & 7) * 4 + (lane >> 3)) * QL + i] =
           make_uint4(d[0][i] | (uint32_t)d[1][i] << 16, d[2][i] | (uint32_t)d[3][i] << 16,
                      d[4][i] | (uint32_t)d[5][i] << 16, d[6][i] | (uint32_t)d[7][i] << 16);
     __syncwarp();
 #pragma unroll
     for (int cs = 0; cs < 8; ++cs) {
       uint4 *dst = reinterpret_cast<uint4 *>(
-          ql + ((((size_t)(c0 + cs) * nh + hf) * kblk + kb) * nbh + bl0) * 64);
-      dst[lane] = st[cs * 32 + lane];  // polynomial bl0 + lane / 8, limb lane % 8
+          ql + ((((size_t)(c0 + cs) * nh + hf) * kblk + kb) * nbh + bl0) * (QL * 8));
+      // polynomial bl0 + lane / QL, limb lane % QL
+      if (lane < 4 * QL) dst[lane] = st[cs * 4 * QL + lane];
     }
   }
 }
@@ -486,49 +564,85 @@ bool tc_scan_supported(int n1, int n_rest) {
 
 size_t tc_db_limb_bytes(int n1, int n_rest) { return (size_t)kN * n1 * n_rest * 16; }
 namespace {
-// Geometry of the pass of `pb` queries starting at query b0.
-TcGeom pass_geom(int n1, int n_rest, int pb) {
-  // 8 query polynomials per epilogue group; two 32-polynomial halves above 16 queries
-  const int padded = pb > kTcHalfNB / 2 ? kTcMaxNB / 2 : (pb + 3) / 4 * 4;
+int g_tc_limbs = -1;  // OPIR_TC_LIMBS: force the query limb width (tests, sweeps)
+
+// query polynomials per column half of a pass of pb queries with ql limbs:
+// 8-polynomial epilogue groups, N = ql nbh a multiple of 16, two
+// 32-polynomial halves above 16 queries
+int pass_nbh(int pb, int ql, int *nh) {
+  const int gran = ql == 7 ? 8 : 4;
+  const int padded = pb > kTcHalfNB / 2 ? kTcMaxNB / 2 : (pb + gran - 1) / gran * gran;
+  *nh = padded > kTcHalfNB / 2 ? 2 : 1;
+  return 2 * padded / *nh;
+}
+// limbs per query residue of a pass: the forced or requested width, else the
+// one with fewer MMA columns (ties: 9-bit)
+int pass_ql(int pb, int limbs) {
+  if (g_tc_limbs >= 0) limbs = g_tc_limbs;
+  if (limbs == kTcLimbs8) return 8;
+  if (limbs == kTcLimbs9) return 7;
+  int h8, h9;
+  const int n8 = pass_nbh(pb, 8, &h8) * 8 * h8, n9 = pass_nbh(pb, 7, &h9) * 7 * h9;
+  return n9 <= n8 ? 7 : 8;
+}
+// Geometry of the pass of `pb` queries with ql limbs per query residue.
+TcGeom pass_geom(int n1, int n_rest, int pb, int ql) {
   TcGeom G;
   G.n1 = n1;
   G.n_rest = n_rest;
   G.batch = pb;
-  G.nh = padded > kTcHalfNB / 2 ? 2 : 1;
-  G.nbh = 2 * padded / G.nh;
+  G.ql = ql;
+  G.nbh = pass_nbh(pb, ql, &G.nh);
   G.n_rb = n_rest / kTcRows;
   G.units = (long long)kN * G.n_rb * G.nh;
   G.nseg = (n1 + kTcMaxSegment - 1) / kTcMaxSegment;
   G.b_bytes = 0;  // per stage: set by the launcher for its stage size
-  G.idesc = make_idesc(G.nbh * 8);
+  G.idesc = make_idesc(G.nbh * ql);
   return G;
 }
 // query limbs of one pass (elements); passes follow each other in ql
-size_t pass_limb_elems(int n1, int pb) {
-  const TcGeom G = pass_geom(n1, kTcRows, pb);
-  return (size_t)kN * G.nh * (n1 / 8) * G.nbh * 64;
+size_t pass_limb_elems(int n1, int pb, int ql) {
+  const TcGeom G = pass_geom(n1, kTcRows, pb, ql);
+  return (size_t)kN * G.nh * (n1 / 8) * G.nbh * ql * 8;
 }
 }  // namespace
 
 size_t tc_query_limb_bytes(int n1, int batch) {
-  size_t e = 0;
-  for (int b0 = 0; b0 < batch; b0 += kTcMaxNB / 2)
-    e += pass_limb_elems(n1, batch - b0 < kTcMaxNB / 2 ? batch - b0 : kTcMaxNB / 2);
-  return e * sizeof(uint16_t);
+  size_t e8 = 0, e9 = 0;
+  for (int b0 = 0; b0 < batch; b0 += kTcMaxNB / 2) {
+    const int pb = batch - b0 < kTcMaxNB / 2 ? batch - b0 : kTcMaxNB / 2;
+    e8 += pass_limb_elems(n1, pb, 8);
+    e9 += pass_limb_elems(n1, pb, 7);
+  }
+  return (e8 > e9 ? e8 : e9) * sizeof(uint16_t);
 }
+
+int tc_query_limb_width(int batch, int limbs) {
+  return pass_ql(batch < kTcMaxNB / 2 ? batch : kTcMaxNB / 2, limbs) == 7 ? 9 : 8;
+}
+
+namespace {
+template <int KC, int STAGES, int QL>
+cudaError_t set_tc_smem() {
+  return cudaFuncSetAttribute(tc_scan_kernel<KC, STAGES, QL>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)tc_smem<KC, STAGES>());
+}
+}  // namespace
 
 cudaError_t init_tc_attributes() {
   g_tc_ring = -1;
   if (const char *v = getenv("OPIR_TC_RING")) g_tc_ring = atoi(v);
+  g_tc_limbs = -1;
+  if (const char *v = getenv("OPIR_TC_LIMBS")) g_tc_limbs = atoi(v);
   int dev;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&g_tc_sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaError_t e = cudaFuncSetAttribute(tc_scan_kernel<64, 4>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)tc_smem<64, 4>());
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(tc_scan_kernel<32, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)tc_smem<32, 8>());
+  cudaError_t e = set_tc_smem<64, 4, 8>();
+  if (e == cudaSuccess) e = set_tc_smem<32, 8, 8>();
+  if (e == cudaSuccess) e = set_tc_smem<64, 4, 7>();
+  if (e == cudaSuccess) e = set_tc_smem<32, 8, 7>();
+  return e;
 }
 
 void launch_db_limbs(const uint64_t *dbs, uint16_t *dbl, int n1, int n_rest, cudaStream_t s) {
@@ -538,24 +652,42 @@ void launch_db_limbs(const uint64_t *dbs, uint16_t *dbl, int n1, int n_rest, cud
 }
 
 void launch_tc_query_limbs(const uint64_t *plane, uint16_t *ql, int n1, int batch,
-                           cudaStream_t s) {
+                           cudaStream_t s, int limbs) {
   size_t off = 0;
   for (int b0 = 0; b0 < batch; b0 += kTcMaxNB / 2) {
     const int pb = batch - b0 < kTcMaxNB / 2 ? batch - b0 : kTcMaxNB / 2;
-    const TcGeom G = pass_geom(n1, kTcRows, pb);
+    const int qlc = pass_ql(pb, limbs);
+    const TcGeom G = pass_geom(n1, kTcRows, pb, qlc);
     const long long qtotal = (long long)kN * G.nh * (n1 / 8) * G.nbh;
     const long long qblocks = (qtotal + 255) / 256;
-    query_limb_kernel<<<(unsigned)(qblocks < 65536 ? qblocks : 65536), 256, 0, s>>>(
-        plane, ql + off, n1, b0, G.nh, G.nbh, pb);
-    off += pass_limb_elems(n1, pb);
+    const unsigned grid = (unsigned)(qblocks < 65536 ? qblocks : 65536);
+    if (qlc == 7)
+      query_limb_kernel<7><<<grid, 256, 0, s>>>(plane, ql + off, n1, b0, G.nh, G.nbh, pb);
+    else
+      query_limb_kernel<8><<<grid, 256, 0, s>>>(plane, ql + off, n1, b0, G.nh, G.nbh, pb);
+    off += pass_limb_elems(n1, pb, qlc);
   }
 }
 
 bool tc_ring_valid(int ring, int n1) { return ring == kTcRing32x8 || (ring == kTcRing64x4 && n1 % 64 == 0); }
 
+namespace {
+template <int KC, int STAGES, int QL>
+void launch_tc_pass(TcGeom G, const uint16_t *dbl, const uint16_t *ql, uint64_t *out,
+                    size_t out_stride, int b0, uint64_t q, uint64_t mu_lo, uint64_t mu_hi,
+                    uint64_t r64, uint64_t r128, uint32_t *status, cudaStream_t s) {
+  const int sms = g_tc_sms > 0 ? g_tc_sms : 152;
+  const long long grid = G.units < sms ? G.units : sms;
+  G.b_bytes = (uint32_t)(KC / 8 * G.nbh * QL * 16);
+  tc_scan_kernel<KC, STAGES, QL><<<(unsigned)grid, kTcThreads, tc_smem<KC, STAGES>(), s>>>(
+      dbl, ql, out, out_stride, b0, G, q, mu_lo, mu_hi, r64, r128, status);
+}
+}  // namespace
+
 int launch_tc_scan(const uint16_t *dbl, const uint16_t *ql, uint64_t *out, size_t out_stride,
                    int n1, int n_rest, int batch, uint64_t q, uint64_t mu_lo, uint64_t mu_hi,
-                   uint64_t r64, uint64_t r128, uint32_t *status, cudaStream_t s, int ring) {
+                   uint64_t r64, uint64_t r128, uint32_t *status, cudaStream_t s, int ring,
+                   int limbs) {
   if (g_tc_ring >= 0) ring = g_tc_ring;
   // every segment length is a multiple of 64 when n1 is (segments of 512)
   if (!tc_ring_valid(ring, n1)) ring = n1 % 64 == 0 ? kTcRing64x4 : kTcRing32x8;
@@ -563,20 +695,26 @@ int launch_tc_scan(const uint16_t *dbl, const uint16_t *ql, uint64_t *out, size_
   size_t off = 0;
   for (int b0 = 0; b0 < batch; b0 += kTcMaxNB / 2) {
     const int pb = batch - b0 < kTcMaxNB / 2 ? batch - b0 : kTcMaxNB / 2;
-    TcGeom G = pass_geom(n1, n_rest, pb);
-    const int sms = g_tc_sms > 0 ? g_tc_sms : 152;
-    const long long grid = G.units < sms ? G.units : sms;
+    const int qlc = pass_ql(pb, limbs);
+    const TcGeom G = pass_geom(n1, n_rest, pb, qlc);
+    const uint16_t *qp = ql + off;
     if (ring == kTcRing64x4) {
-      G.b_bytes = (uint32_t)(64 / 8 * G.nbh * 128);
-      tc_scan_kernel<64, 4><<<(unsigned)grid, kTcThreads, tc_smem<64, 4>(), s>>>(
-          dbl, ql + off, out, out_stride, b0, G, q, mu_lo, mu_hi, r64, r128, status);
+      if (qlc == 7)
+        launch_tc_pass<64, 4, 7>(G, dbl, qp, out, out_stride, b0, q, mu_lo, mu_hi, r64, r128,
+                                 status, s);
+      else
+        launch_tc_pass<64, 4, 8>(G, dbl, qp, out, out_stride, b0, q, mu_lo, mu_hi, r64, r128,
+                                 status, s);
     } else {
-      G.b_bytes = (uint32_t)(32 / 8 * G.nbh * 128);
-      tc_scan_kernel<32, 8><<<(unsigned)grid, kTcThreads, tc_smem<32, 8>(), s>>>(
-          dbl, ql + off, out, out_stride, b0, G, q, mu_lo, mu_hi, r64, r128, status);
+      if (qlc == 7)
+        launch_tc_pass<32, 8, 7>(G, dbl, qp, out, out_stride, b0, q, mu_lo, mu_hi, r64, r128,
+                                 status, s);
+      else
+        launch_tc_pass<32, 8, 8>(G, dbl, qp, out, out_stride, b0, q, mu_lo, mu_hi, r64, r128,
+                                 status, s);
     }
     launches++;
-    off += pass_limb_elems(n1, pb);
+    off += pass_limb_elems(n1, pb, qlc);
   }
   return launches;
 }

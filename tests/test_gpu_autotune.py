@@ -46,6 +46,9 @@ def test_autotune_choices_and_parity(gpu_lib, oracle_lib, shape):
     rings = [r["ms"] for r in rep["tc_rings"]]
     if any(m >= 0 for m in rings):
         assert near_best(rings, rep["tc_ring_choice"])
+    widths = [r["ms"] for r in rep["tc_limbs"]]
+    if all(m >= 0 for m in widths):
+        assert near_best(widths, rep["tc_limbs_choice"] - 8)
     assert rep["forms"] and all(f["form"] is not None for f in rep["forms"])
     names = ("one_cta", "two_cta", "cluster")
     for f in rep["forms"]:
@@ -84,15 +87,18 @@ def test_autotune_refused_while_serving(gpu_lib):
 
 
 @pytest.mark.parametrize("shape", [(4096, 256), (1 << 14, 1024)])
-@pytest.mark.parametrize("ring,threshold,pair", [(0, 100000, 0), (1, 0, 100000), (0, 0, 0)])
+@pytest.mark.parametrize("ring,limbs,threshold,pair", [(0, 0, 100000, 0), (1, 1, 0, 100000),
+                                                       (0, 1, 0, 0), (1, 0, 0, 0)])
 def test_every_tuning_candidate_is_bit_exact(oracle_lib, gpu_lib, monkeypatch, shape, ring,
-                                             threshold, pair):
+                                             limbs, threshold, pair):
     """Every candidate the autotuner chooses among gives the oracle's bits:
-    both tensor-kernel rings (64 k x 4 stages, 32 k x 8 stages) and every
-    tree-stage form (all clusters, all two-CTA forms, all one-CTA forms),
-    on two database shapes, single queries and a batch on the tensor engine."""
+    both tensor-kernel rings (64 k x 4 stages, 32 k x 8 stages) with both
+    query limb widths (8 and 9 bits) and every tree-stage form (all
+    clusters, all two-CTA forms, all one-CTA forms), on two database shapes,
+    single queries and a batch on the tensor engine."""
     from onionpirv2_gb300 import PirParams, PirServer
     monkeypatch.setenv("OPIR_TC_RING", str(ring))
+    monkeypatch.setenv("OPIR_TC_LIMBS", str(limbs))
     monkeypatch.setenv("OPIR_CLUSTER_THRESHOLD", str(threshold))
     monkeypatch.setenv("OPIR_PAIR_THRESHOLD", str(pair))
     monkeypatch.setenv("OPIR_EXPAND_PAIR_THRESHOLD", str(pair))
