@@ -1105,6 +1105,8 @@ def main():
                      "tc_limbs": {"choice_bits": tune["tc_limbs_choice"],
                                   "ms": {f'{r["bits"]}bit': round(r["ms"], 4)
                                          for r in tune["tc_limbs"]}},
+                     "tc_form": {"choice": tune["tc_form_choice"],
+                                 "ms": {r["form"]: round(r["ms"], 4) for r in tune["tc_forms"]}},
                      "tree_forms": [{"stage": f["stage"], "count": f["count"], "form": f["form"],
                                      "ms": {k: round(v, 4) for k, v in f["ms"].items()}}
                                     for f in tune["forms"]]},

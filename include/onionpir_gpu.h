@@ -261,6 +261,9 @@ typedef struct opir_tune_report {
   float tc_limbs_ms[2];    /* query limbs of 8 and 9 bits at the largest batch size (the
                               limb split plus the tensor kernel); < 0: not measured */
   int32_t tc_limbs_choice; /* 0: 8-bit, 1: 9-bit, -1: not tuned */
+  float tc_pair_ms[2];     /* one CTA per tile, CTA pairs (M = 256, cta_group::2) at the
+                              largest batch size; < 0: not measured or not applicable */
+  int32_t tc_pair_choice;  /* 0: one CTA, 1: pairs, -1: not tuned */
 } opir_tune_report;
 int opir_autotune(opir_ctx *ctx, uint32_t db_id, uint32_t max_batch, uint32_t reps,
                   opir_tune_report *report);

@@ -130,6 +130,8 @@ class OpirTuneReport(ctypes.Structure):
         ("form_choice", ctypes.c_int32 * 128),
         ("tc_limbs_ms", ctypes.c_float * 2),
         ("tc_limbs_choice", ctypes.c_int32),
+        ("tc_pair_ms", ctypes.c_float * 2),
+        ("tc_pair_choice", ctypes.c_int32),
     ]
 
 

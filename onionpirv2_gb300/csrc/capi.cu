@@ -114,6 +114,7 @@ struct Db {
   tune::EngineTable engines;
   int tc_ring = -1;   // tensor kernel ring shape (kTcRing*), -1: the default
   int tc_limbs = -1;  // query limb width (kTcLimbs*), -1: the default per pass
+  int tc_pair = -1;   // tensor kernel form: 0 one CTA per tile, 1 CTA pairs, -1: the default
   TreeForms forms;   // tuned launch form per tree-stage work count
   // the synchronous single-query pipeline as CUDA graphs: executables keyed
   // by everything their kernel parameters hold (client keys, buffers, tile
@@ -477,14 +478,16 @@ int enqueue_first_dim(opir_ctx *ctx, Db &db, Workspace &W, const uint64_t *leave
     CK(W.ql.alloc(tc_query_limb_bytes((int)n1, batch)), "alloc query limbs");
     launch_query_prep_plane(leaves, leaves_stride, W.qs.as<uint64_t>(), (int)n1, batch,
                             ctx->Mq.tab, s, pdl_prep);
-    launch_tc_query_limbs(W.qs.as<uint64_t>(), W.ql.as<uint16_t>(), (int)n1, batch, s,
-                          db.tc_limbs);
+    launch_tc_query_limbs(W.qs.as<uint64_t>(), W.ql.as<uint16_t>(), (int)n1, (int)nr, batch, s,
+                          db.tc_limbs, db.tc_pair);
     ctx->launches += (batch + 31) / 32;
     record(ctx, E, 6);
-    ctx->launches += launch_tc_scan(db.dbl.as<uint16_t>(), W.ql.as<uint16_t>(), W.res.as<uint64_t>(),
-                                    res_stride, (int)n1, (int)nr, batch, ctx->Mq.tab.q,
-                                    ctx->Mq.tab.mu_lo, ctx->Mq.tab.mu_hi, ctx->r64, ctx->r128,
-                                    E.status, s, db.tc_ring, db.tc_limbs) - 1;
+    const int tl = launch_tc_scan(db.dbl.as<uint16_t>(), W.ql.as<uint16_t>(), W.res.as<uint64_t>(),
+                                  res_stride, (int)n1, (int)nr, batch, ctx->Mq.tab.q,
+                                  ctx->Mq.tab.mu_lo, ctx->Mq.tab.mu_hi, ctx->r64, ctx->r128,
+                                  E.status, s, db.tc_ring, db.tc_limbs, db.tc_pair);
+    if (tl < 0) return ctx->fail(OPIR_ERR_CUDA, "tensor kernel: tensor copy maps");
+    ctx->launches += tl - 1;
   } else if (batched) {
     launch_query_prep_batched(leaves, leaves_stride, W.qs.as<uint4>(), (int)n1, batch,
                               ctx->Mq.tab, s, pdl_prep);
@@ -1530,11 +1533,10 @@ int opir_autotune(opir_ctx *ctx, uint32_t db_id, uint32_t max_batch, uint32_t re
     R.engine_ms[i][OPIR_ENGINE_TENSOR - 1] = !(tc_ok && limbs) ? -1.0f : time_it([&] {
       launch_query_prep_plane(leaves.as<uint64_t>(), n1 * CTW, qs.as<uint64_t>(), n1, B,
                               ctx->Mq.tab, s);
-      launch_tc_query_limbs(qs.as<uint64_t>(), ql.as<uint16_t>(), n1, B, s);
-      launch_tc_scan(db->dbl.as<uint16_t>(), ql.as<uint16_t>(), res.as<uint64_t>(), res_stride, n1,
+      launch_tc_query_limbs(qs.as<uint64_t>(), ql.as<uint16_t>(), n1, nr, B, s);
+      return launch_tc_scan(db->dbl.as<uint16_t>(), ql.as<uint16_t>(), res.as<uint64_t>(), res_stride, n1,
                      nr, B, ctx->Mq.tab.q, ctx->Mq.tab.mu_lo, ctx->Mq.tab.mu_hi, ctx->r64,
-                     ctx->r128, status, s);
-      return true;
+                     ctx->r128, status, s) >= 0;
     });
   }
   // ---- tensor kernel: both shared-memory rings at the largest batch
@@ -1543,10 +1545,9 @@ int opir_autotune(opir_ctx *ctx, uint32_t db_id, uint32_t max_batch, uint32_t re
   std::memcpy(R.tc_ring_desc, ring_desc, sizeof ring_desc);
   for (int ring = 0; ring < 2; ring++) {
     R.tc_ring_ms[ring] = !(tc_ok && limbs && np && tc_ring_valid(ring, n1)) ? -1.0f : time_it([&] {
-      launch_tc_scan(db->dbl.as<uint16_t>(), ql.as<uint16_t>(), res.as<uint64_t>(), res_stride, n1,
+      return launch_tc_scan(db->dbl.as<uint16_t>(), ql.as<uint16_t>(), res.as<uint64_t>(), res_stride, n1,
                      nr, bmax, ctx->Mq.tab.q, ctx->Mq.tab.mu_lo, ctx->Mq.tab.mu_hi, ctx->r64,
-                     ctx->r128, status, s, ring);
-      return true;
+                     ctx->r128, status, s, ring) >= 0;
     });
   }
   if (R.tc_ring_ms[0] >= 0 || R.tc_ring_ms[1] >= 0)
@@ -1557,17 +1558,34 @@ int opir_autotune(opir_ctx *ctx, uint32_t db_id, uint32_t max_batch, uint32_t re
   R.tc_limbs_choice = -1;
   for (int lw = 0; lw < 2; lw++) {
     R.tc_limbs_ms[lw] = !(tc_ok && limbs && np) ? -1.0f : time_it([&] {
-      launch_tc_query_limbs(qs.as<uint64_t>(), ql.as<uint16_t>(), n1, bmax, s, lw);
-      launch_tc_scan(db->dbl.as<uint16_t>(), ql.as<uint16_t>(), res.as<uint64_t>(), res_stride, n1,
+      launch_tc_query_limbs(qs.as<uint64_t>(), ql.as<uint16_t>(), n1, nr, bmax, s, lw);
+      return launch_tc_scan(db->dbl.as<uint16_t>(), ql.as<uint16_t>(), res.as<uint64_t>(), res_stride, n1,
                      nr, bmax, ctx->Mq.tab.q, ctx->Mq.tab.mu_lo, ctx->Mq.tab.mu_hi, ctx->r64,
-                     ctx->r128, status, s, R.tc_ring_choice, lw);
-      return true;
+                     ctx->r128, status, s, R.tc_ring_choice, lw) >= 0;
     });
   }
   if (R.tc_limbs_ms[0] >= 0 && R.tc_limbs_ms[1] >= 0)
     R.tc_limbs_choice = tune::pick_over(
         R.tc_limbs_ms, 2, tc_query_limb_width(bmax, -1) == 9 ? kTcLimbs9 : kTcLimbs8,
         tune::kTuneMargin);
+  // ---- tensor kernel: one CTA per tile or CTA pairs (cta_group::2), with
+  // the chosen ring and limbs
+  R.tc_pair_choice = -1;
+  for (int pr = 0; pr < 2; pr++) {
+    const bool applies = tc_ok && limbs && np &&
+                         (pr == 0 || tc_pair_form(nr, bmax, R.tc_limbs_choice, 1));
+    R.tc_pair_ms[pr] = !applies ? -1.0f : time_it([&] {
+      launch_tc_query_limbs(qs.as<uint64_t>(), ql.as<uint16_t>(), n1, nr, bmax, s,
+                            R.tc_limbs_choice, pr);
+      return launch_tc_scan(db->dbl.as<uint16_t>(), ql.as<uint16_t>(), res.as<uint64_t>(), res_stride, n1,
+                     nr, bmax, ctx->Mq.tab.q, ctx->Mq.tab.mu_lo, ctx->Mq.tab.mu_hi, ctx->r64,
+                     ctx->r128, status, s, R.tc_ring_choice, R.tc_limbs_choice, pr) >= 0;
+    });
+  }
+  if (R.tc_pair_ms[0] >= 0 && R.tc_pair_ms[1] >= 0)
+    R.tc_pair_choice = tune::pick_over(R.tc_pair_ms, 2, 0, tune::kTuneMargin);
+  else if (R.tc_pair_ms[0] >= 0)
+    R.tc_pair_choice = 0;
   // ---- tree stages: every form of every distinct launch of this database's
   // pipeline, at one query and at the batch sizes up to one key chunk
   TreeForms tuned;
@@ -1588,6 +1606,7 @@ int opir_autotune(opir_ctx *ctx, uint32_t db_id, uint32_t max_batch, uint32_t re
   db->scan_cfg = R.scan_choice;
   db->tc_ring = R.tc_ring_choice;
   db->tc_limbs = R.tc_limbs_choice;
+  db->tc_pair = R.tc_pair_choice;
   db->forms = tuned;
   // captured single-query graphs hold the launch forms of their capture
   for (auto &gr : db->graphs)

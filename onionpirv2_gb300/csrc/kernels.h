@@ -181,10 +181,18 @@ void launch_db_limbs(const uint64_t *dbs, uint16_t *dbl, int n1, int n_rest, cud
 // with fewer MMA columns for each pass.  launch_tc_query_limbs and
 // launch_tc_scan must be given the same choice.
 enum { kTcLimbs8 = 0, kTcLimbs9 = 1 };
-void launch_tc_query_limbs(const uint64_t *plane, uint16_t *ql, int n1, int batch,
-                           cudaStream_t s, int limbs = -1);
+// pair: the kernel form, one CTA per tile (0, and the default -1) or CTA
+// pairs sharing M = 256 MMAs (1, tcgen05 cta_group::2: each CTA loads half
+// of the query tile; where the rows form pairs of 16-row tiles).  The query
+// limb layout depends on it: give both calls the same.
+void launch_tc_query_limbs(const uint64_t *plane, uint16_t *ql, int n1, int n_rest, int batch,
+                           cudaStream_t s, int limbs = -1, int pair = -1);
 // the query limb width (8 or 9) that a pass of min(batch, 32) queries uses
 int tc_query_limb_width(int batch, int limbs);
+// whether a pass of min(batch, 32) queries runs as CTA pairs
+bool tc_pair_form(int n_rest, int batch, int limbs, int pair);
+// launch_tc_scan returns -1 when a pass could not be launched (the tensor
+// copy maps of a CTA pair could not be made).
 // ring: the shared-memory pipeline of the tensor kernel, 64 k x 4 stages
 // (n1 a multiple of 64) or 32 k x 8 stages; an invalid choice (or -1) takes
 // the first that fits.
@@ -193,7 +201,7 @@ bool tc_ring_valid(int ring, int n1);
 int launch_tc_scan(const uint16_t *dbl, const uint16_t *ql, uint64_t *out, size_t out_stride,
                    int n1, int n_rest, int batch, uint64_t q, uint64_t mu_lo, uint64_t mu_hi,
                    uint64_t r64, uint64_t r128, uint32_t *status, cudaStream_t s, int ring = -1,
-                   int limbs = -1);
+                   int limbs = -1, int pair = -1);
 
 // ---- one folding level (other_dim_mux) on ciphertexts held in NTT form:
 // res[b][j] += RGSW x INTT(res[j+half] - res[j]) for j < half (the

@@ -360,6 +360,10 @@ class PirServer:
             "tc_ring_choice": int(r.tc_ring_choice),
             "tc_limbs": [{"bits": 8 + i, "ms": float(r.tc_limbs_ms[i])} for i in range(2)],
             "tc_limbs_choice": (8 + int(r.tc_limbs_choice)) if r.tc_limbs_choice >= 0 else None,
+            "tc_forms": [{"form": ("one_cta", "cta_pair")[i], "ms": float(r.tc_pair_ms[i])}
+                         for i in range(2)],
+            "tc_form_choice": (("one_cta", "cta_pair")[r.tc_pair_choice]
+                               if r.tc_pair_choice >= 0 else None),
             "forms": [{"stage": stages[r.form_stage[i]], "count": int(r.form_count[i]),
                        "ms": {forms[f]: float(r.form_ms[i][f]) for f in range(3)},
                        "form": forms[r.form_choice[i]] if r.form_choice[i] >= 0 else None}

@@ -49,6 +49,9 @@ def test_autotune_choices_and_parity(gpu_lib, oracle_lib, shape):
     widths = [r["ms"] for r in rep["tc_limbs"]]
     if all(m >= 0 for m in widths):
         assert near_best(widths, rep["tc_limbs_choice"] - 8)
+    forms = [r["ms"] for r in rep["tc_forms"]]
+    if all(m >= 0 for m in forms):
+        assert near_best(forms, ("one_cta", "cta_pair").index(rep["tc_form_choice"]))
     assert rep["forms"] and all(f["form"] is not None for f in rep["forms"])
     names = ("one_cta", "two_cta", "cluster")
     for f in rep["forms"]:

@@ -345,17 +345,23 @@ def test_batched_scan_matches_single_and_oracle(oracle_lib, gpu_lib, monkeypatch
     ((1 << 14, 1024), 40),  # the same in two passes (32 + 8 queries)
     ((1536, 128), 4),       # 96 x 16: 32-k pipeline stages (96 is not a multiple of 64)
     ((8704, 1024), 3),      # 544 x 16: k segments of 512 and 32, 32-k pipeline stages
+    ((1 << 15, 1024), 33),  # 1024 x 32: one row-tile pair, two k segments, two passes
+    ((3072, 128), 5),       # 96 x 32: a pair with 32-k pipeline stages
+    ((17408, 1024), 3),     # 544 x 32: a pair over k segments of 512 and 32
 ])
 @pytest.mark.parametrize("limbs", ["8", "9"])
+@pytest.mark.parametrize("form", ["one_cta", "cta_pair"])
 def test_tensor_core_first_dim_matches_single_queries(oracle_lib, gpu_lib, monkeypatch, shape,
-                                                      batch, limbs):
+                                                      batch, limbs, form):
     """The tensor-core batched product gives every query the response of the
     per-query scan (which the oracle pins) for several shapes and batch
-    sizes, with 8-bit and 9-bit query limbs, and the oracle's response for
-    the first and last query."""
+    sizes, with 8-bit and 9-bit query limbs, one CTA per tile or CTA pairs
+    sharing M = 256 MMAs (where the rows form pairs of 16-row tiles), and
+    the oracle's response for the first and last query."""
     from onionpirv2_gb300 import PirParams, PirServer
     monkeypatch.setenv("OPIR_TC", "1")
     monkeypatch.setenv("OPIR_TC_LIMBS", "0" if limbs == "8" else "1")
+    monkeypatch.setenv("OPIR_TC_PAIR", "0" if form == "one_cta" else "1")
     o = oracle_lib.Oracle(*shape)
     P = o.P
     server = PirServer(PirParams(num_entries=shape[0], max_fst_dim=shape[1]))

@@ -56,14 +56,16 @@ def test_extreme_residues_are_below_q():
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("limbs", [8, 9])
-@pytest.mark.parametrize("shape", [(8192, 512), (16384, 1024)])
+@pytest.mark.parametrize("shape", [(8192, 512), (16384, 1024), (16384, 512), (32768, 1024)])
 @pytest.mark.parametrize("db_end,q_end", [("low", "low"), ("low", "high"), ("high", "high")])
 def test_limb_sums_at_the_exactness_bound(gpu_lib, monkeypatch, limbs, shape, db_end, q_end):
     """Both query limb widths give n1 * v_db * v_q mod q in every slot when
     every limb product sits at the end of its range: one 512-k segment and
-    two segments summed in the epilogue."""
+    two segments summed in the epilogue, one CTA per 16-row tile (n_rest =
+    16) and CTA pairs (n_rest = 32)."""
     from onionpirv2_gb300 import PirParams, PirServer, _capi
     monkeypatch.setenv("OPIR_TC_LIMBS", "0" if limbs == 8 else "1")
+    monkeypatch.setenv("OPIR_TC_PAIR", "1")  # pairs wherever the rows pair up
     monkeypatch.setenv("OPIR_GRAPHS", "0")
     P = PirParams(num_entries=shape[0], max_fst_dim=shape[1])
     n, n1, nr, q = 2048, P.get_fst_dim_sz(), P.get_other_dim_sz(), P.coeff_modulus[0]
