@@ -245,18 +245,26 @@ def serve_leg(server, qsets, rate, seconds, seed=7, max_batch=32, lanes=2, max_w
     return stats, n, same, ok
 
 
-def tensor_roofline(params, B, ms, workload):
+def tensor_engine(limb_bits):
+    return ("tensor (tcgen05, 8-bit database limbs x %d-bit query limbs in bf16, exact)"
+            % limb_bits)
+
+
+def tensor_roofline(params, B, ms, workload, limb_bits=9):
     """Roofline of tc_scan_kernel: algorithmic bf16 flops of the limb GEMM
-    (64 limb products of 2 flops per 60x60-bit MAC, N * n_rest * n1 * 2B
-    MACs) over the kernel's time, against the measured burst bf16 peak (the
-    kernel is timed per launch, not over a seconds-long loop)."""
+    (8 database limbs x 7 query limbs of 9 bits = 56 limb products, or 64
+    with 8-bit query limbs, of 2 flops per 60x60-bit MAC; N * n_rest * n1 *
+    2B MACs) over the kernel's time, against the measured burst bf16 peak
+    (the kernel is timed per launch, not over a seconds-long loop)."""
     n1, nrest = params.get_fst_dim_sz(), params.get_other_dim_sz()
-    flops = 2.0 * 64 * nrest * 2 * B * n1 * N
+    products = 8 * (7 if limb_bits == 9 else 8)
+    flops = 2.0 * products * nrest * 2 * B * n1 * N
     peak, kind = measured_peak("bf16_tflops")
     ach = flops / (ms / 1e3) / 1e12
     return {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
             "frac": ach / peak, "traffic": read_traffic(f"{workload}_b{B}", "tc_scan_kernel"),
             "kernel": "tc_scan_kernel (first dimension of the batch)",
+            "limb_products_per_mac": products,
             "flops_per_step": flops, "kernel_ms": ms,
             "peak_source": f"{kind} bf16_tflops (burst)"}
 
@@ -342,7 +350,7 @@ def large_leg(args, local, clocks=None):
         "workload": args.large_workload, "db_plaintexts": params.get_num_pt(),
         "n1": params.get_fst_dim_sz(), "n_rest": params.get_other_dim_sz(),
         "ndim": len(params.get_dims()), "ntt_db_bytes": db_bytes, "batch": B,
-        "engine": "tensor (tcgen05, 8-bit limbs in bf16, exact)",
+        "engine": tensor_engine(9),
         "value": B / (bms / 1e3), "unit": "queries/s", "ms_per_batch": bms,
         "steps": args.large_steps, "stages_ms": stages,
         "single_query": {"value": 1e3 / single_ms, "unit": "queries/s", "ms_per_query": single_ms,
@@ -1022,10 +1030,11 @@ def main():
         tensor = run_batched("tensor")
         imad = run_batched("imad")
         # tensor-core kernel roofline (limb-GEMM flops / kernel time, burst peak)
-        batched = dict(tensor, batch=B, engine="tensor (tcgen05, 8-bit limbs in bf16, exact)",
+        bits = tune.get("tc_limbs_choice") or 9  # the tuned width (9 bits for full passes)
+        batched = dict(tensor, batch=B, engine=tensor_engine(bits),
                        speedup_vs_single=tensor["value"] / qps,
                        roofline=tensor_roofline(params, B, tensor["stages_ms"]["scan_kernel"],
-                                                args.workload),
+                                                args.workload, bits),
                        imad=dict(imad, engine="integer multiply-add GEMM"))
     # ---- client side: every response of the timed queries (rewritten by
     # the batched passes, which equal them) decodes to its database entry
