@@ -905,6 +905,9 @@ int opir_ctx_create_rns(const opir_rns_params *P, int device, opir_ctx **out) {
   if (device < 0 || device >= ndev) return OPIR_ERR_ARG;
   std::unique_ptr<opir_ctx> ctx(new opir_ctx());
   ctx->device = device;
+  // the first dimension runs on the one-modulus streaming scan, once per prime
+  if (cudaSetDevice(device) != cudaSuccess || init_scan_attributes() != cudaSuccess)
+    return OPIR_ERR_CUDA;
   std::string err;
   const int rc = RnsServer::create(*P, device, &ctx->rns, &err);
   if (rc) return rc;

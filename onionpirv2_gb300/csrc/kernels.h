@@ -146,6 +146,17 @@ void launch_query_prep_batched(const uint64_t *leaves, size_t leaves_stride, uin
 int launch_scan(const uint64_t *dbs, const uint4 *qs, size_t qs_stride, uint64_t *out,
                 size_t out_stride, int n1, int n_rest, int batch, const Consts &C,
                 uint64_t mu_lo, uint64_t mu_hi, uint32_t *status, cudaStream_t s, int cfg = -1);
+// The bulk-copy kernel over `planes` NTT slots, writing slot c of row `row`
+// at out[row o_row + c] and out[row o_row + o_poly + c]; slots below
+// mod_planes reduce mod C0 (q, 2^30 and 2^60 mod q with Shoup companions,
+// Barrett mu0), the rest mod C1: the multi-modulus path runs both primes in
+// one launch.  Returns the configuration that ran, -1 when the shape does
+// not fit it (nothing launched).
+int launch_scan_planes(const uint64_t *dbs, const uint4 *qs, size_t qs_stride, uint64_t *out,
+                       size_t out_stride, int n1, int n_rest, int batch, int planes,
+                       size_t o_row, size_t o_poly, int mod_planes, const Consts &C0,
+                       const uint64_t mu0[2], const Consts &C1, const uint64_t mu1[2],
+                       uint32_t *status, cudaStream_t s);
 // compiled tile configurations of the bulk scan: {rows per thread, warps,
 // k-steps per stage, stages, CTAs per SM, Karatsuba products}
 int scan_config_count();

@@ -20,6 +20,7 @@
 #include <cmath>
 #include <cstring>
 
+#include "async.cuh"
 #include "common.cuh"
 #include "entry.cuh"
 #include "hostmath.h"
@@ -256,7 +257,42 @@ __device__ __forceinline__ uint64_t reduce_wide(U128 x, uint32_t w, const RnsMod
   return r;
 }
 
-// CTA (cc = i N + c, row block): out[row][poly][i][c] = sum_k db[cc][k][row] qn[k][poly][i][c]
+// the streaming scan's storage form of a residue < 2^60 (the database
+// planes hold it): lo30 | hi30 << 32
+__device__ __forceinline__ uint64_t split30(uint64_t v) {
+  return (v & 0x3FFFFFFFULL) | ((v >> 30) << 32);
+}
+__device__ __forceinline__ uint64_t join30(uint64_t w) {
+  return (w & 0x3FFFFFFFULL) | ((w >> 32) << 30);
+}
+
+// The operand of the streaming scan: qs[(i N + c) n1 + k] = the 30-bit halves
+// of qn[k][0][i][c] and qn[k][1][i][c], through a 32 x 32 shared-memory tile
+// (reads coalesced along c, writes along k).
+__global__ void rns_scan_operand_kernel(const uint64_t *qn, uint4 *qs, int n1, RnsConsts C) {
+  __shared__ uint4 tile[32][33];  // [c][k]
+  const int n = C.n, R = C.R, i = blockIdx.z;
+  const int c0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+  for (int kk = threadIdx.y; kk < 32; kk += blockDim.y) {
+    const int k = k0 + kk, c = c0 + threadIdx.x;
+    uint4 v = make_uint4(0, 0, 0, 0);
+    if (k < n1 && c < n) {
+      const uint64_t a = qn[((size_t)k * 2 * R + i) * n + c];
+      const uint64_t b = qn[((size_t)(k * 2 + 1) * R + i) * n + c];
+      v = make_uint4((uint32_t)(a & 0x3FFFFFFFu), (uint32_t)(a >> 30), (uint32_t)(b & 0x3FFFFFFFu),
+                     (uint32_t)(b >> 30));
+    }
+    tile[threadIdx.x][kk] = v;
+  }
+  __syncthreads();
+  for (int cc = threadIdx.y; cc < 32; cc += blockDim.y) {
+    const int c = c0 + cc, k = k0 + threadIdx.x;
+    if (k < n1 && c < n) qs[((size_t)i * n + c) * n1 + k] = tile[cc][threadIdx.x];
+  }
+}
+
+// Shapes the streaming scan does not take: CTA (cc = i N + c, row block):
+// out[row][poly][i][c] = sum_k db[cc][k][row] qn[k][poly][i][c]
 __global__ void rns_scan_kernel(const uint64_t *dbs, const uint64_t *qn, uint64_t *out, int n1,
                                 int n_rest, RnsConsts C) {
   extern __shared__ uint64_t sq[];  // [n1][2]
@@ -270,12 +306,28 @@ __global__ void rns_scan_kernel(const uint64_t *dbs, const uint64_t *qn, uint64_
   const int row = blockIdx.y * blockDim.x + threadIdx.x;
   if (row >= n_rest) return;
   const uint64_t *a = dbs + (size_t)cc * n1 * n_rest + row;
+  const ulonglong2 *sq2 = reinterpret_cast<const ulonglong2 *>(sq);
   U128 s0{0, 0}, s1{0, 0};
   uint32_t w0 = 0, w1 = 0;
-  for (int k = 0; k < n1; ++k) {
-    const uint64_t v = a[(size_t)k * n_rest];
-    add_wide(s0, w0, mul_wide(v, sq[2 * k]));
-    add_wide(s1, w1, mul_wide(v, sq[2 * k + 1]));
+  // eight independent loads ahead of their multiply-adds: the scan is bound
+  // by the loads a thread keeps in flight, not by its arithmetic
+  int k = 0;
+  for (; k + 8 <= n1; k += 8) {
+    uint64_t v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) v[u] = join30(__ldg(a + (size_t)(k + u) * n_rest));
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const ulonglong2 qv = sq2[k + u];
+      add_wide(s0, w0, mul_wide(v[u], qv.x));
+      add_wide(s1, w1, mul_wide(v[u], qv.y));
+    }
+  }
+  for (; k < n1; ++k) {
+    const uint64_t v = join30(__ldg(a + (size_t)k * n_rest));
+    const ulonglong2 qv = sq2[k];
+    add_wide(s0, w0, mul_wide(v, qv.x));
+    add_wide(s1, w1, mul_wide(v, qv.y));
   }
   const size_t CT = 2 * (size_t)R * n;
   out[row * CT + (size_t)i * n + c] = reduce_wide(s0, w0, C.m[i], C.two128[i]);
@@ -375,7 +427,7 @@ __global__ void __launch_bounds__(kRT) rns_db_ntt_scatter_kernel(const uint64_t 
   const size_t pt = pt0 + blockIdx.x, row = pt / n1, col = pt % n1;
   const size_t plane = (size_t)n1 * n_rest;
   for (int c = threadIdx.x; c < n; c += blockDim.x)
-    dbs[((size_t)i * n + c) * plane + col * n_rest + row] = sm[c];
+    dbs[((size_t)i * n + c) * plane + col * n_rest + row] = split30(sm[c]);
 }
 
 // reference layout db_aligned[cc num_pt + row n1 + col] -> planes
@@ -385,7 +437,7 @@ __global__ void rns_db_from_aligned_kernel(const uint64_t *aligned, uint64_t *db
   for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < total;
        x += (size_t)gridDim.x * blockDim.x) {
     const size_t cc = x / plane, rem = x % plane, col = rem / n_rest, row = rem % n_rest;
-    dbs[x] = aligned[cc * plane + row * n1 + col];
+    dbs[x] = split30(aligned[cc * plane + row * n1 + col]);
   }
 }
 
@@ -521,6 +573,23 @@ int RnsServer::create(const opir_rns_params &P, int device, std::unique_ptr<RnsS
   }
   C.fwd = static_cast<const ulonglong2 *>(s->fwd_.p);
   C.inv = static_cast<const ulonglong2 *>(s->inv_.p);
+  for (uint32_t i = 0; i < R; i++) {
+    const uint64_t q = mods[i];
+    Consts &K = s->scan_c_[i];
+    K.q = q;
+    K.two30 = (1ULL << 30) % q;
+    K.two30_s = shoup(K.two30, q);
+    K.two60 = (1ULL << 60) % q;
+    K.two60_s = shoup(K.two60, q);
+    const u128 mu = (~(u128)0) / q;
+    s->scan_mu_[i][0] = (uint64_t)mu;
+    s->scan_mu_[i][1] = (uint64_t)(mu >> 64);
+  }
+  if ((e = s->status_.alloc(kStatusWords * sizeof(uint32_t))) != cudaSuccess ||
+      (e = cudaMemset(s->status_.p, 0, kStatusWords * sizeof(uint32_t))) != cudaSuccess) {
+    *err = std::string("status word: ") + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? OPIR_ERR_OOM : OPIR_ERR_CUDA;
+  }
   for (auto &ev : s->ev_)
     if ((e = cudaEventCreate(&ev)) != cudaSuccess) {
       *err = std::string("events: ") + cudaGetErrorString(e);
@@ -730,13 +799,32 @@ int RnsServer::make_query(uint32_t db_id, uint64_t client, const uint64_t *query
   // the inverse NTT of the n_rest results
   ntt_launch(leaves, 0, qn_.u64(), 0, n1 * 2 * R, 1, R, false, s);
   {
-    int bd = ((nr + 31) / 32) * 32;
-    if (bd > 256) bd = 256;
-    mark(6);
-    rns_scan_kernel<<<dim3(R * n, (nr + bd - 1) / bd), bd, (size_t)n1 * 16, s>>>(
-        db.dbs.u64(), qn_.u64(), res_.u64(), n1, nr, C_);
+    // the one-modulus streaming scan over both primes' planes (bulk copies
+    // into a shared-memory ring, 30-bit half products), where the shape fits
+    bool streamed = false;
+    if (nr >= 2 && n1 % 8 == 0) {
+      RCK(scan_qs_.alloc((size_t)R * n * n1 * sizeof(uint4)), "alloc scan operand");
+      rns_scan_operand_kernel<<<dim3((n + 31) / 32, (n1 + 31) / 32, R), dim3(32, 8), 0, s>>>(
+          qn_.u64(), static_cast<uint4 *>(scan_qs_.p), n1, C_);
+      launches_++;
+      mark(6);
+      // the R N planes of both primes in one launch (slot i N + c reduces mod q_i)
+      streamed = launch_scan_planes(db.dbs.u64(), static_cast<const uint4 *>(scan_qs_.p),
+                                    (size_t)R * n * n1, res_.u64(), (size_t)nr * CT, n1, nr, 1,
+                                    R * n, CT, (size_t)R * n, n, scan_c_[0], scan_mu_[0],
+                                    scan_c_[R - 1], scan_mu_[R - 1],
+                                    static_cast<uint32_t *>(status_.p), s) >= 0;
+      if (streamed) launches_++;
+    }
+    if (!streamed) {
+      mark(6);
+      int bd = ((nr + 31) / 32) * 32;
+      if (bd > 256) bd = 256;
+      rns_scan_kernel<<<dim3(R * n, (nr + bd - 1) / bd), bd, (size_t)n1 * 16, s>>>(
+          db.dbs.u64(), qn_.u64(), res_.u64(), n1, nr, C_);
+      launches_++;
+    }
     mark(7);
-    launches_++;
   }
   ntt_launch(res_.u64(), 0, res_.u64(), 0, nr * 2 * R, 1, R, true, s);
   mark(3);
@@ -779,6 +867,21 @@ int RnsServer::make_query(uint32_t db_id, uint64_t client, const uint64_t *query
           "trace");
   }
   RCK(cudaStreamSynchronize(s), "query");
+  {
+    // a bounded device wait of the scan that gave up (async.cuh)
+    uint32_t st = 0;
+    RCK(cudaMemcpy(&st, status_.p, sizeof st, cudaMemcpyDeviceToHost), "read status");
+    if (st) {
+      RCK(cudaMemset(status_.p, 0, sizeof st), "clear status");
+      return fail(OPIR_ERR_TIMEOUT, "device pipeline wait timed out (status 0x" +
+                                        [&] {
+                                          char b[16];
+                                          snprintf(b, sizeof b, "%x", st);
+                                          return std::string(b);
+                                        }() +
+                                        ")");
+    }
+  }
   stage_valid_ = timed;
   (void)w;
   return OPIR_OK;

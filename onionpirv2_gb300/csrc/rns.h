@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "../../include/onionpir_gpu.h"
+#include "kernels.h"
 
 namespace opir {
 
@@ -127,6 +128,13 @@ class RnsServer {
   uint32_t next_db_ = 1;
   std::map<uint64_t, std::unique_ptr<Client>> clients_;
   // workspace (grown on demand)
+  // the first dimension on the one-modulus streaming scan, once per prime:
+  // its constants (q, 2^30 and 2^60 mod q with Shoup companions) and Barrett
+  // mu per prime, its operand (30-bit halves per prime, slot and k) and its
+  // bounded-wait status words
+  Consts scan_c_[kRnsMaxPrimes] = {};
+  uint64_t scan_mu_[kRnsMaxPrimes][2] = {};
+  RnsBuf scan_qs_, status_;
   RnsBuf exp0_, exp1_, lift_, acc_, s0_, gsw_, digits_, qn_, res_, e_, query_, resp_, packed_,
       coeffs_;
   uint64_t resp_bytes_ = 0;

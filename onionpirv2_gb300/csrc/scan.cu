@@ -103,16 +103,24 @@ __device__ __forceinline__ void acc3_unkaratsuba(Acc3 &a) {
       : "+l"(a.MID.lo), "+l"(a.MID.hi)
       : "l"(a.HH.lo), "l"(a.HH.hi));
 }
-__device__ __forceinline__ uint64_t acc3_reduce(Acc3 &a, const Consts &C, uint64_t mu_lo,
-                                                uint64_t mu_hi, bool karatsuba = false) {
+// the reduction constants of one modulus (a second one rides in ScanGeom)
+struct ScanMod {
+  uint64_t q, two30, two30_s, two60, two60_s, mu_lo, mu_hi;
+};
+__device__ __forceinline__ uint64_t acc3_reduce(Acc3 &a, const ScanMod &m, bool karatsuba) {
   acc3_flush(a);
   if (karatsuba) acc3_unkaratsuba(a);
-  const uint64_t q = C.q;
-  const uint64_t rl = barrett128(a.LL, q, mu_lo, mu_hi);
-  const uint64_t rm = barrett128(a.MID, q, mu_lo, mu_hi);
-  const uint64_t rh = barrett128(a.HH, q, mu_lo, mu_hi);
-  uint64_t r = add_mod(rl, mul_shoup(rm, C.two30, C.two30_s, q), q);
-  return add_mod(r, mul_shoup(rh, C.two60, C.two60_s, q), q);
+  const uint64_t q = m.q;
+  const uint64_t rl = barrett128(a.LL, q, m.mu_lo, m.mu_hi);
+  const uint64_t rm = barrett128(a.MID, q, m.mu_lo, m.mu_hi);
+  const uint64_t rh = barrett128(a.HH, q, m.mu_lo, m.mu_hi);
+  uint64_t r = add_mod(rl, mul_shoup(rm, m.two30, m.two30_s, q), q);
+  return add_mod(r, mul_shoup(rh, m.two60, m.two60_s, q), q);
+}
+__device__ __forceinline__ uint64_t acc3_reduce(Acc3 &a, const Consts &C, uint64_t mu_lo,
+                                                uint64_t mu_hi, bool karatsuba = false) {
+  return acc3_reduce(a, ScanMod{C.q, C.two30, C.two30_s, C.two60, C.two60_s, mu_lo, mu_hi},
+                     karatsuba);
 }
 
 // ---------------------------------------------------------------------------
@@ -201,14 +209,19 @@ struct ScanGeom {
   int pc;       // planes per tile           (512 / rt)
   int row_tiles;  // n_rest / rt
   int nkb;      // n1 / kStepK
-  long long items;  // batch * (kN / pc) * row_tiles
+  long long items;  // batch * (planes / pc) * row_tiles
   int q_bytes;      // pc * kStepK * 16
+  int planes;       // NTT slots (kN; R N for the multi-modulus path)
+  size_t o_row, o_poly;  // output strides of a row and of the second polynomial
+  int mod_planes;   // slots of the first modulus; the rest reduce mod m1
+  ScanMod m1;
 };
 
 // kRows rows per consumer thread, kWarps consumer warps (kRows * kWarps * 32
 // == 512), kStepK k-steps per stage, kStages stages, kMinBlocks CTAs per SM;
 // kKara: Karatsuba products (acc3_mac_k).
-template <int kRows, int kWarps, int kStepK, int kStages, int kMinBlocks, int kKara>
+template <int kRows, int kWarps, int kStepK, int kStages, int kMinBlocks, int kKara,
+          bool kTwoMods = false>
 __global__ void __launch_bounds__(kWarps * 32 + 32, kMinBlocks)
     scan_bulk_kernel(const uint64_t *__restrict__ dbs, const uint4 *__restrict__ qs,
                      size_t qs_stride, uint64_t *out, size_t out_stride, ScanGeom G, Consts C,
@@ -234,7 +247,7 @@ __global__ void __launch_bounds__(kWarps * 32 + 32, kMinBlocks)
   __syncthreads();
 
   const size_t plane_words = (size_t)G.n1 * G.n_rest;
-  const long long per_b = (long long)(kN / G.pc) * G.row_tiles;
+  const long long per_b = (long long)(G.planes / G.pc) * G.row_tiles;
   // test hook (async.cuh): CTA 0 withholds its first stage, and its waits
   // for stages give up after `limit` polls; the drain below keeps the
   // production limit, since every copy it waits for was issued
@@ -413,11 +426,24 @@ __global__ void __launch_bounds__(kWarps * 32 + 32, kMinBlocks)
     }
     const size_t c = (size_t)g * G.pc + p;
     uint64_t *o = out + b * out_stride;
+    if constexpr (kTwoMods) {
+      // slots from mod_planes on belong to the second modulus
+      const ScanMod m = c < (size_t)G.mod_planes
+                            ? ScanMod{C.q, C.two30, C.two30_s, C.two60, C.two60_s, mu_lo, mu_hi}
+                            : G.m1;
 #pragma unroll
-    for (int rr = 0; rr < kRows; ++rr) {
-      const size_t row = (size_t)rt * G.rt + r + rr;
-      o[row * 2 * kN + c] = acc3_reduce(acc[rr][0], C, mu_lo, mu_hi, kKara != 0);
-      o[row * 2 * kN + kN + c] = acc3_reduce(acc[rr][1], C, mu_lo, mu_hi, kKara != 0);
+      for (int rr = 0; rr < kRows; ++rr) {
+        const size_t row = (size_t)rt * G.rt + r + rr;
+        o[row * G.o_row + c] = acc3_reduce(acc[rr][0], m, kKara != 0);
+        o[row * G.o_row + G.o_poly + c] = acc3_reduce(acc[rr][1], m, kKara != 0);
+      }
+    } else {
+#pragma unroll
+      for (int rr = 0; rr < kRows; ++rr) {
+        const size_t row = (size_t)rt * G.rt + r + rr;
+        o[row * G.o_row + c] = acc3_reduce(acc[rr][0], C, mu_lo, mu_hi, kKara != 0);
+        o[row * G.o_row + G.o_poly + c] = acc3_reduce(acc[rr][1], C, mu_lo, mu_hi, kKara != 0);
+      }
     }
   }
 }
@@ -685,19 +711,21 @@ constexpr int kDefaultCfg = 8;
 int g_cfg = kDefaultCfg;
 int g_batch_form = 3;  // accumulate spelling of scan_batch_kernel (OPIR_BATCH_MAC)
 
-template <int R, int W, int K, int S, int B, int KA>
+template <int R, int W, int K, int S, int B, int KA, bool TWO = false>
 cudaError_t set_attr() {
   constexpr int kTileRows = R * W * 32;
   const int max_smem = S * (K * kTileRows * 8 + (kTileRows / 2) * K * 16) + 2 * S * 8;
-  return cudaFuncSetAttribute(scan_bulk_kernel<R, W, K, S, B, KA>,
+  return cudaFuncSetAttribute(scan_bulk_kernel<R, W, K, S, B, KA, TWO>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize,
                               max_smem > 227 * 1024 ? 227 * 1024 : max_smem);
 }
 
-template <int R, int W, int K, int S, int B, int KA>
+template <int R, int W, int K, int S, int B, int KA, bool TWO = false>
 bool launch_bulk(const uint64_t *dbs, const uint4 *qs, size_t qs_stride, uint64_t *out,
                  size_t out_stride, int n1, int n_rest, int batch, const Consts &C,
-                 uint64_t mu_lo, uint64_t mu_hi, uint32_t *status, cudaStream_t s) {
+                 uint64_t mu_lo, uint64_t mu_hi, uint32_t *status, cudaStream_t s,
+                 int planes = kN, size_t o_row = 2 * (size_t)kN, size_t o_poly = kN,
+                 int mod_planes = kN, const ScanMod *m1 = nullptr) {
   if (n1 % K != 0) return false;
   constexpr int kTileRows = R * W * 32;
   ScanGeom G;
@@ -708,18 +736,24 @@ bool launch_bulk(const uint64_t *dbs, const uint4 *qs, size_t qs_stride, uint64_
   if (G.rt < R) return false;
   G.row_tiles = n_rest / G.rt;
   G.nkb = n1 / K;
-  G.items = (long long)batch * (kN / G.pc) * G.row_tiles;
+  if (planes % G.pc != 0) return false;
+  G.planes = planes;
+  G.o_row = o_row;
+  G.o_poly = o_poly;
+  G.mod_planes = mod_planes;
+  G.m1 = m1 ? *m1 : ScanMod{C.q, C.two30, C.two30_s, C.two60, C.two60_s, mu_lo, mu_hi};
+  G.items = (long long)batch * (planes / G.pc) * G.row_tiles;
   G.q_bytes = G.pc * K * 16;
   const int smem = S * (K * kTileRows * 8 + G.q_bytes) + 2 * S * 8;
   if (smem > 227 * 1024) return false;  // tiny planes: many query runs per stage
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, scan_bulk_kernel<R, W, K, S, B, KA>,
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, scan_bulk_kernel<R, W, K, S, B, KA, TWO>,
                                                 W * 32 + 32, smem);
   if (per_sm < 1) per_sm = 1;
   const int sms = g_num_sms > 0 ? g_num_sms : 152;
   long long grid = (long long)per_sm * sms;
   if (grid > G.items) grid = G.items;
-  scan_bulk_kernel<R, W, K, S, B, KA><<<(unsigned)grid, W * 32 + 32, smem, s>>>(
+  scan_bulk_kernel<R, W, K, S, B, KA, TWO><<<(unsigned)grid, W * 32 + 32, smem, s>>>(
       dbs, qs, qs_stride, out, out_stride, G, C, mu_lo, mu_hi, status);
   return true;
 }
@@ -738,6 +772,9 @@ bool launch_bulk(const uint64_t *dbs, const uint4 *qs, size_t qs_stride, uint64_
   X(8, 2, 8, 16, 3, 1, 1)
 constexpr int kNumCfgs = 9;
 static_assert(kDefaultCfg < kNumCfgs, "default scan configuration");
+// the default configuration's template arguments (kDefaultCfg = 8 above):
+// the two-modulus instantiation of the multi-modulus path
+constexpr int kPlanesCfg[6] = {2, 8, 16, 3, 1, 1};
 
 }  // namespace
 
@@ -747,6 +784,9 @@ cudaError_t init_scan_attributes() {
   if (e == cudaSuccess) e = set_attr<R, W, K, S, B, KA>();
   OPIR_SCAN_CONFIGS(OPIR_SET)
 #undef OPIR_SET
+  if (e == cudaSuccess)
+    e = set_attr<kPlanesCfg[0], kPlanesCfg[1], kPlanesCfg[2], kPlanesCfg[3], kPlanesCfg[4],
+                 kPlanesCfg[5], true>();
   if (e != cudaSuccess) return e;
   int dev;
   cudaGetDevice(&dev);
@@ -799,6 +839,22 @@ bool launch_scan_batched(const uint64_t *dbs, const uint4 *qsb, uint64_t *out, s
 #undef OPIR_BATCH
   }
   return true;
+}
+
+int launch_scan_planes(const uint64_t *dbs, const uint4 *qs, size_t qs_stride, uint64_t *out,
+                       size_t out_stride, int n1, int n_rest, int batch, int planes,
+                       size_t o_row, size_t o_poly, int mod_planes, const Consts &C0,
+                       const uint64_t mu0[2], const Consts &C1, const uint64_t mu1[2],
+                       uint32_t *status, cudaStream_t s) {
+  if (n_rest < 2 || n1 % 8 != 0) return -1;
+  const ScanMod m1{C1.q, C1.two30, C1.two30_s, C1.two60, C1.two60_s, mu1[0], mu1[1]};
+  // the default tile configuration, with the per-slot choice of modulus
+  return launch_bulk<kPlanesCfg[0], kPlanesCfg[1], kPlanesCfg[2], kPlanesCfg[3], kPlanesCfg[4],
+                     kPlanesCfg[5], true>(dbs, qs, qs_stride, out, out_stride, n1, n_rest, batch,
+                                          C0, mu0[0], mu0[1], status, s, planes, o_row, o_poly,
+                                          mod_planes, &m1)
+             ? kDefaultCfg
+             : -1;
 }
 
 int scan_config_count() { return kNumCfgs; }
