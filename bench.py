@@ -72,11 +72,16 @@ def parse():
     ap.add_argument("--cpu-queries", type=int, default=10,
                     help="timed queries of the CPU baseline (after 3 untimed ones, as tests.cpp:16)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the library's default choices (profiling runs: timings taken "
+                         "under a profiler would make the autotuner's choices meaningless)")
     ap.add_argument("--batch", type=int, default=32,
                     help="batch size of the batched measurement (0 = skip)")
     ap.add_argument("--batch-steps", type=int, default=10)
-    ap.add_argument("--micro", choices=["ntt"], default=None,
-                    help="kernel micro-benchmark instead of the query benchmark")
+    ap.add_argument("--micro", choices=["ntt", "tc"], default=None,
+                    help="kernel micro-benchmark instead of the query benchmark (tc: the "
+                         "tensor-core first dimension of --batch random leaf sets on "
+                         "--workload's database, --steps calls; a profiling target)")
     ap.add_argument("--count", type=int, default=152 * 64, help="polynomials for --micro ntt")
     ap.add_argument("--serve-rate", type=float, default=1500.0,
                     help="offered queries/s of the serving measurement (0 = skip)")
@@ -432,8 +437,9 @@ def rns_leg(args, local, clocks=None, cpu=True):
                   "response and packed bytes out)",
         "stages_ms": stages,
         "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
-                     "frac": ach / peak, "traffic": None,
-                     "kernel": "rns_scan_kernel (first dimension, every prime)",
+                     "frac": ach / peak,
+                     "traffic": read_traffic(args.rns_workload, "scan_bulk_kernel"),
+                     "kernel": "scan_bulk_kernel (first dimension, both primes in one launch)",
                      "peak_source": f"{kind} hbm_gbs"},
         "inputs": "seeded uniform residues as keys and queries (value-independent work; "
                   "bit-exactness against the oracle is the -m gpu tests' job)",
@@ -873,12 +879,50 @@ def run_micro_ntt(args):
     return 0
 
 
+def run_micro_tc(args):
+    """The tensor-core first dimension alone (query transform, limb split,
+    tc_scan_kernel) of args.batch random leaf sets on the workload's database,
+    through the first-dimension hook: args.warmup + args.steps calls, host
+    leaves in and results out on every call.  For kernel profiles."""
+    import ctypes
+
+    from onionpirv2_gb300 import PirParams, PirServer, _capi
+    P = PirParams.preset(args.workload)
+    n1, nr, B = P.get_fst_dim_sz(), P.get_other_dim_sz(), max(2, args.batch)
+    server = PirServer(P)
+    server.gen_data(DB_SEED)
+    server.set_batch_engine("tensor")
+    leaves = np.random.default_rng(1).integers(0, P.coeff_modulus[0], size=(B, n1, 2, N),
+                                               dtype=np.uint64)
+    out = np.zeros((B, nr, 2, N), np.uint64)
+    p64 = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))
+
+    def call():
+        _capi.check(server.ctx, server._L.opir_debug_first_dim(server.ctx, server.db_id, B,
+                                                                p64(leaves), p64(out)))
+    for _ in range(args.warmup):
+        call()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        call()
+    wall = (time.perf_counter() - t0) / max(1, args.steps)
+    server.close()
+    print(json.dumps({"micro": "tc", "workload": args.workload, "batch": B, "n1": n1,
+                      "n_rest": nr, "calls": args.steps,
+                      "wall_ms_per_call": wall * 1e3,
+                      "what": "host leaves in, first dimension out (coefficient form)"}),
+          flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
     if args.micro == "ntt":
         return run_micro_ntt(args)
+    if args.micro == "tc":
+        return run_micro_tc(args)
     if args.serve:
         return serve_main(args)
     if args.batch_sweep:
@@ -916,7 +960,7 @@ def main():
     # the autotuner picks the scan tile configuration and the engine per batch
     # size for this database on this GPU (untimed; all choices are bit-exact)
     t_tune = time.perf_counter()
-    tune = server.autotune(max_batch=max(2, args.batch))
+    tune = None if args.no_autotune else server.autotune(max_batch=max(2, args.batch))
     tune_s = time.perf_counter() - t_tune
     rb = server.resp_bytes
     nq = queries.shape[0]
@@ -1030,7 +1074,7 @@ def main():
         tensor = run_batched("tensor")
         imad = run_batched("imad")
         # tensor-core kernel roofline (limb-GEMM flops / kernel time, burst peak)
-        bits = tune.get("tc_limbs_choice") or 9  # the tuned width (9 bits for full passes)
+        bits = (tune or {}).get("tc_limbs_choice") or 9  # the tuned width (9 bits for full passes)
         batched = dict(tensor, batch=B, engine=tensor_engine(bits),
                        speedup_vs_single=tensor["value"] / qps,
                        roofline=tensor_roofline(params, B, tensor["stages_ms"]["scan_kernel"],
@@ -1102,7 +1146,7 @@ def main():
         "gpu_launches": launches,
         "clocks": clocks.summary(t0, t1),
         "ingest_s": ingest_s,
-        "autotune": {"seconds": tune_s, "scan_choice": tune["scan_choice"],
+        "autotune": None if tune is None else {"seconds": tune_s, "scan_choice": tune["scan_choice"],
                      "scan_ms": [round(c["ms"], 4) for c in tune["scan_configs"]],
                      "engine_by_batch": {str(b["batch"]): b["engine"] for b in tune["batches"]},
                      "first_dim_ms_by_batch": {str(b["batch"]): {k: round(v, 3) for k, v in
