@@ -73,6 +73,121 @@ __device__ void smem_ntt_inv(uint64_t *s, const ulonglong2 *tw, const RnsMod &M,
   __syncthreads();
 }
 
+// ---------------------------------------------------------------------------
+// Register-resident transform of N = 4096 (the two-prime presets): 512
+// threads x 8 coefficients, four register passes of three radix-2 stages
+// (index bits 11-9, 8-6, 5-3, 2-0) separated by shared-memory exchanges --
+// the one-prime transform's scheme at twice the size -- with the same lazy
+// Harvey butterflies (forward values in [0, 8q), inverse in [0, 4q); every
+// prime < 2^60) and the same twiddle tables as smem_ntt_fwd / smem_ntt_inv
+// (stage on index bit b: twiddle m + (x >> (b + 1)), m = N / 2^(b+1)).
+// Forward: natural order in, SEAL's bit-reversed order out; inverse the
+// reverse, scaled by N^-1; both fully reduced.
+// ---------------------------------------------------------------------------
+constexpr int kLogN4096 = 12;
+constexpr int kT4096 = 512;
+constexpr int kSmem4096 = 4096 + (4096 / 16) * 2;  // padded exchange buffer (u64 words)
+
+template <int LO>
+__device__ __forceinline__ void ct_pass3_4096(uint64_t r[8], int tid, const ulonglong2 *tw,
+                                              uint64_t q, uint64_t q4) {
+  const int base = pass_index(tid, 0, LO);
+#pragma unroll
+  for (int st = 2; st >= 0; --st) {
+    const int b = LO + st, half = 1 << st;
+    const int m = 1 << (kLogN4096 - 1 - b);
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      if (e & half) continue;
+      ct_bf(r[e], r[e | half], __ldg(tw + m + ((base | (e << LO)) >> (b + 1))), q, q4);
+    }
+  }
+}
+template <int LO>
+__device__ __forceinline__ void gs_pass3_4096(uint64_t r[8], int tid, const ulonglong2 *tw,
+                                              uint64_t q, uint64_t q4) {
+  const int base = pass_index(tid, 0, LO);
+#pragma unroll
+  for (int st = 0; st <= 2; ++st) {
+    const int b = LO + st, half = 1 << st;
+    const int m = 1 << (kLogN4096 - 1 - b);
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      if (e & half) continue;
+      gs_bf(r[e], r[e | half], __ldg(tw + m + ((base | (e << LO)) >> (b + 1))), q, q4);
+    }
+  }
+}
+// exchange between passes through one buffer: every thread's loads of the
+// previous exchange are done before anyone stores again
+template <int FROM, int TO>
+__device__ __forceinline__ void exchange_4096(uint64_t *s, uint64_t r[8], int tid) {
+  __syncthreads();
+  store_pass(s, r, tid, FROM);
+  __syncthreads();
+  load_pass(s, r, tid, TO);
+}
+
+__global__ void __launch_bounds__(kT4096) rns_ntt4096_kernel(const uint64_t *src, size_t src_stride,
+                                                             uint64_t *dst, size_t dst_stride,
+                                                             int period, int inverse, RnsConsts C) {
+  __shared__ uint64_t s[kSmem4096];
+  const int tid = threadIdx.x;
+  const size_t x = blockIdx.x, y = blockIdx.y;
+  const int mi = (int)(x % (size_t)period);
+  const uint64_t q = C.m[mi].q, q2 = 2 * q, q4 = 4 * q;
+  const uint64_t *in = src + y * src_stride + x * 4096;
+  uint64_t *out = dst + y * dst_stride + x * 4096;
+  uint64_t r[8];
+  if (!inverse) {
+    const ulonglong2 *tw = C.fwd + (size_t)mi * 4096;
+#pragma unroll
+    for (int e = 0; e < 8; ++e) r[e] = in[tid + kT4096 * e];
+    ct_pass3_4096<9>(r, tid, tw, q, q4);
+    exchange_4096<9, 6>(s, r, tid);
+    ct_pass3_4096<6>(r, tid, tw, q, q4);
+    exchange_4096<6, 3>(s, r, tid);
+    ct_pass3_4096<3>(r, tid, tw, q, q4);
+    exchange_4096<3, 0>(s, r, tid);
+    ct_pass3_4096<0>(r, tid, tw, q, q4);
+    ulonglong2 *o = reinterpret_cast<ulonglong2 *>(out + 8 * tid);
+#pragma unroll
+    for (int e = 0; e < 8; e += 2) {
+      uint64_t v[2];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        uint64_t w = r[e + h] >= q4 ? r[e + h] - q4 : r[e + h];
+        w = w >= q2 ? w - q2 : w;
+        v[h] = w >= q ? w - q : w;
+      }
+      o[e / 2] = make_ulonglong2(v[0], v[1]);
+    }
+  } else {
+    const ulonglong2 *tw = C.inv + (size_t)mi * 4096;
+    const ulonglong2 *i2 = reinterpret_cast<const ulonglong2 *>(in + 8 * tid);
+#pragma unroll
+    for (int e = 0; e < 8; e += 2) {
+      const ulonglong2 v = i2[e / 2];
+      r[e] = v.x;
+      r[e + 1] = v.y;
+    }
+    gs_pass3_4096<0>(r, tid, tw, q, q4);
+    exchange_4096<0, 3>(s, r, tid);
+    gs_pass3_4096<3>(r, tid, tw, q, q4);
+    exchange_4096<3, 6>(s, r, tid);
+    gs_pass3_4096<6>(r, tid, tw, q, q4);
+    exchange_4096<6, 9>(s, r, tid);
+    gs_pass3_4096<9>(r, tid, tw, q, q4);
+    const RnsMod &M = C.m[mi];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      uint64_t v = mul_shoup_lazy4(r[e], M.n_inv, M.n_inv_s, q);
+      v = v >= q2 ? v - q2 : v;
+      out[tid + kT4096 * e] = v >= q ? v - q : v;
+    }
+  }
+}
+
 // Batched transform: polynomial x of group y is src + y src_stride + x N
 // (out: dst, same indexing; in place when src == dst); its modulus is
 // x mod `period` (ciphertext arrays: period R; key-switching arrays: R + 1).
@@ -603,8 +718,12 @@ void RnsServer::ntt_launch(const uint64_t *src, size_t src_stride, uint64_t *dst
                            size_t dst_stride, int polys, int groups, int period, bool inverse,
                            cudaStream_t s) {
   if (polys <= 0 || groups <= 0) return;
-  rns_ntt_kernel<<<dim3((unsigned)polys, (unsigned)groups), kRT, (size_t)C_.n * 8, s>>>(
-      src, src_stride, dst, dst_stride, period, inverse ? 1 : 0, C_);
+  if (C_.n == 4096)
+    rns_ntt4096_kernel<<<dim3((unsigned)polys, (unsigned)groups), kT4096, 0, s>>>(
+        src, src_stride, dst, dst_stride, period, inverse ? 1 : 0, C_);
+  else
+    rns_ntt_kernel<<<dim3((unsigned)polys, (unsigned)groups), kRT, (size_t)C_.n * 8, s>>>(
+        src, src_stride, dst, dst_stride, period, inverse ? 1 : 0, C_);
   launches_++;
 }
 
