@@ -32,6 +32,13 @@ namespace {
 using u128 = unsigned __int128;
 constexpr int kRT = 512;  // threads of the transform and ingest CTAs
 constexpr int kPT = 256;  // threads of the pointwise CTAs
+// The pointwise kernels give every thread one coefficient: blockIdx.x runs
+// over (unit, chunk of kPT coefficients) -- narrow tree levels (a node or a
+// pair) still spread over N / kPT CTAs per polynomial.
+__device__ __forceinline__ int pw_unit(int n) { return (int)blockIdx.x / (n / kPT); }
+__device__ __forceinline__ int pw_coeff(int n) {
+  return (int)(blockIdx.x % (unsigned)(n / kPT)) * kPT + (int)threadIdx.x;
+}
 
 __device__ __forceinline__ uint64_t rmod(U128 x, const RnsMod &M) {
   return barrett128(x, M.q, M.mu_lo, M.mu_hi);
@@ -219,7 +226,7 @@ __global__ void __launch_bounds__(kPT) rns_expand_lift_kernel(const uint64_t *cu
                                                               uint64_t *s0, uint64_t g,
                                                               RnsConsts C) {
   const int n = C.n, R = C.R, M = R + 1;
-  const int node = blockIdx.x, j = blockIdx.y, m = blockIdx.z;
+  const int node = pw_unit(n), j = blockIdx.y, m = blockIdx.z;
   const size_t CT = 2 * (size_t)R * n;
   const uint64_t *c0 = cur + node * CT + (size_t)j * n;
   const uint64_t *c1 = cur + node * CT + (size_t)(R + j) * n;
@@ -227,7 +234,8 @@ __global__ void __launch_bounds__(kPT) rns_expand_lift_kernel(const uint64_t *cu
   uint64_t *L = lift + (((size_t)node * R + j) * M + m) * n;
   uint64_t *S = s0 + ((size_t)node * R + j) * n;
   const uint64_t mask = 2 * (uint64_t)n - 1;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+  {
+    const int i = pw_coeff(n);
     const uint64_t e = ((uint64_t)i * g) & mask;
     const bool wrap = e >= (uint64_t)n;
     const int d = (int)(wrap ? e - n : e);
@@ -242,9 +250,10 @@ __global__ void __launch_bounds__(kPT) rns_ks_mac_kernel(const uint64_t *lift,
                                                          const uint64_t *key, uint64_t *acc,
                                                          RnsConsts C) {
   const int n = C.n, R = C.R, M = R + 1;
-  const int node = blockIdx.x, k = blockIdx.y, m = blockIdx.z;
+  const int node = pw_unit(n), k = blockIdx.y, m = blockIdx.z;
   uint64_t *A = acc + (((size_t)node * 2 + k) * M + m) * n;
-  for (int c = threadIdx.x; c < n; c += blockDim.x) {
+  {
+    const int c = pw_coeff(n);
     U128 s{0, 0};
     for (int j = 0; j < R; ++j)
       mac_to(s, lift[(((size_t)node * R + j) * M + m) * n + c], key[(((size_t)j * 2 + k) * M + m) * n + c]);
@@ -262,7 +271,7 @@ __global__ void __launch_bounds__(kPT) rns_expand_combine_kernel(const uint64_t 
                                                                  uint64_t *nxt, int kshift,
                                                                  RnsConsts C) {
   const int n = C.n, R = C.R, M = R + 1;
-  const int node = blockIdx.x, poly = blockIdx.y, i = blockIdx.z;
+  const int node = pw_unit(n), poly = blockIdx.y, i = blockIdx.z;
   const size_t CT = 2 * (size_t)R * n;
   const uint64_t q = C.m[i].q, p = C.m[R].q;
   const uint64_t *xq = acc + (((size_t)node * 2 + poly) * M + i) * n;
@@ -270,7 +279,8 @@ __global__ void __launch_bounds__(kPT) rns_expand_combine_kernel(const uint64_t 
   const uint64_t *x = cur + node * CT + ((size_t)poly * R + i) * n;
   uint64_t *even = nxt + (2 * (size_t)node) * CT + ((size_t)poly * R + i) * n;
   uint64_t *odd = even + CT;
-  for (int c = threadIdx.x; c < n; c += blockDim.x) {
+  {
+    const int c = pw_coeff(n);
     const uint64_t r = add_mod(xp[c], C.p_half, p);
     const uint64_t rq = r >= q ? r - q : r;
     uint64_t v = sub_mod(add_mod(xq[c], C.p_half_mod[i], q), rq, q);
@@ -298,12 +308,13 @@ __global__ void __launch_bounds__(kPT) rns_decompose_kernel(const uint64_t *src,
                                                             size_t sub_off, int l, int b,
                                                             uint64_t *digits, RnsConsts C) {
   const int n = C.n, R = C.R;
-  const int e = blockIdx.x, poly = blockIdx.y;
+  const int e = pw_unit(n), poly = blockIdx.y;
   const uint64_t q0 = C.m[0].q, q1 = R > 1 ? C.m[1].q : 0;
   const uint64_t *x = src + (size_t)e * ct_stride + (size_t)poly * R * n;
   const u128 mask = (((u128)1) << b) - 1;
   uint64_t *out = digits + ((size_t)e * 2 * l + (size_t)poly * l) * R * n;
-  for (int c = threadIdx.x; c < n; c += blockDim.x) {
+  {
+    const int c = pw_coeff(n);
     uint64_t r0 = x[c], r1 = R > 1 ? x[n + c] : 0;
     if (sub_off) {
       r0 = sub_mod(x[sub_off + c], r0, q0);
@@ -330,12 +341,13 @@ __global__ void __launch_bounds__(kPT) rns_extprod_mac_kernel(const uint64_t *di
                                                               int grp, int grp_stride, int off,
                                                               RnsConsts C) {
   const int n = C.n, R = C.R;
-  const int e = blockIdx.x, k = blockIdx.y, i = blockIdx.z;
+  const int e = pw_unit(n), k = blockIdx.y, i = blockIdx.z;
   const size_t CT = 2 * (size_t)R * n;
   uint64_t *o = out + ((size_t)(e / grp) * grp_stride + off + e % grp) * CT + ((size_t)k * R + i) * n;
   const uint64_t *d = digits + (size_t)e * nd * R * n + (size_t)i * n;
   const uint64_t *g = rows + ((size_t)k * R + i) * n;
-  for (int c = threadIdx.x; c < n; c += blockDim.x) {
+  {
+    const int c = pw_coeff(n);
     U128 s{0, 0};
     for (int j = 0; j < nd; ++j) mac_to(s, d[(size_t)j * R * n + c], g[(size_t)j * CT + c]);
     o[c] = rmod(s, C.m[i]);
@@ -347,9 +359,10 @@ __global__ void __launch_bounds__(kPT) rns_add_kernel(uint64_t *res, const uint6
                                                       RnsConsts C) {
   const int n = C.n, R = C.R;
   const size_t CT = 2 * (size_t)R * n;
-  const size_t off = blockIdx.x * CT + ((size_t)blockIdx.y * R + blockIdx.z) * n;
+  const size_t off = (size_t)pw_unit(n) * CT + ((size_t)blockIdx.y * R + blockIdx.z) * n;
   const uint64_t q = C.m[blockIdx.z].q;
-  for (int c = threadIdx.x; c < n; c += blockDim.x) res[off + c] = add_mod(res[off + c], e[off + c], q);
+  const int c = pw_coeff(n);
+  res[off + c] = add_mod(res[off + c], e[off + c], q);
 }
 
 // ---------------------------------------------------------------------------
@@ -868,6 +881,7 @@ int RnsServer::make_query(uint32_t db_id, uint64_t client, const uint64_t *query
   int rc = ensure_workspace(db);
   if (rc) return rc;
   const int n = C_.n, R = C_.R, M = R + 1;
+  const int nch = n / kPT;  // coefficient chunks of the pointwise kernels
   const size_t CT = 2 * (size_t)R * n;
   const int h = db.h, u = db.u, l = C_.l, lk = C_.l_key;
   const size_t w = (size_t)1 << h;
@@ -888,12 +902,12 @@ int RnsServer::make_query(uint32_t db_id, uint64_t client, const uint64_t *query
     const int k = 1 << a;
     const uint64_t g = (uint64_t)n / k + 1;
     uint64_t *nxt = bufs[a & 1];
-    rns_expand_lift_kernel<<<dim3(live, R, M), kPT, 0, s>>>(cur, lift_.u64(), s0_.u64(), g, C_);
+    rns_expand_lift_kernel<<<dim3(live * nch, R, M), kPT, 0, s>>>(cur, lift_.u64(), s0_.u64(), g, C_);
     ntt_launch(lift_.u64(), 0, lift_.u64(), 0, live * R * M, 1, M, false, s);
-    rns_ks_mac_kernel<<<dim3(live, 2, M), kPT, 0, s>>>(lift_.u64(), cl.galois.u64() + a * key_level,
+    rns_ks_mac_kernel<<<dim3(live * nch, 2, M), kPT, 0, s>>>(lift_.u64(), cl.galois.u64() + a * key_level,
                                                       acc_.u64(), C_);
     ntt_launch(acc_.u64(), 0, acc_.u64(), 0, live * 2 * M, 1, M, true, s);
-    rns_expand_combine_kernel<<<dim3(live, 2, R), kPT, 0, s>>>(cur, s0_.u64(), acc_.u64(), nxt, k, C_);
+    rns_expand_combine_kernel<<<dim3(live * nch, 2, R), kPT, 0, s>>>(cur, s0_.u64(), acc_.u64(), nxt, k, C_);
     launches_ += 3;
     cur = nxt;
   }
@@ -907,9 +921,9 @@ int RnsServer::make_query(uint32_t db_id, uint64_t client, const uint64_t *query
     const uint64_t *first = leaves + (size_t)n1 * CT;
     ntt_launch(first, (size_t)l * CT, gsw_.u64(), (size_t)2 * l * CT, l * 2 * R, db.ndim - 1, R,
                false, s);
-    rns_decompose_kernel<<<dim3(E, 2), kPT, 0, s>>>(first, CT, 0, lk, C_.b_key, digits_.u64(), C_);
+    rns_decompose_kernel<<<dim3(E * nch, 2), kPT, 0, s>>>(first, CT, 0, lk, C_.b_key, digits_.u64(), C_);
     ntt_launch(digits_.u64(), 0, digits_.u64(), 0, E * 2 * lk * R, 1, R, false, s);
-    rns_extprod_mac_kernel<<<dim3(E, 2, R), kPT, 0, s>>>(digits_.u64(), 2 * lk, cl.gsw.u64(),
+    rns_extprod_mac_kernel<<<dim3(E * nch, 2, R), kPT, 0, s>>>(digits_.u64(), 2 * lk, cl.gsw.u64(),
                                                         gsw_.u64(), l, 2 * l, l, C_);
     launches_ += 2;
   }
@@ -955,13 +969,13 @@ int RnsServer::make_query(uint32_t db_id, uint64_t client, const uint64_t *query
   for (int d = 1; d < db.ndim; d++) {
     const int half = cnt / 2;
     const uint64_t *sel = gsw_.u64() + (size_t)(d - 1) * 2 * l * CT;
-    rns_decompose_kernel<<<dim3(half, 2), kPT, 0, s>>>(res_.u64(), CT, (size_t)half * CT, l, C_.b,
+    rns_decompose_kernel<<<dim3(half * nch, 2), kPT, 0, s>>>(res_.u64(), CT, (size_t)half * CT, l, C_.b,
                                                       digits_.u64(), C_);
     ntt_launch(digits_.u64(), 0, digits_.u64(), 0, half * 2 * l * R, 1, R, false, s);
-    rns_extprod_mac_kernel<<<dim3(half, 2, R), kPT, 0, s>>>(digits_.u64(), 2 * l, sel, e_.u64(), 1,
+    rns_extprod_mac_kernel<<<dim3(half * nch, 2, R), kPT, 0, s>>>(digits_.u64(), 2 * l, sel, e_.u64(), 1,
                                                            1, 0, C_);
     ntt_launch(e_.u64(), 0, e_.u64(), 0, half * 2 * R, 1, R, true, s);
-    rns_add_kernel<<<dim3(half, 2, R), kPT, 0, s>>>(res_.u64(), e_.u64(), C_);
+    rns_add_kernel<<<dim3(half * nch, 2, R), kPT, 0, s>>>(res_.u64(), e_.u64(), C_);
     launches_ += 3;
     cnt = half;
   }
