@@ -1625,6 +1625,7 @@ int opir_set_graphs(opir_ctx *ctx, int enable) {
   if (!ctx) return OPIR_ERR_ARG;
   std::lock_guard<std::mutex> g(ctx->mu);
   ctx->graphs = enable != 0;
+  if (ctx->rns) ctx->rns->set_graphs(enable != 0);
   return OPIR_OK;
 }
 

@@ -593,8 +593,20 @@ int RnsServer::cuda_fail(cudaError_t e, const char *what) {
   } while (0)
 
 RnsServer::~RnsServer() {
+  clear_graphs();
   for (auto &e : ev_)
     if (e) cudaEventDestroy(e);
+}
+
+void RnsServer::clear_graphs() {
+  for (auto &g : graphs_cache_)
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+  graphs_cache_.clear();
+}
+
+void RnsServer::set_graphs(bool on) {
+  graphs_ = on;
+  if (!on) clear_graphs();
 }
 
 int RnsServer::create(const opir_rns_params &P, int device, std::unique_ptr<RnsServer> *out,
@@ -723,6 +735,7 @@ int RnsServer::create(const opir_rns_params &P, int device, std::unique_ptr<RnsS
       *err = std::string("events: ") + cudaGetErrorString(e);
       return OPIR_ERR_CUDA;
     }
+  if (const char *v = getenv("OPIR_GRAPHS")) s->graphs_ = atoi(v) != 0;
   *out = std::move(s);
   return OPIR_OK;
 }
@@ -856,6 +869,7 @@ int RnsServer::ensure_workspace(const Db &db) {
   const size_t dig = std::max(cts * 2 * C_.l_key, (nr / 2 ? nr / 2 : 1) * 2 * C_.l);
   RCK(digits_.alloc(dig * R * n * 8), "alloc digits");
   RCK(qn_.alloc(n1 * CT * 8), "alloc query operand");
+  RCK(scan_qs_.alloc(R * n * n1 * 16), "alloc scan operand");
   RCK(res_.alloc(nr * CT * 8), "alloc first-dimension result");
   RCK(e_.alloc((nr / 2 ? nr / 2 : 1) * CT * 8), "alloc folding");
   RCK(query_.alloc(CT * 8), "alloc query");
@@ -864,33 +878,17 @@ int RnsServer::ensure_workspace(const Db &db) {
   return OPIR_OK;
 }
 
-int RnsServer::make_query(uint32_t db_id, uint64_t client, const uint64_t *query, uint64_t *resp,
-                          uint8_t *packed, const RnsTrace *trace, cudaStream_t s) {
-  auto dit = dbs_.find(db_id);
-  if (dit == dbs_.end()) return fail(OPIR_ERR_UNKNOWN_DB, "unknown database");
-  Db &db = *dit->second;
-  if (!db.dbs.p) return fail(OPIR_ERR_STATE, "database has no data");
-  auto cit = clients_.find(client);
-  if (cit == clients_.end() || !cit->second->has_galois)
-    return fail(OPIR_ERR_UNKNOWN_CLIENT, "no Galois keys for client " + std::to_string(client));
-  Client &cl = *cit->second;
-  if (cl.levels < (uint32_t)db.h)
-    return fail(OPIR_ERR_ARG, "the client's Galois keys have too few levels for this database");
-  if (db.ndim > 1 && !cl.has_gsw)
-    return fail(OPIR_ERR_UNKNOWN_CLIENT, "no RGSW key for client " + std::to_string(client));
-  int rc = ensure_workspace(db);
-  if (rc) return rc;
+int RnsServer::enqueue_query(Db &db, Client &cl, const RnsTrace *trace, bool timed,
+                             cudaStream_t s) {
   const int n = C_.n, R = C_.R, M = R + 1;
   const int nch = n / kPT;  // coefficient chunks of the pointwise kernels
   const size_t CT = 2 * (size_t)R * n;
   const int h = db.h, u = db.u, l = C_.l, lk = C_.l_key;
   const size_t w = (size_t)1 << h;
   const int n1 = (int)db.shape.fst_dim_sz, nr = (int)db.shape.other_dim_sz;
-  const bool timed = timing_ && !trace;
   auto mark = [&](int i) {
     if (timed) cudaEventRecord(ev_[i], s);
   };
-  RCK(cudaMemcpyAsync(query_.p, query, CT * 8, cudaMemcpyHostToDevice, s), "upload query");
   mark(0);
   // ---- expansion (fast_expand_qry): live nodes of level a are those whose
   // subtree holds one of the u useful leaves
@@ -936,7 +934,6 @@ int RnsServer::make_query(uint32_t db_id, uint64_t client, const uint64_t *query
     // into a shared-memory ring, 30-bit half products), where the shape fits
     bool streamed = false;
     if (nr >= 2 && n1 % 8 == 0) {
-      RCK(scan_qs_.alloc((size_t)R * n * n1 * sizeof(uint4)), "alloc scan operand");
       rns_scan_operand_kernel<<<dim3((n + 31) / 32, (n1 + 31) / 32, R), dim3(32, 8), 0, s>>>(
           qn_.u64(), static_cast<uint4 *>(scan_qs_.p), n1, C_);
       launches_++;
@@ -987,10 +984,6 @@ int RnsServer::make_query(uint32_t db_id, uint64_t client, const uint64_t *query
       C_.small_w);
   launches_ += 2;
   mark(5);
-  RCK(cudaGetLastError(), "query launch");
-  if (resp) RCK(cudaMemcpyAsync(resp, resp_.p, 2 * (size_t)n * 8, cudaMemcpyDeviceToHost, s), "download response");
-  if (packed)
-    RCK(cudaMemcpyAsync(packed, packed_.p, resp_bytes_, cudaMemcpyDeviceToHost, s), "download response");
   if (trace) {
     if (trace->leaves)
       RCK(cudaMemcpyAsync(trace->leaves, leaves, (size_t)u * CT * 8, cudaMemcpyDeviceToHost, s), "trace");
@@ -999,6 +992,90 @@ int RnsServer::make_query(uint32_t db_id, uint64_t client, const uint64_t *query
                           cudaMemcpyDeviceToHost, s),
           "trace");
   }
+  (void)w;
+  return OPIR_OK;
+}
+
+int RnsServer::make_query(uint32_t db_id, uint64_t client, const uint64_t *query, uint64_t *resp,
+                          uint8_t *packed, const RnsTrace *trace, cudaStream_t s) {
+  auto dit = dbs_.find(db_id);
+  if (dit == dbs_.end()) return fail(OPIR_ERR_UNKNOWN_DB, "unknown database");
+  Db &db = *dit->second;
+  if (!db.dbs.p) return fail(OPIR_ERR_STATE, "database has no data");
+  auto cit = clients_.find(client);
+  if (cit == clients_.end() || !cit->second->has_galois)
+    return fail(OPIR_ERR_UNKNOWN_CLIENT, "no Galois keys for client " + std::to_string(client));
+  Client &cl = *cit->second;
+  if (cl.levels < (uint32_t)db.h)
+    return fail(OPIR_ERR_ARG, "the client's Galois keys have too few levels for this database");
+  if (db.ndim > 1 && !cl.has_gsw)
+    return fail(OPIR_ERR_UNKNOWN_CLIENT, "no RGSW key for client " + std::to_string(client));
+  int rc = ensure_workspace(db);
+  if (rc) return rc;
+  const int n = C_.n, R = C_.R;
+  const size_t CT = 2 * (size_t)R * n;
+  const bool timed = timing_ && !trace;
+  RCK(cudaMemcpyAsync(query_.p, query, CT * 8, cudaMemcpyHostToDevice, s), "upload query");
+  if (graphs_ && !trace && !timed) {
+    // every pointer and shape the kernels take: a graph whose key matches
+    // launches exactly what enqueue_query would
+    const std::vector<uint64_t> key = {
+        (uint64_t)db.dbs.p, (uint64_t)cl.galois.p, (uint64_t)cl.gsw.p, (uint64_t)db.h,
+        (uint64_t)db.u, (uint64_t)db.ndim, db.shape.fst_dim_sz, db.shape.other_dim_sz,
+        (uint64_t)exp0_.p, (uint64_t)exp1_.p, (uint64_t)lift_.p, (uint64_t)acc_.p,
+        (uint64_t)s0_.p, (uint64_t)gsw_.p, (uint64_t)digits_.p, (uint64_t)qn_.p,
+        (uint64_t)scan_qs_.p, (uint64_t)res_.p, (uint64_t)e_.p, (uint64_t)query_.p,
+        (uint64_t)resp_.p, (uint64_t)packed_.p, (uint64_t)status_.p};
+    Graph *hit = nullptr;
+    for (auto &g : graphs_cache_)
+      if (g.key == key) hit = &g;
+    if (!hit) {
+      cudaGraph_t graph = nullptr;
+      const uint64_t before = launches_;
+      cudaError_t ce = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+      int erc = ce == cudaSuccess ? enqueue_query(db, cl, nullptr, false, s) : OPIR_ERR_CUDA;
+      if (ce == cudaSuccess) ce = cudaStreamEndCapture(s, &graph);
+      cudaGraphExec_t exec = nullptr;
+      if (!erc && ce == cudaSuccess && graph)
+        ce = cudaGraphInstantiate(&exec, graph, 0);
+      if (graph) cudaGraphDestroy(graph);
+      const uint64_t captured = launches_ - before;
+      launches_ = before;
+      if (!erc && ce == cudaSuccess && exec) {
+        if ((int)graphs_cache_.size() < kMaxGraphs) {
+          graphs_cache_.emplace_back();
+          hit = &graphs_cache_.back();
+        } else {
+          hit = &graphs_cache_[0];
+          for (auto &g : graphs_cache_)
+            if (g.used < hit->used) hit = &g;
+          cudaGraphExecDestroy(hit->exec);
+        }
+        hit->key = key;
+        hit->exec = exec;
+        hit->launches = captured;
+      } else {
+        // capture failed: launch the kernels directly
+        if (exec) cudaGraphExecDestroy(exec);
+        cudaGetLastError();
+      }
+    }
+    if (hit) {
+      hit->used = ++graph_clock_;
+      RCK(cudaGraphLaunch(hit->exec, s), "query graph");
+      launches_ += hit->launches;
+    } else {
+      const int rc2 = enqueue_query(db, cl, nullptr, false, s);
+      if (rc2) return rc2;
+    }
+  } else {
+    const int rc2 = enqueue_query(db, cl, trace, timed, s);
+    if (rc2) return rc2;
+  }
+  RCK(cudaGetLastError(), "query launch");
+  if (resp) RCK(cudaMemcpyAsync(resp, resp_.p, 2 * (size_t)n * 8, cudaMemcpyDeviceToHost, s), "download response");
+  if (packed)
+    RCK(cudaMemcpyAsync(packed, packed_.p, resp_bytes_, cudaMemcpyDeviceToHost, s), "download response");
   RCK(cudaStreamSynchronize(s), "query");
   {
     // a bounded device wait of the scan that gave up (async.cuh)
@@ -1016,7 +1093,6 @@ int RnsServer::make_query(uint32_t db_id, uint64_t client, const uint64_t *query
     }
   }
   stage_valid_ = timed;
-  (void)w;
   return OPIR_OK;
 }
 

@@ -98,6 +98,8 @@ class RnsServer {
   uint64_t response_bytes() const { return resp_bytes_; }
   uint64_t launches() const { return launches_; }
   void set_timing(bool on) { timing_ = on; }
+  // replay each (database, client, workspace) query as a CUDA graph
+  void set_graphs(bool on);
   bool stage_times(float *ms6) const;
   const std::string &error() const { return err_; }
 
@@ -117,6 +119,8 @@ class RnsServer {
   int fail(int code, const std::string &msg);
   int cuda_fail(cudaError_t e, const char *what);
   int ensure_workspace(const Db &db);
+  // every kernel of one query, on stream s (captured into a graph or launched)
+  int enqueue_query(Db &db, Client &cl, const RnsTrace *trace, bool timed, cudaStream_t s);
   void ntt_launch(const uint64_t *src, size_t src_stride, uint64_t *dst, size_t dst_stride,
                   int polys, int groups, int period, bool inverse, cudaStream_t s);
 
@@ -140,6 +144,19 @@ class RnsServer {
   uint64_t resp_bytes_ = 0;
   uint64_t launches_ = 0;
   bool timing_ = false, stage_valid_ = false;
+  // the synchronous query as CUDA graphs: executables keyed by every pointer
+  // and shape their kernel parameters hold; the least recently used of
+  // kMaxGraphs is replaced on a miss
+  struct Graph {
+    std::vector<uint64_t> key;
+    cudaGraphExec_t exec = nullptr;
+    uint64_t used = 0, launches = 0;
+  };
+  static constexpr int kMaxGraphs = 8;
+  bool graphs_ = true;
+  std::vector<Graph> graphs_cache_;
+  uint64_t graph_clock_ = 0;
+  void clear_graphs();
   cudaEvent_t ev_[8] = {};  // stage boundaries 0-5, scan kernel 6-7
   std::string err_;
 };

@@ -174,3 +174,33 @@ def test_generic_kernels_with_one_prime_match_the_single_modulus_oracle(oracle_l
             assert np.array_equal(resp, want.reshape(-1)) and np.array_equal(packed, wpacked)
     finally:
         L.opir_ctx_destroy(ctx)
+
+
+def test_graph_replay_matches_direct_launches(oracle_lib, gpu_lib):
+    """Synchronous queries are replayed as CUDA graphs keyed by client and
+    workspace: two clients (two executables) alternating, each replayed,
+    equal the oracle and the same queries launched directly."""
+    from onionpirv2_gb300 import PirParams, PirServer
+    params = PirParams.preset("rns1024")
+    o = _rns_oracle(oracle_lib, params)
+    server = PirServer(params)
+    server.gen_data(31)
+    db = o.build_db(31)
+    keys = []
+    for c in (1, 2):
+        sk = o.keygen(40 + c)
+        gk, gsw = o.galois_keys(sk, 50 + c), o.gsw_key(sk, 60 + c)
+        server.set_client_galois_key(c, gk)
+        server.set_client_gsw_key(c, gsw)
+        keys.append((sk, gk, o.gsw_to_ntt(gsw)))
+    asked = [(1 + j % 2, (97 * j + 5) % params.num_entries) for j in range(6)]
+    queries = [o.make_query(keys[c - 1][0], 70 + j, i) for j, (c, i) in enumerate(asked)]
+    replayed = [server.make_query(c, q) for (c, _), q in zip(asked, queries)]
+    server.set_graphs(False)
+    direct = [server.make_query(c, q) for (c, _), q in zip(asked, queries)]
+    for j, ((c, i), q) in enumerate(zip(asked, queries)):
+        _, gk, gsn = keys[c - 1]
+        ref, packed, _ = o.make_query_server(db, gk, gsn, q)
+        assert np.array_equal(replayed[j], ref) and replayed[j].packed == packed.tobytes(), j
+        assert np.array_equal(direct[j], ref), j
+    server.close()
