@@ -170,6 +170,7 @@ struct PipeEnv {
   bool timed;        // record the stage events
   bool keep_pins;    // leave the batch's clients pinned (serving: until the batch completes)
   bool graph = false;  // launches recorded into a CUDA graph
+  bool fork = false;   // one query: RGSW reconstruction on the context's side stream
 };
 
 // ---- serving (continuous batching)
@@ -238,6 +239,11 @@ struct opir_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   cudaStream_t own_stream = nullptr;
+  // a single query's RGSW reconstruction runs on `side`, beside its first
+  // dimension, inside the captured graph (fork and join events)
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+  bool fork_convert = true;  // OPIR_FORK=0: keep it on the query's stream
   opir_params prm{};
   Consts C{};
   ModTables Mq, Mp;
@@ -566,18 +572,26 @@ int run_pipeline(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
   const uint64_t *leaves = cur;
   const size_t leaves_stride = cur_stride;
   record(ctx, E, 1);
-  // ---- convert
+  // ---- convert: for one query on its own stream, so that it runs beside
+  // the first dimension's query transform; the folds wait for it
   const size_t gsw_stride = (size_t)(db.ndim > 1 ? db.ndim - 1 : 1) * 2 * l * CTW;
+  const bool fork = E.fork && ctx->side && db.ndim > 1 && batch == 1 && !trace && !E.timed;
+  if (fork) {
+    CK(cudaEventRecord(ctx->fork_ev, s), "fork");
+    CK(cudaStreamWaitEvent(ctx->side, ctx->fork_ev, 0), "fork");
+  }
   if (db.ndim > 1) {
     launch_query_to_gsw(leaves, leaves_stride, W.gsw.as<uint64_t>(), gsw_stride, qd, (int)n1,
-                        (db.ndim - 1) * l, batch, ctx->Mq.tab, ctx->C, s,
-                        (pdl & kPdlQtg) && h > 0, &db.forms);
+                        (db.ndim - 1) * l, batch, ctx->Mq.tab, ctx->C, fork ? ctx->side : s,
+                        (pdl & kPdlQtg) && h > 0 && !fork, &db.forms);
     ctx->launches++;
   }
+  if (fork) CK(cudaEventRecord(ctx->join_ev, ctx->side), "join");
   record(ctx, E, 2);
   // ---- first dimension
   const size_t res_stride = nr * CTW;
-  const bool pdl_prep = (pdl & kPdlPrep) && (h > 0 || db.ndim > 1);  // a kernel precedes
+  const bool pdl_prep =
+      (pdl & kPdlPrep) && (h > 0 || (db.ndim > 1 && !fork));  // a kernel precedes on s
   rc = enqueue_first_dim(ctx, db, W, leaves, leaves_stride, batch, pdl_prep, E);
   if (rc) return rc;
   record(ctx, E, 7);
@@ -596,11 +610,13 @@ int run_pipeline(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
     CK(cudaStreamSynchronize(s), "trace first dim");
   }
   // ---- other dimensions
+  if (fork) CK(cudaStreamWaitEvent(s, ctx->join_ev, 0), "join");
   size_t cnt = nr;
   for (int i = 1; i < db.ndim; i++) {
     const int half = (int)(cnt / 2);
     launch_fold(W.res.as<uint64_t>(), res_stride, W.gsw.as<uint64_t>() + (size_t)(i - 1) * 2 * l * CTW,
-                gsw_stride, half, batch, ctx->Mq.tab, ctx->C, s, (pdl & kPdlFold) != 0, &db.forms);
+                gsw_stride, half, batch, ctx->Mq.tab, ctx->C, s,
+                (pdl & kPdlFold) != 0 && !(fork && i == 1), &db.forms);
     ctx->launches++;
     cnt = half;
   }
@@ -685,6 +701,7 @@ int run_sync(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
   CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin graph capture");
   PipeEnv Eg = E;
   Eg.graph = true;
+  Eg.fork = ctx->side != nullptr && ctx->fork_convert;
   rc = run_pipeline(ctx, db, 1, client_ids, d_queries, d_resp, d_packed, nullptr, Eg);
   cudaGraph_t g = nullptr;
   const cudaError_t ce = cudaStreamEndCapture(s, &g);
@@ -968,12 +985,16 @@ int opir_ctx_create(const opir_params *P, int device, opir_ctx **out) {
   if (c->status.alloc(kStatusWords * sizeof(uint32_t)) != cudaSuccess ||
       cudaMemset(c->status.p, 0, kStatusWords * sizeof(uint32_t)) != cudaSuccess)
     return OPIR_ERR_CUDA;
-  if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess)
+  if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming) != cudaSuccess)
     return OPIR_ERR_CUDA;
   c->stream = c->own_stream;
   // test and sweep overrides of the engine choice
   if (const char *v = getenv("OPIR_TC")) c->engine = atoi(v) ? OPIR_ENGINE_TENSOR : OPIR_ENGINE_IMAD;
   if (const char *v = getenv("OPIR_GRAPHS")) c->graphs = atoi(v) != 0;
+  if (const char *v = getenv("OPIR_FORK")) c->fork_convert = atoi(v) != 0;
   if (const char *v = getenv("OPIR_HOST_COPIES")) c->host_copies = atoi(v) != 0;
   if (const char *v = getenv("OPIR_BATCH_SCAN"))
     if (!atoi(v)) c->engine = OPIR_ENGINE_SCAN;
@@ -1021,11 +1042,15 @@ void opir_ctx_destroy(opir_ctx *ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (auto &e : ctx->ev)
     if (e) cudaEventDestroy(e);
+  if (ctx->side) cudaStreamSynchronize(ctx->side);
+  if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
+  if (ctx->join_ev) cudaEventDestroy(ctx->join_ev);
   ctx->dbs.clear();
   ctx->clients.clear();
-  cudaStream_t own = ctx->own_stream;
+  cudaStream_t own = ctx->own_stream, side = ctx->side;
   delete ctx;
   if (own) cudaStreamDestroy(own);
+  if (side) cudaStreamDestroy(side);
 }
 
 int opir_ctx_set_stream(opir_ctx *ctx, void *stream) {
