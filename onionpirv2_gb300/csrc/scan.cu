@@ -709,6 +709,7 @@ int g_num_sms = 0;
 // fastest on the 262,144-plaintext database (0.655 against 0.674 ms)
 constexpr int kDefaultCfg = 8;
 int g_cfg = kDefaultCfg;
+bool g_balance_rounds = true;  // OPIR_SCAN_BALANCE=0: one CTA per resident slot
 int g_batch_form = 3;  // accumulate spelling of scan_batch_kernel (OPIR_BATCH_MAC)
 
 template <int R, int W, int K, int S, int B, int KA, bool TWO = false>
@@ -753,6 +754,12 @@ bool launch_bulk(const uint64_t *dbs, const uint4 *qs, size_t qs_stride, uint64_
   const int sms = g_num_sms > 0 ? g_num_sms : 152;
   long long grid = (long long)per_sm * sms;
   if (grid > G.items) grid = G.items;
+  if (g_balance_rounds) {
+    // as many CTAs as the rounds need: the last round then keeps them all
+    // busy (2048 tiles: 147 CTAs of 14 rounds instead of 152 ending with 72)
+    const long long rounds = (G.items + grid - 1) / grid;
+    grid = (G.items + rounds - 1) / rounds;
+  }
   scan_bulk_kernel<R, W, K, S, B, KA, TWO><<<(unsigned)grid, W * 32 + 32, smem, s>>>(
       dbs, qs, qs_stride, out, out_stride, G, C, mu_lo, mu_hi, status);
   return true;
@@ -802,6 +809,8 @@ cudaError_t init_scan_attributes() {
     g_batch_form = 3;  // measured fastest: carry-chained 32-bit multiply-adds
     if (const char *v = getenv("OPIR_BATCH_MAC")) g_batch_form = atoi(v) & 3;
   }
+  g_balance_rounds = true;
+  if (const char *v = getenv("OPIR_SCAN_BALANCE")) g_balance_rounds = atoi(v) != 0;
   g_cfg = kDefaultCfg;
   if (const char *v = getenv("OPIR_SCAN_CFG")) {
     const int i = atoi(v);
