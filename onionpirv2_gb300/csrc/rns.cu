@@ -135,6 +135,50 @@ __device__ __forceinline__ void exchange_4096(uint64_t *s, uint64_t r[8], int ti
   load_pass(s, r, tid, TO);
 }
 
+// forward core: r strided (values < 8q) -> r in SEAL's order, 8 tid + e
+// (fully reduced)
+__device__ __forceinline__ void ntt4096_fwd(uint64_t r[8], uint64_t *s, int tid,
+                                            const ulonglong2 *tw, uint64_t q) {
+  const uint64_t q2 = 2 * q, q4 = 4 * q;
+  ct_pass3_4096<9>(r, tid, tw, q, q4);
+  exchange_4096<9, 6>(s, r, tid);
+  ct_pass3_4096<6>(r, tid, tw, q, q4);
+  exchange_4096<6, 3>(s, r, tid);
+  ct_pass3_4096<3>(r, tid, tw, q, q4);
+  exchange_4096<3, 0>(s, r, tid);
+  ct_pass3_4096<0>(r, tid, tw, q, q4);
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    uint64_t w = r[e] >= q4 ? r[e] - q4 : r[e];
+    w = w >= q2 ? w - q2 : w;
+    r[e] = w >= q ? w - q : w;
+  }
+}
+// inverse core: r in SEAL's order, 8 tid + e (values < 4q) -> r strided,
+// scaled by N^-1 (fully reduced)
+__device__ __forceinline__ void ntt4096_inv(uint64_t r[8], uint64_t *s, int tid,
+                                            const ulonglong2 *tw, const RnsMod &M) {
+  const uint64_t q = M.q, q2 = 2 * q, q4 = 4 * q;
+  gs_pass3_4096<0>(r, tid, tw, q, q4);
+  exchange_4096<0, 3>(s, r, tid);
+  gs_pass3_4096<3>(r, tid, tw, q, q4);
+  exchange_4096<3, 6>(s, r, tid);
+  gs_pass3_4096<6>(r, tid, tw, q, q4);
+  exchange_4096<6, 9>(s, r, tid);
+  gs_pass3_4096<9>(r, tid, tw, q, q4);
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    uint64_t v = mul_shoup_lazy4(r[e], M.n_inv, M.n_inv_s, q);
+    v = v >= q2 ? v - q2 : v;
+    r[e] = v >= q ? v - q : v;
+  }
+}
+__device__ __forceinline__ void store_slot8(uint64_t *out, const uint64_t r[8], int tid) {
+  ulonglong2 *o = reinterpret_cast<ulonglong2 *>(out + 8 * tid);
+#pragma unroll
+  for (int e = 0; e < 8; e += 2) o[e / 2] = make_ulonglong2(r[e], r[e + 1]);
+}
+
 __global__ void __launch_bounds__(kT4096) rns_ntt4096_kernel(const uint64_t *src, size_t src_stride,
                                                              uint64_t *dst, size_t dst_stride,
                                                              int period, int inverse, RnsConsts C) {
@@ -142,35 +186,15 @@ __global__ void __launch_bounds__(kT4096) rns_ntt4096_kernel(const uint64_t *src
   const int tid = threadIdx.x;
   const size_t x = blockIdx.x, y = blockIdx.y;
   const int mi = (int)(x % (size_t)period);
-  const uint64_t q = C.m[mi].q, q2 = 2 * q, q4 = 4 * q;
   const uint64_t *in = src + y * src_stride + x * 4096;
   uint64_t *out = dst + y * dst_stride + x * 4096;
   uint64_t r[8];
   if (!inverse) {
-    const ulonglong2 *tw = C.fwd + (size_t)mi * 4096;
 #pragma unroll
     for (int e = 0; e < 8; ++e) r[e] = in[tid + kT4096 * e];
-    ct_pass3_4096<9>(r, tid, tw, q, q4);
-    exchange_4096<9, 6>(s, r, tid);
-    ct_pass3_4096<6>(r, tid, tw, q, q4);
-    exchange_4096<6, 3>(s, r, tid);
-    ct_pass3_4096<3>(r, tid, tw, q, q4);
-    exchange_4096<3, 0>(s, r, tid);
-    ct_pass3_4096<0>(r, tid, tw, q, q4);
-    ulonglong2 *o = reinterpret_cast<ulonglong2 *>(out + 8 * tid);
-#pragma unroll
-    for (int e = 0; e < 8; e += 2) {
-      uint64_t v[2];
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        uint64_t w = r[e + h] >= q4 ? r[e + h] - q4 : r[e + h];
-        w = w >= q2 ? w - q2 : w;
-        v[h] = w >= q ? w - q : w;
-      }
-      o[e / 2] = make_ulonglong2(v[0], v[1]);
-    }
+    ntt4096_fwd(r, s, tid, C.fwd + (size_t)mi * 4096, C.m[mi].q);
+    store_slot8(out, r, tid);
   } else {
-    const ulonglong2 *tw = C.inv + (size_t)mi * 4096;
     const ulonglong2 *i2 = reinterpret_cast<const ulonglong2 *>(in + 8 * tid);
 #pragma unroll
     for (int e = 0; e < 8; e += 2) {
@@ -178,21 +202,67 @@ __global__ void __launch_bounds__(kT4096) rns_ntt4096_kernel(const uint64_t *src
       r[e] = v.x;
       r[e + 1] = v.y;
     }
-    gs_pass3_4096<0>(r, tid, tw, q, q4);
-    exchange_4096<0, 3>(s, r, tid);
-    gs_pass3_4096<3>(r, tid, tw, q, q4);
-    exchange_4096<3, 6>(s, r, tid);
-    gs_pass3_4096<6>(r, tid, tw, q, q4);
-    exchange_4096<6, 9>(s, r, tid);
-    gs_pass3_4096<9>(r, tid, tw, q, q4);
-    const RnsMod &M = C.m[mi];
+    ntt4096_inv(r, s, tid, C.inv + (size_t)mi * 4096, C.m[mi]);
 #pragma unroll
-    for (int e = 0; e < 8; ++e) {
-      uint64_t v = mul_shoup_lazy4(r[e], M.n_inv, M.n_inv_s, q);
-      v = v >= q2 ? v - q2 : v;
-      out[tid + kT4096 * e] = v >= q ? v - q : v;
-    }
+    for (int e = 0; e < 8; ++e) out[tid + kT4096 * e] = r[e];
   }
+}
+
+// One expansion level's key switch at N = 4096, fused: CTA x = (node R + j) M
+// + m gathers sigma_g(c1 mod q_j) through the inverse automorphism (target d
+// takes c1[e] or -c1[e - N], e = d g^-1 mod 2N), lifts it to modulus m and
+// transforms it into lift[x] (the m = 0 CTAs also write sigma_g(c0 mod q_j)
+// into s0, natural order) -- rns_expand_lift_kernel followed by the forward
+// transform.
+__global__ void __launch_bounds__(kT4096) rns_expand_lift_ntt4096_kernel(
+    const uint64_t *cur, uint64_t *lift, uint64_t *s0, uint64_t ginv, RnsConsts C) {
+  __shared__ uint64_t s[kSmem4096];
+  const int R = C.R, M = R + 1, tid = threadIdx.x;
+  const int x = blockIdx.x, m = x % M, j = (x / M) % R, node = x / (M * R);
+  const size_t CT = 2 * (size_t)R * 4096;
+  const uint64_t *c0 = cur + node * CT + (size_t)j * 4096;
+  const uint64_t *c1 = cur + node * CT + (size_t)(R + j) * 4096;
+  const uint64_t qj = C.m[j].q, qm = C.m[m].q;
+  uint64_t *S = s0 + ((size_t)node * R + j) * 4096;
+  uint64_t r[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const int d = tid + kT4096 * e;
+    const uint64_t src = ((uint64_t)d * ginv) & (2 * 4096 - 1);
+    const bool wrap = src >= 4096;
+    const int i = (int)(wrap ? src - 4096 : src);
+    const uint64_t v = wrap ? neg_mod(c1[i], qj) : c1[i];
+    r[e] = v >= qm ? v - qm : v;
+    if (m == 0) S[d] = wrap ? neg_mod(c0[i], qj) : c0[i];
+  }
+  ntt4096_fwd(r, s, tid, C.fwd + (size_t)m * 4096, qm);
+  store_slot8(lift + (size_t)x * 4096, r, tid);
+}
+
+// ... and CTA x = (node 2 + k) M + m sums lift[node][j][m] key[j][k][m] over
+// the decomposition primes j (NTT form) and transforms the sum back into
+// acc[x] (natural order) -- rns_ks_mac_kernel followed by the inverse
+// transform.
+__global__ void __launch_bounds__(kT4096) rns_ks_intt4096_kernel(const uint64_t *lift,
+                                                                 const uint64_t *key, uint64_t *acc,
+                                                                 RnsConsts C) {
+  __shared__ uint64_t s[kSmem4096];
+  const int R = C.R, M = R + 1, tid = threadIdx.x;
+  const int x = blockIdx.x, m = x % M, k = (x / M) % 2, node = x / (2 * M);
+  uint64_t r[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const int c = 8 * tid + e;
+    U128 sum{0, 0};
+    for (int j = 0; j < R; ++j)
+      mac_to(sum, lift[(((size_t)node * R + j) * M + m) * 4096 + c],
+             key[(((size_t)j * 2 + k) * M + m) * 4096 + c]);
+    r[e] = rmod(sum, C.m[m]);
+  }
+  ntt4096_inv(r, s, tid, C.inv + (size_t)m * 4096, C.m[m]);
+  uint64_t *out = acc + (size_t)x * 4096;
+#pragma unroll
+  for (int e = 0; e < 8; ++e) out[tid + kT4096 * e] = r[e];
 }
 
 // Batched transform: polynomial x of group y is src + y src_stride + x N
@@ -900,13 +970,26 @@ int RnsServer::enqueue_query(Db &db, Client &cl, const RnsTrace *trace, bool tim
     const int k = 1 << a;
     const uint64_t g = (uint64_t)n / k + 1;
     uint64_t *nxt = bufs[a & 1];
-    rns_expand_lift_kernel<<<dim3(live * nch, R, M), kPT, 0, s>>>(cur, lift_.u64(), s0_.u64(), g, C_);
-    ntt_launch(lift_.u64(), 0, lift_.u64(), 0, live * R * M, 1, M, false, s);
-    rns_ks_mac_kernel<<<dim3(live * nch, 2, M), kPT, 0, s>>>(lift_.u64(), cl.galois.u64() + a * key_level,
-                                                      acc_.u64(), C_);
-    ntt_launch(acc_.u64(), 0, acc_.u64(), 0, live * 2 * M, 1, M, true, s);
+    if (n == 4096) {
+      // the lift fused into the forward transforms, the key-switch sums into
+      // the inverse ones
+      const uint64_t ginv = hostmath::powmod(g, (uint64_t)n - 1, 2 * (uint64_t)n);  // g odd
+      rns_expand_lift_ntt4096_kernel<<<live * R * M, kT4096, 0, s>>>(cur, lift_.u64(), s0_.u64(),
+                                                                     ginv, C_);
+      rns_ks_intt4096_kernel<<<live * 2 * M, kT4096, 0, s>>>(
+          lift_.u64(), cl.galois.u64() + a * key_level, acc_.u64(), C_);
+      launches_ += 2;
+    } else {
+      rns_expand_lift_kernel<<<dim3(live * nch, R, M), kPT, 0, s>>>(cur, lift_.u64(), s0_.u64(), g,
+                                                                   C_);
+      ntt_launch(lift_.u64(), 0, lift_.u64(), 0, live * R * M, 1, M, false, s);
+      rns_ks_mac_kernel<<<dim3(live * nch, 2, M), kPT, 0, s>>>(
+          lift_.u64(), cl.galois.u64() + a * key_level, acc_.u64(), C_);
+      ntt_launch(acc_.u64(), 0, acc_.u64(), 0, live * 2 * M, 1, M, true, s);
+      launches_ += 2;
+    }
     rns_expand_combine_kernel<<<dim3(live * nch, 2, R), kPT, 0, s>>>(cur, s0_.u64(), acc_.u64(), nxt, k, C_);
-    launches_ += 3;
+    launches_ += 1;
     cur = nxt;
   }
   const uint64_t *leaves = cur;
