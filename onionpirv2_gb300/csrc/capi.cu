@@ -486,7 +486,7 @@ int enqueue_first_dim(opir_ctx *ctx, Db &db, Workspace &W, const uint64_t *leave
                             ctx->Mq.tab, s, pdl_prep);
     launch_tc_query_limbs(W.qs.as<uint64_t>(), W.ql.as<uint16_t>(), (int)n1, (int)nr, batch, s,
                           db.tc_limbs, db.tc_pair);
-    ctx->launches += (batch + 31) / 32;
+    ctx->launches += tc_pass_count(batch);
     record(ctx, E, 6);
     const int tl = launch_tc_scan(db.dbl.as<uint16_t>(), W.ql.as<uint16_t>(), W.res.as<uint64_t>(),
                                   res_stride, (int)n1, (int)nr, batch, ctx->Mq.tab.q,

@@ -198,9 +198,11 @@ enum { kTcLimbs8 = 0, kTcLimbs9 = 1 };
 // limb layout depends on it: give both calls the same.
 void launch_tc_query_limbs(const uint64_t *plane, uint16_t *ql, int n1, int n_rest, int batch,
                            cudaStream_t s, int limbs = -1, int pair = -1);
-// the query limb width (8 or 9) that a pass of min(batch, 32) queries uses
+// the passes (of up to 64 queries) a batch takes, and the query limb width
+// (8 or 9) that a pass of min(batch, 64) queries uses
+int tc_pass_count(int batch);
 int tc_query_limb_width(int batch, int limbs);
-// whether a pass of min(batch, 32) queries runs as CTA pairs
+// whether a pass of min(batch, 64) queries runs as CTA pairs
 bool tc_pair_form(int n_rest, int batch, int limbs, int pair);
 // launch_tc_scan returns -1 when a pass could not be launched (the tensor
 // copy maps of a CTA pair could not be made).

@@ -54,8 +54,8 @@ namespace {
 
 constexpr int kTcRows = 16;                 // database rows per tile
 constexpr int kTcKC = 32;                   // k granularity of the first dimension
-constexpr int kTcMaxNB = 64;                // query polynomials per pass (32 queries)
-constexpr int kTcHalfNB = 32;               // query polynomials per tile (256 TMEM columns)
+constexpr int kTcMaxNB = 128;               // query polynomials per pass (64 queries)
+constexpr int kTcHalfNB = 32;               // query polynomials per tile (<= 256 TMEM columns)
 static_assert(kTcHalfNB / 8 <= 4, "the epilogue holds two groups per warp part");
 // pipeline stages: KC k per stage (64, or 32 when the segment length is an
 // odd multiple of 32), STAGES stages; the 64-k ring (4 x 48 KB) measured
@@ -84,6 +84,8 @@ constexpr uint32_t kErrTcRange = 128u;
 
 constexpr int kTcMaxSegment = 512;  // k per exact fp32 accumulation
 int g_tc_ring = -1;                 // OPIR_TC_RING: force a ring shape (tests, sweeps)
+int g_tc_pass = kTcMaxNB / 2;       // OPIR_TC_PASS: queries per pass (16, 32, 48 or 64)
+int pass_max() { return g_tc_pass; }
 
 struct TcGeom {
   int n1, n_rest, batch;      // batch: queries of the pass
@@ -770,14 +772,19 @@ size_t tc_db_limb_bytes(int n1, int n_rest) { return (size_t)kN * n1 * n_rest * 
 namespace {
 int g_tc_limbs = -1;  // OPIR_TC_LIMBS: force the query limb width (tests, sweeps)
 
-// query polynomials per column half of a pass of pb queries with ql limbs:
-// 8-polynomial epilogue groups, N = ql nbh a multiple of 16, two
-// 32-polynomial halves above 16 queries
+// query polynomials per column block of a pass of pb queries with ql limbs:
+// 8-polynomial epilogue groups, N = ql nbh a multiple of 16; above 16
+// queries, blocks of 32 polynomials (16 queries), up to four per pass -- a
+// pass of 64 queries streams each database tile once from DRAM and three
+// times from L2, where two passes of 32 would stream it twice from DRAM
 int pass_nbh(int pb, int ql, int *nh) {
+  if (pb > kTcHalfNB / 2) {
+    *nh = (pb + kTcHalfNB / 2 - 1) / (kTcHalfNB / 2);
+    return kTcHalfNB;
+  }
   const int gran = ql == 7 ? 8 : 4;
-  const int padded = pb > kTcHalfNB / 2 ? kTcMaxNB / 2 : (pb + gran - 1) / gran * gran;
-  *nh = padded > kTcHalfNB / 2 ? 2 : 1;
-  return 2 * padded / *nh;
+  *nh = 1;
+  return 2 * ((pb + gran - 1) / gran * gran);
 }
 // limbs per query residue of a pass: the forced or requested width, else the
 // one with fewer MMA columns (ties: 9-bit)
@@ -834,16 +841,18 @@ bool pass_pair(int n_rest, int pb, int ql, int pair) {
 
 size_t tc_query_limb_bytes(int n1, int batch) {
   size_t e8 = 0, e9 = 0;
-  for (int b0 = 0; b0 < batch; b0 += kTcMaxNB / 2) {
-    const int pb = batch - b0 < kTcMaxNB / 2 ? batch - b0 : kTcMaxNB / 2;
+  for (int b0 = 0; b0 < batch; b0 += pass_max()) {
+    const int pb = batch - b0 < pass_max() ? batch - b0 : pass_max();
     e8 += pass_limb_elems(n1, pb, 8);
     e9 += pass_limb_elems(n1, pb, 7);
   }
   return (e8 > e9 ? e8 : e9) * sizeof(uint16_t);
 }
 
+int tc_pass_count(int batch) { return (batch + pass_max() - 1) / pass_max(); }
+
 int tc_query_limb_width(int batch, int limbs) {
-  return pass_ql(batch < kTcMaxNB / 2 ? batch : kTcMaxNB / 2, limbs) == 7 ? 9 : 8;
+  return pass_ql(batch < pass_max() ? batch : pass_max(), limbs) == 7 ? 9 : 8;
 }
 
 namespace {
@@ -863,6 +872,11 @@ cudaError_t init_tc_attributes() {
   if (const char *v = getenv("OPIR_TC_LIMBS")) g_tc_limbs = atoi(v);
   g_tc_pair = -1;
   if (const char *v = getenv("OPIR_TC_PAIR")) g_tc_pair = atoi(v);
+  g_tc_pass = kTcMaxNB / 2;
+  if (const char *v = getenv("OPIR_TC_PASS")) {
+    const int q = atoi(v);
+    if (q >= 16 && q <= kTcMaxNB / 2 && q % 16 == 0) g_tc_pass = q;
+  }
   int dev;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&g_tc_sms, cudaDevAttrMultiProcessorCount, dev);
@@ -886,8 +900,8 @@ void launch_db_limbs(const uint64_t *dbs, uint16_t *dbl, int n1, int n_rest, cud
 void launch_tc_query_limbs(const uint64_t *plane, uint16_t *ql, int n1, int n_rest, int batch,
                            cudaStream_t s, int limbs, int pair) {
   size_t off = 0;
-  for (int b0 = 0; b0 < batch; b0 += kTcMaxNB / 2) {
-    const int pb = batch - b0 < kTcMaxNB / 2 ? batch - b0 : kTcMaxNB / 2;
+  for (int b0 = 0; b0 < batch; b0 += pass_max()) {
+    const int pb = batch - b0 < pass_max() ? batch - b0 : pass_max();
     const int qlc = pass_ql(pb, limbs);
     const TcGeom G = pass_geom(n1, kTcRows, pb, qlc);
     // a pair's CTAs each load half of a column block: blocks of nbh / 2
@@ -991,8 +1005,8 @@ int launch_tc_scan(const uint16_t *dbl, const uint16_t *ql, uint64_t *out, size_
   if (!tc_ring_valid(ring, n1)) ring = n1 % 64 == 0 ? kTcRing64x4 : kTcRing32x8;
   int launches = 0;
   size_t off = 0;
-  for (int b0 = 0; b0 < batch; b0 += kTcMaxNB / 2) {
-    const int pb = batch - b0 < kTcMaxNB / 2 ? batch - b0 : kTcMaxNB / 2;
+  for (int b0 = 0; b0 < batch; b0 += pass_max()) {
+    const int pb = batch - b0 < pass_max() ? batch - b0 : pass_max();
     const int qlc = pass_ql(pb, limbs);
     const bool pr = pass_pair(n_rest, pb, qlc, pair);
     const TcGeom G = pass_geom(n1, n_rest, pb, qlc, pr);
@@ -1016,7 +1030,7 @@ int launch_tc_scan(const uint16_t *dbl, const uint16_t *ql, uint64_t *out, size_
 }
 
 bool tc_pair_form(int n_rest, int batch, int limbs, int pair) {
-  const int pb = batch < kTcMaxNB / 2 ? batch : kTcMaxNB / 2;
+  const int pb = batch < pass_max() ? batch : pass_max();
   return pass_pair(n_rest, pb, pass_ql(pb, limbs), pair);
 }
 
