@@ -256,7 +256,8 @@ typedef struct opir_tune_report {
   uint32_t form_points;    /* distinct tree-stage launches measured (<= 128) */
   uint32_t form_stage[128]; /* 0 expansion, 1 RGSW reconstruction, 2 folding */
   uint32_t form_count[128]; /* work items: nodes / ciphertexts / pairs x queries */
-  float form_ms[128][3];   /* one CTA, two CTAs, cluster per ciphertext */
+  float form_ms[128][4];   /* one CTA, two CTAs, cluster, ten-CTA cluster (folding) per
+                              ciphertext; the stage's whole launch sequence */
   int32_t form_choice[128];
   float tc_limbs_ms[2];    /* query limbs of 8 and 9 bits at the largest batch size (the
                               limb split plus the tensor kernel); < 0: not measured */

@@ -126,7 +126,7 @@ class OpirTuneReport(ctypes.Structure):
         ("form_points", ctypes.c_uint32),
         ("form_stage", ctypes.c_uint32 * 128),
         ("form_count", ctypes.c_uint32 * 128),
-        ("form_ms", (ctypes.c_float * 3) * 128),
+        ("form_ms", (ctypes.c_float * 4) * 128),
         ("form_choice", ctypes.c_int32 * 128),
         ("tc_limbs_ms", ctypes.c_float * 2),
         ("tc_limbs_choice", ctypes.c_int32),

@@ -840,53 +840,88 @@ int tune_tree_forms(opir_ctx *ctx, const Db &db, opir_tune_report &R, TreeForms 
     d.galois_s = keys.as<uint64_t>() + gwords;
     d.gsw_key = gswk.as<uint64_t>();
   }
+  CK(fill(exp1.as<uint64_t>(), (size_t)bmax * w * CTW), "autotune operands");
+  // A level's form is timed where it runs: inside its stage's whole sequence
+  // of launches (each level reading its predecessor's output, programmatic
+  // launches as the pipeline makes them), replayed from a CUDA graph for one
+  // query as the synchronous path does; timed alone and back to back, a form
+  // can look faster than it is in the pipeline.  The other levels keep the
+  // choices made so far.
+  auto time_graph = [&](auto &&seq) -> float {
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      cudaGetLastError();
+      return -1.0f;
+    }
+    seq();
+    if (cudaStreamEndCapture(s, &g) != cudaSuccess || g == nullptr) {
+      cudaGetLastError();
+      return -1.0f;
+    }
+    float ms = -1.0f;
+    if (cudaGraphInstantiate(&ge, g, 0) == cudaSuccess) {
+      ms = time_it([&] { return cudaGraphLaunch(ge, s) == cudaSuccess; });
+      cudaGraphExecDestroy(ge);
+    }
+    cudaGraphDestroy(g);
+    cudaGetLastError();
+    return ms;
+  };
   R.form_points = 0;
-  auto measure = [&](int stage, int count, auto &&launch) {
+  auto measure = [&](int stage, int count, int B, auto &&seq) {
     if (out.pick(stage, count) != kFormDefault) return;  // measured already
     if (R.form_points >= 128) return;
-    float ms[3];
-    for (int f = 0; f < 3; f++) {
+    float ms[kTreeForms];
+    for (int f = 0; f < kTreeForms; f++) {
       if (!tree_form_valid(stage, f, ctx->C)) {
         ms[f] = -1.0f;
         continue;
       }
-      TreeForms force;
-      force.set(stage, count, f);
-      ms[f] = time_it([&] {
-        launch(force);
+      TreeForms trial = out;
+      trial.set(stage, count, f);
+      ms[f] = B == 1 ? time_graph([&] { seq(trial); }) : time_it([&] {
+        seq(trial);
         return true;
       });
     }
-    // the default form was chosen from sweeps of the whole pipeline, where
-    // a launch follows its producer; a form timed on its own replaces it only
-    // when it is clearly faster
+    // the stage's time moves by a level's difference only: a form replaces
+    // the default when it saves more than the sequence's timing noise
     const int dflt = tree_default_form(stage, count, ctx->C);
-    const int best = tune::pick_over(ms, 3, dflt, tune::kTuneMargin);
+    const int best = tune::pick_over(ms, kTreeForms, dflt, tune::kSeqMargin);
     out.set(stage, count, best);
     const uint32_t i = R.form_points++;
     R.form_stage[i] = (uint32_t)stage;
     R.form_count[i] = (uint32_t)count;
-    for (int f = 0; f < 3; f++) R.form_ms[i][f] = ms[f];
+    for (int f = 0; f < kTreeForms; f++) R.form_ms[i][f] = ms[f];
     R.form_choice[i] = best;
   };
+  uint64_t *ebuf[2] = {exp0.as<uint64_t>(), exp1.as<uint64_t>()};
   for (int B : batches) {
+    const int pdl = B == 1 ? g_pdl_graph : g_pdl_direct;
+    auto expand_seq = [&](const TreeForms &f) {
+      for (int a = 0; a < db.h; a++) {
+        const int live = (int)((db.u + ((size_t)1 << (db.h - a)) - 1) >> (db.h - a));
+        launch_expand_level(ebuf[(a + 1) & 1], ebuf[a & 1], w * CTW, w * CTW, qd.data(), a, live, B,
+                            ctx->Mq.tab, ctx->Mp.tab, ctx->C, s, (pdl & kPdlExpand) && a > 0, &f);
+      }
+    };
     for (int a = 0; a < db.h; a++) {
       const int live = (int)((db.u + ((size_t)1 << (db.h - a)) - 1) >> (db.h - a));
-      measure(kStageExpand, live * B, [&](const TreeForms &f) {
-        launch_expand_level(exp0.as<uint64_t>(), exp1.as<uint64_t>(), w * CTW, w * CTW, qd.data(),
-                            a, live, B, ctx->Mq.tab, ctx->Mp.tab, ctx->C, s, false, &f);
-      });
+      measure(kStageExpand, live * B, B, expand_seq);
     }
     if (db.ndim > 1)
-      measure(kStageQtg, num_cts * B, [&](const TreeForms &f) {
+      measure(kStageQtg, num_cts * B, B, [&](const TreeForms &f) {
         launch_query_to_gsw(exp0.as<uint64_t>(), w * CTW, gsw.as<uint64_t>(), gsw_stride, qd.data(),
                             n1, num_cts, B, ctx->Mq.tab, ctx->C, s, false, &f);
       });
-    for (int half = nr / 2; half >= 1; half /= 2)
-      measure(kStageFold, half * B, [&](const TreeForms &f) {
-        launch_fold(res.as<uint64_t>(), (size_t)nr * CTW, gsw.as<uint64_t>(), gsw_stride, half, B,
-                    ctx->Mq.tab, ctx->C, s, false, &f);
-      });
+    auto fold_seq = [&](const TreeForms &f) {
+      int i = 1;
+      for (int half = nr / 2; half >= 1; half /= 2, i++)
+        launch_fold(res.as<uint64_t>(), (size_t)nr * CTW, gsw.as<uint64_t>() + (size_t)(i - 1) * 2 * l * CTW,
+                    gsw_stride, half, B, ctx->Mq.tab, ctx->C, s, (pdl & kPdlFold) != 0 && i > 1, &f);
+    };
+    for (int half = nr / 2; half >= 1; half /= 2) measure(kStageFold, half * B, B, fold_seq);
   }
   CK(cudaStreamSynchronize(s), "autotune tree stages");
   return OPIR_OK;

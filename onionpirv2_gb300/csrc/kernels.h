@@ -83,13 +83,15 @@ void launch_ntt_groups(const ModTab &M, uint64_t *polys, int count, int groups,
 // ---- launch forms of the tree stages
 // Every tree stage has a one-CTA form (a whole ciphertext per CTA), a
 // two-CTA form (expansion and folding: the two polynomials' transforms on two
-// CTAs) and a thread-block-cluster form (one ciphertext's independent
-// transforms spread over 4-6 CTAs).  Which is fastest depends on the launch's
+// CTAs), a thread-block-cluster form (one ciphertext's independent
+// transforms spread over 4-6 CTAs) and, for folding, a wide cluster (ten
+// CTAs per pair: one transform each).  Which is fastest depends on the launch's
 // work count (nodes, RGSW ciphertexts or fold pairs, times the queries of the
 // launch) and on the GPU: TreeForms holds the autotuner's choice per count;
 // a count it does not hold takes the measured default thresholds.
 enum { kStageExpand = 0, kStageQtg = 1, kStageFold = 2 };
-enum { kFormDefault = -1, kFormOne = 0, kFormPair = 1, kFormCluster = 2 };
+enum { kFormDefault = -1, kFormOne = 0, kFormPair = 1, kFormCluster = 2, kFormWide = 3 };
+constexpr int kTreeForms = 4;
 struct TreeForms {
   static constexpr int kMax = 96;
   int n[3] = {0, 0, 0};

@@ -495,61 +495,93 @@ __device__ __forceinline__ void digit_mac(uint64_t d[8], const uint64_t *row, ui
 }
 
 // Sum over cluster ranks 0 .. R-1 of the 8 slots 8 tid .. 8 tid + 7 of
-// `src` (a shared-memory array at the same offset in every CTA), mod q.  All
-// 4R 16-byte remote loads are in flight before the first addition: summing
-// element by element serialised the distributed-shared-memory latency.
+// `src` (a shared-memory array at the same offset in every CTA), mod q.  The
+// 16-byte remote loads of up to five ranks are in flight before the first
+// addition (summing element by element serialised the distributed-shared-
+// memory latency; five ranks at a time bound the registers they hold).
 template <int R>
 __device__ __forceinline__ void cluster_sum8(cg::cluster_group &cluster, uint64_t *src, uint64_t q,
                                              uint64_t sum[8]) {
-  ulonglong2 v[R][4];
+  constexpr int kChunk = 5;
 #pragma unroll
-  for (int rr = 0; rr < R; ++rr) {
-    const ulonglong2 *pr = reinterpret_cast<const ulonglong2 *>(
-        cluster.map_shared_rank(src, rr) + slot_idx(threadIdx.x, 0));
+  for (int r0 = 0; r0 < R; r0 += kChunk) {
+    constexpr int kMaxIn = R < kChunk ? R : kChunk;
+    const int nin = R - r0 < kChunk ? R - r0 : kChunk;
+    ulonglong2 v[kMaxIn][4];
 #pragma unroll
-    for (int h = 0; h < 4; ++h) v[rr][h] = pr[h];
-  }
+    for (int rr = 0; rr < kMaxIn; ++rr) {
+      if (rr >= nin) break;
+      const ulonglong2 *pr = reinterpret_cast<const ulonglong2 *>(
+          cluster.map_shared_rank(src, r0 + rr) + slot_idx(threadIdx.x, 0));
 #pragma unroll
-  for (int h = 0; h < 4; ++h) {
-    uint64_t s0 = v[0][h].x, s1 = v[0][h].y;
-#pragma unroll
-    for (int rr = 1; rr < R; ++rr) {
-      s0 = add_mod(s0, v[rr][h].x, q);
-      s1 = add_mod(s1, v[rr][h].y, q);
+      for (int h = 0; h < 4; ++h) v[rr][h] = pr[h];
     }
-    sum[2 * h] = s0;
-    sum[2 * h + 1] = s1;
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+      uint64_t s0 = r0 == 0 ? v[0][h].x : add_mod(sum[2 * h], v[0][h].x, q);
+      uint64_t s1 = r0 == 0 ? v[0][h].y : add_mod(sum[2 * h + 1], v[0][h].y, q);
+#pragma unroll
+      for (int rr = 1; rr < kMaxIn; ++rr) {
+        if (rr >= nin) break;
+        s0 = add_mod(s0, v[rr][h].x, q);
+        s1 = add_mod(s1, v[rr][h].y, q);
+      }
+      sum[2 * h] = s0;
+      sum[2 * h + 1] = s1;
+    }
   }
 }
 
-// Folding (other_dim_mux), 5 CTAs per ciphertext pair (l = 5): CTA r
-// decomposes y - x at digit level l-1-r for both polynomials, transforms and
-// multiplies them with RGSW rows r and l + r, and leaves its partial sums
-// (reduced mod q) in shared memory; CTAs 0 and 1 add the five partials of
-// output polynomial 0 / 1, transform back and add x.
+// Cluster barrier halves: arrive (no memory ordering) and wait.  A CTA may
+// touch another CTA's shared memory only once that CTA has started; an
+// arrive at kernel entry and a wait just before the first remote access
+// guarantee it without stalling the CTAs that have work before it.
+__device__ __forceinline__ void cluster_arrive_relaxed() {
+  asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait() {
+  asm volatile("barrier.cluster.wait.aligned;" ::: "memory");
+}
+
+// Folding (other_dim_mux), a cluster of CS CTAs per ciphertext pair (l = 5,
+// digits of at most 16 bits).  CTAs 0 and 1 transform polynomial 0 / 1 of
+// y - x back to coefficient form, split it into its l digits and store each
+// digit plane (2 bytes a coefficient) into the shared memory of the CTA that
+// multiplies it: with CS = l, CTA k takes digit k of both polynomials (RGSW
+// rows k and l + k); with CS = 2 l, CTA p l + k takes digit k of polynomial
+// p alone (one transform per CTA, for the narrowest levels).  Each CTA
+// leaves its partial sums (reduced mod q) in shared memory, and the sums
+// x + sum of partials are split over the cluster: CTA r adds up its share of
+// the 2 N coefficients from every CTA and writes it.  Moving digit planes
+// instead of 8-byte coefficients, and spreading the final sums, keeps the
+// distributed-shared-memory traffic of any one SM small: it, not the
+// transforms, bounded these launches.
 constexpr int kFoldCluster = 5;
-__global__ void __cluster_dims__(kFoldCluster, 1, 1) __launch_bounds__(T)
-    fold_cluster_kernel(uint64_t *res, size_t res_stride, const uint64_t *gsw, size_t gsw_stride,
-                        int half, ModTab M, Consts C) {
+constexpr int kFoldWide = 2 * kFoldCluster;
+template <int CS>
+__device__ __forceinline__ void fold_cluster_body(uint64_t *res, size_t res_stride,
+                                                  const uint64_t *gsw, size_t gsw_stride, int half,
+                                                  const ModTab &M, const Consts &C) {
   cg::cluster_group cluster = cg::this_cluster();
   const int r = (int)cluster.block_rank();
   extern __shared__ uint64_t smem[];
   uint64_t *sa = smem, *sb = smem + kSmemPoly;
-  uint64_t *part = smem + 2 * kSmemPoly;  // [kk][slot]
+  uint64_t *part = smem + 2 * kSmemPoly;  // [kk][slot]: this CTA's partial sums
+  // [polynomial][coefficient]: the digits this CTA multiplies (shares the
+  // space of `part`, which is written only after they have been read)
+  uint16_t *dig = reinterpret_cast<uint16_t *>(part);
   ulonglong2 *s_fwd = reinterpret_cast<ulonglong2 *>(part + 2 * kN);  // staged by cp.async
   const int tid = threadIdx.x;
-  const int j = blockIdx.x / kFoldCluster, b = blockIdx.y;
+  const int j = blockIdx.x / CS, b = blockIdx.y;
   const uint64_t q = C.q;
   const int l = kFoldCluster;
+  const int digit = r % l;
   uint64_t *xp = res + b * res_stride + (size_t)j * 2 * kN;
   const uint64_t *yp = res + b * res_stride + (size_t)(j + half) * 2 * kN;
   const uint64_t *rgsw = gsw + b * gsw_stride;
+  cluster_arrive_relaxed();
   prefetch_tw(s_fwd, M.fwd);
   grid_dep_sync();
-  const int sh = (l - 1 - r) * C.base_log2;
-  const uint64_t mask = (1ULL << C.base_log2) - 1;
-  // CTAs 0 and 1: polynomial r of y - x, held in NTT form, back to
-  // coefficient form in `part` for every CTA of the cluster to decompose
   if (r < 2) {
     uint64_t d[8], xv[8];
     ldg_slot8(yp + (size_t)r * kN, d);
@@ -557,40 +589,75 @@ __global__ void __cluster_dims__(kFoldCluster, 1, 1) __launch_bounds__(T)
 #pragma unroll
     for (int e = 0; e < 8; ++e) d[e] = sub_mod(d[e], xv[e], q);
     ntt_inv(d, sa, sb, M);
+    cluster_wait();
+    const uint64_t mask = (1ULL << C.base_log2) - 1;
 #pragma unroll
-    for (int e = 0; e < 8; ++e) part[strided_idx(tid, e)] = d[e];
+    for (int k = 0; k < l; ++k) {
+      uint16_t *dst = cluster.map_shared_rank(dig, CS == kFoldWide ? r * l + k : k) + r * kN;
+      const int sh = (l - 1 - k) * C.base_log2;
+#pragma unroll
+      for (int e = 0; e < 8; ++e) dst[strided_idx(tid, e)] = (uint16_t)((d[e] >> sh) & mask);
+    }
+  } else {
+    cluster_wait();
   }
-  cluster.sync();
+  cluster.sync();  // digit planes in place
   U128 acc0[8], acc1[8];
 #pragma unroll
   for (int e = 0; e < 8; ++e) acc0[e] = acc1[e] = U128{0, 0};
+  constexpr int kPolys = CS == kFoldWide ? 1 : 2;
 #pragma unroll
-  for (int poly = 0; poly < 2; ++poly) {
-    const uint64_t *src = cluster.map_shared_rank(part, poly);
+  for (int pi = 0; pi < kPolys; ++pi) {
+    const int poly = CS == kFoldWide ? r / l : pi;
     uint64_t d[8];
 #pragma unroll
-    for (int e = 0; e < 8; ++e) d[e] = (src[strided_idx(tid, e)] >> sh) & mask;
-    if (poly == 0) tw_wait();
-    digit_mac(d, rgsw + (size_t)(poly * l + r) * 2 * kN, sa, sb, s_fwd, M, acc0, acc1);
+    for (int e = 0; e < 8; ++e) d[e] = dig[poly * kN + strided_idx(tid, e)];
+    if (pi == 0) tw_wait();
+    // the transform's barriers order every thread's digit reads before the
+    // partial sums below overwrite them
+    digit_mac(d, rgsw + (size_t)(poly * l + digit) * 2 * kN, sa, sb, s_fwd, M, acc0, acc1);
   }
-  cluster.sync();  // every CTA has read the differences before `part` is reused
 #pragma unroll
   for (int e = 0; e < 8; ++e) {
     const int si = slot_idx(tid, e);
     part[si] = barrett128(acc0[e], q, M.mu_lo, M.mu_hi);
     part[kN + si] = barrett128(acc1[e], q, M.mu_lo, M.mu_hi);
   }
-  cluster.sync();
-  if (r < 2) {
-    // x + RGSW (x) (y - x), staying in NTT form
-    uint64_t sum[8], xv[8];
-    cluster_sum8<kFoldCluster>(cluster, part + (size_t)r * kN, q, sum);
-    ld_slot8(xp + (size_t)r * kN, xv);
+  cluster.sync();  // partial sums in place
+  // x + RGSW (x) (y - x), staying in NTT form: CTA r's share of the N
+  // 16-byte units of the two polynomials
+  const ulonglong2 *src[CS];
 #pragma unroll
-    for (int e = 0; e < 8; ++e) xv[e] = add_mod(xv[e], sum[e], q);
-    stg_slot8(xp + (size_t)r * kN, xv);
+  for (int rr = 0; rr < CS; ++rr)
+    src[rr] = reinterpret_cast<const ulonglong2 *>(cluster.map_shared_rank(part, rr));
+  ulonglong2 *xu = reinterpret_cast<ulonglong2 *>(xp);
+  for (int u = r * kN / CS + tid; u < (r + 1) * kN / CS; u += T) {
+    ulonglong2 v[CS];
+#pragma unroll
+    for (int rr = 0; rr < CS; ++rr) v[rr] = src[rr][u];
+    const ulonglong2 xv = xu[u];
+    uint64_t s0 = xv.x, s1 = xv.y;
+#pragma unroll
+    for (int rr = 0; rr < CS; ++rr) {
+      s0 = add_mod(s0, v[rr].x, q);
+      s1 = add_mod(s1, v[rr].y, q);
+    }
+    xu[u] = make_ulonglong2(s0, s1);
   }
-  cluster.sync();
+  cluster.sync();  // no CTA leaves while another reads its partial sums
+}
+
+__global__ void __cluster_dims__(kFoldCluster, 1, 1) __launch_bounds__(T)
+    fold_cluster_kernel(uint64_t *res, size_t res_stride, const uint64_t *gsw, size_t gsw_stride,
+                        int half, ModTab M, Consts C) {
+  fold_cluster_body<kFoldCluster>(res, res_stride, gsw, gsw_stride, half, M, C);
+}
+
+// ten CTAs per pair: a non-portable cluster size, given at launch
+__global__ void __launch_bounds__(T)
+    fold_wide_kernel(uint64_t *res, size_t res_stride, const uint64_t *gsw, size_t gsw_stride,
+                     int half, ModTab M, Consts C) {
+  fold_cluster_body<kFoldWide>(res, res_stride, gsw, gsw_stride, half, M, C);
 }
 
 // Folding, 2 CTAs per ciphertext pair (the wide levels of few queries): CTA
@@ -749,6 +816,13 @@ int g_pair_threshold = 130;
 // 0.212 ms; its 279-node level and 4- or 32-query batches were slower)
 int g_expand_pair_threshold = 150;
 int g_qtg_threshold = 64;
+// wide fold cluster (10 CTAs per pair) below this many pairs per launch, if
+// the GPU can place a 10-CTA cluster (g_wide_ok): one query's 8 .. 1-pair
+// levels (folding 0.2935 -> 0.287 ms; with the 16- and 32-pair levels too,
+// 0.289 and 0.291)
+int g_wide_threshold = 9;
+bool g_wide_ok = false;
+int g_wide_clusters = 0;  // 10-CTA clusters resident at once (occupancy query)
 
 }  // namespace
 
@@ -795,6 +869,33 @@ cudaError_t init_kernel_attributes() {
   if ((e = cudaFuncSetAttribute(fold_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)kClusterSmem)) != cudaSuccess)
     return e;
+  if ((e = cudaFuncSetAttribute(fold_wide_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)kClusterSmem)) != cudaSuccess)
+    return e;
+  {
+    // a 10-CTA cluster is beyond the portable 8: allowed per kernel, and
+    // usable where the occupancy query places at least one
+    g_wide_ok = false;
+    if (cudaFuncSetAttribute(fold_wide_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+        cudaSuccess) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(kFoldWide);
+      cfg.blockDim = dim3(T);
+      cfg.dynamicSmemBytes = kClusterSmem;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = kFoldWide;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      int nc = 0;
+      if (cudaOccupancyMaxActiveClusters(&nc, fold_wide_kernel, &cfg) == cudaSuccess && nc > 0)
+        g_wide_ok = true;
+      g_wide_clusters = nc;
+    }
+    cudaGetLastError();  // a refused attribute or query leaves the wide form off
+  }
   if ((e = cudaFuncSetAttribute(fold_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)kClusterSmem)) != cudaSuccess)
     return e;
@@ -819,6 +920,8 @@ cudaError_t init_kernel_attributes() {
     g_expand_threshold = g_fold_threshold = g_qtg_threshold = atoi(v);
   if (const char *v = getenv("OPIR_EXPAND_THRESHOLD")) g_expand_threshold = atoi(v);
   if (const char *v = getenv("OPIR_FOLD_THRESHOLD")) g_fold_threshold = atoi(v);
+  g_wide_threshold = 9;
+  if (const char *v = getenv("OPIR_WIDE_THRESHOLD")) g_wide_threshold = atoi(v);
   if (const char *v = getenv("OPIR_QTG_THRESHOLD")) g_qtg_threshold = atoi(v);
   if (const char *v = getenv("OPIR_PAIR_THRESHOLD")) g_pair_threshold = atoi(v);
   if (const char *v = getenv("OPIR_EXPAND_PAIR_THRESHOLD")) g_expand_pair_threshold = atoi(v);
@@ -836,8 +939,11 @@ bool tree_form_valid(int stage, int form, const Consts &C) {
     case kFormPair:
       return stage != kStageQtg;
     case kFormCluster:
-      return stage == kStageExpand || (stage == kStageFold && C.l == kFoldCluster) ||
+      return stage == kStageExpand ||
+             (stage == kStageFold && C.l == kFoldCluster && C.base_log2 <= 16) ||
              (stage == kStageQtg && C.l_key == 2 * (kQtgCluster - 1));
+    case kFormWide:
+      return stage == kStageFold && C.l == kFoldCluster && C.base_log2 <= 16 && g_wide_ok;
     default:
       return false;
   }
@@ -856,6 +962,7 @@ int form_for(int stage, int count, const Consts &C, const TreeForms *forms) {
       return tree_form_valid(kStageQtg, kFormCluster, C) && count < g_qtg_threshold ? kFormCluster
                                                                                       : kFormOne;
     default:
+      if (tree_form_valid(kStageFold, kFormWide, C) && count < g_wide_threshold) return kFormWide;
       return tree_form_valid(kStageFold, kFormCluster, C) && count < g_fold_threshold
                  ? kFormCluster
                  : count < g_pair_threshold ? kFormPair : kFormOne;
@@ -917,7 +1024,23 @@ void launch_fold(uint64_t *res, size_t res_stride, const uint64_t *gsw, size_t g
                  int half, int batch, const ModTab &Mq, const Consts &C, cudaStream_t s,
                  bool pdl, const TreeForms *forms) {
   const int form = form_for(kStageFold, half * batch, C, forms);
-  if (form == kFormCluster)
+  if (form == kFormWide) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(kFoldWide * half, batch);
+    cfg.blockDim = dim3(T);
+    cfg.dynamicSmemBytes = kClusterSmem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[2];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = kFoldWide;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[1].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl ? 2 : 1;
+    cudaLaunchKernelEx(&cfg, fold_wide_kernel, res, res_stride, gsw, gsw_stride, half, Mq, C);
+  } else if (form == kFormCluster)
     launch_kernel(pdl, fold_cluster_kernel, dim3(kFoldCluster * half, batch), dim3(T),
                   kClusterSmem, s, res, res_stride, gsw, gsw_stride, half, Mq, C);
   else if (form == kFormPair)

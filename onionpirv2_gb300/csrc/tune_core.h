@@ -28,6 +28,9 @@ inline int pick(const float *ms, int n) {
 // Launch forms and ring shapes timed on their own, outside the pipeline,
 // replace the default only when at least this much faster.
 constexpr float kTuneMargin = 0.03f;
+// A form timed inside its stage's whole launch sequence replaces the
+// default when the sequence gets at least this much faster.
+constexpr float kSeqMargin = 0.01f;
 
 // the fastest of n measurements if it beats measurement `dflt` by more than
 // `margin` (a fraction of dflt's time), else dflt; pick() when dflt is

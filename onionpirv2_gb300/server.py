@@ -345,7 +345,7 @@ class PirServer:
         names = {1: "scan", 2: "imad", 3: "tensor"}
         keys = ("rows", "warps", "ksteps", "stages", "ctas_per_sm", "karatsuba")
         stages = ("expand", "query_to_gsw", "fold")
-        forms = ("one_cta", "two_cta", "cluster")
+        forms = ("one_cta", "two_cta", "cluster", "wide_cluster")
         return {
             "scan_configs": [dict(zip(keys, list(r.scan_desc[i])), ms=float(r.scan_ms[i]))
                              for i in range(r.scan_configs)],
@@ -365,7 +365,7 @@ class PirServer:
             "tc_form_choice": (("one_cta", "cta_pair")[r.tc_pair_choice]
                                if r.tc_pair_choice >= 0 else None),
             "forms": [{"stage": stages[r.form_stage[i]], "count": int(r.form_count[i]),
-                       "ms": {forms[f]: float(r.form_ms[i][f]) for f in range(3)},
+                       "ms": {forms[f]: float(r.form_ms[i][f]) for f in range(4)},
                        "form": forms[r.form_choice[i]] if r.form_choice[i] >= 0 else None}
                       for i in range(r.form_points)],
         }

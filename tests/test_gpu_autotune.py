@@ -36,9 +36,9 @@ def test_autotune_choices_and_parity(gpu_lib, oracle_lib, shape):
         ms = [b["ms"][k] for k in ("scan", "imad", "tensor")]
         assert b["ms"]["scan"] > 0
         assert b["engine"] == ("scan", "imad", "tensor")[_argmin(ms)]
-    # the tensor kernel's ring and every tree launch's form are the fastest
+    # the tensor kernel's ring, limb width and form are the fastest
     # measurement or within the 3 % by which a candidate timed on its own
-    # must beat the default; the tree launches of one query were measured
+    # must beat the default
     def near_best(ms, chosen):
         best = min(m for m in ms if m >= 0)
         return ms[chosen] >= 0 and ms[chosen] * 0.97 <= best + 1e-9
@@ -53,9 +53,14 @@ def test_autotune_choices_and_parity(gpu_lib, oracle_lib, shape):
     if all(m >= 0 for m in forms):
         assert near_best(forms, ("one_cta", "cta_pair").index(rep["tc_form_choice"]))
     assert rep["forms"] and all(f["form"] is not None for f in rep["forms"])
-    names = ("one_cta", "two_cta", "cluster")
+    # tree forms are timed inside their stage's whole launch sequence and
+    # replace the default when that sequence is more than 1 % faster
+    names = ("one_cta", "two_cta", "cluster", "wide_cluster")
     for f in rep["forms"]:
-        assert near_best([f["ms"][k] for k in names], names.index(f["form"]))
+        ms = [f["ms"][k] for k in names]
+        best = min(m for m in ms if m >= 0)
+        chosen = ms[names.index(f["form"])]
+        assert chosen >= 0 and chosen * 0.99 <= best + 1e-9, f
     assert {f["stage"] for f in rep["forms"]} >= {"expand", "fold"}
     # same bits after tuning: single queries and batches of every size
     o = oracle_lib.Oracle(*shape)

@@ -216,15 +216,18 @@ def test_scan_configs_and_shapes(oracle_lib, gpu_lib, monkeypatch, shape, cfg):
     server.close()
 
 
-@pytest.mark.parametrize("threshold,pair", [(0, 0), (1 << 30, 0), (0, 1 << 30)])
-def test_one_cta_and_cluster_tree_forms(oracle_lib, gpu_lib, monkeypatch, threshold, pair):
+@pytest.mark.parametrize("threshold,pair,wide", [(0, 0, 0), (1 << 30, 0, 0), (0, 1 << 30, 0),
+                                                 (0, 0, 1 << 30)])
+def test_one_cta_and_cluster_tree_forms(oracle_lib, gpu_lib, monkeypatch, threshold, pair, wide):
     """Expansion, RGSW reconstruction and folding give the oracle's results
-    in every kernel form (one CTA per ciphertext, a cluster of CTAs, and for
-    expansion and folding a pair of CTAs per node / ciphertext pair)."""
+    in every kernel form (one CTA per ciphertext, a cluster of CTAs, for
+    expansion and folding a pair of CTAs per node / ciphertext pair, and for
+    folding the ten-CTA cluster)."""
     from onionpirv2_gb300 import PirParams, PirServer
     monkeypatch.setenv("OPIR_CLUSTER_THRESHOLD", str(threshold))
     monkeypatch.setenv("OPIR_PAIR_THRESHOLD", str(pair))
     monkeypatch.setenv("OPIR_EXPAND_PAIR_THRESHOLD", str(pair))
+    monkeypatch.setenv("OPIR_WIDE_THRESHOLD", str(wide))
     o = oracle_lib.Oracle(4096, 256)
     P = o.P
     server = PirServer(PirParams(num_entries=4096, max_fst_dim=256))
