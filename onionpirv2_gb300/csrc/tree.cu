@@ -266,6 +266,18 @@ __global__ void __launch_bounds__(T, 2) fold_kernel(uint64_t *res, size_t res_st
 // cluster forms
 // ---------------------------------------------------------------------------
 
+// Cluster barrier halves: arrive (no memory ordering) and wait.  A CTA may
+// touch another CTA's shared memory only once that CTA has started; an
+// arrive at kernel entry and a wait just before the first remote access
+// guarantee it without stalling the CTAs that have work before it.
+__device__ __forceinline__ void cluster_arrive_relaxed() {
+  asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait() {
+  asm volatile("barrier.cluster.wait.aligned;" ::: "memory");
+}
+
+
 // Expansion, 4 CTAs per tree node; CTA rank = 2 m + kk handles modulus m
 // (0 = q, 1 = p) and key polynomial kk: NTT_m(sigma(c1)) * K[kk][m], INTT.
 // The q-CTA kk then combines with the p-CTA kk through distributed shared
@@ -289,6 +301,7 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(T)
   uint64_t *s_key = reinterpret_cast<uint64_t *>(s_inv + kN);  // key polynomial, companions
   const int node = blockIdx.x >> 2, b = blockIdx.y;
   const size_t key_off = (size_t)level * 4 * kN + (size_t)(2 * kk + m) * kN;
+  cluster_arrive_relaxed();
   // staging groups, completed in this order: forward twiddles, key,
   // companions, inverse twiddles
   prefetch_tw(s_fwd, m ? Mp.fwd : Mq.fwd);
@@ -347,9 +360,17 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(T)
     ntt_inv(t, sa, sb, M);
   }
   if (m == 1) {
+    // the p result goes straight into the shared memory of the q-CTA of the
+    // same key polynomial (rank kk), which combines the two: a remote store
+    // costs the consumer no round trip
+    cluster_wait();
+    uint64_t *dst = cluster.map_shared_rank(s_out, kk);
 #pragma unroll
-    for (int e = 0; e < 8; ++e) s_out[strided_idx(tid, e)] = t[e];
-  } else if (kk == 0) {
+    for (int e = 0; e < 8; ++e) dst[strided_idx(tid, e)] = t[e];
+    cluster.sync();
+    return;  // nothing reads this CTA's shared memory any more
+  }
+  if (kk == 0) {
     // sigma(c0) into s_sig (its last reads were before the transforms' barriers)
 #pragma unroll
     for (int e = 0; e < 8; ++e) {
@@ -362,28 +383,28 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(T)
         s_sig[j - kN] = neg_mod(v, q);
     }
   }
-  cluster.sync();
-  if (m == 0) {
-    const uint64_t *rp = cluster.map_shared_rank(s_out, 2 + kk);
-    uint64_t *ce = nxt + b * out_stride + (size_t)(2 * node) * 2 * kN + (size_t)kk * kN;
-    uint64_t *co = ce + 2 * kN;
+  uint64_t xv[8];
 #pragma unroll
-    for (int e = 0; e < 8; ++e) {
-      const int i = strided_idx(tid, e);
-      const uint64_t rr = add_mod(rp[i], C.p_half, p);
-      const uint64_t v = mul_shoup(sub_mod(add_mod(t[e], C.p_half_mod_q, q), rr, q), C.p_inv_q,
-                                   C.p_inv_q_s, q);
-      const uint64_t cp = kk == 0 ? add_mod(s_sig[i], v, q) : v;
-      const uint64_t x = ci[(size_t)kk * kN + i];
-      ce[i] = add_mod(x, cp, q);
-      const uint64_t d = sub_mod(x, cp, q);
-      if (i >= k)
-        co[i - k] = d;
-      else
-        co[kN - k + i] = neg_mod(d, q);
-    }
+  for (int e = 0; e < 8; ++e) xv[e] = ci[(size_t)kk * kN + strided_idx(tid, e)];
+  cluster_wait();
+  cluster.sync();  // the p result is in s_out
+  uint64_t *ce = nxt + b * out_stride + (size_t)(2 * node) * 2 * kN + (size_t)kk * kN;
+  uint64_t *co = ce + 2 * kN;
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const int i = strided_idx(tid, e);
+    const uint64_t rr = add_mod(s_out[i], C.p_half, p);
+    const uint64_t v = mul_shoup(sub_mod(add_mod(t[e], C.p_half_mod_q, q), rr, q), C.p_inv_q,
+                                 C.p_inv_q_s, q);
+    const uint64_t cp = kk == 0 ? add_mod(s_sig[i], v, q) : v;
+    const uint64_t x = xv[e];
+    ce[i] = add_mod(x, cp, q);
+    const uint64_t d = sub_mod(x, cp, q);
+    if (i >= k)
+      co[i - k] = d;
+    else
+      co[kN - k + i] = neg_mod(d, q);
   }
-  cluster.sync();
 }
 
 // Expansion, 2 CTAs per tree node (levels too wide for the 4-CTA cluster to
@@ -530,17 +551,6 @@ __device__ __forceinline__ void cluster_sum8(cg::cluster_group &cluster, uint64_
       sum[2 * h + 1] = s1;
     }
   }
-}
-
-// Cluster barrier halves: arrive (no memory ordering) and wait.  A CTA may
-// touch another CTA's shared memory only once that CTA has started; an
-// arrive at kernel entry and a wait just before the first remote access
-// guarantee it without stalling the CTAs that have work before it.
-__device__ __forceinline__ void cluster_arrive_relaxed() {
-  asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory");
-}
-__device__ __forceinline__ void cluster_wait() {
-  asm volatile("barrier.cluster.wait.aligned;" ::: "memory");
 }
 
 // Folding (other_dim_mux), a cluster of CS CTAs per ciphertext pair (l = 5,
