@@ -99,7 +99,7 @@ struct ModTables {
   uint64_t psi = 0;
 };
 
-constexpr int kGraphKey = 14;  // words identifying a captured single-query graph
+constexpr int kGraphKey = 15;  // words identifying a captured single-query graph
 
 struct Db {
   opir_db_shape shape{};
@@ -171,6 +171,9 @@ struct PipeEnv {
   bool keep_pins;    // leave the batch's clients pinned (serving: until the batch completes)
   bool graph = false;  // launches recorded into a CUDA graph
   bool fork = false;   // one query: RGSW reconstruction on the context's side stream
+  // where the last kernel copies the status word (the host-mapped staging
+  // buffer of a host-buffer call), else nullptr
+  uint32_t *status_out = nullptr;
 };
 
 // ---- serving (continuous batching)
@@ -627,7 +630,7 @@ int run_pipeline(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
   record(ctx, E, 4);
   // ---- mod switch + pack
   launch_modswitch_pack(W.res.as<uint64_t>(), res_stride, d_resp, d_packed, ctx->resp_bytes, batch,
-                        ctx->C, s, (pdl & kPdlModswitch) != 0);
+                        ctx->C, s, (pdl & kPdlModswitch) != 0, E.status, E.status_out);
   ctx->launches++;
   record(ctx, E, 5);
   CK(cudaGetLastError(), "kernel launch");
@@ -661,8 +664,10 @@ PipeEnv sync_env(opir_ctx *ctx) {
 constexpr size_t kGraphs = 16;
 
 int run_sync(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
-             const uint64_t *d_queries, uint64_t *d_resp, uint8_t *d_packed, const Trace *trace) {
-  const PipeEnv E = sync_env(ctx);
+             const uint64_t *d_queries, uint64_t *d_resp, uint8_t *d_packed, const Trace *trace,
+             uint32_t *d_status_out = nullptr) {
+  PipeEnv E = sync_env(ctx);
+  E.status_out = d_status_out;
   cudaStream_t s = E.s;
   bool capturable = s != nullptr && s != cudaStreamLegacy && s != cudaStreamPerThread;
   if (capturable) {
@@ -685,7 +690,7 @@ int run_sync(opir_ctx *ctx, Db &db, int batch, const uint64_t *client_ids,
       client_ids[0],      (uint64_t)qd.galois, (uint64_t)qd.galois_s, (uint64_t)qd.gsw_key,
       (uint64_t)d_queries, (uint64_t)d_resp,   (uint64_t)d_packed,    (uint64_t)W.exp0.p,
       (uint64_t)W.exp1.p,  (uint64_t)W.gsw.p,  (uint64_t)W.qs.p,      (uint64_t)W.res.p,
-      (uint64_t)db.dbs.p,  (uint64_t)(int64_t)db.scan_cfg};
+      (uint64_t)db.dbs.p,  (uint64_t)(int64_t)db.scan_cfg, (uint64_t)d_status_out};
   Db::Graph *hit = nullptr, *lru = nullptr;
   for (auto &g : db.graphs) {
     if (std::memcmp(g.key, key, sizeof key) == 0) hit = &g;
@@ -1397,9 +1402,12 @@ static int query_host(opir_ctx *ctx, uint32_t db_id, uint32_t batch, const uint6
       cudaHostGetDevicePointer(reinterpret_cast<void **>(&d_in), W.h_in.p, 0) == cudaSuccess &&
       cudaHostGetDevicePointer(reinterpret_cast<void **>(&d_out), W.h_out.p, 0) == cudaSuccess;
   int rc;
+  // the status word travels with the responses: one synchronisation per
+  // call; the last kernel copies it into the mapped buffer itself
+  uint32_t *h_status = reinterpret_cast<uint32_t *>(h_resp + status_off);
   if (mapped) {
     rc = run_sync(ctx, *db, (int)batch, client_ids, d_in, reinterpret_cast<uint64_t *>(d_out),
-                  d_out + batch * CTB, trace);
+                  d_out + batch * CTB, trace, reinterpret_cast<uint32_t *>(d_out + status_off));
   } else {
     cudaGetLastError();
     CK(cudaMemcpyAsync(W.queries.p, W.h_in.p, batch * CTB, cudaMemcpyHostToDevice, ctx->stream),
@@ -1415,11 +1423,10 @@ static int query_host(opir_ctx *ctx, uint32_t db_id, uint32_t batch, const uint6
     CK(cudaMemcpyAsync(h_packed, W.packed.p, batch * ctx->resp_bytes, cudaMemcpyDeviceToHost,
                        ctx->stream),
        "download responses");
-  // the status word travels with the responses: one synchronisation per call
-  uint32_t *h_status = reinterpret_cast<uint32_t *>(h_resp + status_off);
-  CK(cudaMemcpyAsync(h_status, ctx->status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost,
-                     ctx->stream),
-     "read status");
+  if (!mapped)
+    CK(cudaMemcpyAsync(h_status, ctx->status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                       ctx->stream),
+       "read status");
   CK(cudaStreamSynchronize(ctx->stream), "query");
   if (*h_status) {
     const uint32_t st = *h_status;

@@ -106,7 +106,9 @@ constexpr int kModSlices = 16;
 template <bool kSwitch>
 __global__ void __launch_bounds__(T) modswitch_pack_kernel(const uint64_t *res, size_t res_stride,
                                                            uint64_t *resp, uint8_t *packed,
-                                                           int packed_bytes, Consts C) {
+                                                           int packed_bytes, Consts C,
+                                                           const uint32_t *status,
+                                                           uint32_t *status_out) {
   extern __shared__ uint32_t words[];
   const int tid = threadIdx.x, slice = blockIdx.x, b = blockIdx.y;
   const int w = C.small_q_width;
@@ -116,6 +118,8 @@ __global__ void __launch_bounds__(T) modswitch_pack_kernel(const uint64_t *res, 
   for (int i = tid; i < nwords; i += T) words[i] = 0;
   __syncthreads();
   grid_dep_sync();
+  if (status_out && tid == 0 && slice == 0 && b == 0)
+    *status_out = *reinterpret_cast<const volatile uint32_t *>(status);
   const uint64_t *ct = res + b * res_stride;
   const uint64_t mask = (1ULL << w) - 1;
   for (int i = i0 + tid; i < i0 + per; i += T) {
@@ -277,18 +281,20 @@ void launch_query_prep_plane(const uint64_t *leaves, size_t leaves_stride, uint6
 
 void launch_modswitch_pack(const uint64_t *res, size_t res_stride, uint64_t *resp,
                            uint8_t *packed, size_t packed_bytes, int batch, const Consts &C,
-                           cudaStream_t s, bool pdl) {
+                           cudaStream_t s, bool pdl, const uint32_t *status,
+                           uint32_t *status_out) {
   // the packed stream is 2N w bits exactly; each slice fills its own words
   const size_t smem = ((size_t)(2 * kN / kModSlices) * C.small_q_width / 32 + 2) * sizeof(uint32_t);
   launch_kernel(pdl, modswitch_pack_kernel<true>, dim3(kModSlices, batch), dim3(T), smem, s, res,
-                res_stride, resp, packed, (int)packed_bytes, C);
+                res_stride, resp, packed, (int)packed_bytes, C, status, status_out);
 }
 
 void launch_pack_response(const uint64_t *resps, size_t stride, uint8_t *packed,
                           size_t packed_bytes, int batch, const Consts &C, cudaStream_t s) {
   const size_t smem = ((size_t)(2 * kN / kModSlices) * C.small_q_width / 32 + 2) * sizeof(uint32_t);
   launch_kernel(false, modswitch_pack_kernel<false>, dim3(kModSlices, batch), dim3(T), smem, s,
-                resps, stride, (uint64_t *)nullptr, packed, (int)packed_bytes, C);
+                resps, stride, (uint64_t *)nullptr, packed, (int)packed_bytes, C,
+                (const uint32_t *)nullptr, (uint32_t *)nullptr);
 }
 
 void launch_db_pack(const uint8_t *entries, uint64_t *coeffs, size_t num_pt, int entry_size,

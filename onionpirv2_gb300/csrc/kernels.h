@@ -227,9 +227,12 @@ void launch_fold(uint64_t *res, size_t res_stride, const uint64_t *gsw, size_t g
                  bool pdl = false, const TreeForms *forms = nullptr);
 
 // ---- mod switch to small_q + response bit packing
+// (status_out: block 0 also copies the device status word *status there,
+// once every earlier kernel of the stream has completed)
 void launch_modswitch_pack(const uint64_t *res, size_t res_stride, uint64_t *resp,
                            uint8_t *packed, size_t packed_bytes, int batch, const Consts &C,
-                           cudaStream_t s, bool pdl = false);
+                           cudaStream_t s, bool pdl = false, const uint32_t *status = nullptr,
+                           uint32_t *status_out = nullptr);
 
 // ---- response bit packing alone (save_resp_to_stream of any response
 // mod small_q): resps[b] at stride words -> packed[b][packed_bytes]

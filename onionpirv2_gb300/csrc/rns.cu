@@ -557,11 +557,16 @@ __global__ void rns_finish_kernel(const uint64_t *res, uint64_t *resp, RnsConsts
 }
 
 // one thread per output byte: the LSB-first stream of ncoeff coefficients of
-// w bits each, every coefficient masked to w bits (server.cpp:603-622)
+// w bits each, every coefficient masked to w bits (server.cpp:603-622);
+// status_out: also copy the device status word *status there (every earlier
+// kernel of the stream has completed)
 __global__ void rns_pack_kernel(const uint64_t *resp, size_t resp_stride, uint8_t *packed,
-                                size_t nbytes, int ncoeff, int w) {
+                                size_t nbytes, int ncoeff, int w, const uint32_t *status,
+                                uint32_t *status_out) {
   const size_t byte = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (byte >= nbytes) return;
+  if (status_out && byte == 0 && blockIdx.y == 0)
+    *status_out = *reinterpret_cast<const volatile uint32_t *>(status);
   const uint64_t *r = resp + blockIdx.y * resp_stride;
   const uint64_t mask = (1ULL << w) - 1;
   uint64_t pos = byte * 8;
@@ -666,6 +671,7 @@ RnsServer::~RnsServer() {
   clear_graphs();
   for (auto &e : ev_)
     if (e) cudaEventDestroy(e);
+  if (h_io_) cudaFreeHost(h_io_);
 }
 
 void RnsServer::clear_graphs() {
@@ -799,6 +805,21 @@ int RnsServer::create(const opir_rns_params &P, int device, std::unique_ptr<RnsS
       (e = cudaMemset(s->status_.p, 0, kStatusWords * sizeof(uint32_t))) != cudaSuccess) {
     *err = std::string("status word: ") + cudaGetErrorString(e);
     return e == cudaErrorMemoryAllocation ? OPIR_ERR_OOM : OPIR_ERR_CUDA;
+  }
+  {
+    // [query 2 R N words][response 2 N words][packed bytes][status word],
+    // each part 16-byte aligned
+    auto up16 = [](size_t x) { return (x + 15) / 16 * 16; };
+    s->io_resp_off_ = up16(2 * (size_t)R * n * 8);
+    s->io_packed_off_ = s->io_resp_off_ + up16(2 * (size_t)n * 8);
+    s->io_status_off_ = s->io_packed_off_ + up16(s->resp_bytes_);
+    if ((e = cudaMallocHost(&s->h_io_, s->io_status_off_ + 16)) != cudaSuccess ||
+        (e = cudaHostGetDevicePointer(reinterpret_cast<void **>(&s->d_io_), s->h_io_, 0)) !=
+            cudaSuccess) {
+      *err = std::string("pinned staging: ") + cudaGetErrorString(e);
+      return e == cudaErrorMemoryAllocation ? OPIR_ERR_OOM : OPIR_ERR_CUDA;
+    }
+    std::memset(s->h_io_, 0, s->io_status_off_ + 16);
   }
   for (auto &ev : s->ev_)
     if ((e = cudaEventCreate(&ev)) != cudaSuccess) {
@@ -942,9 +963,6 @@ int RnsServer::ensure_workspace(const Db &db) {
   RCK(scan_qs_.alloc(R * n * n1 * 16), "alloc scan operand");
   RCK(res_.alloc(nr * CT * 8), "alloc first-dimension result");
   RCK(e_.alloc((nr / 2 ? nr / 2 : 1) * CT * 8), "alloc folding");
-  RCK(query_.alloc(CT * 8), "alloc query");
-  RCK(resp_.alloc(2 * n * 8), "alloc response");
-  RCK(packed_.alloc(resp_bytes_ + 16), "alloc packed");
   return OPIR_OK;
 }
 
@@ -962,7 +980,7 @@ int RnsServer::enqueue_query(Db &db, Client &cl, const RnsTrace *trace, bool tim
   mark(0);
   // ---- expansion (fast_expand_qry): live nodes of level a are those whose
   // subtree holds one of the u useful leaves
-  const uint64_t *cur = query_.u64();
+  const uint64_t *cur = reinterpret_cast<const uint64_t *>(d_io_);
   uint64_t *bufs[2] = {exp0_.u64(), exp1_.u64()};
   const size_t key_level = (size_t)R * 2 * M * n;
   for (int a = 0; a < h; a++) {
@@ -1061,10 +1079,11 @@ int RnsServer::enqueue_query(Db &db, Client &cl, const RnsTrace *trace, bool tim
   }
   mark(4);
   // ---- modulus switches and packing
-  rns_finish_kernel<<<(2 * n + kPT - 1) / kPT, kPT, 0, s>>>(res_.u64(), resp_.u64(), C_);
+  uint64_t *d_resp = reinterpret_cast<uint64_t *>(d_io_ + io_resp_off_);
+  rns_finish_kernel<<<(2 * n + kPT - 1) / kPT, kPT, 0, s>>>(res_.u64(), d_resp, C_);
   rns_pack_kernel<<<dim3((unsigned)((resp_bytes_ + kPT - 1) / kPT), 1), kPT, 0, s>>>(
-      resp_.u64(), 2 * (size_t)n, static_cast<uint8_t *>(packed_.p), resp_bytes_, 2 * n,
-      C_.small_w);
+      d_resp, 2 * (size_t)n, d_io_ + io_packed_off_, resp_bytes_, 2 * n, C_.small_w,
+      static_cast<const uint32_t *>(status_.p), reinterpret_cast<uint32_t *>(d_io_ + io_status_off_));
   launches_ += 2;
   mark(5);
   if (trace) {
@@ -1098,7 +1117,7 @@ int RnsServer::make_query(uint32_t db_id, uint64_t client, const uint64_t *query
   const int n = C_.n, R = C_.R;
   const size_t CT = 2 * (size_t)R * n;
   const bool timed = timing_ && !trace;
-  RCK(cudaMemcpyAsync(query_.p, query, CT * 8, cudaMemcpyHostToDevice, s), "upload query");
+  std::memcpy(h_io_, query, CT * 8);  // nothing in flight: the previous call synchronised
   if (graphs_ && !trace && !timed) {
     // every pointer and shape the kernels take: a graph whose key matches
     // launches exactly what enqueue_query would
@@ -1107,8 +1126,8 @@ int RnsServer::make_query(uint32_t db_id, uint64_t client, const uint64_t *query
         (uint64_t)db.u, (uint64_t)db.ndim, db.shape.fst_dim_sz, db.shape.other_dim_sz,
         (uint64_t)exp0_.p, (uint64_t)exp1_.p, (uint64_t)lift_.p, (uint64_t)acc_.p,
         (uint64_t)s0_.p, (uint64_t)gsw_.p, (uint64_t)digits_.p, (uint64_t)qn_.p,
-        (uint64_t)scan_qs_.p, (uint64_t)res_.p, (uint64_t)e_.p, (uint64_t)query_.p,
-        (uint64_t)resp_.p, (uint64_t)packed_.p, (uint64_t)status_.p};
+        (uint64_t)scan_qs_.p, (uint64_t)res_.p, (uint64_t)e_.p, (uint64_t)d_io_,
+        (uint64_t)status_.p};
     Graph *hit = nullptr;
     for (auto &g : graphs_cache_)
       if (g.key == key) hit = &g;
@@ -1156,14 +1175,12 @@ int RnsServer::make_query(uint32_t db_id, uint64_t client, const uint64_t *query
     if (rc2) return rc2;
   }
   RCK(cudaGetLastError(), "query launch");
-  if (resp) RCK(cudaMemcpyAsync(resp, resp_.p, 2 * (size_t)n * 8, cudaMemcpyDeviceToHost, s), "download response");
-  if (packed)
-    RCK(cudaMemcpyAsync(packed, packed_.p, resp_bytes_, cudaMemcpyDeviceToHost, s), "download response");
   RCK(cudaStreamSynchronize(s), "query");
   {
-    // a bounded device wait of the scan that gave up (async.cuh)
-    uint32_t st = 0;
-    RCK(cudaMemcpy(&st, status_.p, sizeof st, cudaMemcpyDeviceToHost), "read status");
+    // a bounded device wait of the scan that gave up (async.cuh): the pack
+    // kernel copied the status word next to the response
+    const uint32_t st =
+        *reinterpret_cast<const volatile uint32_t *>(static_cast<uint8_t *>(h_io_) + io_status_off_);
     if (st) {
       RCK(cudaMemset(status_.p, 0, sizeof st), "clear status");
       return fail(OPIR_ERR_TIMEOUT, "device pipeline wait timed out (status 0x" +
@@ -1175,6 +1192,8 @@ int RnsServer::make_query(uint32_t db_id, uint64_t client, const uint64_t *query
                                         ")");
     }
   }
+  if (resp) std::memcpy(resp, static_cast<uint8_t *>(h_io_) + io_resp_off_, 2 * (size_t)n * 8);
+  if (packed) std::memcpy(packed, static_cast<uint8_t *>(h_io_) + io_packed_off_, resp_bytes_);
   stage_valid_ = timed;
   return OPIR_OK;
 }
@@ -1218,7 +1237,7 @@ int RnsServer::pack_response(const uint64_t *resps, uint32_t count, uint8_t *pac
   RCK(cudaMemcpyAsync(din.p, resps, in, cudaMemcpyHostToDevice, s), "upload");
   rns_pack_kernel<<<dim3((unsigned)((resp_bytes_ + kPT - 1) / kPT), count), kPT, 0, s>>>(
       din.u64(), 2 * (size_t)C_.n, static_cast<uint8_t *>(dout.p), resp_bytes_, 2 * C_.n,
-      C_.small_w);
+      C_.small_w, (const uint32_t *)nullptr, (uint32_t *)nullptr);
   launches_++;
   RCK(cudaGetLastError(), "pack launch");
   RCK(cudaMemcpyAsync(packed, dout.p, out, cudaMemcpyDeviceToHost, s), "download");

@@ -139,9 +139,15 @@ class RnsServer {
   Consts scan_c_[kRnsMaxPrimes] = {};
   uint64_t scan_mu_[kRnsMaxPrimes][2] = {};
   RnsBuf scan_qs_, status_;
-  RnsBuf exp0_, exp1_, lift_, acc_, s0_, gsw_, digits_, qn_, res_, e_, query_, resp_, packed_,
-      coeffs_;
+  RnsBuf exp0_, exp1_, lift_, acc_, s0_, gsw_, digits_, qn_, res_, e_, coeffs_;
   uint64_t resp_bytes_ = 0;
+  // the synchronous call's staging, pinned and device-mapped:
+  // [query][response][packed bytes][status word]; the first expansion level
+  // reads the query and the last kernels write the rest across the host
+  // link themselves (no copy-engine transfers)
+  void *h_io_ = nullptr;
+  uint8_t *d_io_ = nullptr;  // the device address of h_io_
+  size_t io_resp_off_ = 0, io_packed_off_ = 0, io_status_off_ = 0;
   uint64_t launches_ = 0;
   bool timing_ = false, stage_valid_ = false;
   // the synchronous query as CUDA graphs: executables keyed by every pointer
