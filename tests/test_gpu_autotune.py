@@ -62,6 +62,8 @@ def test_autotune_choices_and_parity(gpu_lib, oracle_lib, shape):
         chosen = ms[names.index(f["form"])]
         assert chosen >= 0 and chosen * 0.99 <= best + 1e-9, f
     assert {f["stage"] for f in rep["forms"]} >= {"expand", "fold"}
+    # the ten-CTA folding cluster (a non-portable size) can be placed here
+    assert any(f["stage"] == "fold" and f["ms"]["wide_cluster"] >= 0 for f in rep["forms"])
     # same bits after tuning: single queries and batches of every size
     o = oracle_lib.Oracle(*shape)
     db = o.build_db(777)
