@@ -832,7 +832,6 @@ int g_qtg_threshold = 64;
 // 0.289 and 0.291)
 int g_wide_threshold = 9;
 bool g_wide_ok = false;
-int g_wide_clusters = 0;  // 10-CTA clusters resident at once (occupancy query)
 
 }  // namespace
 
@@ -902,7 +901,6 @@ cudaError_t init_kernel_attributes() {
       int nc = 0;
       if (cudaOccupancyMaxActiveClusters(&nc, fold_wide_kernel, &cfg) == cudaSuccess && nc > 0)
         g_wide_ok = true;
-      g_wide_clusters = nc;
     }
     cudaGetLastError();  // a refused attribute or query leaves the wide form off
   }
