@@ -58,6 +58,16 @@ int main() {
   CHECK(pick_over(gone, 3, 0, kTuneMargin) == 1);  // default unavailable
   CHECK(pick_over(near, 3, -1, kTuneMargin) == 1);
 
+  // tree forms, timed inside their stage's whole launch sequence, take the
+  // smaller kSeqMargin; a form the GPU cannot place (the ten-CTA cluster)
+  // is -1 and never chosen
+  const float seq[4] = {0.2504f, 0.2480f, 0.2530f, -1.0f};
+  CHECK(pick_over(seq, 4, 2, kSeqMargin) == 1);   // 2 % faster than the default
+  const float seq_near[4] = {0.2504f, 0.2500f, 0.2510f, 0.2499f};
+  CHECK(pick_over(seq_near, 4, 1, kSeqMargin) == 1);  // within 1 %: keep the default
+  const float seq_wide[4] = {0.2811f, 0.2647f, 0.2536f, 0.2503f};
+  CHECK(pick_over(seq_wide, 4, 2, kSeqMargin) == 3);  // the ten-CTA form, 1.3 % faster
+
   if (failures) return 1;
   std::printf("all checks passed\n");
   return 0;
