@@ -343,12 +343,12 @@ def test_batched_scan_matches_single_and_oracle(oracle_lib, gpu_lib, monkeypatch
     ((4096, 256), 2),       # 256 x 16: one row tile per slot
     ((4096, 256), 20),      # 40 query polynomials: a 256 + 64 column split
     ((1 << 15, 512), 5),    # 512 x 64
-    ((1 << 15, 512), 32),   # a full pass: 512 tensor-memory columns
+    ((1 << 15, 512), 32),   # 64 query polynomials: two column blocks
     ((1 << 14, 1024), 6),   # 1024 x 16: two k segments of 512 summed in the epilogue
-    ((1 << 14, 1024), 40),  # the same in two passes (32 + 8 queries)
+    ((1 << 14, 1024), 40),  # the same for 40 queries: one pass of three column blocks
     ((1536, 128), 4),       # 96 x 16: 32-k pipeline stages (96 is not a multiple of 64)
     ((8704, 1024), 3),      # 544 x 16: k segments of 512 and 32, 32-k pipeline stages
-    ((1 << 15, 1024), 33),  # 1024 x 32: one row-tile pair, two k segments, two passes
+    ((1 << 15, 1024), 33),  # 1024 x 32: one row-tile pair, two k segments, 66 polynomials
     ((3072, 128), 5),       # 96 x 32: a pair with 32-k pipeline stages
     ((17408, 1024), 3),     # 544 x 32: a pair over k segments of 512 and 32
 ])
@@ -388,6 +388,34 @@ def test_tensor_core_first_dim_matches_single_queries(oracle_lib, gpu_lib, monke
         assert np.array_equal(resp[j], ref), j
         plain, _ = o.decrypt(sk, resp[j], 2)
         assert np.array_equal(o.entry_from_plain(idxs[j], plain), server.direct_get_entry(idxs[j]))
+    server.close()
+
+
+@pytest.mark.parametrize("per_pass", ["16", "32", "48", "64"])
+def test_tensor_pass_sizes_give_the_same_responses(oracle_lib, gpu_lib, monkeypatch, per_pass):
+    """A batch split into tensor-core launches of 16, 32, 48 or 64 queries
+    (OPIR_TC_PASS) answers every query as the per-query scan does: 70
+    queries make several passes and a ragged last one, over two k segments."""
+    from onionpirv2_gb300 import PirParams, PirServer
+    monkeypatch.setenv("OPIR_TC", "1")
+    monkeypatch.setenv("OPIR_TC_PASS", per_pass)
+    shape, batch = (1 << 14, 1024), 70
+    o = oracle_lib.Oracle(*shape)
+    P = o.P
+    server = PirServer(PirParams(num_entries=shape[0], max_fst_dim=shape[1]))
+    server.gen_data(77)
+    keys = [make_client(o, 300 + j) for j in range(2)]
+    for j, (sk, gk, gswk) in enumerate(keys):
+        server.set_client_galois_key(j, gk)
+        server.set_client_gsw_key(j, gswk)
+    ids = [j % 2 for j in range(batch)]
+    idxs = [(j * 104729 + 5) % P.num_entries for j in range(batch)]
+    queries = [o.make_query(keys[ids[j]][0], 70 + j, idxs[j]) for j in range(batch)]
+    resp, packed = server.make_query_batch(ids, np.stack(queries))
+    for j in range(batch):
+        single = server.make_query(ids[j], queries[j])
+        assert np.array_equal(resp[j], single), (per_pass, j)
+        assert packed[j].tobytes() == single.packed
     server.close()
 
 
