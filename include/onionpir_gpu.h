@@ -278,9 +278,11 @@ int opir_autotune(opir_ctx *ctx, uint32_t db_id, uint32_t max_batch, uint32_t re
  * when the device is otherwise idle; while another batch runs it waits for a
  * full batch or until the oldest request has waited max_wait_us.  Every
  * response is the one opir_make_query returns for the same query.  While
- * serving is active, opir_make_query* and database changes return
- * OPIR_ERR_STATE; keys can be registered (a client's keys cannot change while
- * its queries are in flight). */
+ * serving is active, opir_make_query and opir_make_query_batch submit their
+ * queries as tickets and wait for them (same responses); the trace, device
+ * and allocation-free calls and database changes return OPIR_ERR_STATE; keys
+ * can be registered (a client's keys cannot change while its queries are in
+ * flight). */
 typedef struct opir_serve_config {
   uint32_t max_batch;    /* queries per batch (>= 1)                    */
   uint32_t lanes;        /* batches on the device at once (1 .. 4)      */

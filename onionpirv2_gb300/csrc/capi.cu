@@ -1438,24 +1438,61 @@ static int query_host(opir_ctx *ctx, uint32_t db_id, uint32_t batch, const uint6
   return collect_times(ctx);
 }
 
+// While serving runs, the synchronous query calls become tickets of the
+// serving lanes (continuous batching) that the call waits for: the same
+// responses, and the caller need not know whether serving is on.  Returns
+// OPIR_ERR_STATE when serving stopped before every query was submitted (the
+// tickets already out are waited for and dropped), so that the caller can
+// answer the whole call synchronously instead.
+static constexpr uint32_t kSyncServeWaitMs = 600000;
+static int query_via_serving(opir_ctx *ctx, uint32_t db_id, uint32_t batch, const uint64_t *client_ids,
+                      const uint64_t *queries, uint64_t *resps, uint8_t *packed) {
+  std::vector<uint64_t> tickets(batch);
+  for (uint32_t i = 0; i < batch; i++) {
+    const int rc = opir_submit(ctx, db_id, client_ids[i], queries + (size_t)i * 2 * kN, &tickets[i]);
+    if (rc) {
+      // leave no ticket of this call behind
+      for (uint32_t j = 0; j < i; j++) opir_wait(ctx, tickets[j], kSyncServeWaitMs, nullptr, nullptr);
+      return rc;
+    }
+  }
+  int first = OPIR_OK;
+  for (uint32_t i = 0; i < batch; i++) {
+    const int rc = opir_wait(ctx, tickets[i], kSyncServeWaitMs,
+                             resps ? resps + (size_t)i * 2 * kN : nullptr,
+                             packed ? packed + (size_t)i * ctx->resp_bytes : nullptr);
+    if (rc && !first) first = rc;
+  }
+  return first;
+}
+
+static int query_sync_or_served(opir_ctx *ctx, uint32_t db_id, uint32_t batch,
+                         const uint64_t *client_ids, const uint64_t *queries, uint64_t *resps,
+                         uint8_t *packed) {
+  {
+    std::lock_guard<std::mutex> g(ctx->mu);
+    if (!serving_active(ctx))
+      return query_host(ctx, db_id, batch, client_ids, queries, resps, packed, nullptr);
+  }
+  const int rc = query_via_serving(ctx, db_id, batch, client_ids, queries, resps, packed);
+  if (rc != OPIR_ERR_STATE) return rc;
+  std::lock_guard<std::mutex> g(ctx->mu);  // serving stopped meanwhile
+  if (serving_active(ctx)) return rc;
+  return query_host(ctx, db_id, batch, client_ids, queries, resps, packed, nullptr);
+}
+
 int opir_make_query(opir_ctx *ctx, uint32_t db_id, uint64_t client_id, const uint64_t *query,
                     uint64_t *resp, uint8_t *packed) {
   RNS_DISPATCH(query ? ctx->rns->make_query(db_id, client_id, query, resp, packed, nullptr, ctx->stream) : OPIR_ERR_ARG)
   if (!ctx || !query) return OPIR_ERR_ARG;
-  std::lock_guard<std::mutex> g(ctx->mu);
-  if (serving_active(ctx))
-    return ctx->fail(OPIR_ERR_STATE, "serving is active: submit queries with opir_submit");
-  return query_host(ctx, db_id, 1, &client_id, query, resp, packed, nullptr);
+  return query_sync_or_served(ctx, db_id, 1, &client_id, query, resp, packed);
 }
 
 int opir_make_query_batch(opir_ctx *ctx, uint32_t db_id, uint32_t batch, const uint64_t *client_ids,
                           const uint64_t *queries, uint64_t *resps, uint8_t *packed) {
   RNS_DISPATCH(queries && client_ids && batch ? rns_batch(ctx, db_id, batch, client_ids, queries, resps, packed) : OPIR_ERR_ARG)
   if (!ctx || !queries || !client_ids || !batch) return OPIR_ERR_ARG;
-  std::lock_guard<std::mutex> g(ctx->mu);
-  if (serving_active(ctx))
-    return ctx->fail(OPIR_ERR_STATE, "serving is active: submit queries with opir_submit");
-  return query_host(ctx, db_id, batch, client_ids, queries, resps, packed, nullptr);
+  return query_sync_or_served(ctx, db_id, batch, client_ids, queries, resps, packed);
 }
 
 int opir_make_query_device(opir_ctx *ctx, uint32_t db_id, uint32_t batch, const uint64_t *client_ids,

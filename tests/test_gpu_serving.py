@@ -48,8 +48,10 @@ def test_results_same_alone_and_in_the_mix(oracle_lib, gpu_lib):
         work.append((cid, db, idx, o.make_query(keys[cid][0], 1000 + j, idx)))
 
     server.serve_start(max_batch=8, lanes=2, max_wait_us=500)
-    with pytest.raises(Exception):            # synchronous queries wait for serving to stop
-        server.make_query(0, work[0][3])
+    # synchronous calls while serving go through the lanes as tickets
+    during = server.make_query(work[0][0], work[0][3], db_id=work[0][1])
+    during_batch, _ = server.make_query_batch([work[1][0], work[2][0]],
+                                              np.stack([work[1][3], work[2][3]]))
     tickets = [None] * len(work)
 
     def submitter(part):
@@ -67,7 +69,8 @@ def test_results_same_alone_and_in_the_mix(oracle_lib, gpu_lib):
     mixed = [server.wait(t, 60000) for t in tickets]
     stats = server.serve_stats()
     server.serve_stop()
-    assert stats["completed"] == len(work) and stats["failed"] == 0
+    # the work and the three synchronous queries
+    assert stats["completed"] == len(work) + 3 and stats["failed"] == 0
     assert stats["batches"] >= 2 and stats["mean_batch"] >= 1.0
     assert 0 < stats["p50_ms"] <= stats["p99_ms"] <= stats["max_ms"]
     assert stats["queries_per_s"] > 0
@@ -79,11 +82,15 @@ def test_results_same_alone_and_in_the_mix(oracle_lib, gpu_lib):
         alone = server.make_query(cid, q, db_id=db)
         assert np.array_equal(mixed[j], alone), j
         assert mixed[j].packed == alone.packed
+        if j == 0:
+            assert np.array_equal(during, alone) and during.packed == alone.packed
         o = oa if db == db_a else ob
         plain, _ = o.decrypt(keys[cid][0], mixed[j], 2)
         want = (server.direct_get_entry(idx) if db == db_a else
                 synthetic_entries(72, idx, 1, pb.get_entry_size())[0])
         assert np.array_equal(o.entry_from_plain(idx, plain), want), j
+    for i, j in enumerate((1, 2)):                # the batch ran on the default database
+        assert np.array_equal(during_batch[i], server.make_query(work[j][0], work[j][3]))
     server.close()
 
 
