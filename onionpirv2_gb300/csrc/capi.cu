@@ -78,6 +78,7 @@ struct DevBuf {
 
 struct PinnedBuf {
   void *p = nullptr;
+  void *d = nullptr;  // its device address (mapped), looked up once per allocation
   size_t bytes = 0;
   ~PinnedBuf() {
     if (p) cudaFreeHost(p);
@@ -85,10 +86,16 @@ struct PinnedBuf {
   cudaError_t alloc(size_t n) {
     if (n <= bytes && p) return cudaSuccess;
     if (p) cudaFreeHost(p);
-    p = nullptr;
+    p = d = nullptr;
     bytes = 0;
     cudaError_t e = cudaMallocHost(&p, n ? n : 16);
-    if (e == cudaSuccess) bytes = n;
+    if (e == cudaSuccess) {
+      bytes = n;
+      if (cudaHostGetDevicePointer(&d, p, 0) != cudaSuccess) {
+        d = nullptr;
+        cudaGetLastError();
+      }
+    }
     return e;
   }
 };
@@ -1395,12 +1402,9 @@ static int query_host(opir_ctx *ctx, uint32_t db_id, uint32_t batch, const uint6
   // reads the queries and the mod-switch kernel writes the responses across
   // the host link themselves, which saves the copy engine's three round trips
   // (set OPIR_HOST_COPIES=1 for copies through device buffers).
-  uint64_t *d_in = nullptr;
-  uint8_t *d_out = nullptr;
-  const bool mapped =
-      !ctx->host_copies &&
-      cudaHostGetDevicePointer(reinterpret_cast<void **>(&d_in), W.h_in.p, 0) == cudaSuccess &&
-      cudaHostGetDevicePointer(reinterpret_cast<void **>(&d_out), W.h_out.p, 0) == cudaSuccess;
+  uint64_t *d_in = static_cast<uint64_t *>(W.h_in.d);
+  uint8_t *d_out = static_cast<uint8_t *>(W.h_out.d);
+  const bool mapped = !ctx->host_copies && d_in && d_out;
   int rc;
   // the status word travels with the responses: one synchronisation per
   // call; the last kernel copies it into the mapped buffer itself
@@ -1409,7 +1413,6 @@ static int query_host(opir_ctx *ctx, uint32_t db_id, uint32_t batch, const uint6
     rc = run_sync(ctx, *db, (int)batch, client_ids, d_in, reinterpret_cast<uint64_t *>(d_out),
                   d_out + batch * CTB, trace, reinterpret_cast<uint32_t *>(d_out + status_off));
   } else {
-    cudaGetLastError();
     CK(cudaMemcpyAsync(W.queries.p, W.h_in.p, batch * CTB, cudaMemcpyHostToDevice, ctx->stream),
        "upload queries");
     rc = run_sync(ctx, *db, (int)batch, client_ids, W.queries.as<uint64_t>(),
