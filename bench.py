@@ -421,6 +421,16 @@ def rns_leg(args, local, clocks=None, cpu=True):
         st.append(server.stage_times())
     server.set_timing(False)
     stages = {k: statistics.mean(x[k] for x in st) for k in st[0]}
+    # batches: the queries spread over the path's concurrent lanes
+    B = 32
+    bq = np.stack([queries[(3 + i) % len(queries)] for i in range(B)])
+    server.make_query_batch([0] * B, bq)
+    reps = max(1, steps // B)
+    t = time.perf_counter()
+    for _ in range(reps):
+        bresp, _ = server.make_query_batch([0] * B, bq)
+    bel = time.perf_counter() - t
+    same = all(np.array_equal(bresp[j], server.make_query(0, bq[j])) for j in (0, B // 2, B - 1))
     server.close()
     R, n = params.get_rns_mod_cnt(), params.poly_degree
     db_bytes = params.get_num_pt() * n * R * 8
@@ -436,6 +446,9 @@ def rns_leg(args, local, clocks=None, cpu=True):
         "timing": "wall clock around blocking opir_make_query calls (host query in, "
                   "response and packed bytes out)",
         "stages_ms": stages,
+        "batched": {"value": B * reps / bel, "unit": "queries/s", "batch": B, "batches": reps,
+                    "what": "opir_make_query_batch, host buffers; queries on concurrent lanes",
+                    "matches_single_query_responses": bool(same)},
         "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
                      "frac": ach / peak,
                      "traffic": read_traffic(args.rns_workload, "scan_bulk_kernel"),

@@ -939,18 +939,12 @@ int tune_tree_forms(opir_ctx *ctx, const Db &db, opir_tune_report &R, TreeForms 
   return OPIR_OK;
 }
 
-// make_query_batch on a multi-modulus context: the queries one after another
-// (queries [batch][2][R][N], resps [batch][2][N], packed [batch][bytes]).
+// make_query_batch on a multi-modulus context (queries [batch][2][R][N],
+// resps [batch][2][N], packed [batch][bytes]): the queries spread over the
+// path's concurrent lanes, each the single-query pipeline.
 int rns_batch(opir_ctx *ctx, uint32_t db_id, uint32_t batch, const uint64_t *ids,
               const uint64_t *queries, uint64_t *resps, uint8_t *packed) {
-  const size_t qw = 2 * (size_t)ctx->prm.poly_degree * ctx->rns_count;
-  const size_t rw = 2 * (size_t)ctx->prm.poly_degree, pb = ctx->resp_bytes;
-  for (uint32_t b = 0; b < batch; b++) {
-    const int rc = ctx->rns->make_query(db_id, ids[b], queries + b * qw, resps ? resps + b * rw : nullptr,
-                                        packed ? packed + b * pb : nullptr, nullptr, ctx->stream);
-    if (rc) return rc;
-  }
-  return OPIR_OK;
+  return ctx->rns->make_query_batch(db_id, batch, ids, queries, resps, packed, ctx->stream);
 }
 
 }  // namespace

@@ -671,7 +671,26 @@ RnsServer::~RnsServer() {
   clear_graphs();
   for (auto &e : ev_)
     if (e) cudaEventDestroy(e);
+}
+
+RnsServer::Lane::~Lane() {
+  if (stream) cudaStreamSynchronize(stream);
   if (h_io_) cudaFreeHost(h_io_);
+  if (stream) cudaStreamDestroy(stream);
+}
+
+int RnsServer::prepare_lane(Lane &L) {
+  if (!L.status_.p) {
+    RCK(L.status_.alloc(kStatusWords * sizeof(uint32_t)), "status word");
+    RCK(cudaMemset(L.status_.p, 0, kStatusWords * sizeof(uint32_t)), "status word");
+  }
+  if (!L.h_io_) {
+    RCK(cudaMallocHost(&L.h_io_, io_status_off_ + 16), "pinned staging");
+    RCK(cudaHostGetDevicePointer(reinterpret_cast<void **>(&L.d_io_), L.h_io_, 0),
+        "pinned staging");
+    std::memset(L.h_io_, 0, io_status_off_ + 16);
+  }
+  return OPIR_OK;
 }
 
 void RnsServer::clear_graphs() {
@@ -801,25 +820,18 @@ int RnsServer::create(const opir_rns_params &P, int device, std::unique_ptr<RnsS
     s->scan_mu_[i][0] = (uint64_t)mu;
     s->scan_mu_[i][1] = (uint64_t)(mu >> 64);
   }
-  if ((e = s->status_.alloc(kStatusWords * sizeof(uint32_t))) != cudaSuccess ||
-      (e = cudaMemset(s->status_.p, 0, kStatusWords * sizeof(uint32_t))) != cudaSuccess) {
-    *err = std::string("status word: ") + cudaGetErrorString(e);
-    return e == cudaErrorMemoryAllocation ? OPIR_ERR_OOM : OPIR_ERR_CUDA;
-  }
   {
-    // [query 2 R N words][response 2 N words][packed bytes][status word],
-    // each part 16-byte aligned
+    // a lane's staging: [query 2 R N words][response 2 N words][packed
+    // bytes][status word], each part 16-byte aligned
     auto up16 = [](size_t x) { return (x + 15) / 16 * 16; };
     s->io_resp_off_ = up16(2 * (size_t)R * n * 8);
     s->io_packed_off_ = s->io_resp_off_ + up16(2 * (size_t)n * 8);
     s->io_status_off_ = s->io_packed_off_ + up16(s->resp_bytes_);
-    if ((e = cudaMallocHost(&s->h_io_, s->io_status_off_ + 16)) != cudaSuccess ||
-        (e = cudaHostGetDevicePointer(reinterpret_cast<void **>(&s->d_io_), s->h_io_, 0)) !=
-            cudaSuccess) {
-      *err = std::string("pinned staging: ") + cudaGetErrorString(e);
-      return e == cudaErrorMemoryAllocation ? OPIR_ERR_OOM : OPIR_ERR_CUDA;
+    const int lrc = s->prepare_lane(s->lanes_[0]);
+    if (lrc) {
+      *err = s->err_;
+      return lrc;
     }
-    std::memset(s->h_io_, 0, s->io_status_off_ + 16);
   }
   for (auto &ev : s->ev_)
     if ((e = cudaEventCreate(&ev)) != cudaSuccess) {
@@ -945,29 +957,29 @@ int RnsServer::erase_client(uint64_t id) {
   return OPIR_OK;
 }
 
-int RnsServer::ensure_workspace(const Db &db) {
+int RnsServer::ensure_workspace(Lane &L, const Db &db) {
   const size_t n = C_.n, R = C_.R, M = R + 1, CT = 2 * R * n;
   const size_t w = (size_t)1 << db.h;
   const size_t n1 = db.shape.fst_dim_sz, nr = db.shape.other_dim_sz;
   const size_t live = (w + 1) / 2;  // nodes of the widest level
   const size_t cts = (size_t)(db.ndim > 1 ? db.ndim - 1 : 1) * C_.l;
-  RCK(exp0_.alloc(w * CT * 8), "alloc expansion");
-  RCK(exp1_.alloc(w * CT * 8), "alloc expansion");
-  RCK(lift_.alloc(live * R * M * n * 8), "alloc key switching");
-  RCK(acc_.alloc(live * 2 * M * n * 8), "alloc key switching");
-  RCK(s0_.alloc(live * R * n * 8), "alloc key switching");
-  RCK(gsw_.alloc(cts * 2 * CT * 8), "alloc RGSW rows");
+  RCK(L.exp0_.alloc(w * CT * 8), "alloc expansion");
+  RCK(L.exp1_.alloc(w * CT * 8), "alloc expansion");
+  RCK(L.lift_.alloc(live * R * M * n * 8), "alloc key switching");
+  RCK(L.acc_.alloc(live * 2 * M * n * 8), "alloc key switching");
+  RCK(L.s0_.alloc(live * R * n * 8), "alloc key switching");
+  RCK(L.gsw_.alloc(cts * 2 * CT * 8), "alloc RGSW rows");
   const size_t dig = std::max(cts * 2 * C_.l_key, (nr / 2 ? nr / 2 : 1) * 2 * C_.l);
-  RCK(digits_.alloc(dig * R * n * 8), "alloc digits");
-  RCK(qn_.alloc(n1 * CT * 8), "alloc query operand");
-  RCK(scan_qs_.alloc(R * n * n1 * 16), "alloc scan operand");
-  RCK(res_.alloc(nr * CT * 8), "alloc first-dimension result");
-  RCK(e_.alloc((nr / 2 ? nr / 2 : 1) * CT * 8), "alloc folding");
+  RCK(L.digits_.alloc(dig * R * n * 8), "alloc digits");
+  RCK(L.qn_.alloc(n1 * CT * 8), "alloc query operand");
+  RCK(L.scan_qs_.alloc(R * n * n1 * 16), "alloc scan operand");
+  RCK(L.res_.alloc(nr * CT * 8), "alloc first-dimension result");
+  RCK(L.e_.alloc((nr / 2 ? nr / 2 : 1) * CT * 8), "alloc folding");
   return OPIR_OK;
 }
 
-int RnsServer::enqueue_query(Db &db, Client &cl, const RnsTrace *trace, bool timed,
-                             cudaStream_t s) {
+int RnsServer::enqueue_query(Lane &L, Db &db, Client &cl, const RnsTrace *trace,
+                             bool timed, cudaStream_t s) {
   const int n = C_.n, R = C_.R, M = R + 1;
   const int nch = n / kPT;  // coefficient chunks of the pointwise kernels
   const size_t CT = 2 * (size_t)R * n;
@@ -980,8 +992,8 @@ int RnsServer::enqueue_query(Db &db, Client &cl, const RnsTrace *trace, bool tim
   mark(0);
   // ---- expansion (fast_expand_qry): live nodes of level a are those whose
   // subtree holds one of the u useful leaves
-  const uint64_t *cur = reinterpret_cast<const uint64_t *>(d_io_);
-  uint64_t *bufs[2] = {exp0_.u64(), exp1_.u64()};
+  const uint64_t *cur = reinterpret_cast<const uint64_t *>(L.d_io_);
+  uint64_t *bufs[2] = {L.exp0_.u64(), L.exp1_.u64()};
   const size_t key_level = (size_t)R * 2 * M * n;
   for (int a = 0; a < h; a++) {
     const int live = (int)((u + ((size_t)1 << (h - a)) - 1) >> (h - a));
@@ -992,21 +1004,21 @@ int RnsServer::enqueue_query(Db &db, Client &cl, const RnsTrace *trace, bool tim
       // the lift fused into the forward transforms, the key-switch sums into
       // the inverse ones
       const uint64_t ginv = hostmath::powmod(g, (uint64_t)n - 1, 2 * (uint64_t)n);  // g odd
-      rns_expand_lift_ntt4096_kernel<<<live * R * M, kT4096, 0, s>>>(cur, lift_.u64(), s0_.u64(),
+      rns_expand_lift_ntt4096_kernel<<<live * R * M, kT4096, 0, s>>>(cur, L.lift_.u64(), L.s0_.u64(),
                                                                      ginv, C_);
       rns_ks_intt4096_kernel<<<live * 2 * M, kT4096, 0, s>>>(
-          lift_.u64(), cl.galois.u64() + a * key_level, acc_.u64(), C_);
+          L.lift_.u64(), cl.galois.u64() + a * key_level, L.acc_.u64(), C_);
       launches_ += 2;
     } else {
-      rns_expand_lift_kernel<<<dim3(live * nch, R, M), kPT, 0, s>>>(cur, lift_.u64(), s0_.u64(), g,
+      rns_expand_lift_kernel<<<dim3(live * nch, R, M), kPT, 0, s>>>(cur, L.lift_.u64(), L.s0_.u64(), g,
                                                                    C_);
-      ntt_launch(lift_.u64(), 0, lift_.u64(), 0, live * R * M, 1, M, false, s);
+      ntt_launch(L.lift_.u64(), 0, L.lift_.u64(), 0, live * R * M, 1, M, false, s);
       rns_ks_mac_kernel<<<dim3(live * nch, 2, M), kPT, 0, s>>>(
-          lift_.u64(), cl.galois.u64() + a * key_level, acc_.u64(), C_);
-      ntt_launch(acc_.u64(), 0, acc_.u64(), 0, live * 2 * M, 1, M, true, s);
+          L.lift_.u64(), cl.galois.u64() + a * key_level, L.acc_.u64(), C_);
+      ntt_launch(L.acc_.u64(), 0, L.acc_.u64(), 0, live * 2 * M, 1, M, true, s);
       launches_ += 2;
     }
-    rns_expand_combine_kernel<<<dim3(live * nch, 2, R), kPT, 0, s>>>(cur, s0_.u64(), acc_.u64(), nxt, k, C_);
+    rns_expand_combine_kernel<<<dim3(live * nch, 2, R), kPT, 0, s>>>(cur, L.s0_.u64(), L.acc_.u64(), nxt, k, C_);
     launches_ += 1;
     cur = nxt;
   }
@@ -1018,33 +1030,33 @@ int RnsServer::enqueue_query(Db &db, Client &cl, const RnsTrace *trace, bool tim
   if (db.ndim > 1) {
     const int E = (db.ndim - 1) * l;  // ciphertexts
     const uint64_t *first = leaves + (size_t)n1 * CT;
-    ntt_launch(first, (size_t)l * CT, gsw_.u64(), (size_t)2 * l * CT, l * 2 * R, db.ndim - 1, R,
+    ntt_launch(first, (size_t)l * CT, L.gsw_.u64(), (size_t)2 * l * CT, l * 2 * R, db.ndim - 1, R,
                false, s);
-    rns_decompose_kernel<<<dim3(E * nch, 2), kPT, 0, s>>>(first, CT, 0, lk, C_.b_key, digits_.u64(), C_);
-    ntt_launch(digits_.u64(), 0, digits_.u64(), 0, E * 2 * lk * R, 1, R, false, s);
-    rns_extprod_mac_kernel<<<dim3(E * nch, 2, R), kPT, 0, s>>>(digits_.u64(), 2 * lk, cl.gsw.u64(),
-                                                        gsw_.u64(), l, 2 * l, l, C_);
+    rns_decompose_kernel<<<dim3(E * nch, 2), kPT, 0, s>>>(first, CT, 0, lk, C_.b_key, L.digits_.u64(), C_);
+    ntt_launch(L.digits_.u64(), 0, L.digits_.u64(), 0, E * 2 * lk * R, 1, R, false, s);
+    rns_extprod_mac_kernel<<<dim3(E * nch, 2, R), kPT, 0, s>>>(L.digits_.u64(), 2 * lk, cl.gsw.u64(),
+                                                        L.gsw_.u64(), l, 2 * l, l, C_);
     launches_ += 2;
   }
   mark(2);
   // ---- first dimension: NTT of the n1 selection ciphertexts, the scan,
   // the inverse NTT of the n_rest results
-  ntt_launch(leaves, 0, qn_.u64(), 0, n1 * 2 * R, 1, R, false, s);
+  ntt_launch(leaves, 0, L.qn_.u64(), 0, n1 * 2 * R, 1, R, false, s);
   {
     // the one-modulus streaming scan over both primes' planes (bulk copies
     // into a shared-memory ring, 30-bit half products), where the shape fits
     bool streamed = false;
     if (nr >= 2 && n1 % 8 == 0) {
       rns_scan_operand_kernel<<<dim3((n + 31) / 32, (n1 + 31) / 32, R), dim3(32, 8), 0, s>>>(
-          qn_.u64(), static_cast<uint4 *>(scan_qs_.p), n1, C_);
+          L.qn_.u64(), static_cast<uint4 *>(L.scan_qs_.p), n1, C_);
       launches_++;
       mark(6);
       // the R N planes of both primes in one launch (slot i N + c reduces mod q_i)
-      streamed = launch_scan_planes(db.dbs.u64(), static_cast<const uint4 *>(scan_qs_.p),
-                                    (size_t)R * n * n1, res_.u64(), (size_t)nr * CT, n1, nr, 1,
+      streamed = launch_scan_planes(db.dbs.u64(), static_cast<const uint4 *>(L.scan_qs_.p),
+                                    (size_t)R * n * n1, L.res_.u64(), (size_t)nr * CT, n1, nr, 1,
                                     R * n, CT, (size_t)R * n, n, scan_c_[0], scan_mu_[0],
                                     scan_c_[R - 1], scan_mu_[R - 1],
-                                    static_cast<uint32_t *>(status_.p), s) >= 0;
+                                    static_cast<uint32_t *>(L.status_.p), s) >= 0;
       if (streamed) launches_++;
     }
     if (!streamed) {
@@ -1052,45 +1064,45 @@ int RnsServer::enqueue_query(Db &db, Client &cl, const RnsTrace *trace, bool tim
       int bd = ((nr + 31) / 32) * 32;
       if (bd > 256) bd = 256;
       rns_scan_kernel<<<dim3(R * n, (nr + bd - 1) / bd), bd, (size_t)n1 * 16, s>>>(
-          db.dbs.u64(), qn_.u64(), res_.u64(), n1, nr, C_);
+          db.dbs.u64(), L.qn_.u64(), L.res_.u64(), n1, nr, C_);
       launches_++;
     }
     mark(7);
   }
-  ntt_launch(res_.u64(), 0, res_.u64(), 0, nr * 2 * R, 1, R, true, s);
+  ntt_launch(L.res_.u64(), 0, L.res_.u64(), 0, nr * 2 * R, 1, R, true, s);
   mark(3);
   if (trace && trace->first_dim)
-    RCK(cudaMemcpyAsync(trace->first_dim, res_.p, (size_t)nr * CT * 8, cudaMemcpyDeviceToHost, s),
+    RCK(cudaMemcpyAsync(trace->first_dim, L.res_.p, (size_t)nr * CT * 8, cudaMemcpyDeviceToHost, s),
         "trace");
   // ---- further dimensions (other_dim_mux)
   int cnt = nr;
   for (int d = 1; d < db.ndim; d++) {
     const int half = cnt / 2;
-    const uint64_t *sel = gsw_.u64() + (size_t)(d - 1) * 2 * l * CT;
-    rns_decompose_kernel<<<dim3(half * nch, 2), kPT, 0, s>>>(res_.u64(), CT, (size_t)half * CT, l, C_.b,
-                                                      digits_.u64(), C_);
-    ntt_launch(digits_.u64(), 0, digits_.u64(), 0, half * 2 * l * R, 1, R, false, s);
-    rns_extprod_mac_kernel<<<dim3(half * nch, 2, R), kPT, 0, s>>>(digits_.u64(), 2 * l, sel, e_.u64(), 1,
+    const uint64_t *sel = L.gsw_.u64() + (size_t)(d - 1) * 2 * l * CT;
+    rns_decompose_kernel<<<dim3(half * nch, 2), kPT, 0, s>>>(L.res_.u64(), CT, (size_t)half * CT, l, C_.b,
+                                                      L.digits_.u64(), C_);
+    ntt_launch(L.digits_.u64(), 0, L.digits_.u64(), 0, half * 2 * l * R, 1, R, false, s);
+    rns_extprod_mac_kernel<<<dim3(half * nch, 2, R), kPT, 0, s>>>(L.digits_.u64(), 2 * l, sel, L.e_.u64(), 1,
                                                            1, 0, C_);
-    ntt_launch(e_.u64(), 0, e_.u64(), 0, half * 2 * R, 1, R, true, s);
-    rns_add_kernel<<<dim3(half * nch, 2, R), kPT, 0, s>>>(res_.u64(), e_.u64(), C_);
+    ntt_launch(L.e_.u64(), 0, L.e_.u64(), 0, half * 2 * R, 1, R, true, s);
+    rns_add_kernel<<<dim3(half * nch, 2, R), kPT, 0, s>>>(L.res_.u64(), L.e_.u64(), C_);
     launches_ += 3;
     cnt = half;
   }
   mark(4);
   // ---- modulus switches and packing
-  uint64_t *d_resp = reinterpret_cast<uint64_t *>(d_io_ + io_resp_off_);
-  rns_finish_kernel<<<(2 * n + kPT - 1) / kPT, kPT, 0, s>>>(res_.u64(), d_resp, C_);
+  uint64_t *d_resp = reinterpret_cast<uint64_t *>(L.d_io_ + io_resp_off_);
+  rns_finish_kernel<<<(2 * n + kPT - 1) / kPT, kPT, 0, s>>>(L.res_.u64(), d_resp, C_);
   rns_pack_kernel<<<dim3((unsigned)((resp_bytes_ + kPT - 1) / kPT), 1), kPT, 0, s>>>(
-      d_resp, 2 * (size_t)n, d_io_ + io_packed_off_, resp_bytes_, 2 * n, C_.small_w,
-      static_cast<const uint32_t *>(status_.p), reinterpret_cast<uint32_t *>(d_io_ + io_status_off_));
+      d_resp, 2 * (size_t)n, L.d_io_ + io_packed_off_, resp_bytes_, 2 * n, C_.small_w,
+      static_cast<const uint32_t *>(L.status_.p), reinterpret_cast<uint32_t *>(L.d_io_ + io_status_off_));
   launches_ += 2;
   mark(5);
   if (trace) {
     if (trace->leaves)
       RCK(cudaMemcpyAsync(trace->leaves, leaves, (size_t)u * CT * 8, cudaMemcpyDeviceToHost, s), "trace");
     if (trace->gsw && db.ndim > 1)
-      RCK(cudaMemcpyAsync(trace->gsw, gsw_.p, (size_t)(db.ndim - 1) * 2 * l * CT * 8,
+      RCK(cudaMemcpyAsync(trace->gsw, L.gsw_.p, (size_t)(db.ndim - 1) * 2 * l * CT * 8,
                           cudaMemcpyDeviceToHost, s),
           "trace");
   }
@@ -1098,11 +1110,7 @@ int RnsServer::enqueue_query(Db &db, Client &cl, const RnsTrace *trace, bool tim
   return OPIR_OK;
 }
 
-int RnsServer::make_query(uint32_t db_id, uint64_t client, const uint64_t *query, uint64_t *resp,
-                          uint8_t *packed, const RnsTrace *trace, cudaStream_t s) {
-  auto dit = dbs_.find(db_id);
-  if (dit == dbs_.end()) return fail(OPIR_ERR_UNKNOWN_DB, "unknown database");
-  Db &db = *dit->second;
+int RnsServer::check_query(Db &db, uint64_t client, Client **out) {
   if (!db.dbs.p) return fail(OPIR_ERR_STATE, "database has no data");
   auto cit = clients_.find(client);
   if (cit == clients_.end() || !cit->second->has_galois)
@@ -1112,22 +1120,24 @@ int RnsServer::make_query(uint32_t db_id, uint64_t client, const uint64_t *query
     return fail(OPIR_ERR_ARG, "the client's Galois keys have too few levels for this database");
   if (db.ndim > 1 && !cl.has_gsw)
     return fail(OPIR_ERR_UNKNOWN_CLIENT, "no RGSW key for client " + std::to_string(client));
-  int rc = ensure_workspace(db);
-  if (rc) return rc;
-  const int n = C_.n, R = C_.R;
-  const size_t CT = 2 * (size_t)R * n;
-  const bool timed = timing_ && !trace;
-  std::memcpy(h_io_, query, CT * 8);  // nothing in flight: the previous call synchronised
+  *out = &cl;
+  return OPIR_OK;
+}
+
+int RnsServer::start_query(Lane &L, Db &db, Client &cl, const uint64_t *query,
+                           const RnsTrace *trace, bool timed, cudaStream_t s) {
+  const size_t CT = 2 * (size_t)C_.R * C_.n;
+  std::memcpy(L.h_io_, query, CT * 8);  // nothing of this lane is in flight
   if (graphs_ && !trace && !timed) {
     // every pointer and shape the kernels take: a graph whose key matches
     // launches exactly what enqueue_query would
     const std::vector<uint64_t> key = {
         (uint64_t)db.dbs.p, (uint64_t)cl.galois.p, (uint64_t)cl.gsw.p, (uint64_t)db.h,
         (uint64_t)db.u, (uint64_t)db.ndim, db.shape.fst_dim_sz, db.shape.other_dim_sz,
-        (uint64_t)exp0_.p, (uint64_t)exp1_.p, (uint64_t)lift_.p, (uint64_t)acc_.p,
-        (uint64_t)s0_.p, (uint64_t)gsw_.p, (uint64_t)digits_.p, (uint64_t)qn_.p,
-        (uint64_t)scan_qs_.p, (uint64_t)res_.p, (uint64_t)e_.p, (uint64_t)d_io_,
-        (uint64_t)status_.p};
+        (uint64_t)L.exp0_.p, (uint64_t)L.exp1_.p, (uint64_t)L.lift_.p, (uint64_t)L.acc_.p,
+        (uint64_t)L.s0_.p, (uint64_t)L.gsw_.p, (uint64_t)L.digits_.p, (uint64_t)L.qn_.p,
+        (uint64_t)L.scan_qs_.p, (uint64_t)L.res_.p, (uint64_t)L.e_.p, (uint64_t)L.d_io_,
+        (uint64_t)L.status_.p};
     Graph *hit = nullptr;
     for (auto &g : graphs_cache_)
       if (g.key == key) hit = &g;
@@ -1135,7 +1145,7 @@ int RnsServer::make_query(uint32_t db_id, uint64_t client, const uint64_t *query
       cudaGraph_t graph = nullptr;
       const uint64_t before = launches_;
       cudaError_t ce = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
-      int erc = ce == cudaSuccess ? enqueue_query(db, cl, nullptr, false, s) : OPIR_ERR_CUDA;
+      int erc = ce == cudaSuccess ? enqueue_query(L, db, cl, nullptr, false, s) : OPIR_ERR_CUDA;
       if (ce == cudaSuccess) ce = cudaStreamEndCapture(s, &graph);
       cudaGraphExec_t exec = nullptr;
       if (!erc && ce == cudaSuccess && graph)
@@ -1167,35 +1177,104 @@ int RnsServer::make_query(uint32_t db_id, uint64_t client, const uint64_t *query
       RCK(cudaGraphLaunch(hit->exec, s), "query graph");
       launches_ += hit->launches;
     } else {
-      const int rc2 = enqueue_query(db, cl, nullptr, false, s);
+      const int rc2 = enqueue_query(L, db, cl, nullptr, false, s);
       if (rc2) return rc2;
     }
   } else {
-    const int rc2 = enqueue_query(db, cl, trace, timed, s);
+    const int rc2 = enqueue_query(L, db, cl, trace, timed, s);
     if (rc2) return rc2;
   }
   RCK(cudaGetLastError(), "query launch");
+  return OPIR_OK;
+}
+
+int RnsServer::finish_query(Lane &L, uint64_t *resp, uint8_t *packed, cudaStream_t s) {
   RCK(cudaStreamSynchronize(s), "query");
   {
     // a bounded device wait of the scan that gave up (async.cuh): the pack
     // kernel copied the status word next to the response
-    const uint32_t st =
-        *reinterpret_cast<const volatile uint32_t *>(static_cast<uint8_t *>(h_io_) + io_status_off_);
+    const uint32_t st = *reinterpret_cast<const volatile uint32_t *>(
+        static_cast<uint8_t *>(L.h_io_) + io_status_off_);
     if (st) {
-      RCK(cudaMemset(status_.p, 0, sizeof st), "clear status");
-      return fail(OPIR_ERR_TIMEOUT, "device pipeline wait timed out (status 0x" +
-                                        [&] {
-                                          char b[16];
-                                          snprintf(b, sizeof b, "%x", st);
-                                          return std::string(b);
-                                        }() +
-                                        ")");
+      RCK(cudaMemset(L.status_.p, 0, sizeof st), "clear status");
+      char b[16];
+      snprintf(b, sizeof b, "%x", st);
+      return fail(OPIR_ERR_TIMEOUT, std::string("device pipeline wait timed out (status 0x") + b + ")");
     }
   }
-  if (resp) std::memcpy(resp, static_cast<uint8_t *>(h_io_) + io_resp_off_, 2 * (size_t)n * 8);
-  if (packed) std::memcpy(packed, static_cast<uint8_t *>(h_io_) + io_packed_off_, resp_bytes_);
-  stage_valid_ = timed;
+  const uint8_t *io = static_cast<const uint8_t *>(L.h_io_);
+  if (resp) std::memcpy(resp, io + io_resp_off_, 2 * (size_t)C_.n * 8);
+  if (packed) std::memcpy(packed, io + io_packed_off_, resp_bytes_);
   return OPIR_OK;
+}
+
+int RnsServer::make_query(uint32_t db_id, uint64_t client, const uint64_t *query, uint64_t *resp,
+                          uint8_t *packed, const RnsTrace *trace, cudaStream_t s) {
+  auto dit = dbs_.find(db_id);
+  if (dit == dbs_.end()) return fail(OPIR_ERR_UNKNOWN_DB, "unknown database");
+  Db &db = *dit->second;
+  Client *cl = nullptr;
+  int rc = check_query(db, client, &cl);
+  if (rc) return rc;
+  Lane &L = lanes_[0];
+  rc = ensure_workspace(L, db);
+  if (rc) return rc;
+  const bool timed = timing_ && !trace;
+  rc = start_query(L, db, *cl, query, trace, timed, s);
+  if (!rc) rc = finish_query(L, resp, packed, s);
+  stage_valid_ = timed && !rc;
+  return rc;
+}
+
+int RnsServer::make_query_batch(uint32_t db_id, uint32_t batch, const uint64_t *clients,
+                                const uint64_t *queries, uint64_t *resps, uint8_t *packed,
+                                cudaStream_t s) {
+  auto dit = dbs_.find(db_id);
+  if (dit == dbs_.end()) return fail(OPIR_ERR_UNKNOWN_DB, "unknown database");
+  Db &db = *dit->second;
+  std::vector<Client *> cls(batch);
+  for (uint32_t b = 0; b < batch; ++b) {
+    const int rc = check_query(db, clients[b], &cls[b]);
+    if (rc) return rc;
+  }
+  const int nl = batch < (uint32_t)kLanes ? (int)batch : kLanes;
+  for (int i = 0; i < nl; ++i) {
+    Lane &L = lanes_[i];
+    int rc = prepare_lane(L);
+    if (!rc) rc = ensure_workspace(L, db);
+    if (rc) return rc;
+    if (i > 0 && !L.stream)
+      RCK(cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking), "lane stream");
+  }
+  RCK(cudaStreamSynchronize(s), "batch");  // keys and database written on s are in place
+  const size_t CT = 2 * (size_t)C_.R * C_.n, rw = 2 * (size_t)C_.n;
+  auto stream_of = [&](int i) { return i == 0 ? s : lanes_[i].stream; };
+  std::vector<long long> pending(nl, -1);
+  int first = OPIR_OK;
+  auto finish = [&](int i) {
+    const long long b = pending[i];
+    pending[i] = -1;
+    const int rc = finish_query(lanes_[i], resps ? resps + b * rw : nullptr,
+                                packed ? packed + b * resp_bytes_ : nullptr, stream_of(i));
+    if (rc && !first) first = rc;
+  };
+  // a lane takes its next query as soon as its previous one is out
+  for (uint32_t b = 0; b < batch && !first; ++b) {
+    const int i = (int)(b % (uint32_t)nl);
+    if (pending[i] >= 0) finish(i);
+    if (first) break;
+    const int rc = start_query(lanes_[i], db, *cls[b], queries + (size_t)b * CT, nullptr, false,
+                               stream_of(i));
+    if (rc) {
+      first = rc;
+      break;
+    }
+    pending[i] = b;
+  }
+  for (int i = 0; i < nl; ++i)
+    if (pending[i] >= 0) finish(i);
+  stage_valid_ = false;
+  return first;
 }
 
 bool RnsServer::stage_times(float *ms6) const {

@@ -93,6 +93,12 @@ class RnsServer {
   // one query [2][R][N] (host) -> resp [2][N] mod small_q and packed bytes (host)
   int make_query(uint32_t db, uint64_t client, const uint64_t *query, uint64_t *resp,
                  uint8_t *packed, const RnsTrace *trace, cudaStream_t s);
+  // `batch` queries [batch][2][R][N] of clients `clients` (host) -> resps
+  // [batch][2][N], packed [batch][bytes]: the queries spread over kLanes
+  // lanes that run concurrently, each query the pipeline make_query runs
+  int make_query_batch(uint32_t db, uint32_t batch, const uint64_t *clients,
+                       const uint64_t *queries, uint64_t *resps, uint8_t *packed,
+                       cudaStream_t s);
   int ntt(int mod, bool inverse, uint64_t *polys, uint64_t count, cudaStream_t s);
   int pack_response(const uint64_t *resps, uint32_t count, uint8_t *packed, cudaStream_t s);
   uint64_t response_bytes() const { return resp_bytes_; }
@@ -115,12 +121,35 @@ class RnsServer {
     uint32_t levels = 0;
     bool has_galois = false, has_gsw = false;
   };
+  // One query's device workspace, bounded-wait status words and pinned,
+  // device-mapped staging [query][response][packed bytes][status word] (the
+  // first expansion level reads the query and the last kernels write the rest
+  // across the host link themselves: no copy-engine transfers).  Lane 0 is
+  // the synchronous call's, on the caller's stream; a batch runs lanes 0 ..
+  // kLanes-1 at once, lanes 1 .. on streams of their own, so that the
+  // latency-bound tree stages of different queries overlap.
+  struct Lane {
+    RnsBuf exp0_, exp1_, lift_, acc_, s0_, gsw_, digits_, qn_, scan_qs_, res_, e_, status_;
+    void *h_io_ = nullptr;
+    uint8_t *d_io_ = nullptr;  // the device address of h_io_
+    cudaStream_t stream = nullptr;  // lanes 1 ..: owned
+    ~Lane();
+  };
+  static constexpr int kLanes = 8;
   RnsServer() = default;
   int fail(int code, const std::string &msg);
   int cuda_fail(cudaError_t e, const char *what);
-  int ensure_workspace(const Db &db);
+  int prepare_lane(Lane &L);  // staging and status words of a lane
+  int ensure_workspace(Lane &L, const Db &db);
+  int check_query(Db &db, uint64_t client, Client **cl);
+  // copy the query into the lane's staging and launch its pipeline on s
+  int start_query(Lane &L, Db &db, Client &cl, const uint64_t *query, const RnsTrace *trace,
+                  bool timed, cudaStream_t s);
+  // wait for the lane, check its status word, copy the response out
+  int finish_query(Lane &L, uint64_t *resp, uint8_t *packed, cudaStream_t s);
   // every kernel of one query, on stream s (captured into a graph or launched)
-  int enqueue_query(Db &db, Client &cl, const RnsTrace *trace, bool timed, cudaStream_t s);
+  int enqueue_query(Lane &L, Db &db, Client &cl, const RnsTrace *trace, bool timed,
+                    cudaStream_t s);
   void ntt_launch(const uint64_t *src, size_t src_stride, uint64_t *dst, size_t dst_stride,
                   int polys, int groups, int period, bool inverse, cudaStream_t s);
 
@@ -138,16 +167,10 @@ class RnsServer {
   // bounded-wait status words
   Consts scan_c_[kRnsMaxPrimes] = {};
   uint64_t scan_mu_[kRnsMaxPrimes][2] = {};
-  RnsBuf scan_qs_, status_;
-  RnsBuf exp0_, exp1_, lift_, acc_, s0_, gsw_, digits_, qn_, res_, e_, coeffs_;
+  RnsBuf coeffs_;
+  Lane lanes_[kLanes];
   uint64_t resp_bytes_ = 0;
-  // the synchronous call's staging, pinned and device-mapped:
-  // [query][response][packed bytes][status word]; the first expansion level
-  // reads the query and the last kernels write the rest across the host
-  // link themselves (no copy-engine transfers)
-  void *h_io_ = nullptr;
-  uint8_t *d_io_ = nullptr;  // the device address of h_io_
-  size_t io_resp_off_ = 0, io_packed_off_ = 0, io_status_off_ = 0;
+  size_t io_resp_off_ = 0, io_packed_off_ = 0, io_status_off_ = 0;  // within a lane's staging
   uint64_t launches_ = 0;
   bool timing_ = false, stage_valid_ = false;
   // the synchronous query as CUDA graphs: executables keyed by every pointer
@@ -158,7 +181,7 @@ class RnsServer {
     cudaGraphExec_t exec = nullptr;
     uint64_t used = 0, launches = 0;
   };
-  static constexpr int kMaxGraphs = 8;
+  static constexpr int kMaxGraphs = 16;
   bool graphs_ = true;
   std::vector<Graph> graphs_cache_;
   uint64_t graph_clock_ = 0;

@@ -104,6 +104,19 @@ def test_uploaded_database_and_batches(rns1024, gpu_lib):
     for j in range(3):
         r, p, _ = o.make_query_server(db, gk, gsn, queries[j])
         assert np.array_equal(resps[j], r) and np.array_equal(packed[j], p)
+    # more queries than the path has lanes, two clients: every response the
+    # single query's, the lanes reused in turn
+    sk2 = o.keygen(191)
+    server.set_client_galois_key(2, o.galois_keys(sk2, 192))
+    server.set_client_gsw_key(2, o.gsw_key(sk2, 193))
+    ids = [1 + (j % 2) for j in range(9)]
+    qs = np.stack([o.make_query(sk if ids[j] == 1 else sk2, 300 + j, (j * 131) % 1024)
+                   for j in range(9)])
+    resps9, packed9 = server.make_query_batch(ids, qs)
+    for j in range(9):
+        single = server.make_query(ids[j], qs[j])
+        assert np.array_equal(resps9[j], single), j
+        assert packed9[j].tobytes() == single.packed, j
     # what a multi-modulus context does not offer fails loudly
     L = _capi.load()
     assert L.opir_autotune(server.ctx, server.db_id, 8, 1, None) == -6
