@@ -1229,6 +1229,7 @@ int RnsServer::make_query(uint32_t db_id, uint64_t client, const uint64_t *query
 int RnsServer::make_query_batch(uint32_t db_id, uint32_t batch, const uint64_t *clients,
                                 const uint64_t *queries, uint64_t *resps, uint8_t *packed,
                                 cudaStream_t s) {
+  if (batch == 0) return OPIR_OK;
   auto dit = dbs_.find(db_id);
   if (dit == dbs_.end()) return fail(OPIR_ERR_UNKNOWN_DB, "unknown database");
   Db &db = *dit->second;
